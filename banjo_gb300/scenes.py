@@ -1,0 +1,292 @@
+"""Synthetic lattice workloads for the bonded-lattice substep.
+
+Each builder returns a *case*: a dict of numpy arrays named as the lattice case
+files name them (node/bond arrays of a LatticeAsset + ActiveMatter, packed
+StepSettings<double> and SphereState<double>, the run length). The same dict
+feeds the GPU backend, the CPU checker and the reference harness, so all three
+see identical inputs.
+
+Bonds follow the reference's box generator walk (src/matter/BoxLattice.cpp:117-155:
+node index order, offsets dz, dy, dx over [-h, h] in the positive half-space,
+src/matter/Lattice.cpp:49-52) filtered to the 6 face + 12 edge neighbours
+(|o|^2 <= 2), so an interior node has 9 unique bonds. Node index is
+x + nx*(y + ny*z) (src/matter/BoxLattice.hpp:22-26). Positions are cell
+centres of a box centred on its own origin (BoxLattice.cpp:82-86).
+
+Seeds are counter-based splitmix64 streams (the mixing function of
+src/matter/Lattice.cpp:28-33): draw k of stream s is mix(s + (k+1)*golden).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# Settings packing (oracle/case_layout.hpp, the one order every runner uses).
+K_DT, K_GRAVITY, K_ITER, K_DAMP, K_SPHERE, K_DIRECT = 0, 1, 4, 5, 6, 7
+K_YIELD, K_HARDEN, K_PLATE, K_CONTACT, K_PLANE_COUNT, K_PLANES = 8, 9, 10, 11, 18, 19
+PLANE_WIDTH = 34
+SETTINGS_WIDTH = 19 + 2 * PLANE_WIDTH
+SPHERE_WIDTH = 12
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+DT_SUBSTEP = (1.0 / 240.0) / 10.0
+INF = float("inf")
+
+
+def splitmix64(values: np.ndarray) -> np.ndarray:
+    """The splitmix64 output mix on uint64 values (wrapping arithmetic)."""
+    z = np.asarray(values, dtype=np.uint64).copy()
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform(seed: int, start: int, count: int) -> np.ndarray:
+    """Draws start..start+count-1 of stream `seed`, uniform in [0, 1)."""
+    k = np.arange(start + 1, start + count + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        state = np.uint64(seed) + k * GOLDEN
+    return (splitmix64(state) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def lognormal(seed: int, count: int, median: float, sigma: float) -> np.ndarray:
+    """Box-Muller normals from draw pairs (2k, 2k+1) of the stream."""
+    u = uniform(seed, 0, 2 * count)
+    u1 = 1.0 - u[0::2]  # (0, 1]
+    u2 = u[1::2]
+    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+    return median * np.exp(sigma * z)
+
+
+def half_offsets(horizon: int = 1, max_d2: int | None = 2):
+    """Positive-half integer offsets in the generator's walk order.
+
+    With max_d2 set, the walk over [-horizon, horizon]^3 keeps |o|^2 <= max_d2
+    (horizon 1, max_d2 2: the 6 face + 12 edge neighbours, 9 per node); with
+    max_d2 None it is the reference's own horizon rule |o| <= horizon
+    (src/matter/BoxLattice.cpp:123-129).
+    """
+    out = []
+    for dz in range(-horizon, horizon + 1):
+        for dy in range(-horizon, horizon + 1):
+            for dx in range(-horizon, horizon + 1):
+                if not (dz > 0 or (dz == 0 and dy > 0) or (dz == 0 and dy == 0 and dx > 0)):
+                    continue
+                d2 = dx * dx + dy * dy + dz * dz
+                if max_d2 is not None:
+                    if d2 > max_d2:
+                        continue
+                elif math.sqrt(d2) > horizon + 1e-9:
+                    continue
+                out.append((dx, dy, dz, d2))
+    return out
+
+
+def box_nodes(nx: int, ny: int, nz: int, h: float, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Cell-centre positions (3N float64), node index x + nx*(y + ny*z)."""
+    idx = np.arange(nx * ny * nz, dtype=np.int64)
+    x = idx % nx
+    y = (idx // nx) % ny
+    z = idx // (nx * ny)
+    pos = np.empty((idx.size, 3), dtype=np.float64)
+    pos[:, 0] = (x.astype(np.float64) + 0.5 - 0.5 * nx) * h + center[0]
+    pos[:, 1] = (y.astype(np.float64) + 0.5 - 0.5 * ny) * h + center[1]
+    pos[:, 2] = (z.astype(np.float64) + 0.5 - 0.5 * nz) * h + center[2]
+    return pos.reshape(-1)
+
+
+def box_bonds(nx: int, ny: int, nz: int, max_d2: int | None = 2, horizon: int = 1):
+    """Bond endpoints and grid distance^2, in the reference generator's order."""
+    n = nx * ny * nz
+    idx = np.arange(n, dtype=np.int64)
+    x = idx % nx
+    y = (idx // nx) % ny
+    z = idx // (nx * ny)
+    offs = half_offsets(horizon, max_d2)
+    valid = np.zeros((n, len(offs)), dtype=bool)
+    other = np.zeros((n, len(offs)), dtype=np.int64)
+    d2s = np.zeros((n, len(offs)), dtype=np.int8)
+    for k, (dx, dy, dz, d2) in enumerate(offs):
+        valid[:, k] = (x + dx >= 0) & (x + dx < nx) & (y + dy >= 0) & (y + dy < ny) & (z + dz >= 0) & (z + dz < nz)
+        other[:, k] = idx + dx + nx * (dy + ny * dz)
+        d2s[:, k] = d2
+    mask = valid.reshape(-1)
+    a = np.repeat(idx, len(offs))[mask].astype(np.uint32)
+    b = other.reshape(-1)[mask].astype(np.uint32)
+    d2 = d2s.reshape(-1)[mask]
+    return a, b, d2
+
+
+def slabs(nx: int, ny: int, nz: int, requested: int, layers_per_block: int = 1) -> np.ndarray:
+    """Node offsets of at most `requested` z-slabs (src/matter/BoxLattice.cpp:175-195)."""
+    blocks = max(1, requested)
+    blocks = min(blocks, max(1, nz // layers_per_block))
+    layer = nx * ny
+    begin = [(nz * b // blocks) * layer for b in range(blocks + 1)]
+    begin[-1] = layer * nz
+    return np.asarray(begin, dtype=np.uint32)
+
+
+def plane(point, normal=(0.0, 1.0, 0.0), tangent=(1.0, 0.0, 0.0), bitangent=(0.0, 0.0, 1.0),
+          restitution=0.0, static_friction=0.5, dynamic_friction=0.4, node_radius=0.005,
+          footprints=((0.0, 0.0, INF, INF),)) -> np.ndarray:
+    """A support plane packed as the settings record holds it."""
+    p = np.zeros(PLANE_WIDTH, dtype=np.float64)
+    p[0:3], p[3:6], p[6:9], p[9:12] = point, normal, tangent, bitangent
+    p[12], p[13], p[14], p[15] = restitution, static_friction, dynamic_friction, node_radius
+    capped = any(math.isfinite(f[2]) or math.isfinite(f[3]) for f in footprints)
+    p[16] = 1.0 if capped else 0.0
+    p[17] = len(footprints)
+    for k, f in enumerate(footprints):
+        p[18 + 4 * k: 22 + 4 * k] = f
+    return p
+
+
+def settings(dt=DT_SUBSTEP, gravity=(0.0, -9.81, 0.0), iterations=4, damping_fraction=0.0, sphere_enabled=0,
+             direct=0, yield_stretch=0.0, hardening=0.0, contact=(0.5, 0.4, 0.0, 0.5, 0.005, 1e-5, 0.01),
+             planes=()) -> np.ndarray:
+    s = np.zeros(SETTINGS_WIDTH, dtype=np.float64)
+    s[K_DT] = dt
+    s[K_GRAVITY:K_GRAVITY + 3] = gravity
+    s[K_ITER] = iterations
+    s[K_DAMP] = damping_fraction
+    s[K_SPHERE] = sphere_enabled
+    s[K_DIRECT] = direct
+    s[K_YIELD] = yield_stretch
+    s[K_HARDEN] = hardening
+    s[K_CONTACT:K_CONTACT + 7] = contact
+    s[K_PLANE_COUNT] = len(planes)
+    for k, p in enumerate(planes):
+        s[K_PLANES + PLANE_WIDTH * k: K_PLANES + PLANE_WIDTH * (k + 1)] = p
+    return s
+
+
+def sphere(center=(0.0, 0.0, 0.0), velocity=(0.0, 0.0, 0.0), radius=0.0, density=7870.0) -> np.ndarray:
+    s = np.zeros(SPHERE_WIDTH, dtype=np.float64)
+    s[0:3] = center
+    s[3:6] = velocity
+    if radius > 0.0:
+        mass = density * 4.0 / 3.0 * math.pi * radius ** 3
+        s[9], s[10], s[11] = radius, mass, 0.4 * mass * radius * radius
+    return s
+
+
+def _box_case(nx, ny, nz, h, center, compliance, thresholds, mass=1e-3, blocks=1, max_d2=2):
+    a, b, d2 = box_bonds(nx, ny, nz, max_d2=max_d2, horizon=1)
+    ref = box_nodes(nx, ny, nz, h, center)
+    n = nx * ny * nz
+    nb = a.size
+    thr = np.empty((nb, 6), dtype=np.float64)
+    thr[:] = thresholds if np.ndim(thresholds) == 1 else 0.0
+    if np.ndim(thresholds) == 2:
+        thr[:] = thresholds
+    comp = np.broadcast_to(np.asarray(compliance, dtype=np.float64), (nb,)).copy()
+    return {
+        "node_count": np.array([n], dtype=np.uint32),
+        "bond_count": np.array([nb], dtype=np.uint32),
+        "ref_pos": ref,
+        "pos": ref.copy(),
+        "vel": np.zeros(3 * n, dtype=np.float64),
+        "mass": np.full(n, mass, dtype=np.float64),
+        "bond_a": a,
+        "bond_b": b,
+        "rest_length": np.sqrt(d2.astype(np.float64)) * h,
+        "compliance": comp,
+        "threshold": thr.reshape(-1),
+        "node_block_begin": slabs(nx, ny, nz, blocks),
+        "origin": np.zeros(3, dtype=np.float64),
+        "sphere": sphere(),
+    }
+
+
+def cantilever(nx=32, ny=8, nz=8, h=0.01, steps=240, substeps=10):
+    """A cantilever beam, x=0 face pinned, gravity as an external load.
+
+    Compliance 1e-7 on every bond, tensile damage start = end = 2e-3 (a step),
+    compression and shear disabled (+inf). The pin is the XPBD lane's own way to
+    hold a node: inv_mass 0 with its mass kept; gravity then cannot be a global
+    StepSettings acceleration (it would move the pinned face), so it is applied
+    to every movable node as setExternalForces(m*g) for the whole run.
+    """
+    case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), 1e-7, [2e-3, 2e-3, INF, INF, INF, INF])
+    n = nx * ny * nz
+    x = np.arange(n) % nx
+    pinned = (x == 0).astype(np.uint8)
+    forces = np.zeros((n, 3), dtype=np.float64)
+    forces[pinned == 0, 1] = 1e-3 * -9.81
+    case.update({
+        "pinned": pinned,
+        "forces": forces.reshape(-1),
+        "force_substeps": np.array([steps * substeps], dtype=np.uint64),
+        "settings": settings(gravity=(0.0, 0.0, 0.0)),
+        "steps": np.array([steps * substeps], dtype=np.uint64),
+        "substeps_per_step": np.array([substeps], dtype=np.uint64),
+    })
+    return case
+
+
+def impact_block(nx=256, ny=128, nz=128, h=0.01, blocks=32, steps=120, substeps=10, seed_point=2,
+                 seed_strength=20, median=1.5e-3, sigma=0.3, yield_fraction=0.6, radius=0.2, speed=10.0,
+                 gap=0.002):
+    """A block on an infinite ground plane struck by a rigid iron sphere.
+
+    Per-bond break strain lognormal (median, sigma) as tensile start = end,
+    compression and shear disabled, plastic yield stretch = yield_fraction x
+    median (StepSettings carries one yield per lattice), hardening 0. The
+    sphere starts `gap` above the top face over a point drawn uniformly from the
+    inner half of the top face.
+    """
+    nb_est = None  # noqa: F841 (documentation: B is known only after the walk)
+    case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), 1e-7, [INF] * 6, blocks=blocks)
+    nb = int(case["bond_count"][0])
+    strength = lognormal(seed_strength, nb, median, sigma)
+    thr = np.full((nb, 6), INF, dtype=np.float64)
+    thr[:, 0] = strength
+    thr[:, 1] = strength
+    case["threshold"] = thr.reshape(-1)
+    top = (ny - 1 + 0.5 - 0.5 * ny) * h + 0.5 * h
+    bottom = (0.5 - 0.5 * ny) * h - 0.5 * h
+    p = uniform(seed_point, 0, 2)
+    cx = (p[0] - 0.5) * 0.5 * nx * h
+    cz = (p[1] - 0.5) * 0.5 * nz * h
+    case.update({
+        "settings": settings(sphere_enabled=1, yield_stretch=yield_fraction * median,
+                             contact=(0.5, 0.4, 0.0, 0.5, 0.5 * h, 1e-5, 0.05 * radius),
+                             planes=[plane((0.0, bottom, 0.0), node_radius=0.5 * h)]),
+        "sphere": sphere((cx, top + gap + radius, cz), (0.0, -speed, 0.0), radius),
+        "steps": np.array([steps * substeps], dtype=np.uint64),
+        "substeps_per_step": np.array([substeps], dtype=np.uint64),
+    })
+    return case
+
+
+def drop_trial(nx, ny, nz, compliance, break_strain, drop_height, h=0.01, steps=240, substeps=10):
+    """One batched trial: a box released at rest `drop_height` above the ground."""
+    case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), compliance, [break_strain, break_strain, INF, INF, INF, INF])
+    lift = drop_height + 0.5 * ny * h
+    ref = case["ref_pos"].reshape(-1, 3).copy()
+    ref[:, 1] += lift
+    case["ref_pos"] = ref.reshape(-1)
+    case["pos"] = case["ref_pos"].copy()
+    case.update({
+        "settings": settings(planes=[plane((0.0, 0.0, 0.0), node_radius=0.5 * h)]),
+        "steps": np.array([steps * substeps], dtype=np.uint64),
+        "substeps_per_step": np.array([substeps], dtype=np.uint64),
+    })
+    return case
+
+
+def trial_parameters(count=4096, seed=3, edge_lo=8, edge_hi=48):
+    """Per-trial draws: edges uniform on [lo, hi], compliance log-uniform on
+    [1e-8, 1e-5], break strain uniform on [1e-3, 5e-3], drop height uniform on
+    [0.1, 1] m. Six draws per trial from one stream."""
+    u = uniform(seed, 0, 6 * count).reshape(count, 6)
+    span = edge_hi - edge_lo + 1
+    edges = (edge_lo + np.minimum((u[:, 0:3] * span).astype(np.int64), span - 1)).astype(np.int64)
+    compliance = 10.0 ** (-8.0 + 3.0 * u[:, 3])
+    strain = 1e-3 + 4e-3 * u[:, 4]
+    height = 0.1 + 0.9 * u[:, 5]
+    return edges, compliance, strain, height

@@ -1,0 +1,87 @@
+// Fixed packing of the step settings and sphere records of a lattice case file.
+//
+// Test infrastructure only: the reference harness, the CPU restatement and the
+// Python test/bench side all pack StepSettings<double> and SphereState<double>
+// (src/fastlattice/LatticePhysics.hpp:144-158, 248-284) into these flat f64
+// arrays in this one order.
+#pragma once
+
+namespace lsio {
+
+enum SettingsSlot : int {
+    kDt = 0,
+    kGravity = 1,            // 3
+    kIterations = 4,
+    kDampingFraction = 5,
+    kSphereEnabled = 6,
+    kDirectArithmetic = 7,
+    kPlasticYield = 8,
+    kPlasticHardening = 9,
+    kPlateHalfThickness = 10,
+    kContact = 11,           // 7: static, dynamic, restitution, threshold, node radius, margin, slack
+    kPlaneCount = 18,
+    kPlanes = 19,            // 2 x kPlaneWidth
+    kSettingsWidth = 19 + 2 * 34,
+};
+
+enum PlaneSlot : int {
+    kPlanePoint = 0,         // 3
+    kPlaneNormal = 3,        // 3
+    kPlaneTangent = 6,       // 3
+    kPlaneBitangent = 9,     // 3
+    kPlaneRestitution = 12,
+    kPlaneStatic = 13,
+    kPlaneDynamic = 14,
+    kPlaneNodeRadius = 15,
+    kPlaneReachCapped = 16,
+    kPlaneFootprintCount = 17,
+    kPlaneFootprints = 18,   // 4 x (center_t, center_b, half_t, half_b)
+    kPlaneWidth = 34,
+};
+
+// center 3, velocity 3, angular velocity 3, radius, mass, inertia
+constexpr int kSphereWidth = 12;
+
+// Status packing shared by every runner that reports a RunStatus.
+enum StatusU64Slot : int {
+    kTotalSteps = 0,
+    kFirstFailureStep,
+    kLastFailureStep,
+    kFailureRounds,
+    kBrokenBonds,
+    kLastEnergyGainStep,
+    kLastDamageGainStep,
+    kExitReason,
+    kRankDeficientNodes,
+    kImpulseContacts,
+    kCandidateOverflow,
+    kBallSupportEvents,
+    kLaunches,
+    kStatusU64Width,
+};
+
+enum StatusF64Slot : int {
+    kRemovedEnergy = 0,
+    kMaxDamage,
+    kPlasticWork,
+    kMaxTensile,
+    kMaxCompressive,
+    kMaxShear,
+    kMaxPlasticStretch,
+    kImpulseX,
+    kImpulseY,
+    kImpulseZ,
+    kContactDissipated,
+    kMaxPenetration,
+    kMaxCorrection,
+    kMaxCenterShift,
+    kExternalWork,
+    kExternalImpulseX,
+    kExternalImpulseY,
+    kExternalImpulseZ,
+    kExternalSteps,
+    kWallSeconds,
+    kStatusF64Width,
+};
+
+} // namespace lsio
