@@ -1,0 +1,316 @@
+// Host builders of the C ABI: the lattice schedule and the canonical state.
+//
+// buildSchedule restates buildLatticeSchedule (src/fastlattice/LatticeSchedule.cpp:71-155):
+// a greedy edge colouring in asset bond order (lowest colour free at both
+// ends, at most 64), slab ownership by the lower slab, and the permutation
+// that groups bonds by (owner, boundary, colour) keeping asset order inside a
+// group. The colouring is sequential by definition and is integer work, so it
+// runs here, once per topology, and must match the reference bit for bit.
+//
+// buildState restates buildLatticeState (src/fastlattice/FastLattice.cpp:47-169).
+#include "gbl_internal.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+namespace gbl {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void setLastError(const std::string &m) { g_last_error = m; }
+
+Schedule Schedule::fromView(const gbl_schedule_view &v) {
+    Schedule s;
+    s.node_count = v.node_count;
+    s.bond_count = v.bond_count;
+    s.block_count = v.block_count;
+    s.color_count = v.color_count;
+    s.boundary_bond_count = v.boundary_bond_count;
+    if (s.block_count == 0) invalid("lattice schedule needs at least one block");
+    if (!v.node_block_begin || !v.range_begin || !v.range_end || !v.bond_block_begin ||
+        (s.bond_count && (!v.bond_order || !v.bond_schedule_index || !v.bond_color)))
+        invalid("lattice schedule view has null arrays");
+    const std::size_t ranges = static_cast<std::size_t>(s.block_count) * 2 * std::max(s.color_count, 1U);
+    s.node_block_begin.assign(v.node_block_begin, v.node_block_begin + s.block_count + 1);
+    s.bond_block_begin.assign(v.bond_block_begin, v.bond_block_begin + s.block_count + 1);
+    s.range_begin.assign(v.range_begin, v.range_begin + ranges);
+    s.range_end.assign(v.range_end, v.range_end + ranges);
+    if (s.bond_count) {
+        s.bond_order.assign(v.bond_order, v.bond_order + s.bond_count);
+        s.bond_schedule_index.assign(v.bond_schedule_index, v.bond_schedule_index + s.bond_count);
+        s.bond_color.assign(v.bond_color, v.bond_color + s.bond_count);
+    }
+    if (s.node_block_begin.front() != 0 || s.node_block_begin.back() != s.node_count ||
+        !std::is_sorted(s.node_block_begin.begin(), s.node_block_begin.end()))
+        invalid("lattice schedule needs sorted node block offsets covering every node");
+    for (std::size_t k = 0; k < ranges; ++k)
+        if (s.range_begin[k] > s.range_end[k] || s.range_end[k] > s.bond_count)
+            invalid("lattice schedule range exceeds the bonds");
+    return s;
+}
+
+gbl_schedule_view Schedule::view() const {
+    gbl_schedule_view v{};
+    v.node_count = node_count;
+    v.bond_count = bond_count;
+    v.block_count = block_count;
+    v.color_count = color_count;
+    v.boundary_bond_count = boundary_bond_count;
+    v.node_block_begin = node_block_begin.data();
+    v.bond_order = bond_order.data();
+    v.bond_schedule_index = bond_schedule_index.data();
+    v.bond_block_begin = bond_block_begin.data();
+    v.range_begin = range_begin.data();
+    v.range_end = range_end.data();
+    v.bond_color = bond_color.data();
+    return v;
+}
+
+Schedule buildSchedule(std::uint32_t node_count, std::uint32_t bond_count, const std::uint32_t *a, const std::uint32_t *b,
+                       const std::uint32_t *node_block_begin, std::uint32_t block_count) {
+    if (block_count == 0 || !node_block_begin || (bond_count && (!a || !b)))
+        invalid("lattice schedule needs sorted node block offsets covering every node");
+    if (node_block_begin[0] != 0 || node_block_begin[block_count] != node_count ||
+        !std::is_sorted(node_block_begin, node_block_begin + block_count + 1))
+        invalid("lattice schedule needs sorted node block offsets covering every node");
+    Schedule s;
+    s.node_count = node_count;
+    s.bond_count = bond_count;
+    s.block_count = block_count;
+    s.node_block_begin.assign(node_block_begin, node_block_begin + block_count + 1);
+
+    std::vector<std::uint32_t> slab(node_count);
+    for (std::uint32_t blk = 0; blk < block_count; ++blk)
+        std::fill(slab.begin() + node_block_begin[blk], slab.begin() + node_block_begin[blk + 1], blk);
+
+    // Greedy colouring; one 64-bit set of used colours per node.
+    std::vector<std::uint64_t> taken(node_count, 0);
+    std::vector<std::uint32_t> key(bond_count);
+    std::vector<std::uint8_t> colour(bond_count);
+    std::uint32_t colours = 0;
+    for (std::uint32_t k = 0; k < bond_count; ++k) {
+        const std::uint32_t na = a[k], nb = b[k];
+        if (na >= node_count || nb >= node_count || na == nb) invalid("lattice bond joins invalid nodes");
+        const std::uint64_t open = ~(taken[na] | taken[nb]);
+        if (open == 0) runtime("lattice needs more than 64 bond colours");
+        const unsigned c = static_cast<unsigned>(__builtin_ctzll(open));
+        taken[na] |= 1ULL << c;
+        taken[nb] |= 1ULL << c;
+        colour[k] = static_cast<std::uint8_t>(c);
+        colours = std::max(colours, c + 1);
+        const std::uint32_t lo = std::min(slab[na], slab[nb]), hi = std::max(slab[na], slab[nb]);
+        if (hi - lo > 1) invalid("slab decomposition needs slabs at least one neighbour horizon thick");
+        const std::uint32_t boundary = hi != lo ? 1U : 0U;
+        s.boundary_bond_count += boundary;
+        key[k] = (lo * 2 + boundary) * 64 + c; // provisional: colours not known yet
+    }
+    s.color_count = colours;
+    const std::uint32_t C = std::max(colours, 1U);
+    const std::size_t ranges = static_cast<std::size_t>(block_count) * 2 * C;
+    for (std::uint32_t k = 0; k < bond_count; ++k) key[k] = (key[k] / 64) * C + key[k] % 64;
+
+    // Grouping with asset order kept inside a group: a counting sort by key.
+    std::vector<std::uint32_t> first(ranges + 1, 0);
+    for (std::uint32_t k = 0; k < bond_count; ++k) ++first[key[k] + 1];
+    for (std::size_t q = 0; q < ranges; ++q) first[q + 1] += first[q];
+    s.range_begin.assign(ranges, 0);
+    s.range_end.assign(ranges, 0);
+    for (std::size_t q = 0; q < ranges; ++q)
+        if (first[q + 1] > first[q]) { s.range_begin[q] = first[q]; s.range_end[q] = first[q + 1]; }
+    s.bond_order.resize(bond_count);
+    {
+        std::vector<std::uint32_t> fill(first.begin(), first.end() - 1);
+        for (std::uint32_t k = 0; k < bond_count; ++k) s.bond_order[fill[key[k]]++] = k;
+    }
+    s.bond_schedule_index.resize(bond_count);
+    s.bond_color.resize(bond_count);
+    for (std::uint32_t q = 0; q < bond_count; ++q) {
+        s.bond_schedule_index[s.bond_order[q]] = q;
+        s.bond_color[q] = colour[s.bond_order[q]];
+    }
+    // Bond range of each owner slab; owners without bonds inherit the previous end.
+    s.bond_block_begin.assign(block_count + 1, 0);
+    for (std::uint32_t blk = 0; blk < block_count; ++blk) s.bond_block_begin[blk + 1] = first[(blk + 1) * 2 * C];
+    return s;
+}
+
+gbl_state_view State::view() {
+    gbl_state_view v{};
+    std::memcpy(v.origin, origin, sizeof(origin));
+    v.node_count = node_count;
+    v.bond_count = bond_count;
+    v.max_degree = max_degree;
+    v.x0 = x0.data(); v.u = u.data(); v.u_prev = u_prev.data(); v.v = this->v.data();
+    v.inv_mass = inv_mass.data(); v.mass = mass.data();
+    v.adj_offsets = adj_offsets.data(); v.adj_bonds = adj_bonds.data();
+    v.nbr_bond = nbr_bond.data(); v.nbr_other = nbr_other.data(); v.nbr_rest = nbr_rest.data();
+    v.nbr_weight = nbr_weight.data(); v.nbr_alive = nbr_alive.data();
+    v.bond_slot_a = bond_slot_a.data(); v.bond_slot_b = bond_slot_b.data();
+    v.bond_a = bond_a.data(); v.bond_b = bond_b.data();
+    v.rest_edge = rest_edge.data(); v.rest_length = rest_length.data();
+    v.rest_length_sq_minus = rest_length_sq_minus.data(); v.weight = weight.data();
+    v.compliance = compliance.data(); v.threshold = threshold.data();
+    v.alive = alive.data(); v.failure_mode = failure_mode.data(); v.damage = damage.data();
+    v.prev_tensile = prev_tensile.data(); v.prev_compressive = prev_compressive.data(); v.prev_shear = prev_shear.data();
+    v.plastic_extension = plastic_extension.data(); v.plastic_strain = plastic_strain.data();
+    return v;
+}
+
+State buildState(const gbl_matter_view &m, const Schedule &s, const double origin[3]) {
+    const std::size_t N = m.node_count, B = m.bond_count;
+    if (s.bond_order.size() != B || s.node_block_begin.back() != N)
+        invalid("lattice schedule does not match the lattice");
+    if (!m.reference_position || !m.position || !m.velocity || !m.mass ||
+        (B && (!m.bond_a || !m.bond_b || !m.rest_length || !m.compliance || !m.threshold)))
+        invalid("lattice state needs matching nodes, bonds and reference positions");
+    State st;
+    std::memcpy(st.origin, origin, sizeof(st.origin));
+    st.node_count = m.node_count;
+    st.bond_count = m.bond_count;
+    st.x0.resize(3 * N); st.u.resize(3 * N); st.u_prev.resize(3 * N); st.v.resize(3 * N);
+    st.inv_mass.resize(N); st.mass.resize(N);
+    for (std::size_t i = 0; i < N; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            const double ref = m.reference_position[3 * i + d];
+            st.x0[3 * i + d] = ref - origin[d];
+            st.u[3 * i + d] = m.position[3 * i + d] - ref;
+            st.v[3 * i + d] = m.velocity[3 * i + d];
+        }
+        st.mass[i] = m.mass[i];
+        st.inv_mass[i] = m.mass[i] > 0.0 ? 1.0 / m.mass[i] : 0.0;
+    }
+    st.u_prev = st.u;
+    st.bond_a.resize(B); st.bond_b.resize(B); st.rest_edge.resize(3 * B); st.rest_length.resize(B);
+    st.rest_length_sq_minus.resize(B); st.weight.resize(B); st.compliance.resize(B); st.threshold.resize(6 * B);
+    st.alive.resize(B); st.failure_mode.resize(B); st.damage.resize(B);
+    st.plastic_extension.assign(B, 0.0); st.plastic_strain.assign(B, 0.0);
+    st.prev_tensile.assign(B, 0.0); st.prev_compressive.assign(B, 0.0); st.prev_shear.assign(B, 0.0);
+    for (std::size_t q = 0; q < B; ++q) {
+        const std::uint32_t o = s.bond_order[q];
+        const std::uint32_t na = m.bond_a[o], nb = m.bond_b[o];
+        if (na >= N || nb >= N) invalid("lattice bond joins invalid nodes");
+        st.bond_a[q] = na;
+        st.bond_b[q] = nb;
+        double e[3];
+        for (int d = 0; d < 3; ++d) e[d] = m.reference_position[3 * nb + d] - m.reference_position[3 * na + d];
+        for (int d = 0; d < 3; ++d) st.rest_edge[3 * q + d] = e[d];
+        const double rl = m.rest_length[o];
+        st.rest_length[q] = rl;
+        const double e2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+        st.rest_length_sq_minus[q] = e2 - rl * rl;
+        st.weight[q] = e2 > 1.0e-18 ? 1.0 / e2 : 0.0;
+        st.compliance[q] = m.compliance[o];
+        for (int t = 0; t < 6; ++t) st.threshold[6 * q + t] = m.threshold[6 * static_cast<std::size_t>(o) + t];
+        st.alive[q] = m.alive ? (m.alive[o] ? 1 : 0) : 1;
+        st.failure_mode[q] = m.failure_mode ? m.failure_mode[o] : 0;
+        st.damage[q] = m.damage ? m.damage[o] : 0.0;
+    }
+    // Adjacency in asset bond order (the CPU lane's summation order).
+    std::vector<std::uint32_t> degree(N, 0);
+    for (std::size_t o = 0; o < B; ++o) { ++degree[m.bond_a[o]]; ++degree[m.bond_b[o]]; }
+    st.adj_offsets.assign(N + 1, 0);
+    for (std::size_t i = 0; i < N; ++i) st.adj_offsets[i + 1] = st.adj_offsets[i] + degree[i];
+    st.adj_bonds.resize(st.adj_offsets.back());
+    {
+        std::vector<std::uint32_t> cursor(st.adj_offsets.begin(), st.adj_offsets.end() - 1);
+        for (std::size_t o = 0; o < B; ++o) {
+            const std::uint32_t q = s.bond_schedule_index[o];
+            st.adj_bonds[cursor[m.bond_a[o]]++] = q;
+            st.adj_bonds[cursor[m.bond_b[o]]++] = q;
+        }
+    }
+    std::uint32_t D = 0;
+    for (std::size_t i = 0; i < N; ++i) D = std::max(D, degree[i]);
+    st.max_degree = D;
+    const std::size_t P = static_cast<std::size_t>(D) * N;
+    st.nbr_bond.assign(P, GBL_NO_BOND); st.nbr_other.assign(P, 0); st.nbr_rest.assign(3 * P, 0.0);
+    st.nbr_weight.assign(P, 0.0); st.nbr_alive.assign(P, 0);
+    st.bond_slot_a.assign(B, 0); st.bond_slot_b.assign(B, 0);
+    for (std::size_t i = 0; i < N; ++i)
+        for (std::uint32_t k = 0; k < degree[i]; ++k) {
+            const std::uint32_t q = st.adj_bonds[st.adj_offsets[i] + k];
+            const std::size_t slot = static_cast<std::size_t>(k) * N + i;
+            const bool is_a = st.bond_a[q] == i;
+            st.nbr_bond[slot] = q;
+            st.nbr_alive[slot] = st.alive[q];
+            (is_a ? st.bond_slot_a : st.bond_slot_b)[q] = static_cast<std::uint32_t>(slot);
+            st.nbr_other[slot] = is_a ? st.bond_b[q] : st.bond_a[q];
+            const double sign = is_a ? 1.0 : -1.0;
+            for (int d = 0; d < 3; ++d) st.nbr_rest[3 * slot + d] = sign * st.rest_edge[3 * q + d];
+            st.nbr_weight[slot] = st.weight[q];
+        }
+    return st;
+}
+
+} // namespace gbl
+
+extern "C" {
+
+gbl_result gbl_last_error(char *buffer, size_t capacity) {
+    if (!buffer || capacity == 0) return GBL_INVALID_ARGUMENT;
+    const std::size_t n = std::min(capacity - 1, gbl::g_last_error.size());
+    std::memcpy(buffer, gbl::g_last_error.data(), n);
+    buffer[n] = '\0';
+    return GBL_OK;
+}
+
+size_t gbl_struct_size(const char *name) {
+    if (!name) return 0;
+    const std::string n(name);
+#define GBL_SIZE(T) if (n == #T) return sizeof(T);
+    GBL_SIZE(gbl_schedule_view) GBL_SIZE(gbl_state_view) GBL_SIZE(gbl_footprint) GBL_SIZE(gbl_support_plane)
+    GBL_SIZE(gbl_contact_settings) GBL_SIZE(gbl_node_contact_settings) GBL_SIZE(gbl_step_settings)
+    GBL_SIZE(gbl_sphere) GBL_SIZE(gbl_run_control) GBL_SIZE(gbl_contact_accumulators) GBL_SIZE(gbl_load_ledger)
+    GBL_SIZE(gbl_run_status) GBL_SIZE(gbl_matter_view)
+#undef GBL_SIZE
+    return 0;
+}
+
+gbl_result gbl_build_schedule(uint32_t node_count, uint32_t bond_count, const uint32_t *bond_a, const uint32_t *bond_b,
+                              const uint32_t *node_block_begin, uint32_t block_count, gbl_schedule **out) {
+    return gbl::guard([&] {
+        if (!out) gbl::invalid("null output");
+        auto *s = new gbl_schedule{gbl::buildSchedule(node_count, bond_count, bond_a, bond_b, node_block_begin, block_count)};
+        *out = s;
+    });
+}
+
+gbl_result gbl_schedule_view_of(const gbl_schedule *schedule, gbl_schedule_view *view) {
+    return gbl::guard([&] {
+        if (!schedule || !view) gbl::invalid("null schedule");
+        *view = schedule->s.view();
+    });
+}
+
+void gbl_schedule_free(gbl_schedule *schedule) { delete schedule; }
+
+gbl_result gbl_build_state(const gbl_matter_view *matter, const gbl_schedule *schedule, const double origin[3],
+                           gbl_state **out) {
+    return gbl::guard([&] {
+        if (!matter || !schedule || !out) gbl::invalid("null argument");
+        const double zero[3] = {0, 0, 0};
+        *out = new gbl_state{gbl::buildState(*matter, schedule->s, origin ? origin : zero)};
+    });
+}
+
+gbl_result gbl_state_view_of(gbl_state *state, gbl_state_view *view) {
+    return gbl::guard([&] {
+        if (!state || !view) gbl::invalid("null state");
+        *view = state->s.view();
+    });
+}
+
+gbl_result gbl_state_pin(gbl_state *state, const uint8_t *pinned) {
+    return gbl::guard([&] {
+        if (!state || !pinned) gbl::invalid("null argument");
+        for (std::uint32_t i = 0; i < state->s.node_count; ++i)
+            if (pinned[i]) state->s.inv_mass[i] = 0.0;
+    });
+}
+
+void gbl_state_free(gbl_state *state) { delete state; }
+
+} // extern "C"

@@ -1,0 +1,878 @@
+// Kernels of the bonded-lattice substep.
+//
+// Device layout (one lattice, or many independent lattices concatenated):
+//   nodes  u[i]   = (u.xyz, inv_mass)   v[i] = (v.xyz, mass)   x0[i] = (x0.xyz, 0)
+//          up[i]  = u_prev              strain[2i..2i+1] = (e0..e3 | e4, e5, valid, 0)
+//          rinv   9 x N, unm 3 x N      (component-major, coalesced per node)
+//          nbr[k*N+i] = (rest.xyz, weight if the slot's bond is alive else 0)
+//          nbr_other[k*N+i] (i itself for a padded slot), nbr_bond[k*N+i]
+//   bonds  rec[j] = (a | dead bit, b, rest_length_sq_minus, rest_length)
+//          geo[j] = (rest_edge.xyz, compliance)
+//          prev[j] = (prev_tensile, prev_compressive, prev_shear, damage)
+//          plastic[j] = (extension, strain), thr4/thr2 = six damage thresholds
+// Bonds are stored in schedule order. The projection sweep runs one launch per
+// "level": the union, over the slabs that may run together, of one colour's
+// bond range (node-disjoint by construction), handed out to CTAs as
+// contiguous chunks.
+#pragma once
+
+#include "gbl_math.cuh"
+
+#include <cstdint>
+#include <type_traits>
+
+namespace gbl {
+
+template <class R> struct BondRec;
+template <> struct alignas(16) BondRec<float> { std::uint32_t a, b; float rsm, rest; };
+template <> struct alignas(8) BondRec<double> { std::uint32_t a, b; double rsm, rest; };
+
+// Serial bookkeeping (ContactAccumulators, LatticePhysics.hpp:379-388).
+struct ContactAcc {
+    unsigned long long impulse_contacts;
+    double impulse_x, impulse_y, impulse_z, dissipated, max_penetration, max_correction, max_center_shift;
+    unsigned long long candidate_overflow, ball_support_events;
+};
+
+struct LoadLedger {
+    unsigned long long steps;
+    double elapsed, req_imp[3], imp[3], req_ang[3], ang[3], work;
+};
+
+// One device control block per lattice: the RunStatus accumulators, the
+// RunControl exit rules, and the substep's transient counters.
+struct Ctl {
+    unsigned long long total_steps, first_failure_step, last_failure_step, last_energy_gain_step, last_damage_gain_step;
+    unsigned failure_rounds, broken_bonds, rank_deficient, exit_reason;
+    double removed_energy, max_damage, plastic_work;
+    unsigned max_t, max_c, max_s, max_plastic; // non-negative float bit patterns
+    ContactAcc contact;
+    LoadLedger ext;
+    // RunControl
+    unsigned stop, error;
+    unsigned long long quiet_steps, min_steps, no_failure_steps, energy_flat_steps, calm_steps;
+    double energy_flat_fraction, calm_damage_margin, removable_energy;
+    unsigned long long loads_remaining;
+    // transient
+    unsigned full_restart, dirty_count, ffb_count, loads_kicked;
+    unsigned event_count, ext_count; // loaded nodes; set between runs, read by the kick and the ledger
+};
+
+constexpr unsigned kErrExternalOverflow = 1;
+
+template <class R> struct Dev {
+    std::uint32_t N, B, D, blocks, words_b, tiles_b;
+    Q4<R> *u, *v, *x0, *up, *strain;
+    R *rinv, *unm, *approach;
+    std::uint8_t *dirty, *engaged, *candidate;
+    std::uint32_t *cand_bits;
+    Q4<R> *nbr;
+    std::uint32_t *nbr_other, *nbr_bond;
+    std::uint32_t *slot_a, *slot_b;
+    BondRec<R> *rec;
+    Q4<R> *geo, *prev, *thr4;
+    Q2<R> *thr2, *plastic;
+    R *lambda;
+    std::uint8_t *mode;
+    std::uint32_t *ev_bits, *ev_tile, *ev_list;
+    std::uint8_t *ev_broke;
+    double *ev_removed, *ev_plastic;
+    float *ev_damage;
+    std::uint32_t *node_block_begin, *cand_list, *cand_count, *dirty_list, *ffb;
+    Q4<R> *ext_force;     // applied force (backend precision), w != 0 marks a loaded node
+    double *ext_req;      // requested force, 3 per node
+    double *ext_contrib;  // 13 per node: impulse 3, angular 3, work, requested 3, requested angular 3
+    std::uint32_t *ext_nodes;
+    double origin[3];
+    Sphere<R> *sphere;
+    Ctl *ctl;
+};
+
+constexpr int kThreads = 256;
+
+template <class R> __device__ __forceinline__ V3<R> pos(const Dev<R> &L, std::uint32_t i) {
+    return xyz(L.x0[i]) + xyz(L.u[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Nonlocal node strain (LatticePhysics.hpp:791-907, plate bending off).
+// ---------------------------------------------------------------------------
+template <class R, bool Direct>
+__device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
+    const std::size_t N = L.N;
+    if (L.dirty[i]) {
+        R cov[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        std::uint32_t live = 0;
+        for (std::uint32_t k = 0; k < L.D; ++k) {
+            const Q4<R> q = L.nbr[k * N + i];
+            const R w = q.w;
+            if (w <= R(0)) continue; // dead, padded, or a degenerate rest edge
+            const R rr[3] = {q.x, q.y, q.z};
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) cov[r * 3 + c] += w * rr[r] * rr[c];
+            ++live;
+        }
+        R valid = R(0);
+        if (live >= 1U) {
+            R inv[9], un[3];
+            const int rank = pseudoInverse3(cov, inv, un);
+            if (rank >= 2) {
+                for (int k = 0; k < 9; ++k) L.rinv[k * N + i] = inv[k];
+                for (int k = 0; k < 3; ++k) L.unm[k * N + i] = un[k];
+                valid = R(1);
+            }
+            if (rank < 3) atomicAdd(&L.ctl->rank_deficient, 1U);
+        }
+        L.strain[2 * i + 1].z = valid;
+        L.dirty[i] = 0;
+        if (valid == R(0)) return;
+    } else if (L.strain[2 * i + 1].z == R(0)) {
+        return;
+    }
+    R acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const V3<R> xi = Direct ? pos(L, i) : xyz(L.u[i]);
+#pragma unroll 2
+    for (std::uint32_t k = 0; k < L.D; ++k) {
+        const std::size_t slot = k * N + i;
+        const Q4<R> q = L.nbr[slot];
+        const std::uint32_t other = L.nbr_other[slot];
+        const V3<R> rest{q.x, q.y, q.z};
+        const V3<R> xo = Direct ? pos(L, other) : xyz(L.u[other]);
+        const V3<R> cur = Direct ? (xo - xi) - rest : xo - xi;
+        const R w = q.w;
+        const R cc[3] = {cur.x, cur.y, cur.z};
+        const R rr[3] = {rest.x, rest.y, rest.z};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) acc[r * 3 + c] += w * cc[r] * rr[c];
+    }
+    R inv[9], un[3], e[6];
+    for (int k = 0; k < 9; ++k) inv[k] = L.rinv[k * N + i];
+    for (int k = 0; k < 3; ++k) un[k] = L.unm[k * N + i];
+    strainFromMoments(acc, inv, un, e);
+    L.strain[2 * i] = Q4<R>{e[0], e[1], e[2], e[3]};
+    L.strain[2 * i + 1] = Q4<R>{e[4], e[5], R(1), R(0)};
+}
+
+template <class R, bool Direct>
+__global__ void __launch_bounds__(kThreads) kStrainAll(Dev<R> L) {
+    if (L.ctl->stop) return;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < L.N) nodeStrain<R, Direct>(L, i);
+}
+
+// The start-of-substep restart after an upload (every node) or after a failure
+// round (the dirty nodes only: every other node's strain is unchanged, since
+// positions have not moved since the end sample and its bonds are the same;
+// src/fastlattice/ParallelCpuLatticeBackend.cpp:1718-1757 relies on the same fact).
+template <class R, bool Direct>
+__global__ void __launch_bounds__(kThreads) kRestartStrain(Dev<R> L) {
+    if (L.ctl->stop) return;
+    const bool full = L.ctl->full_restart != 0;
+    const std::uint32_t count = full ? L.N : L.ctl->dirty_count;
+    for (std::uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x)
+        nodeStrain<R, Direct>(L, full ? t : L.dirty_list[t]);
+}
+
+// ---------------------------------------------------------------------------
+// Bond samples (LatticePhysics.hpp:921-959, 1116-1126).
+// ---------------------------------------------------------------------------
+template <class R, bool Direct>
+__device__ __forceinline__ V3<R> bondVector(const Dev<R> &L, std::uint32_t a, std::uint32_t b, V3<R> edge) {
+    if (Direct) return pos(L, b) - pos(L, a);
+    return edge + (xyz(L.u[b]) - xyz(L.u[a]));
+}
+
+template <class R, bool Direct>
+__device__ void sampleBond(const Dev<R> &L, std::uint32_t a, std::uint32_t b, const BondRec<R> &rec, V3<R> edge,
+                           R &t, R &c, R &s) {
+    const V3<R> delta = bondVector<R, Direct>(L, a, b, edge);
+    const R len = length(delta);
+    const R rest = rec.rest;
+    R stretch;
+    if (Direct) {
+        stretch = len / rest - R(1);
+    } else {
+        const V3<R> du = xyz(L.u[b]) - xyz(L.u[a]);
+        const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
+        stretch = num / ((len + rest) * rest);
+    }
+    t = stretch;
+    c = -stretch;
+    s = R(0);
+    const R rl = length(edge);
+    if (rl > R(1.0e-9)) {
+        const V3<R> dir = edge * (R(1) / rl);
+        const std::uint32_t ends[2] = {a, b};
+        for (int q = 0; q < 2; ++q) {
+            const Q4<R> s0 = L.strain[2 * ends[q]], s1 = L.strain[2 * ends[q] + 1];
+            if (s1.z == R(0)) continue;
+            const R e[6] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y};
+            R nn, sh;
+            resolveAlong(e, dir, nn, sh);
+            t = maxR(t, nn);
+            c = maxR(c, -nn);
+            s = maxR(s, sh);
+        }
+    }
+}
+
+template <class R, bool Direct>
+__device__ __forceinline__ void startSample(const Dev<R> &L, std::uint32_t j) {
+    const BondRec<R> rec = L.rec[j];
+    if (rec.a & kDeadBit) return;
+    const Q4<R> g = L.geo[j];
+    R t, c, s;
+    sampleBond<R, Direct>(L, rec.a, rec.b, rec, V3<R>{g.x, g.y, g.z}, t, c, s);
+    Q4<R> p = L.prev[j];
+    p.x = maxR(R(0), t);
+    p.y = maxR(R(0), c);
+    p.z = maxR(R(0), s);
+    L.prev[j] = p;
+}
+
+template <class R, bool Direct>
+__global__ void __launch_bounds__(kThreads) kRestartBonds(Dev<R> L) {
+    if (L.ctl->stop) return;
+    if (L.ctl->full_restart) {
+        for (std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < L.B; j += gridDim.x * blockDim.x)
+            startSample<R, Direct>(L, j);
+        return;
+    }
+    // Live bonds at a dirty node: one thread per (dirty node, neighbour slot).
+    // A bond with both ends dirty is sampled twice to the same values.
+    const std::uint64_t count = static_cast<std::uint64_t>(L.ctl->dirty_count) * L.D;
+    for (std::uint64_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const std::uint32_t node = L.dirty_list[t / L.D];
+        const std::uint32_t k = static_cast<std::uint32_t>(t % L.D);
+        const std::uint32_t j = L.nbr_bond[static_cast<std::size_t>(k) * L.N + node];
+        if (j != kNoBond) startSample<R, Direct>(L, j);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kick and classify (LatticePhysics.hpp:1702-1719), with the external force
+// kick before it (ExternalLoads.hpp:79-148).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ bool sphereCandidate(const Settings<R> &S, const Sphere<R> &sp, V3<R> x, V3<R> vel, R mass) {
+    if (mass <= R(0)) return false;
+    const V3<R> r = x - sp.center;
+    const R distance = length(r);
+    const R gap = distance - (sp.radius + S.c_node_radius);
+    const R bound = length(vel - sp.velocity) + length(sp.angular) * distance;
+    const R reach = maxR(S.c_margin, bound * S.dt) + S.c_slack;
+    return gap <= reach;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kThreads) kKick(Dev<R> L, Settings<R> S) {
+    if (L.ctl->stop) return;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool cand = false;
+    if (i < L.N) {
+        Q4<R> vq = L.v[i];
+        const Q4<R> uq = L.u[i];
+        V3<R> vel = xyz(vq);
+        if (L.ctl->ext_count && L.ctl->loads_remaining > 0) {
+            const Q4<R> f = L.ext_force[i];
+            if (f.w != R(0)) {
+                const V3<R> before = vel;
+                const V3<R> after = before + (S.dt * uq.w) * V3<R>{f.x, f.y, f.z};
+                if (!finiteR(after.x) || !finiteR(after.y) || !finiteR(after.z)) {
+                    atomicOr(&L.ctl->error, kErrExternalOverflow);
+                } else {
+                    vel = after;
+                    const double m = static_cast<double>(vq.w);
+                    const double o[3] = {double(before.x), double(before.y), double(before.z)};
+                    const double n[3] = {double(after.x), double(after.y), double(after.z)};
+                    const double imp[3] = {m * (n[0] - o[0]), m * (n[1] - o[1]), m * (n[2] - o[2])};
+                    const V3<R> p = xyz(L.x0[i]) + xyz(uq);
+                    const double w[3] = {L.origin[0] + double(p.x), L.origin[1] + double(p.y), L.origin[2] + double(p.z)};
+                    const double dt = static_cast<double>(S.dt);
+                    const double rq[3] = {dt * L.ext_req[3 * i], dt * L.ext_req[3 * i + 1], dt * L.ext_req[3 * i + 2]};
+                    double *c = L.ext_contrib + 13 * static_cast<std::size_t>(i);
+                    c[0] = imp[0]; c[1] = imp[1]; c[2] = imp[2];
+                    c[3] = w[1] * imp[2] - w[2] * imp[1];
+                    c[4] = w[2] * imp[0] - w[0] * imp[2];
+                    c[5] = w[0] * imp[1] - w[1] * imp[0];
+                    c[6] = imp[0] * (.5 * (o[0] + n[0])) + imp[1] * (.5 * (o[1] + n[1])) + imp[2] * (.5 * (o[2] + n[2]));
+                    c[7] = rq[0]; c[8] = rq[1]; c[9] = rq[2];
+                    c[10] = w[1] * rq[2] - w[2] * rq[1];
+                    c[11] = w[2] * rq[0] - w[0] * rq[2];
+                    c[12] = w[0] * rq[1] - w[1] * rq[0];
+                }
+            }
+        }
+        vel = vel + S.dt * S.gravity;
+        L.v[i] = Q4<R>{vel.x, vel.y, vel.z, vq.w};
+        L.up[i] = uq;
+        L.engaged[i] = 0;
+        L.engaged[L.N + i] = 0;
+        if (S.sphere_enabled) {
+            Sphere<R> kicked = *L.sphere;
+            kicked.velocity = kicked.velocity + S.dt * S.gravity;
+            cand = sphereCandidate(S, kicked, xyz(L.x0[i]) + xyz(uq), vel, vq.w);
+        }
+        L.candidate[i] = cand ? 1 : 0;
+        if (!cand) {
+            for (std::uint32_t p = 0; p < S.plane_count; ++p) L.approach[p * L.N + i] = dot(vel, S.planes[p].normal);
+            const V3<R> un = xyz(uq) + S.dt * vel;
+            L.u[i] = Q4<R>{un.x, un.y, un.z, uq.w};
+        }
+    }
+    if (S.sphere_enabled) {
+        const unsigned bits = __ballot_sync(0xffffffffU, cand);
+        if ((threadIdx.x & 31) == 0 && i / 32 < (L.N + 31) / 32) L.cand_bits[i / 32] = bits;
+    }
+}
+
+// Ordered candidate lists per slab, capped at 1024 (CpuLatticeBackend.cpp:375-386):
+// one CTA per slab scans its bit words in node order.
+template <class R>
+__global__ void __launch_bounds__(1024) kCandidates(Dev<R> L) {
+    if (L.ctl->stop) return;
+    __shared__ std::uint32_t warp_total[32];
+    __shared__ std::uint32_t carry;
+    const std::uint32_t blk = blockIdx.x;
+    const std::uint32_t nb = L.node_block_begin[blk], ne = L.node_block_begin[blk + 1];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const std::uint32_t w0 = nb / 32, w1 = ne == nb ? w0 : (ne - 1) / 32 + 1;
+    for (std::uint32_t base = w0; base < w1; base += blockDim.x) {
+        const std::uint32_t w = base + threadIdx.x;
+        std::uint32_t bits = 0;
+        if (w < w1) {
+            bits = L.cand_bits[w];
+            const std::uint32_t lo = w * 32, hi = lo + 32;
+            if (nb > lo) bits &= ~0U << (nb - lo);
+            if (ne < hi) bits &= (ne - lo) >= 32 ? ~0U : ((1U << (ne - lo)) - 1U);
+        }
+        const std::uint32_t n = __popc(bits);
+        // Block exclusive scan of n.
+        std::uint32_t x = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const std::uint32_t y = __shfl_up_sync(0xffffffffU, x, o);
+            if ((threadIdx.x & 31) >= static_cast<unsigned>(o)) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warp_total[threadIdx.x / 32] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            std::uint32_t t = warp_total[threadIdx.x];
+            for (int o = 1; o < 32; o <<= 1) {
+                const std::uint32_t y = __shfl_up_sync(0xffffffffU, t, o);
+                if (threadIdx.x >= static_cast<unsigned>(o)) t += y;
+            }
+            warp_total[threadIdx.x] = t;
+        }
+        __syncthreads();
+        std::uint32_t before = carry + x - n + (threadIdx.x >= 32 ? warp_total[threadIdx.x / 32 - 1] : 0U);
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (before < kCandidatesPerBlock) L.cand_list[blk * kCandidatesPerBlock + before] = w * 32 + b;
+            ++before;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_total[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const std::uint32_t total = carry;
+        L.cand_count[blk] = total < kCandidatesPerBlock ? total : kCandidatesPerBlock;
+        if (total > kCandidatesPerBlock) L.ctl->contact.candidate_overflow += total - kCandidatesPerBlock;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sphere contact, one thread, candidates in slab then node order
+// (LatticePhysics.hpp:1322-1428).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ void sphereNode(const Dev<R> &L, const Settings<R> &S, Sphere<R> &sp, std::uint32_t i, bool correct,
+                           ContactAcc &acc) {
+    const Q4<R> vq = L.v[i];
+    const R mass = vq.w;
+    if (mass <= R(0)) return;
+    const R dt = S.dt;
+    const R ism = R(1) / sp.mass;
+    const R iin = R(1) / sp.inertia;
+    const R cr = sp.radius + S.c_node_radius;
+    const Q4<R> uq = L.u[i];
+    const V3<R> r = (xyz(L.x0[i]) + xyz(uq)) - sp.center;
+    const R distance = length(r);
+    const V3<R> normal = normalized(r);
+    const R gap = distance - cr;
+    V3<R> nv = xyz(vq);
+    const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
+    const R vn = dot(rel, normal);
+    if (gap > maxR(S.c_margin, -vn * dt)) return;
+    if (-gap > R(acc.max_penetration)) acc.max_penetration = static_cast<double>(-gap);
+    const R inm = R(1) / mass;
+    const R restitution = -vn > S.c_threshold ? S.c_restitution : R(0);
+    const R desired = gap > S.c_margin ? -gap / dt : -restitution * minR(vn, R(0));
+    const V3<R> rn = cross(r, normal);
+    const R ni = maxR(R(0), (desired - vn) / (inm + ism + iin * dot(rn, rn)));
+    if (ni > R(0)) {
+        const R before = R(0.5) * mass * dot(nv, nv);
+        auto apply = [&](V3<R> imp) {
+            nv = nv + inm * imp;
+            sp.velocity = sp.velocity - ism * imp;
+            const V3<R> ti = -cross(r, imp);
+            sp.angular = sp.angular + iin * ti;
+            acc.impulse_x += static_cast<double>(imp.x);
+            acc.impulse_y += static_cast<double>(imp.y);
+            acc.impulse_z += static_cast<double>(imp.z);
+        };
+        apply(ni * normal);
+        const V3<R> after = nv - sp.velocity - cross(sp.angular, r);
+        const V3<R> tangent = after - dot(after, normal) * normal;
+        const R ts = length(tangent);
+        if (ts > R(1.0e-12)) {
+            const V3<R> d = tangent / ts;
+            const V3<R> rd = cross(r, d);
+            const R stick = ts / (inm + ism + iin * dot(rd, rd));
+            const R fi = stick <= S.c_static * ni ? stick : minR(stick, S.c_dynamic * ni);
+            apply(-fi * d);
+        }
+        L.v[i] = Q4<R>{nv.x, nv.y, nv.z, mass};
+        acc.dissipated += static_cast<double>(before - R(0.5) * mass * dot(nv, nv));
+        ++acc.impulse_contacts;
+    }
+    if (correct && gap < -S.c_margin) {
+        const R corr = minR(-gap - S.c_margin, R(0.2) * maxR(S.c_node_radius, sp.radius * R(0.01)));
+        const R sum = inm + ism;
+        const V3<R> ns = (corr * inm / sum) * normal;
+        const V3<R> ss = -((corr * ism / sum) * normal);
+        const V3<R> un = xyz(uq) + ns;
+        L.u[i] = Q4<R>{un.x, un.y, un.z, uq.w};
+        sp.center = sp.center + ss;
+        if (corr > R(acc.max_correction)) acc.max_correction = static_cast<double>(corr);
+    }
+}
+
+template <class R>
+__global__ void kSpherePass(Dev<R> L, Settings<R> S, int pass) {
+    if (L.ctl->stop || threadIdx.x != 0 || blockIdx.x != 0) return;
+    Sphere<R> sp = *L.sphere;
+    if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
+    ContactAcc acc = L.ctl->contact;
+    const V3<R> c0 = sp.center;
+    const R e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+    for (std::uint32_t b = 0; b < L.blocks; ++b) {
+        const std::uint32_t n = L.cand_count[b];
+        for (std::uint32_t k = 0; k < n; ++k) {
+            const std::uint32_t i = L.cand_list[b * kCandidatesPerBlock + k];
+            sphereNode(L, S, sp, i, pass == 2, acc);
+            if (pass == 1) {
+                const Q4<R> vq = L.v[i];
+                for (std::uint32_t p = 0; p < S.plane_count; ++p)
+                    L.approach[p * L.N + i] = dot(xyz(vq), S.planes[p].normal);
+                const Q4<R> uq = L.u[i];
+                const V3<R> un = xyz(uq) + S.dt * xyz(vq);
+                L.u[i] = Q4<R>{un.x, un.y, un.z, uq.w};
+            }
+        }
+    }
+    const R e1 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+    acc.dissipated += static_cast<double>(e0 - e1);
+    if (pass == 2) {
+        for (std::uint32_t b = 0; b < L.blocks; ++b) {
+            const std::uint32_t n = L.cand_count[b];
+            for (std::uint32_t k = 0; k < n; ++k) {
+                const std::uint32_t i = L.cand_list[b * kCandidatesPerBlock + k];
+                for (std::uint32_t p = 0; p < S.plane_count; ++p) {
+                    if (!L.engaged[p * L.N + i]) continue;
+                    const Q4<R> vq = L.v[i];
+                    const V3<R> nv = supportVelocity(S.planes[p], xyz(vq), L.approach[p * L.N + i]);
+                    L.v[i] = Q4<R>{nv.x, nv.y, nv.z, vq.w};
+                }
+            }
+        }
+    }
+    const R shift = length(sp.center - c0);
+    if (shift > R(acc.max_center_shift)) acc.max_center_shift = static_cast<double>(shift);
+    *L.sphere = sp;
+    L.ctl->contact = acc;
+}
+
+// ---------------------------------------------------------------------------
+// XPBD projection of one level (LatticePhysics.hpp:1132-1168).
+// ---------------------------------------------------------------------------
+struct Chunk { std::uint32_t begin, end; };
+
+template <class R, bool Direct, bool First, bool Last, bool Plastic>
+__global__ void __launch_bounds__(kThreads) kSolve(Dev<R> L, const Chunk *__restrict__ work, R dt) {
+    if (L.ctl->stop) return;
+    const Chunk ch = work[blockIdx.x];
+    const R dt2 = dt * dt;
+    for (std::uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += blockDim.x) {
+        const BondRec<R> rec = L.rec[j];
+        if (rec.a & kDeadBit) continue;
+        const std::uint32_t a = rec.a, b = rec.b;
+        const Q4<R> g = L.geo[j];
+        const Q4<R> qa = L.u[a], qb = L.u[b];
+        const V3<R> ua = xyz(qa), ub = xyz(qb), edge{g.x, g.y, g.z};
+        const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
+        const R cl = length(delta);
+        if (cl <= R(1.0e-12)) continue;
+        const R original = rec.rest;
+        const R plastic = Plastic ? L.plastic[j].x : R(0);
+        const R rest = Plastic ? original + plastic : original;
+        R constraint;
+        if (Direct) {
+            constraint = cl - rest;
+        } else {
+            const V3<R> du = ub - ua;
+            const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
+            constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
+        }
+        const V3<R> dir = delta / cl;
+        const R wa = qa.w, wb = qb.w;
+        const R alpha = g.w / dt2;
+        const R lambda = First ? R(0) : L.lambda[j];
+        const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
+        if (!Last) L.lambda[j] = lambda + dl;
+        const V3<R> na = ua - (wa * dl) * dir;
+        const V3<R> nb = ub + (wb * dl) * dir;
+        L.u[a] = Q4<R>{na.x, na.y, na.z, wa};
+        L.u[b] = Q4<R>{nb.x, nb.y, nb.z, wb};
+    }
+}
+
+// Radial pair damping of one level (LatticePhysics.hpp:1170-1184).
+template <class R, bool Direct>
+__global__ void __launch_bounds__(kThreads) kDamp(Dev<R> L, const Chunk *__restrict__ work, R fraction) {
+    if (L.ctl->stop) return;
+    const Chunk ch = work[blockIdx.x];
+    for (std::uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += blockDim.x) {
+        const BondRec<R> rec = L.rec[j];
+        if (rec.a & kDeadBit) continue;
+        const std::uint32_t a = rec.a, b = rec.b;
+        const Q4<R> va = L.v[a], vb = L.v[b];
+        const R ma = va.w, mb = vb.w;
+        if (ma <= R(0) || mb <= R(0)) continue;
+        const Q4<R> g = L.geo[j];
+        const V3<R> n = normalized(bondVector<R, Direct>(L, a, b, V3<R>{g.x, g.y, g.z}));
+        const R rel = dot(xyz(vb) - xyz(va), n);
+        const R im = R(1) / ma + R(1) / mb;
+        const R impulse = -fraction * rel / im;
+        const V3<R> na = xyz(va) - (impulse / ma) * n;
+        const V3<R> nb = xyz(vb) + (impulse / mb) * n;
+        L.v[a] = Q4<R>{na.x, na.y, na.z, ma};
+        L.v[b] = Q4<R>{nb.x, nb.y, nb.z, mb};
+    }
+}
+
+// Support projection after a sweep (LatticePhysics.hpp:1255-1261).
+template <class R>
+__global__ void __launch_bounds__(kThreads) kSupport(Dev<R> L, Settings<R> S) {
+    if (L.ctl->stop) return;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.N) return;
+    const Q4<R> uq = L.u[i];
+    V3<R> u = xyz(uq);
+    const V3<R> x0 = xyz(L.x0[i]);
+    bool projected = false;
+    for (std::uint32_t p = 0; p < S.plane_count; ++p) {
+        bool here = false;
+        const R depth = projectSupport(S.planes[p], x0, u, L.approach[p * L.N + i], S.dt, here);
+        if (depth > R(0)) L.engaged[p * L.N + i] = 1;
+        projected = projected || here;
+    }
+    // Written back whenever a projection ran, even by a zero distance, so the
+    // sign of a zero component is whatever the projection made it.
+    if (projected) L.u[i] = Q4<R>{u.x, u.y, u.z, uq.w};
+}
+
+// Velocity from accepted positions, then the support response of
+// non-candidates when no damping sweep follows (LatticePhysics.hpp:1725-1730).
+template <class R>
+__global__ void __launch_bounds__(kThreads) kVelocity(Dev<R> L, Settings<R> S, int respond) {
+    if (L.ctl->stop) return;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.N) return;
+    const Q4<R> vq = L.v[i];
+    V3<R> vel = (xyz(L.u[i]) - xyz(L.up[i])) / S.dt;
+    if (respond && !L.candidate[i])
+        for (std::uint32_t p = 0; p < S.plane_count; ++p)
+            if (L.engaged[p * L.N + i]) vel = supportVelocity(S.planes[p], vel, L.approach[p * L.N + i]);
+    L.v[i] = Q4<R>{vel.x, vel.y, vel.z, vq.w};
+}
+
+// Support response of non-candidates after the damping sweep (CpuLatticeBackend.cpp:414-415).
+template <class R>
+__global__ void __launch_bounds__(kThreads) kSupportVelocity(Dev<R> L, Settings<R> S) {
+    if (L.ctl->stop) return;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.N || L.candidate[i]) return;
+    const Q4<R> vq = L.v[i];
+    V3<R> vel = xyz(vq);
+    for (std::uint32_t p = 0; p < S.plane_count; ++p)
+        if (L.engaged[p * L.N + i]) vel = supportVelocity(S.planes[p], vel, L.approach[p * L.N + i]);
+    L.v[i] = Q4<R>{vel.x, vel.y, vel.z, vq.w};
+}
+
+// ---------------------------------------------------------------------------
+// End-of-substep sample, plastic return and failure (LatticePhysics.hpp:1018-1114).
+// One thread per bond in schedule order. A bond is an event when it breaks,
+// flows, or raises its damage above the run's maximum; events are flagged in
+// one bit per bond and folded in bond order by kLedger.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned floatBits(float x) { return __float_as_uint(x); }
+
+template <class R, bool Direct, bool Plastic>
+__global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) {
+    __shared__ unsigned tile_count[kThreads / 32];
+    __shared__ unsigned peak[4];
+    if (L.ctl->stop) return;
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (threadIdx.x < 4) peak[threadIdx.x] = 0;
+    __syncthreads();
+    bool event = false;
+    if (j < L.B) {
+        const BondRec<R> rec = L.rec[j];
+        if (!(rec.a & kDeadBit)) {
+            const std::uint32_t a = rec.a, b = rec.b;
+            const Q4<R> g = L.geo[j];
+            const V3<R> edge{g.x, g.y, g.z};
+            double plastic_work = 0.0;
+            float plastic_stretch = 0.0F;
+            R pext = R(0);
+            if (Plastic) {
+                Q2<R> pl = L.plastic[j];
+                pext = pl.x;
+                if (S.yield_stretch > R(0)) {
+                    const R elastic = length(bondVector<R, Direct>(L, a, b, edge)) - rec.rest - pl.x;
+                    const R magnitude = absR(elastic);
+                    const R h = S.hardening;
+                    const R yield = S.yield_stretch * rec.rest + h * pl.y;
+                    if (magnitude > yield) {
+                        const R inc = (magnitude - yield) / (R(1) + h);
+                        pl.x = pl.x + (elastic < R(0) ? -inc : inc);
+                        pl.y = pl.y + inc;
+                        L.plastic[j] = pl;
+                        pext = pl.x;
+                        const R c = g.w;
+                        if (c > R(0)) {
+                            const R yield_end = yield + h * inc;
+                            plastic_work = static_cast<double>(R(0.5) * (yield + yield_end) * inc / c);
+                        }
+                    }
+                    plastic_stretch = static_cast<float>(absR(pl.x) / rec.rest);
+                }
+            }
+            R t, c, s;
+            sampleBond<R, Direct>(L, a, b, rec, edge, t, c, s);
+            Q4<R> pv = L.prev[j];
+            const R pt = maxR(R(0), maxR(pv.x, t));
+            const R pc = maxR(R(0), maxR(pv.y, c));
+            const R ps = maxR(R(0), maxR(pv.z, s));
+            pv.x = maxR(R(0), t);
+            pv.y = maxR(R(0), c);
+            pv.z = maxR(R(0), s);
+            const Q4<R> t4 = L.thr4[j];
+            const Q2<R> t2 = L.thr2[j];
+            const R dtn = damageProgress(pt, t4.x, t4.y);
+            const R dcp = damageProgress(pc, t4.z, t4.w);
+            const R dsh = damageProgress(ps, t2.x, t2.y);
+            R damage = dtn;
+            std::uint8_t mode = 1;
+            if (dcp > damage) { damage = dcp; mode = 2; }
+            if (dsh > damage) { damage = dsh; mode = 3; }
+            if (damage > pv.w) {
+                pv.w = damage;
+                L.mode[j] = mode;
+            }
+            L.prev[j] = pv;
+            const float dmg = static_cast<float>(pv.w);
+            const bool broke = pv.w >= R(1);
+            if (broke) {
+                const R cc = g.w;
+                R energy = R(0);
+                if (!(cc <= R(0))) {
+                    const R ext = length(bondVector<R, Direct>(L, a, b, edge)) - rec.rest - pext;
+                    energy = R(0.5) * ext * ext / cc;
+                }
+                L.rec[j].a = a | kDeadBit;
+                L.nbr[L.slot_a[j]].w = R(0);
+                L.nbr[L.slot_b[j]].w = R(0);
+                L.ev_removed[j] = static_cast<double>(energy);
+            }
+            event = broke || plastic_work != 0.0 || static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6;
+            if (event) {
+                L.ev_broke[j] = broke ? 1 : 0;
+                L.ev_plastic[j] = plastic_work;
+                L.ev_damage[j] = dmg;
+            }
+            // Peaks are non-negative, so their bit patterns order as the values do.
+            atomicMax(&peak[0], floatBits(static_cast<float>(pt)));
+            atomicMax(&peak[1], floatBits(static_cast<float>(pc)));
+            atomicMax(&peak[2], floatBits(static_cast<float>(ps)));
+            if (Plastic && S.yield_stretch > R(0)) atomicMax(&peak[3], floatBits(plastic_stretch));
+        }
+    }
+    const unsigned bits = __ballot_sync(0xffffffffU, event);
+    if ((threadIdx.x & 31) == 0) {
+        if (j / 32 < L.words_b) L.ev_bits[j / 32] = bits;
+        tile_count[threadIdx.x / 32] = __popc(bits);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned total = 0;
+        for (int w = 0; w < kThreads / 32; ++w) total += tile_count[w];
+        L.ev_tile[blockIdx.x] = total;
+        if (peak[0]) atomicMax(&L.ctl->max_t, peak[0]);
+        if (peak[1]) atomicMax(&L.ctl->max_c, peak[1]);
+        if (peak[2]) atomicMax(&L.ctl->max_s, peak[2]);
+        if (peak[3]) atomicMax(&L.ctl->max_plastic, peak[3]);
+    }
+}
+
+// Exclusive scan of the per-tile event counts, one CTA.
+template <class R>
+__global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L) {
+    if (L.ctl->stop) return;
+    __shared__ unsigned warp_sum[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned T = L.tiles_b;
+    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
+    const unsigned first = threadIdx.x * per;
+    unsigned local = 0;
+    for (unsigned t = first; t < first + per && t < T; ++t) local += L.ev_tile[t];
+    unsigned x = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
+        if ((threadIdx.x & 31) >= static_cast<unsigned>(o)) x += y;
+    }
+    if ((threadIdx.x & 31) == 31) warp_sum[threadIdx.x / 32] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned s = warp_sum[threadIdx.x];
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffU, s, o);
+            if (threadIdx.x >= static_cast<unsigned>(o)) s += y;
+        }
+        warp_sum[threadIdx.x] = s;
+    }
+    __syncthreads();
+    unsigned run = x - local + (threadIdx.x >= 32 ? warp_sum[threadIdx.x / 32 - 1] : 0U);
+    for (unsigned t = first; t < first + per && t < T; ++t) {
+        const unsigned n = L.ev_tile[t];
+        L.ev_tile[t] = run;
+        run += n;
+    }
+    if (threadIdx.x == blockDim.x - 1) L.ctl->event_count = run;
+}
+
+// Writes the event bond indices in bond order: one warp per end-sample tile.
+template <class R>
+__global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
+    if (L.ctl->stop || L.ctl->event_count == 0) return;
+    const unsigned tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const unsigned lane = threadIdx.x & 31;
+    if (tile >= L.tiles_b) return;
+    const unsigned base = L.ev_tile[tile];
+    const unsigned next = tile + 1 < L.tiles_b ? L.ev_tile[tile + 1] : L.ctl->event_count;
+    if (next == base) return;
+    constexpr unsigned kWords = kThreads / 32;
+    const unsigned w = tile * kWords + lane;
+    unsigned bits = (lane < kWords && w < L.words_b) ? L.ev_bits[w] : 0U;
+    unsigned n = __popc(bits), x = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
+        if (lane >= static_cast<unsigned>(o)) x += y;
+    }
+    unsigned at = base + x - n;
+    while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        L.ev_list[at++] = w * 32 + static_cast<unsigned>(b);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The serial tail of a substep, one thread: the external-load ledger, the FP64
+// failure and plastic ledgers in bond order (CpuLatticeBackend.cpp:441-488),
+// the sphere drift and support contact, the failure-round bookkeeping and the
+// exit rules (CpuLatticeBackend.cpp:279-298).
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void kLedger(Dev<R> L, Settings<R> S) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    if (c.error) {
+        c.stop = 1;
+        return;
+    }
+    const unsigned long long step = c.total_steps;
+    // External loads: this substep's change, folded in node order, then added.
+    if (c.ext_count && c.loads_remaining > 0) {
+        double ch[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (std::uint32_t k = 0; k < c.ext_count; ++k) {
+            const double *x = L.ext_contrib + 13 * static_cast<std::size_t>(L.ext_nodes[k]);
+            for (int q = 0; q < 13; ++q) ch[q] += x[q];
+        }
+        LoadLedger &g = c.ext;
+        g.steps += 1;
+        g.elapsed += static_cast<double>(S.dt);
+        for (int q = 0; q < 3; ++q) {
+            g.req_imp[q] = g.req_imp[q] + ch[7 + q];
+            g.req_ang[q] = g.req_ang[q] + ch[10 + q];
+            g.imp[q] = g.imp[q] + ch[q];
+            g.ang[q] = g.ang[q] + ch[3 + q];
+        }
+        g.work = g.work + ch[6];
+        c.loads_remaining -= 1;
+    }
+    c.dirty_count = 0;
+    c.full_restart = 0;
+    const bool first_round = c.broken_bonds == 0;
+    bool any = false;
+    for (unsigned e = 0; e < c.event_count; ++e) {
+        const std::uint32_t j = L.ev_list[e];
+        c.plastic_work += L.ev_plastic[j];
+        const float dmg = L.ev_damage[j];
+        if (static_cast<double>(dmg) > c.max_damage + 1.0e-6) {
+            c.max_damage = dmg;
+            c.last_damage_gain_step = step;
+        }
+        if (!L.ev_broke[j]) continue;
+        any = true;
+        if (first_round) L.ffb[c.ffb_count++] = j;
+        const double removed = L.ev_removed[j];
+        c.removed_energy += removed;
+        if (removed > c.energy_flat_fraction * (c.removed_energy < 1.0e-12 ? 1.0e-12 : c.removed_energy))
+            c.last_energy_gain_step = step;
+        ++c.broken_bonds;
+        const std::uint32_t ends[2] = {L.rec[j].a & ~kDeadBit, L.rec[j].b};
+        for (int q = 0; q < 2; ++q)
+            if (!L.dirty[ends[q]]) {
+                L.dirty[ends[q]] = 1;
+                L.dirty_list[c.dirty_count++] = ends[q];
+            }
+    }
+    c.event_count = 0;
+    Sphere<R> sp = *L.sphere;
+    if (!S.sphere_enabled) sp.velocity = sp.velocity + S.dt * S.gravity;
+    sp.center = sp.center + S.dt * sp.velocity;
+    sphereSupport(S, sp, c.contact);
+    *L.sphere = sp;
+    c.total_steps = step + 1;
+    if (any) {
+        if (c.first_failure_step == ~0ULL) c.first_failure_step = step;
+        c.last_failure_step = step;
+        ++c.failure_rounds;
+    }
+    const double available = c.removable_energy + c.ext.work;
+    c.exit_reason = c.removable_energy > 0 && available <= 0
+        ? 6U
+        : exitReason(c.total_steps, c.broken_bonds, c.last_failure_step, c.quiet_steps, c.min_steps, c.no_failure_steps,
+                     c.energy_flat_steps, c.last_energy_gain_step, c.calm_steps, c.last_damage_gain_step, c.max_damage,
+                     c.calm_damage_margin, c.removed_energy, c.removable_energy > 0 ? available : 0.0);
+    if (c.exit_reason != 0) c.stop = 1;
+}
+
+} // namespace gbl

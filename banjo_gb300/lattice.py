@@ -1,0 +1,568 @@
+"""Python mirror of the reference's lattice step API over the C ABI (include/gbl.h).
+
+Names follow src/fastlattice/FastLattice.hpp: build_lattice_schedule
+(buildLatticeSchedule), build_lattice_state (buildLatticeState),
+make_gb300_lattice_backend (the makeCudaLatticeBackend factory this library
+replaces) returning a backend with upload / set_external_forces / run /
+download / status / first_failure_bonds / take_frames. Errors raise the
+Python image of the reference's exception types: ValueError for
+std::invalid_argument, RuntimeError for std::runtime_error, OverflowError for
+std::overflow_error.
+
+The library is the product; there is no fallback. If libgbl.so cannot be
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+from . import scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbl.so")
+
+u8p, u32p, f64p, f32p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_float)
+NO_BOND = 0xFFFFFFFF
+
+
+class ScheduleView(C.Structure):
+    _fields_ = [("node_count", C.c_uint32), ("bond_count", C.c_uint32), ("block_count", C.c_uint32),
+                ("color_count", C.c_uint32), ("boundary_bond_count", C.c_uint32),
+                ("node_block_begin", u32p), ("bond_order", u32p), ("bond_schedule_index", u32p),
+                ("bond_block_begin", u32p), ("range_begin", u32p), ("range_end", u32p), ("bond_color", u8p)]
+
+
+_STATE_ARRAYS = [("x0", f64p), ("u", f64p), ("u_prev", f64p), ("v", f64p), ("inv_mass", f64p), ("mass", f64p),
+                 ("adj_offsets", u32p), ("adj_bonds", u32p), ("nbr_bond", u32p), ("nbr_other", u32p),
+                 ("nbr_rest", f64p), ("nbr_weight", f64p), ("nbr_alive", u8p), ("bond_slot_a", u32p),
+                 ("bond_slot_b", u32p), ("bond_a", u32p), ("bond_b", u32p), ("rest_edge", f64p),
+                 ("rest_length", f64p), ("rest_length_sq_minus", f64p), ("weight", f64p), ("compliance", f64p),
+                 ("threshold", f64p), ("alive", u8p), ("failure_mode", u8p), ("damage", f64p),
+                 ("prev_tensile", f64p), ("prev_compressive", f64p), ("prev_shear", f64p),
+                 ("plastic_extension", f64p), ("plastic_strain", f64p)]
+
+
+class StateView(C.Structure):
+    _fields_ = [("origin", C.c_double * 3), ("node_count", C.c_uint32), ("bond_count", C.c_uint32),
+                ("max_degree", C.c_uint32)] + _STATE_ARRAYS
+
+
+class MatterView(C.Structure):
+    _fields_ = [("node_count", C.c_uint32), ("bond_count", C.c_uint32), ("reference_position", f64p),
+                ("position", f64p), ("velocity", f64p), ("mass", f64p), ("bond_a", u32p), ("bond_b", u32p),
+                ("rest_length", f64p), ("compliance", f64p), ("threshold", f64p), ("alive", u8p),
+                ("damage", f64p), ("failure_mode", u8p)]
+
+
+class Footprint(C.Structure):
+    _fields_ = [("center_t", C.c_double), ("center_b", C.c_double), ("half_t", C.c_double), ("half_b", C.c_double)]
+
+
+class SupportPlane(C.Structure):
+    _fields_ = [("point", C.c_double * 3), ("normal", C.c_double * 3), ("tangent", C.c_double * 3),
+                ("bitangent", C.c_double * 3), ("restitution", C.c_double), ("static_friction", C.c_double),
+                ("dynamic_friction", C.c_double), ("node_radius", C.c_double), ("reach_capped", C.c_uint8),
+                ("footprint_count", C.c_uint32), ("footprints", Footprint * 4)]
+
+
+class ContactSettings(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("static_friction", "dynamic_friction", "restitution",
+                                          "restitution_speed_threshold", "node_contact_radius", "contact_margin",
+                                          "prefilter_slack")]
+
+
+class NodeContactSettings(C.Structure):
+    _fields_ = [("mode", C.c_uint8)] + [(n, C.c_double) for n in (
+        "radius", "skin", "margin", "restitution", "restitution_speed_threshold", "static_friction",
+        "dynamic_friction")] + [("bucket_mask", C.c_uint32)]
+
+
+class StepSettings(C.Structure):
+    _fields_ = [("dt", C.c_double), ("gravity", C.c_double * 3), ("constraint_iterations", C.c_uint32),
+                ("bond_integrator", C.c_uint8), ("damping_fraction", C.c_double), ("sphere_enabled", C.c_uint8),
+                ("direct_arithmetic", C.c_uint8), ("audit_energy", C.c_uint8),
+                ("plastic_yield_stretch", C.c_double), ("plastic_hardening", C.c_double),
+                ("plate_half_thickness", C.c_double), ("contact", ContactSettings),
+                ("node_contact", NodeContactSettings), ("plane_count", C.c_uint32), ("planes", SupportPlane * 2)]
+
+
+class Sphere(C.Structure):
+    _fields_ = [("center", C.c_double * 3), ("velocity", C.c_double * 3), ("angular_velocity", C.c_double * 3),
+                ("radius", C.c_double), ("mass", C.c_double), ("inertia", C.c_double)]
+
+
+class RunControlC(C.Structure):
+    _fields_ = [("max_steps", C.c_uint64), ("quiet_steps", C.c_uint64), ("min_steps", C.c_uint64),
+                ("no_failure_steps", C.c_uint64), ("energy_flat_steps", C.c_uint64),
+                ("energy_flat_fraction", C.c_double), ("calm_steps", C.c_uint64),
+                ("calm_damage_margin", C.c_double), ("removable_energy_j", C.c_double),
+                ("capture_stride", C.c_uint64), ("max_frames", C.c_uint32), ("steps_per_launch", C.c_uint64),
+                ("abandon", C.c_void_p)]
+
+
+class ContactAccumulators(C.Structure):
+    _fields_ = [("impulse_contacts", C.c_ulonglong), ("impulse_to_material_x", C.c_double),
+                ("impulse_to_material_y", C.c_double), ("impulse_to_material_z", C.c_double),
+                ("dissipated_kinetic_energy_j", C.c_double), ("maximum_penetration_m", C.c_double),
+                ("maximum_position_correction_m", C.c_double), ("maximum_center_shift_m", C.c_double),
+                ("candidate_overflow", C.c_ulonglong), ("ball_support_events", C.c_ulonglong)]
+
+
+class LoadLedger(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("elapsed_s", C.c_double), ("requested_impulse_n_s", C.c_double * 3),
+                ("impulse_n_s", C.c_double * 3), ("requested_angular_impulse_kg_m2_s", C.c_double * 3),
+                ("angular_impulse_kg_m2_s", C.c_double * 3), ("work_j", C.c_double)]
+
+
+class RunStatus(C.Structure):
+    _fields_ = [("total_steps", C.c_uint64), ("first_failure_step", C.c_uint64), ("last_failure_step", C.c_uint64),
+                ("failure_rounds", C.c_uint32), ("broken_bonds", C.c_uint32), ("removed_energy_j", C.c_double),
+                ("last_energy_gain_step", C.c_uint64), ("max_damage", C.c_double),
+                ("last_damage_gain_step", C.c_uint64), ("contact", ContactAccumulators),
+                ("external_load", LoadLedger), ("exit_reason", C.c_uint), ("launches", C.c_uint),
+                ("kernel_seconds", C.c_double), ("wall_seconds", C.c_double), ("frames_captured", C.c_uint32),
+                ("phase_seconds", C.c_double * 16), ("max_tensile_stretch", C.c_float),
+                ("max_compressive_strain", C.c_float), ("max_shear_strain", C.c_float),
+                ("rank_deficient_nodes", C.c_uint32), ("plastic_work_j", C.c_double),
+                ("max_plastic_stretch", C.c_float)]
+
+
+PHASE_NAMES = ["capture", "start_sample_nodes", "start_sample_bonds", "kick_classify", "contact_pass_1",
+               "sweep_interior", "sweep_boundary", "support_project", "velocity_update", "damping",
+               "contact_pass_2", "end_sample_nodes", "end_sample_bonds", "sphere_exit", "node_contact_broad",
+               "node_contact_narrow"]
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """The loaded libgbl.so; raises if it is missing (no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"lattice library not built: {LIB_PATH} (run banjo_gb300.build.build())")
+    lib = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    sigs = {
+        "gbl_available": ([], C.c_int), "gbl_description": ([C.c_char_p, C.c_size_t], C.c_int),
+        "gbl_multiprocessor_count": ([], C.c_uint), "gbl_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
+        "gbl_struct_size": ([C.c_char_p], C.c_size_t),
+        "gbl_create": ([C.POINTER(ScheduleView), C.c_int, C.c_uint, C.POINTER(vp)], C.c_int),
+        "gbl_destroy": ([vp], None), "gbl_name": ([vp, C.c_char_p, C.c_size_t], C.c_int),
+        "gbl_upload": ([vp, C.POINTER(StateView), C.POINTER(StepSettings), C.POINTER(Sphere)], C.c_int),
+        "gbl_set_external_forces": ([vp, f64p, C.c_uint64, C.c_uint64], C.c_int),
+        "gbl_run": ([vp, C.POINTER(RunControlC), C.POINTER(RunStatus)], C.c_int),
+        "gbl_status": ([vp, C.POINTER(RunStatus)], C.c_int),
+        "gbl_download": ([vp, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
+        "gbl_first_failure_bonds": ([vp, u32p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_frame_count": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_take_frame": ([vp, C.c_uint64, C.POINTER(C.c_uint64), f32p, u8p, f32p, C.POINTER(Sphere)], C.c_int),
+        "gbl_clear_frames": ([vp], C.c_int), "gbl_set_stream": ([vp, vp], C.c_int),
+        "gbl_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
+        "gbl_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_build_schedule": ([C.c_uint32, C.c_uint32, u32p, u32p, u32p, C.c_uint32, C.POINTER(vp)], C.c_int),
+        "gbl_schedule_view_of": ([vp, C.POINTER(ScheduleView)], C.c_int), "gbl_schedule_free": ([vp], None),
+        "gbl_build_state": ([C.POINTER(MatterView), vp, f64p, C.POINTER(vp)], C.c_int),
+        "gbl_state_view_of": ([vp, C.POINTER(StateView)], C.c_int), "gbl_state_pin": ([vp, u8p], C.c_int),
+        "gbl_state_free": ([vp], None),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    for name, cls in [("gbl_schedule_view", ScheduleView), ("gbl_state_view", StateView),
+                      ("gbl_matter_view", MatterView), ("gbl_support_plane", SupportPlane),
+                      ("gbl_step_settings", StepSettings), ("gbl_sphere", Sphere),
+                      ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus)]:
+        if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
+            raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
+    _lib = lib
+    return lib
+
+
+def _error(rc: int):
+    buf = C.create_string_buffer(1024)
+    library().gbl_last_error(buf, len(buf))
+    msg = buf.value.decode()
+    if rc == 1:
+        return ValueError(msg)
+    if rc == 3:
+        return OverflowError(msg)
+    return RuntimeError(msg)
+
+
+def _call(fn, *args):
+    rc = fn(*args)
+    if rc != 0:
+        raise _error(rc)
+
+
+def _ptr(arr, ctype):
+    return arr.ctypes.data_as(C.POINTER(ctype)) if arr is not None else None
+
+
+def available() -> bool:
+    return bool(library().gbl_available())
+
+
+def description() -> str:
+    buf = C.create_string_buffer(512)
+    _call(library().gbl_description, buf, len(buf))
+    return buf.value.decode()
+
+
+def multiprocessor_count() -> int:
+    return int(library().gbl_multiprocessor_count())
+
+
+class Schedule:
+    """A LatticeSchedule built by the library (buildLatticeSchedule)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self.view = ScheduleView()
+        _call(library().gbl_schedule_view_of, handle, C.byref(self.view))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_schedule_free(self._h)
+            self._h = None
+
+    def _arr(self, name, count, dtype):
+        p = getattr(self.view, name)
+        return np.ctypeslib.as_array(p, shape=(count,)).astype(dtype, copy=True) if count else np.zeros(0, dtype)
+
+    @property
+    def block_count(self):
+        return self.view.block_count
+
+    @property
+    def color_count(self):
+        return self.view.color_count
+
+    @property
+    def boundary_bond_count(self):
+        return self.view.boundary_bond_count
+
+    def arrays(self) -> dict:
+        v = self.view
+        ranges = v.block_count * 2 * max(v.color_count, 1)
+        return {
+            "sched_bond_order": self._arr("bond_order", v.bond_count, np.uint32),
+            "sched_color": self._arr("bond_color", v.bond_count, np.uint8),
+            "sched_range_begin": self._arr("range_begin", ranges, np.uint32),
+            "sched_range_end": self._arr("range_end", ranges, np.uint32),
+            "sched_bond_block_begin": self._arr("bond_block_begin", v.block_count + 1, np.uint32),
+            "sched_color_count": np.array([v.color_count], np.uint32),
+            "sched_boundary_bond_count": np.array([v.boundary_bond_count], np.uint32),
+        }
+
+
+def build_lattice_schedule(node_count, bond_a, bond_b, node_block_begin) -> Schedule:
+    a = np.ascontiguousarray(bond_a, dtype=np.uint32)
+    b = np.ascontiguousarray(bond_b, dtype=np.uint32)
+    blocks = np.ascontiguousarray(node_block_begin, dtype=np.uint32)
+    h = C.c_void_p()
+    _call(library().gbl_build_schedule, int(node_count), a.size, _ptr(a, C.c_uint32), _ptr(b, C.c_uint32),
+          _ptr(blocks, C.c_uint32), blocks.size - 1, C.byref(h))
+    return Schedule(h)
+
+
+class State:
+    """A LatticeState owned by the library (buildLatticeState); arrays are numpy views."""
+
+    _SIZES = {"x0": 3, "u": 3, "u_prev": 3, "v": 3, "inv_mass": 1, "mass": 1}
+
+    def __init__(self, handle):
+        self._h = handle
+        self.view = StateView()
+        _call(library().gbl_state_view_of, handle, C.byref(self.view))
+        v = self.view
+        n, b, p = v.node_count, v.bond_count, v.node_count * v.max_degree
+        counts = {"x0": 3 * n, "u": 3 * n, "u_prev": 3 * n, "v": 3 * n, "inv_mass": n, "mass": n,
+                  "adj_offsets": n + 1, "adj_bonds": 2 * b, "nbr_bond": p, "nbr_other": p, "nbr_rest": 3 * p,
+                  "nbr_weight": p, "nbr_alive": p, "bond_slot_a": b, "bond_slot_b": b, "bond_a": b, "bond_b": b,
+                  "rest_edge": 3 * b, "rest_length": b, "rest_length_sq_minus": b, "weight": b,
+                  "compliance": b, "threshold": 6 * b, "alive": b, "failure_mode": b, "damage": b,
+                  "prev_tensile": b, "prev_compressive": b, "prev_shear": b, "plastic_extension": b,
+                  "plastic_strain": b}
+        self.arrays = {}
+        for name, _ in _STATE_ARRAYS:
+            cnt = counts[name]
+            ptr = getattr(v, name)
+            self.arrays[name] = np.ctypeslib.as_array(ptr, shape=(cnt,)) if cnt else np.zeros(0)
+
+    def __getattr__(self, name):
+        arrays = self.__dict__.get("arrays")
+        if arrays is not None and name in arrays:
+            return arrays[name]
+        raise AttributeError(name)
+
+    @property
+    def node_count(self):
+        return self.view.node_count
+
+    @property
+    def bond_count(self):
+        return self.view.bond_count
+
+    def pin(self, pinned) -> None:
+        p = np.ascontiguousarray(pinned, dtype=np.uint8)
+        _call(library().gbl_state_pin, self._h, _ptr(p, C.c_uint8))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_state_free(self._h)
+            self._h = None
+
+
+def build_lattice_state(case: dict, schedule: Schedule) -> State:
+    """buildLatticeState from a case's asset and matter arrays (asset bond order)."""
+    n = int(case["node_count"][0])
+    b = int(case["bond_count"][0])
+    keep = {k: np.ascontiguousarray(case[k]) for k in ("ref_pos", "pos", "vel", "mass", "rest_length", "compliance",
+                                                        "threshold")}
+    keep["bond_a"] = np.ascontiguousarray(case["bond_a"], dtype=np.uint32)
+    keep["bond_b"] = np.ascontiguousarray(case["bond_b"], dtype=np.uint32)
+    alive = np.ascontiguousarray(case["alive"], dtype=np.uint8) if "alive" in case else None
+    m = MatterView(n, b, _ptr(keep["ref_pos"], C.c_double), _ptr(keep["pos"], C.c_double),
+                   _ptr(keep["vel"], C.c_double), _ptr(keep["mass"], C.c_double), _ptr(keep["bond_a"], C.c_uint32),
+                   _ptr(keep["bond_b"], C.c_uint32), _ptr(keep["rest_length"], C.c_double),
+                   _ptr(keep["compliance"], C.c_double), _ptr(keep["threshold"], C.c_double),
+                   _ptr(alive, C.c_uint8) if alive is not None else None, None, None)
+    origin = np.ascontiguousarray(case.get("origin", np.zeros(3)), dtype=np.float64)
+    h = C.c_void_p()
+    _call(library().gbl_build_state, C.byref(m), schedule._h, _ptr(origin, C.c_double), C.byref(h))
+    st = State(h)
+    if "pinned" in case:
+        st.pin(case["pinned"])
+    return st
+
+
+def step_settings(packed: np.ndarray) -> StepSettings:
+    """StepSettings<double> from the packed settings record (scenes.settings)."""
+    s = StepSettings()
+    s.dt = packed[scenes.K_DT]
+    s.gravity[:] = packed[scenes.K_GRAVITY:scenes.K_GRAVITY + 3]
+    s.constraint_iterations = int(packed[scenes.K_ITER])
+    s.bond_integrator = 0
+    s.damping_fraction = packed[scenes.K_DAMP]
+    s.sphere_enabled = int(packed[scenes.K_SPHERE])
+    s.direct_arithmetic = int(packed[scenes.K_DIRECT])
+    s.audit_energy = 0
+    s.plastic_yield_stretch = packed[scenes.K_YIELD]
+    s.plastic_hardening = packed[scenes.K_HARDEN]
+    s.plate_half_thickness = packed[scenes.K_PLATE]
+    c = packed[scenes.K_CONTACT:scenes.K_CONTACT + 7]
+    s.contact = ContactSettings(*c)
+    s.plane_count = int(packed[scenes.K_PLANE_COUNT])
+    for p in range(2):
+        q = packed[scenes.K_PLANES + scenes.PLANE_WIDTH * p: scenes.K_PLANES + scenes.PLANE_WIDTH * (p + 1)]
+        pl = s.planes[p]
+        pl.point[:], pl.normal[:], pl.tangent[:], pl.bitangent[:] = q[0:3], q[3:6], q[6:9], q[9:12]
+        pl.restitution, pl.static_friction, pl.dynamic_friction, pl.node_radius = q[12], q[13], q[14], q[15]
+        pl.reach_capped = int(q[16])
+        pl.footprint_count = int(q[17])
+        for f in range(4):
+            pl.footprints[f] = Footprint(*q[18 + 4 * f: 22 + 4 * f])
+    return s
+
+
+def sphere_state(packed: np.ndarray) -> Sphere:
+    s = Sphere()
+    s.center[:], s.velocity[:], s.angular_velocity[:] = packed[0:3], packed[3:6], packed[6:9]
+    s.radius, s.mass, s.inertia = packed[9], packed[10], packed[11]
+    return s
+
+
+def pack_sphere(s: Sphere) -> np.ndarray:
+    return np.array(list(s.center) + list(s.velocity) + list(s.angular_velocity) + [s.radius, s.mass, s.inertia])
+
+
+@dataclasses.dataclass
+class RunControl:
+    """RunControl (FastLattice.hpp:79-128); exit rules are off at 0."""
+    max_steps: int = 0
+    quiet_steps: int = 0
+    min_steps: int = 0
+    no_failure_steps: int = 0
+    energy_flat_steps: int = 0
+    energy_flat_fraction: float = 1.0e-3
+    calm_steps: int = 0
+    calm_damage_margin: float = 0.5
+    removable_energy_j: float = 0.0
+    capture_stride: int = 0
+    max_frames: int = 0
+    steps_per_launch: int = 0
+    abandon: object = None  # a numpy uint8 array of one element, or None
+
+    def c(self) -> RunControlC:
+        ab = self.abandon.ctypes.data if self.abandon is not None else None
+        return RunControlC(self.max_steps, self.quiet_steps, self.min_steps, self.no_failure_steps,
+                           self.energy_flat_steps, self.energy_flat_fraction, self.calm_steps,
+                           self.calm_damage_margin, self.removable_energy_j, self.capture_stride, self.max_frames,
+                           self.steps_per_launch, ab)
+
+
+class Backend:
+    """The GB300 LatticeBackend (FastLattice.hpp:255-369)."""
+
+    def __init__(self, schedule: Schedule, precision: str = "float", threads_per_block: int = 0):
+        self._h = None
+        prec = 1 if precision == "double" else 0
+        h = C.c_void_p()
+        _call(library().gbl_create, C.byref(schedule.view), prec, threads_per_block, C.byref(h))
+        self._h = h
+        self.precision = precision
+        self._node_count = 0
+        self._bond_count = 0
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_destroy(self._h)
+            self._h = None
+
+    def name(self) -> str:
+        buf = C.create_string_buffer(64)
+        _call(library().gbl_name, self._h, buf, len(buf))
+        return buf.value.decode()
+
+    def upload(self, state: State, settings: StepSettings, sphere: Sphere) -> None:
+        _call(library().gbl_upload, self._h, C.byref(state.view), C.byref(settings), C.byref(sphere))
+        self._node_count = state.node_count
+        self._bond_count = state.bond_count
+
+    def set_external_forces(self, forces, substeps: int) -> None:
+        if forces is None or len(forces) == 0:
+            _call(library().gbl_set_external_forces, self._h, None, 0, int(substeps))
+            return
+        f = np.ascontiguousarray(forces, dtype=np.float64).reshape(-1)
+        _call(library().gbl_set_external_forces, self._h, _ptr(f, C.c_double), f.size // 3, int(substeps))
+
+    def run(self, control: RunControl) -> RunStatus:
+        st = RunStatus()
+        ctl = control.c()
+        _call(library().gbl_run, self._h, C.byref(ctl), C.byref(st))
+        return st
+
+    def status(self) -> RunStatus:
+        st = RunStatus()
+        _call(library().gbl_status, self._h, C.byref(st))
+        return st
+
+    def download(self, state: State) -> Sphere:
+        sp = Sphere()
+        _call(library().gbl_download, self._h, C.byref(state.view), C.byref(sp))
+        return sp
+
+    def first_failure_bonds(self) -> np.ndarray:
+        n = C.c_uint64()
+        _call(library().gbl_first_failure_bonds, self._h, None, 0, C.byref(n))
+        out = np.zeros(n.value, dtype=np.uint32)
+        _call(library().gbl_first_failure_bonds, self._h, _ptr(out, C.c_uint32), n.value, C.byref(n))
+        return out
+
+    def take_frames(self) -> list:
+        n = C.c_uint64()
+        _call(library().gbl_frame_count, self._h, C.byref(n))
+        frames = []
+        for k in range(n.value):
+            step = C.c_uint64()
+            u = np.zeros(3 * self._node_count, dtype=np.float32)
+            alive = np.zeros(self._bond_count, dtype=np.uint8)
+            damage = np.zeros(self._bond_count, dtype=np.float32)
+            sp = Sphere()
+            _call(library().gbl_take_frame, self._h, k, C.byref(step), _ptr(u, C.c_float), _ptr(alive, C.c_uint8),
+                  _ptr(damage, C.c_float), C.byref(sp))
+            frames.append({"step": step.value, "u": u, "alive": alive, "damage": damage, "sphere": pack_sphere(sp)})
+        _call(library().gbl_clear_frames, self._h)
+        return frames
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _call(library().gbl_set_stream, self._h, C.c_void_p(stream_ptr) if stream_ptr else None)
+
+    def kernels_per_substep(self) -> int:
+        n = C.c_uint64()
+        _call(library().gbl_kernels_per_substep, self._h, C.byref(n))
+        return int(n.value)
+
+    def profile_phases(self, substeps: int) -> dict:
+        out = np.zeros(16, dtype=np.float64)
+        _call(library().gbl_profile_phases, self._h, int(substeps), _ptr(out, C.c_double))
+        return {PHASE_NAMES[k]: float(out[k]) for k in range(16)}
+
+
+def make_gb300_lattice_backend(schedule: Schedule, precision: str = "float", threads_per_block: int = 0) -> Backend:
+    """The factory that replaces makeCudaLatticeBackend (FastLattice.hpp:401-402)."""
+    return Backend(schedule, precision, threads_per_block)
+
+
+def status_arrays(st: RunStatus) -> dict:
+    """RunStatus packed as the case files pack it (oracle/case_layout.hpp)."""
+    u = np.zeros(13, dtype=np.uint64)
+    u[:] = [st.total_steps, st.first_failure_step, st.last_failure_step, st.failure_rounds, st.broken_bonds,
+            st.last_energy_gain_step, st.last_damage_gain_step, st.exit_reason, st.rank_deficient_nodes,
+            st.contact.impulse_contacts, st.contact.candidate_overflow, st.contact.ball_support_events, st.launches]
+    d = np.zeros(20, dtype=np.float64)
+    d[:] = [st.removed_energy_j, st.max_damage, st.plastic_work_j, st.max_tensile_stretch,
+            st.max_compressive_strain, st.max_shear_strain, st.max_plastic_stretch,
+            st.contact.impulse_to_material_x, st.contact.impulse_to_material_y, st.contact.impulse_to_material_z,
+            st.contact.dissipated_kinetic_energy_j, st.contact.maximum_penetration_m,
+            st.contact.maximum_position_correction_m, st.contact.maximum_center_shift_m, st.external_load.work_j,
+            st.external_load.impulse_n_s[0], st.external_load.impulse_n_s[1], st.external_load.impulse_n_s[2],
+            float(st.external_load.steps), st.wall_seconds]
+    return {"status_u64": u, "status_f64": d}
+
+
+def run_case(case: dict, precision: str = "float", per_substep: bool = False, threads_per_block: int = 0) -> dict:
+    """Runs a scene case through the GPU backend the way a reference caller
+    would (schedule, state, upload, loads, run, download) and returns the same
+    output arrays the CPU checkers return."""
+    n = int(case["node_count"][0])
+    sched = build_lattice_schedule(n, case["bond_a"], case["bond_b"], case["node_block_begin"])
+    state = build_lattice_state(case, sched)
+    backend = make_gb300_lattice_backend(sched, precision, threads_per_block)
+    settings = step_settings(case["settings"])
+    settings.direct_arithmetic = 1 if precision == "double" else 0
+    backend.upload(state, settings, sphere_state(case["sphere"]))
+    steps = int(case["steps"][0])
+    per_step = int(case.get("substeps_per_step", [1])[0])
+    ramp = "force_ramp_steps" in case
+    base = case.get("forces")
+    if base is not None and not ramp:
+        backend.set_external_forces(base, int(case["force_substeps"][0]))
+    break_step = np.full(int(case["bond_count"][0]), NO_BOND, dtype=np.uint32)
+    alive_before = state.alive.copy()
+    chunk = 1 if per_substep else (per_step if ramp else steps)
+    done = 0
+    st = None
+    while done < steps:
+        if ramp and done % per_step == 0:
+            scale = float(case["force_ramp_scale"][0]) * (done // per_step) / float(case["force_ramp_steps"][0])
+            backend.set_external_forces(scale * base, per_step)
+        nsteps = min(chunk, steps - done)
+        st = backend.run(RunControl(max_steps=nsteps))
+        done += nsteps
+        if per_substep:
+            backend.download(state)
+            newly = (alive_before != 0) & (state.alive == 0)
+            break_step[newly] = done - 1
+            alive_before = state.alive.copy()
+    sp = backend.download(state)
+    out = {"u": state.u.copy(), "u_prev": state.u_prev.copy(), "v": state.v.copy(), "alive": state.alive.copy(),
+           "failure_mode": state.failure_mode.copy(), "damage": state.damage.copy(),
+           "plastic_extension": state.plastic_extension.copy(), "plastic_strain": state.plastic_strain.copy(),
+           "prev_tensile": state.prev_tensile.copy(), "prev_compressive": state.prev_compressive.copy(),
+           "prev_shear": state.prev_shear.copy(), "sphere_out": pack_sphere(sp),
+           "first_failure_bonds": backend.first_failure_bonds(), "state_nbr_other": state.nbr_other.copy(),
+           "state_max_degree": np.array([state.view.max_degree], np.uint32)}
+    out.update(sched.arrays())
+    out.update(status_arrays(st))
+    if per_substep:
+        out["break_step"] = break_step
+    return out

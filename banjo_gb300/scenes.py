@@ -35,30 +35,47 @@ INF = float("inf")
 
 
 def splitmix64(values: np.ndarray) -> np.ndarray:
-    """The splitmix64 output mix on uint64 values (wrapping arithmetic)."""
-    z = np.asarray(values, dtype=np.uint64).copy()
+    """The splitmix64 output mix on uint64 values (wrapping arithmetic), in place
+    on a copy so that tens of millions of draws stay cheap."""
+    z = np.array(values, dtype=np.uint64, copy=True)
+    t = np.empty_like(z)
     with np.errstate(over="ignore"):
-        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-        z = z ^ (z >> np.uint64(31))
+        for shift, mult in ((30, 0xBF58476D1CE4E5B9), (27, 0x94D049BB133111EB)):
+            np.right_shift(z, np.uint64(shift), out=t)
+            np.bitwise_xor(z, t, out=z)
+            np.multiply(z, np.uint64(mult), out=z)
+        np.right_shift(z, np.uint64(31), out=t)
+        np.bitwise_xor(z, t, out=z)
     return z
 
 
 def uniform(seed: int, start: int, count: int) -> np.ndarray:
     """Draws start..start+count-1 of stream `seed`, uniform in [0, 1)."""
-    k = np.arange(start + 1, start + count + 1, dtype=np.uint64)
+    state = np.arange(start + 1, start + count + 1, dtype=np.uint64)
     with np.errstate(over="ignore"):
-        state = np.uint64(seed) + k * GOLDEN
-    return (splitmix64(state) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        np.multiply(state, GOLDEN, out=state)
+        np.add(state, np.uint64(seed), out=state)
+    z = splitmix64(state)
+    np.right_shift(z, np.uint64(11), out=z)
+    out = z.astype(np.float64)
+    out *= 1.0 / 9007199254740992.0
+    return out
 
 
 def lognormal(seed: int, count: int, median: float, sigma: float) -> np.ndarray:
     """Box-Muller normals from draw pairs (2k, 2k+1) of the stream."""
     u = uniform(seed, 0, 2 * count)
     u1 = 1.0 - u[0::2]  # (0, 1]
-    u2 = u[1::2]
-    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
-    return median * np.exp(sigma * z)
+    np.log(u1, out=u1)
+    u1 *= -2.0
+    np.sqrt(u1, out=u1)
+    u2 = u[1::2] * (2.0 * math.pi)
+    np.cos(u2, out=u2)
+    u1 *= u2
+    u1 *= sigma
+    np.exp(u1, out=u1)
+    u1 *= median
+    return u1
 
 
 def half_offsets(horizon: int = 1, max_d2: int | None = 2):
@@ -101,22 +118,22 @@ def box_nodes(nx: int, ny: int, nz: int, h: float, center=(0.0, 0.0, 0.0)) -> np
 def box_bonds(nx: int, ny: int, nz: int, max_d2: int | None = 2, horizon: int = 1):
     """Bond endpoints and grid distance^2, in the reference generator's order."""
     n = nx * ny * nz
-    idx = np.arange(n, dtype=np.int64)
-    x = idx % nx
-    y = (idx // nx) % ny
-    z = idx // (nx * ny)
     offs = half_offsets(horizon, max_d2)
-    valid = np.zeros((n, len(offs)), dtype=bool)
-    other = np.zeros((n, len(offs)), dtype=np.int64)
-    d2s = np.zeros((n, len(offs)), dtype=np.int8)
-    for k, (dx, dy, dz, d2) in enumerate(offs):
-        valid[:, k] = (x + dx >= 0) & (x + dx < nx) & (y + dy >= 0) & (y + dy < ny) & (z + dz >= 0) & (z + dz < nz)
-        other[:, k] = idx + dx + nx * (dy + ny * dz)
-        d2s[:, k] = d2
-    mask = valid.reshape(-1)
-    a = np.repeat(idx, len(offs))[mask].astype(np.uint32)
-    b = other.reshape(-1)[mask].astype(np.uint32)
-    d2 = d2s.reshape(-1)[mask]
+    K = len(offs)
+    idx3 = np.arange(n, dtype=np.int64).reshape(nz, ny, nx)
+    other = np.full((nz, ny, nx, K), -1, dtype=np.int64)
+
+    def span(d, size):  # source range whose neighbour at offset d is inside
+        return slice(max(0, -d), min(size, size - d))
+
+    for k, (dx, dy, dz, _) in enumerate(offs):
+        sz, sy, sx = span(dz, nz), span(dy, ny), span(dx, nx)
+        other[sz, sy, sx, k] = idx3[sz, sy, sx] + (dx + nx * (dy + ny * dz))
+    flat = other.reshape(-1)
+    mask = flat >= 0
+    a = (np.nonzero(mask)[0] // K).astype(np.uint32)
+    b = flat[mask].astype(np.uint32)
+    d2 = np.tile(np.asarray([o[3] for o in offs], dtype=np.int8), n)[mask]
     return a, b, d2
 
 

@@ -1,0 +1,347 @@
+"""Benchmark of the bonded-lattice XPBD fracture substep on one GB300.
+
+Workload (default, --workload impact): the single large lattice impact -- a
+256x128x128 block of cells (4,194,304 nodes, 37,340,160 face+edge bonds, FP32)
+on a ground plane, struck by a rigid iron sphere (r 0.2 m, 10 m/s) at a seeded
+point, per-bond lognormal break strain (median 1.5e-3, sigma 0.3), plastic
+yield at 60% of the median, 32 z-slabs, dt = 1/240 s in 10 substeps with 4
+colour sweeps. Synthetic, generated from those constants (banjo_gb300.scenes).
+
+A step is one rigid step: 10 substeps. The metric is bond projections/s: one
+projection is one XPBD bond solve on a live bond, so a substep makes
+4 x live bonds of them.
+
+  value   device time (CUDA events on the backend's stream) of K steps, state
+          resident in HBM; the working set (about 6 GB) is far larger than L2.
+  e2e     the same metric through the C ABI from host buffers: upload of the
+          host LatticeState, K steps, download, timed on the host clock.
+  roofline  the projection sweep, the dominant phase: algorithmic bytes of one
+          substep's sweeps (4 x (N x 24 + B x 40)) over its event-timed
+          duration, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU checker (a restatement of the reference CPU lane) on the
+          same lattice, all host threads, steady-state substeps only.
+
+--impl reference times the reference's CPU lane on the same workload and metric.
+The reference tree does not travel to the GPU machine, so there it is the CPU
+restatement of that lane (oracle/), all host threads, one substep per step.
+
+--gpus N (torchrun, one rank per GPU): the path does not shard (one lattice);
+each rank runs an independent replica and value is the sum of the replicas'
+projections over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bond projections/s"
+ITERATIONS = 4
+SUBSTEPS_PER_STEP = 10
+
+
+def peaks() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        self.tmp = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.tmp.flush()
+
+    def summary(self) -> dict:
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_case(workload: str) -> tuple[dict, str]:
+    from banjo_gb300 import scenes
+
+    if workload == "impact":
+        return scenes.impact_block(), "impact 256x128x128, 4194304 nodes, 37340160 bonds, 32 slabs, sphere 10 m/s"
+    if workload == "cantilever":
+        return scenes.cantilever(), "cantilever 32x8x8, 2048 nodes, 15648 bonds, pinned, loaded"
+    raise SystemExit(f"unknown workload {workload}")
+
+
+def bytes_per_substep(n: int, b: int, plastic: bool) -> dict:
+    """Algorithmic bytes of one FP32 substep: every compulsory array counted once
+    per pass that needs it."""
+    nodes = n * (44 + 24)
+    strain = n * (36 + 12 + 1)
+    bond_const = b * 56
+    bond_state = b * (34 + (16 if plastic else 0))
+    sweep = ITERATIONS * (n * 24 + b * 40)
+    return {"total": nodes + strain + bond_const + bond_state + sweep, "sweep": sweep}
+
+
+def cpu_baseline(case: dict, threads: int, substeps: int = 3) -> dict:
+    """The CPU checker on `substeps` substeps of the workload; the first substep
+    (the post-upload restart) is left out of the rate."""
+    import oracle
+
+    sample = dict(case)
+    sample["steps"] = np.array([substeps], dtype=np.uint64)
+    out = oracle.run_port(sample, threads=threads)
+    secs = out["substep_seconds"][1:]
+    live = int(case["bond_count"][0]) - int(out["status_u64"][4])
+    rate = ITERATIONS * live * len(secs) / float(np.sum(secs))
+    return {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{substeps} substeps of the same lattice on {threads} host threads, the first "
+                      f"(restart) substep excluded; {float(np.sum(secs)):.2f} s timed"}
+
+
+def distributed():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist, torch
+    return rank, world, local, None, None
+
+
+def barrier(dist, torch):
+    if dist is not None:
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(x: float, dist, torch) -> float:
+    if dist is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x: float, dist, torch) -> float:
+    if dist is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_gb300(args) -> None:
+    rank, world, local, dist, torch = distributed()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    from banjo_gb300 import build as lib_build
+    from banjo_gb300 import lattice
+
+    lib_build.build()
+    case, desc = make_case(args.workload)
+    n, b = int(case["node_count"][0]), int(case["bond_count"][0])
+    sched = lattice.build_lattice_schedule(n, case["bond_a"], case["bond_b"], case["node_block_begin"])
+    state = lattice.build_lattice_state(case, sched)
+    settings = lattice.step_settings(case["settings"])
+    sphere = lattice.sphere_state(case["sphere"])
+    backend = lattice.make_gb300_lattice_backend(sched)
+    backend.upload(state, settings, sphere)
+    if "forces" in case:
+        backend.set_external_forces(case["forces"], int(case["force_substeps"][0]))
+    substeps_w = args.warmup * SUBSTEPS_PER_STEP
+    substeps_k = args.steps * SUBSTEPS_PER_STEP
+    backend.run(lattice.RunControl(max_steps=substeps_w))
+    launches = backend.kernels_per_substep()
+
+    # Timed region: K steps, device-timed with the backend's CUDA events.
+    before = backend.status()
+    sampler = ClockSampler(local)
+    barrier(dist, torch)
+    with sampler:
+        t0 = time.perf_counter()
+        st = backend.run(lattice.RunControl(max_steps=substeps_k))
+        host_s = time.perf_counter() - t0
+    barrier(dist, torch)
+    device_s = st.kernel_seconds - before.kernel_seconds
+    # Live bonds counted after each failure round of the window (a lower bound
+    # on projections: a bond that breaks in a substep was live through it).
+    live_end = b - st.broken_bonds
+    projections = ITERATIONS * live_end * substeps_k
+    device_s_max = max_over_ranks(device_s, dist, torch)
+    total_proj = sum_over_ranks(float(projections), dist, torch)
+    clocks = sampler.summary()
+
+    # Roofline of the projection sweep: event-timed phases of a few substeps.
+    phases = backend.profile_phases(args.profile_substeps)
+    sweep_ms = (phases["sweep_interior"] + phases["sweep_boundary"]) / args.profile_substeps
+    plastic = float(case["settings"][8]) > 0.0
+    algo = bytes_per_substep(n, b, plastic)
+    peak, peak_kind = peaks()
+    achieved = algo["sweep"] / (sweep_ms * 1e-3) / 1e9
+    sub_per_s = substeps_k / device_s
+    total_gbs = algo["total"] * sub_per_s / 1e9
+
+    # e2e: through the C ABI from host buffers (upload, K steps, download).
+    e2e_state = lattice.build_lattice_state(case, sched)
+    e2e_backend = lattice.make_gb300_lattice_backend(sched)
+    t0 = time.perf_counter()
+    e2e_backend.upload(e2e_state, settings, sphere)
+    e2e_st = e2e_backend.run(lattice.RunControl(max_steps=substeps_k))
+    e2e_backend.download(e2e_state)
+    e2e_s = time.perf_counter() - t0
+    e2e_proj = ITERATIONS * (b - e2e_st.broken_bonds) * substeps_k
+    e2e_s_max = max_over_ranks(e2e_s, dist, torch)
+    e2e_total = sum_over_ranks(float(e2e_proj), dist, torch)
+    d = max(1, state.view.max_degree)
+    h2d = n * 4 * 16 + b * (16 + 16 + 16 + 16 + 8 + 8 + 1 + 8) + n * d * (16 + 4 + 4)
+    d2h = n * 3 * 16 + b * (16 + 16 + 8 + 1)
+
+    line = {
+        "metric": METRIC,
+        "value": total_proj / device_s_max,
+        "unit": "projections/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": device_s_max / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (f64 ledgers)",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": desc, "substeps_per_step": SUBSTEPS_PER_STEP, "iterations": ITERATIONS,
+                   "nodes": n, "bonds": b, "parallelism": f"replicas{world}" if world > 1 else "single lattice",
+                   "l2": "working set ~6 GB >> 129 MB L2 (no flush needed)",
+                   "live_bonds_end": live_end, "broken_in_window": st.broken_bonds - before.broken_bonds},
+        "e2e": {"value": e2e_total / e2e_s_max, "unit": "projections/s", "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps,
+                "note": "one upload of the host LatticeState, K steps, one download; wall clock"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "kSolve (projection sweep)",
+                     "sweep_ms_per_substep": sweep_ms, "whole_substep_gbs": total_gbs,
+                     "whole_substep_frac": total_gbs / peak},
+        "gpu_launches": launches * substeps_k,
+        "clocks": clocks,
+        "host_seconds": host_s,
+        "phase_ms_per_substep": {k: v / args.profile_substeps for k, v in phases.items() if v > 0},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(case, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build_port()
+    case, desc = make_case(args.workload)
+    threads = os.cpu_count() or 1
+    b = int(case["bond_count"][0])
+    # One step = one substep of the workload (bounded so the run ends in minutes);
+    # warm-up substeps (including the post-upload restart) are run, not timed.
+    sample = dict(case)
+    sample["steps"] = np.array([args.warmup + args.steps], dtype=np.uint64)
+    out = oracle.run_port(sample, threads=threads)
+    secs = out["substep_seconds"][args.warmup:]
+    live = b - int(out["status_u64"][4])
+    value = ITERATIONS * live * len(secs) / float(np.sum(secs))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "projections/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": float(np.mean(secs)) * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (f64 ledgers)",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": desc, "substeps_per_step": 1, "iterations": ITERATIONS},
+        "cpu_baseline": {"value": value, "unit": "projections/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} substeps after {args.warmup} warm-up substeps, {threads} threads; "
+                                   "the reference tree is absent here, so its CPU lane runs as the restatement"},
+        "e2e": {"value": value, "unit": "projections/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main() -> None:
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=6)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="impact", choices=["impact", "cantilever"])
+    p.add_argument("--profile-substeps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("warm-up must be at least 3 steps")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,329 @@
+/*
+ * gbl.h -- C ABI of the GB300 bonded-lattice XPBD fracture substep.
+ *
+ * This is the drop-in boundary for the reference's lattice step API
+ * (src/fastlattice/FastLattice.hpp:255-405, class LatticeBackend and its
+ * factories). It replaces the removed CUDA backend, whose factory survives as a
+ * stub that throws (src/fastlattice/CudaLatticeUnavailable.cpp:11-25). Every
+ * struct below mirrors a reference struct field for field, in plain C types, so
+ * a C++ adapter converts by member copies and the library needs
+ * no reference headers. No torch or CUDA types appear in any signature.
+ *
+ * Errors: every entry point returns a gbl_result. A non-zero value is the C
+ * image of the exception the reference throws in the same situation
+ * (FastLattice.hpp:263-358): GBL_INVALID_ARGUMENT for std::invalid_argument,
+ * GBL_RUNTIME_ERROR for std::runtime_error (no device, device failure),
+ * GBL_OVERFLOW_ERROR for std::overflow_error, GBL_LOGIC_ERROR for
+ * std::logic_error. gbl_last_error() returns the message of the last failure
+ * on the calling thread.
+ *
+ * Threading: one host thread per backend between run calls; a backend is not
+ * reentrant (FastLattice.hpp:293-295 states the same rule for the reference
+ * backends). Different backends may be used from different threads.
+ */
+#ifndef GBL_H
+#define GBL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gbl_result;
+#define GBL_OK 0
+#define GBL_INVALID_ARGUMENT 1
+#define GBL_RUNTIME_ERROR 2
+#define GBL_OVERFLOW_ERROR 3
+#define GBL_LOGIC_ERROR 4
+
+/* Precision (FastLattice.hpp:32). */
+#define GBL_PRECISION_FLOAT 0
+#define GBL_PRECISION_DOUBLE 1
+
+#define GBL_MAX_SUPPORT_PLANES 2      /* LatticePhysics.hpp:103 */
+#define GBL_MAX_FOOTPRINTS 4          /* LatticePhysics.hpp:104 */
+#define GBL_MAX_CANDIDATES_PER_BLOCK 1024 /* LatticePhysics.hpp:105 */
+#define GBL_PHASE_COUNT 16            /* FastLattice.hpp:130 */
+#define GBL_NO_BOND 0xffffffffu       /* LatticePhysics.hpp:106 */
+
+/* ---- Schedule: mirrors LatticeSchedule (LatticeSchedule.hpp:28-44). ---- */
+typedef struct gbl_schedule_view {
+    uint32_t node_count;
+    uint32_t bond_count;
+    uint32_t block_count;
+    uint32_t color_count;
+    uint32_t boundary_bond_count;
+    const uint32_t *node_block_begin;    /* block_count + 1 */
+    const uint32_t *bond_order;          /* bond_count: schedule index -> asset bond */
+    const uint32_t *bond_schedule_index; /* bond_count: asset bond -> schedule index */
+    const uint32_t *bond_block_begin;    /* block_count + 1 */
+    const uint32_t *range_begin;         /* block_count * 2 * max(color_count, 1) */
+    const uint32_t *range_end;
+    const uint8_t *bond_color;           /* bond_count, per schedule index */
+} gbl_schedule_view;
+
+/* ---- Canonical state: mirrors LatticeState (FastLattice.hpp:37-55). ----
+ * Host double arrays in schedule order, caller-owned. For gbl_upload every
+ * pointer is read; for gbl_download only u, u_prev, v, alive, failure_mode,
+ * damage, plastic_extension, plastic_strain and prev_* are written (the
+ * reference's WorkingLattice::toState, LatticeWorking.hpp:126-142), into
+ * caller buffers of the uploaded sizes. */
+typedef struct gbl_state_view {
+    double origin[3];
+    uint32_t node_count;
+    uint32_t bond_count;
+    uint32_t max_degree;
+    const double *x0;          /* 3N */
+    double *u;                 /* 3N */
+    double *u_prev;            /* 3N */
+    double *v;                 /* 3N */
+    const double *inv_mass;    /* N */
+    const double *mass;        /* N */
+    const uint32_t *adj_offsets; /* N + 1 */
+    const uint32_t *adj_bonds;
+    const uint32_t *nbr_bond;  /* max_degree * N, k-major */
+    const uint32_t *nbr_other; /* max_degree * N */
+    const double *nbr_rest;    /* 3 * max_degree * N */
+    const double *nbr_weight;  /* max_degree * N */
+    const uint8_t *nbr_alive;  /* max_degree * N */
+    const uint32_t *bond_slot_a; /* B */
+    const uint32_t *bond_slot_b; /* B */
+    const uint32_t *bond_a;    /* B */
+    const uint32_t *bond_b;    /* B */
+    const double *rest_edge;   /* 3B */
+    const double *rest_length; /* B */
+    const double *rest_length_sq_minus; /* B */
+    const double *weight;      /* B */
+    const double *compliance;  /* B */
+    const double *threshold;   /* 6B: ds, de, cs, ce, ss, se */
+    uint8_t *alive;            /* B */
+    uint8_t *failure_mode;     /* B */
+    double *damage;            /* B */
+    double *prev_tensile;      /* B */
+    double *prev_compressive;  /* B */
+    double *prev_shear;        /* B */
+    double *plastic_extension; /* B */
+    double *plastic_strain;    /* B */
+} gbl_state_view;
+
+/* ---- Step settings: mirrors StepSettings<double> (LatticePhysics.hpp:114-158, 188-202, 248-284). */
+typedef struct gbl_footprint {
+    double center_t, center_b, half_t, half_b;
+} gbl_footprint;
+
+typedef struct gbl_support_plane {
+    double point[3], normal[3], tangent[3], bitangent[3];
+    double restitution, static_friction, dynamic_friction;
+    double node_radius;
+    uint8_t reach_capped;
+    uint32_t footprint_count;
+    gbl_footprint footprints[GBL_MAX_FOOTPRINTS];
+} gbl_support_plane;
+
+typedef struct gbl_contact_settings {
+    double static_friction, dynamic_friction, restitution, restitution_speed_threshold;
+    double node_contact_radius, contact_margin;
+    double prefilter_slack;
+} gbl_contact_settings;
+
+typedef struct gbl_node_contact_settings {
+    uint8_t mode; /* 0 off; node-to-node contact modes 1 and 2 are refused */
+    double radius, skin, margin, restitution, restitution_speed_threshold, static_friction, dynamic_friction;
+    uint32_t bucket_mask;
+} gbl_node_contact_settings;
+
+typedef struct gbl_step_settings {
+    double dt;
+    double gravity[3];
+    uint32_t constraint_iterations;
+    uint8_t bond_integrator;   /* 0 XPBD; 1 (Verlet reference) is refused */
+    double damping_fraction;
+    uint8_t sphere_enabled;
+    uint8_t direct_arithmetic; /* must be 0 for float, 1 for double */
+    uint8_t audit_energy;
+    double plastic_yield_stretch;
+    double plastic_hardening;
+    double plate_half_thickness; /* > 0 (plate bending) is refused */
+    gbl_contact_settings contact;
+    gbl_node_contact_settings node_contact;
+    uint32_t plane_count;
+    gbl_support_plane planes[GBL_MAX_SUPPORT_PLANES];
+} gbl_step_settings;
+
+/* SphereState<double> (LatticePhysics.hpp:144-148). */
+typedef struct gbl_sphere {
+    double center[3], velocity[3], angular_velocity[3];
+    double radius, mass, inertia;
+} gbl_sphere;
+
+/* RunControl (FastLattice.hpp:79-128). `abandon`, when not null, is read
+ * between substeps; once it holds a non-zero byte the run stops, exit reason 7. */
+typedef struct gbl_run_control {
+    uint64_t max_steps;
+    uint64_t quiet_steps;
+    uint64_t min_steps;
+    uint64_t no_failure_steps;
+    uint64_t energy_flat_steps;
+    double energy_flat_fraction; /* reference default 1e-3 */
+    uint64_t calm_steps;
+    double calm_damage_margin;   /* reference default 0.5 */
+    double removable_energy_j;
+    uint64_t capture_stride;
+    uint32_t max_frames;
+    uint64_t steps_per_launch;
+    const volatile uint8_t *abandon;
+} gbl_run_control;
+
+/* RunStatus (FastLattice.hpp:182-245), the fields the XPBD lane fills. */
+typedef struct gbl_contact_accumulators {
+    unsigned long long impulse_contacts;
+    double impulse_to_material_x, impulse_to_material_y, impulse_to_material_z;
+    double dissipated_kinetic_energy_j;
+    double maximum_penetration_m;
+    double maximum_position_correction_m;
+    double maximum_center_shift_m;
+    unsigned long long candidate_overflow;
+    unsigned long long ball_support_events;
+} gbl_contact_accumulators;
+
+typedef struct gbl_load_ledger {
+    uint64_t steps;
+    double elapsed_s;
+    double requested_impulse_n_s[3], impulse_n_s[3];
+    double requested_angular_impulse_kg_m2_s[3], angular_impulse_kg_m2_s[3];
+    double work_j;
+} gbl_load_ledger;
+
+typedef struct gbl_run_status {
+    uint64_t total_steps;
+    uint64_t first_failure_step;
+    uint64_t last_failure_step;
+    uint32_t failure_rounds;
+    uint32_t broken_bonds;
+    double removed_energy_j;
+    uint64_t last_energy_gain_step;
+    double max_damage;
+    uint64_t last_damage_gain_step;
+    gbl_contact_accumulators contact;
+    gbl_load_ledger external_load;
+    unsigned exit_reason;
+    unsigned launches;
+    double kernel_seconds;
+    double wall_seconds;
+    uint32_t frames_captured;
+    double phase_seconds[GBL_PHASE_COUNT];
+    float max_tensile_stretch, max_compressive_strain, max_shear_strain;
+    uint32_t rank_deficient_nodes;
+    double plastic_work_j;
+    float max_plastic_stretch;
+} gbl_run_status;
+
+typedef struct gbl_backend gbl_backend;
+
+/* ---- Device queries: cudaLatticeAvailable / Description / MultiprocessorCount
+ * (FastLattice.hpp:403-405). ---- */
+int gbl_available(void);
+gbl_result gbl_description(char *buffer, size_t capacity);
+unsigned gbl_multiprocessor_count(void);
+gbl_result gbl_last_error(char *buffer, size_t capacity);
+
+/* makeCudaLatticeBackend(schedule, precision, threads_per_block)
+ * (FastLattice.hpp:401-402). The schedule is copied. threads_per_block 0
+ * picks the default. Fails with GBL_RUNTIME_ERROR when there is no device. */
+gbl_result gbl_create(const gbl_schedule_view *schedule, int precision, unsigned threads_per_block,
+                      gbl_backend **out);
+void gbl_destroy(gbl_backend *backend);
+/* LatticeBackend::name (FastLattice.hpp:266). */
+gbl_result gbl_name(const gbl_backend *backend, char *buffer, size_t capacity);
+/* LatticeBackend::upload (FastLattice.hpp:267-268). Clears status, loads,
+ * frames and the first-failure record, as the reference's upload does. */
+gbl_result gbl_upload(gbl_backend *backend, const gbl_state_view *state, const gbl_step_settings *settings,
+                      const gbl_sphere *sphere);
+/* LatticeBackend::setExternalForces (FastLattice.hpp:274-277, the CPU rules of
+ * ExternalLoads.hpp:28-50): forces_world_n holds 3 * count doubles in schedule
+ * node order; count 0 with substeps 0 cancels. */
+gbl_result gbl_set_external_forces(gbl_backend *backend, const double *forces_world_n, uint64_t count,
+                                   uint64_t substeps);
+/* LatticeBackend::run (FastLattice.hpp:360); the status accumulates across calls. */
+gbl_result gbl_run(gbl_backend *backend, const gbl_run_control *control, gbl_run_status *status_out);
+/* LatticeBackend::status (FastLattice.hpp:364). */
+gbl_result gbl_status(const gbl_backend *backend, gbl_run_status *status_out);
+/* LatticeBackend::download (FastLattice.hpp:361). */
+gbl_result gbl_download(gbl_backend *backend, gbl_state_view *state, gbl_sphere *sphere);
+/* LatticeBackend::firstFailureBonds (FastLattice.hpp:368): schedule indices
+ * removed in the substep of the first failure since upload. `count` receives
+ * the full length; at most `capacity` are written. */
+gbl_result gbl_first_failure_bonds(const gbl_backend *backend, uint32_t *out, uint64_t capacity, uint64_t *count);
+/* LatticeBackend::takeFrames (FastLattice.hpp:363). Frames captured since the
+ * last take, oldest first: gbl_frame_count, then gbl_take_frame for each index
+ * with caller buffers (u: 3N floats, alive: B bytes, damage: B floats), then
+ * gbl_clear_frames. */
+gbl_result gbl_frame_count(const gbl_backend *backend, uint64_t *count);
+gbl_result gbl_take_frame(const gbl_backend *backend, uint64_t index, uint64_t *step, float *u, uint8_t *alive,
+                          float *damage, gbl_sphere *sphere);
+gbl_result gbl_clear_frames(gbl_backend *backend);
+
+/* Issue work on this CUDA stream (a cudaStream_t passed as void*; null: the
+ * backend's own stream). For callers that time or order the substep against
+ * their own work. */
+gbl_result gbl_set_stream(gbl_backend *backend, void *cuda_stream);
+
+/* Kernel launches one substep makes (the nodes of the captured substep graph). */
+gbl_result gbl_kernels_per_substep(gbl_backend *backend, uint64_t *count);
+
+/* Per-phase device time (milliseconds, 16 phases named as
+ * latticePhaseName, FastLattice.cpp:22-27) of `substeps` substeps run outside
+ * the captured graph with an event between phases. Advances the state like
+ * gbl_run with max_steps = substeps and exit rules off. */
+gbl_result gbl_profile_phases(gbl_backend *backend, uint64_t substeps, double *phase_ms);
+
+/* sizeof of a struct of this header by its name ("gbl_step_settings", ...),
+ * 0 for an unknown name: lets a binding check its own layout. */
+size_t gbl_struct_size(const char *name);
+
+/* ---- Host builders, for callers without the reference's C++: ----
+ * buildLatticeSchedule (LatticeSchedule.cpp:71-155) and buildLatticeState
+ * (FastLattice.cpp:47-169) restated. Outputs live in library-owned objects
+ * whose views stay valid until freed. */
+typedef struct gbl_schedule gbl_schedule;
+gbl_result gbl_build_schedule(uint32_t node_count, uint32_t bond_count, const uint32_t *bond_a, const uint32_t *bond_b,
+                              const uint32_t *node_block_begin, uint32_t block_count, gbl_schedule **out);
+gbl_result gbl_schedule_view_of(const gbl_schedule *schedule, gbl_schedule_view *view);
+void gbl_schedule_free(gbl_schedule *schedule);
+
+typedef struct gbl_state gbl_state;
+/* The asset (reference positions, bonds and their rest records) and the
+ * matter (node positions, velocities, masses, bond aliveness/damage/mode), in
+ * asset order, as ActiveMatter holds them (fracture/ActiveMatter.hpp). */
+typedef struct gbl_matter_view {
+    uint32_t node_count;
+    uint32_t bond_count;
+    const double *reference_position; /* 3N world */
+    const double *position;           /* 3N world */
+    const double *velocity;           /* 3N */
+    const double *mass;               /* N */
+    const uint32_t *bond_a;           /* B */
+    const uint32_t *bond_b;           /* B */
+    const double *rest_length;        /* B */
+    const double *compliance;         /* B */
+    const double *threshold;          /* 6B */
+    const uint8_t *alive;             /* B or null (all alive) */
+    const double *damage;             /* B or null */
+    const uint8_t *failure_mode;      /* B or null */
+} gbl_matter_view;
+gbl_result gbl_build_state(const gbl_matter_view *matter, const gbl_schedule *schedule, const double origin[3],
+                           gbl_state **out);
+/* A view whose arrays are owned by the state object (writable, so the same
+ * object can receive a download). */
+gbl_result gbl_state_view_of(gbl_state *state, gbl_state_view *view);
+/* Sets inv_mass of the flagged nodes to 0 (a pinned node keeps its mass). */
+gbl_result gbl_state_pin(gbl_state *state, const uint8_t *pinned);
+void gbl_state_free(gbl_state *state);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBL_H */

@@ -949,6 +949,7 @@ public:
     Status status;
     Loads<R> loads;
     std::vector<std::uint32_t> first_failure_bonds;
+    std::vector<double> substep_seconds; // wall time of every substep run
     double energy_flat_fraction{1.0e-3};
 
     // CpuLatticeBackend.cpp:255-304 for one RunControl with exit rules off.
@@ -957,7 +958,9 @@ public:
         std::uint64_t done = 0;
         while (done < max_steps) {
             const std::uint64_t step = status.total_steps;
+            const auto t0 = std::chrono::steady_clock::now();
             const bool failed = advance();
+            substep_seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
             status.total_steps = step + 1;
             ++done;
             if (failed) {
@@ -1203,6 +1206,7 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     out.put("status_f64", d);
     out.putScalar<double>("wall_seconds", wall);
     out.putScalar<std::uint32_t>("threads", threads);
+    out.put("substep_seconds", run.substep_seconds);
 }
 
 thread_local std::string g_error;

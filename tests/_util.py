@@ -1,0 +1,72 @@
+"""Shared helpers of the test suite: golden fixtures and exact comparisons."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# Outputs held bit for bit between runners (status excludes wall time and the
+# launch count, which differ by construction).
+STATE_KEYS = ["u", "u_prev", "v", "alive", "failure_mode", "damage", "plastic_extension", "plastic_strain",
+              "prev_tensile", "prev_compressive", "prev_shear", "sphere_out", "first_failure_bonds"]
+SCHEDULE_KEYS = ["sched_bond_order", "sched_color", "sched_range_begin", "sched_range_end",
+                 "sched_bond_block_begin", "sched_color_count", "sched_boundary_bond_count"]
+STATUS_U64 = {"total_steps": 0, "first_failure_step": 1, "last_failure_step": 2, "failure_rounds": 3,
+              "broken_bonds": 4, "last_energy_gain_step": 5, "last_damage_gain_step": 6, "exit_reason": 7,
+              "rank_deficient_nodes": 8, "impulse_contacts": 9, "candidate_overflow": 10, "ball_support_events": 11}
+STATUS_F64 = {"removed_energy_j": 0, "max_damage": 1, "plastic_work_j": 2, "max_tensile": 3, "max_compressive": 4,
+              "max_shear": 5, "max_plastic_stretch": 6, "impulse_x": 7, "impulse_y": 8, "impulse_z": 9,
+              "contact_dissipated": 10, "max_penetration": 11, "max_correction": 12, "max_center_shift": 13,
+              "external_work": 14, "external_impulse_x": 15, "external_impulse_y": 16, "external_impulse_z": 17,
+              "external_steps": 18}
+
+
+def golden_names() -> list[str]:
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name: str):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    case = {k[len("case__"):]: z[k] for k in z.files if k.startswith("case__")}
+    ref = {k[len("ref__"):]: z[k] for k in z.files if k.startswith("ref__")}
+    return case, ref, str(z["precision"][0])
+
+
+def same_bits(a, b) -> bool:
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.dtype.kind == "f" and b.dtype.kind == "f" and a.dtype != b.dtype:
+        # A float32 fixture against a float64 output of the float lane: the
+        # widening is exact, so compare the widened bits.
+        a = a.astype(np.float64)
+        b = b.astype(np.float64)
+    return a.shape == b.shape and a.dtype == b.dtype and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def mismatches(expected: dict, actual: dict, keys) -> list[str]:
+    bad = []
+    for k in keys:
+        if k not in expected or k not in actual:
+            if k in expected or k in actual:
+                bad.append(k + " (missing)")
+            continue
+        if not same_bits(expected[k], actual[k]):
+            bad.append(k)
+    return bad
+
+
+def status_mismatches(expected: dict, actual: dict, skip=()) -> list[str]:
+    bad = []
+    for name, i in STATUS_U64.items():
+        if name not in skip and int(expected["status_u64"][i]) != int(actual["status_u64"][i]):
+            bad.append(f"{name}: {int(expected['status_u64'][i])} != {int(actual['status_u64'][i])}")
+    for name, i in STATUS_F64.items():
+        if name in skip:
+            continue
+        e, a = float(expected["status_f64"][i]), float(actual["status_f64"][i])
+        if not (e == a or (np.isnan(e) and np.isnan(a))):
+            bad.append(f"{name}: {e!r} != {a!r}")
+    return bad

@@ -1,0 +1,78 @@
+"""Generates the golden fixtures of tests/golden from the reference itself.
+
+Each fixture is one lattice case (inputs, as banjo_gb300.scenes builds them) and
+the outputs of the reference's own CPU lane on it: the reference harness
+(oracle/_ref/ref_harness, compiled from the reference's sources) runs
+buildLatticeSchedule, buildLatticeState and CpuLatticeBackend<float|double> and
+records the schedule, the final state, the RunStatus and the substep at which
+every bond broke. Run where the reference tree is present:
+
+    python tests/golden/make_golden.py
+
+Float-lane positions and velocities are stored as float32: the float backend
+widens float values, so the narrowing is exact.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from banjo_gb300 import scenes  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+INF = float("inf")
+
+
+def cases() -> dict:
+    out = {}
+    # The cantilever workload itself (32x8x8), 24 rigid steps: fracture from substep 19.
+    out["cantilever_24"] = (scenes.cantilever(steps=24), "float")
+    # Sphere impact on a 4-slab block with plastic flow, through shattering.
+    out["impact_small"] = (scenes.impact_block(nx=16, ny=10, nz=12, blocks=4, radius=0.03, speed=12.0, steps=30,
+                                               seed_point=5, seed_strength=21), "float")
+    # The same in the double (direct arithmetic) lane, shorter.
+    out["impact_small_double"] = (scenes.impact_block(nx=16, ny=10, nz=12, blocks=4, radius=0.03, speed=12.0,
+                                                      steps=10, seed_point=5, seed_strength=21), "double")
+    # A batched-trial box dropped a few millimetres onto the ground.
+    out["drop_small"] = (scenes.drop_trial(10, 6, 8, compliance=1e-6, break_strain=2e-3, drop_height=0.003, steps=20),
+                         "float")
+    # Radial bond damping on, and a ledge plane with finite footprints (reach cap) over the ground.
+    damped = scenes.drop_trial(12, 6, 10, compliance=3e-7, break_strain=1.5e-3, drop_height=0.004, steps=20)
+    ground = scenes.plane((0.0, 0.0, 0.0), node_radius=0.005)
+    ledge = scenes.plane((0.0, 0.002, 0.0), node_radius=0.005, restitution=0.3,
+                         footprints=((-0.04, 0.0, 0.02, 0.06), (0.04, 0.0, 0.02, 0.06)))
+    damped["settings"] = scenes.settings(damping_fraction=0.05, planes=[ledge, ground])
+    out["damped_ledge"] = (damped, "float")
+    return out
+
+
+def main() -> None:
+    oracle.build_reference()
+    for name, (case, precision) in cases().items():
+        ref = oracle.run_reference(case, precision=precision, per_substep=True)
+        data = {"case__" + k: np.asarray(v) for k, v in case.items()}
+        for k, v in ref.items():
+            if k in ("wall_seconds", "threads", "state_adj_bonds"):
+                continue
+            if precision == "float" and k in ("u", "u_prev", "v", "damage", "prev_tensile", "prev_compressive",
+                                              "prev_shear", "plastic_extension", "plastic_strain"):
+                narrowed = v.astype(np.float32)
+                assert np.array_equal(narrowed.astype(np.float64), v), k
+                v = narrowed
+            data["ref__" + k] = v
+        data["precision"] = np.array([precision])
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **data)
+        su = ref["status_u64"]
+        print(f"{name}: N={case['node_count'][0]} B={case['bond_count'][0]} substeps={su[0]} "
+              f"broken={su[4]} rounds={su[3]} first={su[1]} size={os.path.getsize(path) // 1024} KiB")
+
+
+if __name__ == "__main__":
+    main()
