@@ -115,6 +115,10 @@ def make_case(workload: str) -> tuple[dict, str]:
         return scenes.impact_block(), "impact 256x128x128, 4194304 nodes, 37340160 bonds, 32 slabs, sphere 10 m/s"
     if workload == "cantilever":
         return scenes.cantilever(), "cantilever 32x8x8, 2048 nodes, 15648 bonds, pinned, loaded"
+    if workload == "impact_mid":
+        # The impact scene at an eighth of the volume, for profiler captures.
+        case = scenes.impact_block(nx=128, ny=64, nz=64, radius=0.1)
+        return case, f"impact 128x64x64, {int(case['node_count'][0])} nodes, {int(case['bond_count'][0])} bonds, 32 slabs"
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -150,12 +154,19 @@ def distributed():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        # One GPU per rank, made the only visible device before any CUDA call,
+        # so the lattice library and torch agree on it without coordination.
+        visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+        if visible:
+            os.environ["CUDA_VISIBLE_DEVICES"] = visible.split(",")[local]
+        else:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
         import torch
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
+        torch.cuda.set_device(0)
         dist.init_process_group("nccl")
-        return rank, world, local, dist, torch
+        return rank, world, 0, dist, torch
     return rank, world, local, None, None
 
 
@@ -183,8 +194,6 @@ def sum_over_ranks(x: float, dist, torch) -> float:
 
 def run_gb300(args) -> None:
     rank, world, local, dist, torch = distributed()
-    if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     from banjo_gb300 import build as lib_build
     from banjo_gb300 import lattice
 
@@ -331,7 +340,7 @@ def main() -> None:
     p.add_argument("--steps", type=int, default=6)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="impact", choices=["impact", "cantilever"])
+    p.add_argument("--workload", default="impact", choices=["impact", "impact_mid", "cantilever"])
     p.add_argument("--profile-substeps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     args = p.parse_args()
