@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 DEVICE_FP = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
 HOST_FP = "-ffp-contract=off,-fno-fast-math"
 
-SOURCES_CU = ["gbl_device.cu"]
+SOURCES_CU = ["gbl_device.cu", "gbl_noalloc.cu"]
 SOURCES_CPP = ["gbl_host.cpp"]
 HEADERS = ["gbl_internal.hpp", "gbl_math.cuh", "gbl_kernels.cuh"]
 

@@ -279,6 +279,27 @@ gbl_result gbl_kernels_per_substep(gbl_backend *backend, uint64_t *count);
  * gbl_run with max_steps = substeps and exit rules off. */
 gbl_result gbl_profile_phases(gbl_backend *backend, uint64_t substeps, double *phase_ms);
 
+/* The bonds that broke between two aliveness snapshots (one byte per bond,
+ * schedule order, non-zero = alive), listed in schedule order -- without
+ * allocating anything. This entry point has no counterpart in the reference.
+ * It is for callers that must not allocate device memory while they run:
+ * a real-time frame loop, where cudaMalloc/cudaFree would synchronise the
+ * device and stall the frame, or a caller recording its work into a CUDA
+ * graph, where allocation calls cannot be captured.
+ *
+ * All pointers are device pointers owned by the caller: `broken` has room for
+ * bond_count indices, `broken_count` receives the count. The work is enqueued
+ * on `cuda_stream` (null: the default stream) and the outputs are ready when
+ * the stream reaches that point. At most 134,217,728 bonds (larger counts are
+ * refused with GBL_INVALID_ARGUMENT): the scratch is a fixed 64 KiB static
+ * device array, held by every GPU that loads the library until the process
+ * exits. The first call on a device looks up that array's device address
+ * (with the device current); make it before any stream capture. Calls share
+ * the array: calls whose work overlaps on the GPU race, so order them on one
+ * stream. */
+gbl_result gbl_broken_between_noalloc(const uint8_t *alive_before, const uint8_t *alive_after, uint64_t bond_count,
+                                      uint32_t *broken, uint32_t *broken_count, void *cuda_stream);
+
 /* sizeof of a struct of this header by its name ("gbl_step_settings", ...),
  * 0 for an unknown name: lets a binding check its own layout. */
 size_t gbl_struct_size(const char *name);
