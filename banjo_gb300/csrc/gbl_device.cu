@@ -75,9 +75,13 @@ public:
 
 template <class R> class Backend final : public BackendBase {
     static constexpr bool kDirect = std::is_same<R, double>::value;
+    // x0, u, v of one slab's candidates, staged for the serial contact pass.
+    static constexpr unsigned kSphereSmem = 3 * kCandidatesPerBlock * sizeof(Q4<R>);
 
 public:
     Backend(Schedule s, unsigned threads_per_block) : sched_(std::move(s)), tpb_(threads_per_block) {
+        check(cudaFuncSetAttribute(kSpherePass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSphereSmem),
+              "contact pass shared memory");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "stream");
         stream_ = own_stream_;
         check(cudaEventCreate(&ev0_), "event");
@@ -133,8 +137,10 @@ public:
         arena_.reserve(d.rec, B); arena_.reserve(d.geo, B); arena_.reserve(d.prev, B); arena_.reserve(d.thr4, B);
         arena_.reserve(d.thr2, B); arena_.reserve(d.plastic, B); arena_.reserve(d.lambda, B); arena_.reserve(d.mode, B);
         arena_.reserve(d.ev_bits, d.words_b + 1); arena_.reserve(d.ev_tile, d.tiles_b + 1); arena_.reserve(d.ev_list, B + 1);
-        arena_.reserve(d.ev_broke, B); arena_.reserve(d.ev_removed, B); arena_.reserve(d.ev_plastic, B);
-        arena_.reserve(d.ev_damage, B);
+        arena_.reserve(d.ev_removed, B); arena_.reserve(d.ev_packed, B + 1); arena_.reserve(d.ev_prefix, B + 1);
+        arena_.reserve(d.dmg_bits, d.words_b + 1); arena_.reserve(d.dmg_tile, d.tiles_b + 1);
+        arena_.reserve(d.dmg_list, B + 1); arena_.reserve(d.ev_damage, B); arena_.reserve(d.dmg_value, B + 1);
+        arena_.reserve(d.tile_plastic, d.tiles_b + 1); arena_.reserve(d.tile_removed, d.tiles_b + 1);
         arena_.reserve(d.node_block_begin, sched_.block_count + 1);
         arena_.reserve(d.cand_list, static_cast<std::size_t>(sched_.block_count) * kCandidatesPerBlock);
         arena_.reserve(d.cand_count, sched_.block_count);
@@ -200,6 +206,9 @@ public:
         }
         zero(d.lambda, B);
         zero(d.ev_bits, d.words_b + 1);
+        zero(d.dmg_bits, d.words_b + 1);
+        zero(d.tile_plastic, d.tiles_b + 1);
+        zero(d.tile_removed, d.tiles_b + 1);
         copy(d.node_block_begin, sched_.node_block_begin);
         zero(d.cand_count, sched_.block_count);
         copy(work_d_, work_h_);
@@ -617,7 +626,7 @@ private:
         kKick<R><<<nodes, kThreads, 0, stream_>>>(L, S);
         if (S.sphere_enabled) kCandidates<R><<<sched_.block_count, 1024, 0, stream_>>>(L);
         mark(3);
-        if (S.sphere_enabled) kSpherePass<R><<<1, 1, 0, stream_>>>(L, S, 1);
+        if (S.sphere_enabled) kSpherePass<R><<<1, kSphereThreads, kSphereSmem, stream_>>>(L, S, 1);
         mark(4);
         const unsigned I = S.iterations;
         for (unsigned it = 0; it < I; ++it) {
@@ -639,14 +648,16 @@ private:
             kSupportVelocity<R><<<nodes, kThreads, 0, stream_>>>(L, S);
             mark(9);
         }
-        if (S.sphere_enabled) kSpherePass<R><<<1, 1, 0, stream_>>>(L, S, 2);
+        if (S.sphere_enabled) kSpherePass<R><<<1, kSphereThreads, kSphereSmem, stream_>>>(L, S, 2);
         mark(10);
         kStrainAll<R, kDirect><<<nodes, kThreads, 0, stream_>>>(L);
         mark(11);
         if (plastic_) kEndSample<R, kDirect, true><<<std::max(1U, dev_.tiles_b), kThreads, 0, stream_>>>(L, S);
         else kEndSample<R, kDirect, false><<<std::max(1U, dev_.tiles_b), kThreads, 0, stream_>>>(L, S);
-        kScanTiles<R><<<1, 1024, 0, stream_>>>(L);
+        kScanTiles<R><<<1, 1024, 0, stream_>>>(L, plastic_ ? 1 : 0);
         kEmitEvents<R><<<gridFor(dev_.tiles_b, kThreads / 32), kThreads, 0, stream_>>>(L);
+        kScanRemoved<R><<<1, 1024, 0, stream_>>>(L);
+        kLedgerBroken<R><<<152U * 4U, kThreads, 0, stream_>>>(L);
         mark(12);
         kLedger<R><<<1, 1, 0, stream_>>>(L, S);
         mark(13);

@@ -55,7 +55,9 @@ struct Ctl {
     unsigned long long loads_remaining;
     // transient
     unsigned full_restart, dirty_count, ffb_count, loads_kicked;
-    unsigned event_count, ext_count; // loaded nodes; set between runs, read by the kick and the ledger
+    unsigned event_count, ext_count; // broken bonds this substep; loaded nodes (set between runs)
+    unsigned dmg_count, energy_gain;  // damage-record candidates; any broken bond passed the gain test
+    double plastic_substep, removed_substep;
 };
 
 constexpr unsigned kErrExternalOverflow = 1;
@@ -74,10 +76,16 @@ template <class R> struct Dev {
     Q2<R> *thr2, *plastic;
     R *lambda;
     std::uint8_t *mode;
+    // Substep ledger scratch. ev_*: broken bonds (bit per bond, per-tile count
+    // then offset, ordered list, removed energy by bond and packed in list
+    // order, in-tile inclusive prefix); dmg_*: bonds whose damage passed the
+    // run maximum (the candidates of the damage-record scan); tile_*: per
+    // end-sample tile FP64 partials and their prefix.
     std::uint32_t *ev_bits, *ev_tile, *ev_list;
-    std::uint8_t *ev_broke;
-    double *ev_removed, *ev_plastic;
-    float *ev_damage;
+    double *ev_removed, *ev_packed, *ev_prefix;
+    std::uint32_t *dmg_bits, *dmg_tile, *dmg_list;
+    float *ev_damage, *dmg_value;
+    double *tile_plastic, *tile_removed;
     std::uint32_t *node_block_begin, *cand_list, *cand_count, *dirty_list, *ffb;
     Q4<R> *ext_force;     // applied force (backend precision), w != 0 marks a loaded node
     double *ext_req;      // requested force, 3 per node
@@ -387,18 +395,20 @@ __global__ void __launch_bounds__(1024) kCandidates(Dev<R> L) {
 // Sphere contact, one thread, candidates in slab then node order
 // (LatticePhysics.hpp:1322-1428).
 // ---------------------------------------------------------------------------
+// One candidate against the sphere. The node's data arrive staged in shared
+// memory (x0, u, v with the mass in v.w) and are updated there.
 template <class R>
-__device__ void sphereNode(const Dev<R> &L, const Settings<R> &S, Sphere<R> &sp, std::uint32_t i, bool correct,
-                           ContactAcc &acc) {
-    const Q4<R> vq = L.v[i];
+__device__ void sphereNode(const Settings<R> &S, Sphere<R> &sp, const Q4<R> &x0q, Q4<R> &uq_ref, Q4<R> &vq_ref,
+                           bool correct, ContactAcc &acc) {
+    const Q4<R> vq = vq_ref;
     const R mass = vq.w;
     if (mass <= R(0)) return;
     const R dt = S.dt;
     const R ism = R(1) / sp.mass;
     const R iin = R(1) / sp.inertia;
     const R cr = sp.radius + S.c_node_radius;
-    const Q4<R> uq = L.u[i];
-    const V3<R> r = (xyz(L.x0[i]) + xyz(uq)) - sp.center;
+    const Q4<R> uq = uq_ref;
+    const V3<R> r = (xyz(x0q) + xyz(uq)) - sp.center;
     const R distance = length(r);
     const V3<R> normal = normalized(r);
     const R gap = distance - cr;
@@ -434,7 +444,7 @@ __device__ void sphereNode(const Dev<R> &L, const Settings<R> &S, Sphere<R> &sp,
             const R fi = stick <= S.c_static * ni ? stick : minR(stick, S.c_dynamic * ni);
             apply(-fi * d);
         }
-        L.v[i] = Q4<R>{nv.x, nv.y, nv.z, mass};
+        vq_ref = Q4<R>{nv.x, nv.y, nv.z, mass};
         acc.dissipated += static_cast<double>(before - R(0.5) * mass * dot(nv, nv));
         ++acc.impulse_contacts;
     }
@@ -444,55 +454,81 @@ __device__ void sphereNode(const Dev<R> &L, const Settings<R> &S, Sphere<R> &sp,
         const V3<R> ns = (corr * inm / sum) * normal;
         const V3<R> ss = -((corr * ism / sum) * normal);
         const V3<R> un = xyz(uq) + ns;
-        L.u[i] = Q4<R>{un.x, un.y, un.z, uq.w};
+        uq_ref = Q4<R>{un.x, un.y, un.z, uq.w};
         sp.center = sp.center + ss;
         if (corr > R(acc.max_correction)) acc.max_correction = static_cast<double>(corr);
     }
 }
 
+// The sequential contact pass (LatticePhysics.hpp:1389-1428), one CTA. The
+// candidates of a slab are staged into shared memory by the whole CTA, one
+// thread runs the contacts in list order -- the order is physics: every
+// contact moves the sphere the next one sees -- and the CTA writes the nodes
+// back. What the reference does per candidate after its contact (pass 1:
+// record the approach speed and predict; pass 2: the support velocity
+// response) touches that node alone, so it runs in the parallel write-back.
+constexpr unsigned kSphereThreads = 1024;
+
 template <class R>
-__global__ void kSpherePass(Dev<R> L, Settings<R> S, int pass) {
-    if (L.ctl->stop || threadIdx.x != 0 || blockIdx.x != 0) return;
-    Sphere<R> sp = *L.sphere;
-    if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
-    ContactAcc acc = L.ctl->contact;
-    const V3<R> c0 = sp.center;
-    const R e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+__global__ void __launch_bounds__(kSphereThreads) kSpherePass(Dev<R> L, Settings<R> S, int pass) {
+    extern __shared__ __align__(16) unsigned char sphere_smem[];
+    Q4<R> *sx = reinterpret_cast<Q4<R> *>(sphere_smem);
+    Q4<R> *su = sx + kCandidatesPerBlock;
+    Q4<R> *sv = su + kCandidatesPerBlock;
+    if (L.ctl->stop) return;
+    Sphere<R> sp{};
+    ContactAcc acc{};
+    V3<R> c0{};
+    R e0 = R(0);
+    if (threadIdx.x == 0) {
+        sp = *L.sphere;
+        if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
+        acc = L.ctl->contact;
+        c0 = sp.center;
+        e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+    }
     for (std::uint32_t b = 0; b < L.blocks; ++b) {
         const std::uint32_t n = L.cand_count[b];
-        for (std::uint32_t k = 0; k < n; ++k) {
-            const std::uint32_t i = L.cand_list[b * kCandidatesPerBlock + k];
-            sphereNode(L, S, sp, i, pass == 2, acc);
+        if (n == 0) continue;
+        const std::uint32_t *list = L.cand_list + b * kCandidatesPerBlock;
+        for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+            const std::uint32_t i = list[k];
+            sx[k] = L.x0[i];
+            su[k] = L.u[i];
+            sv[k] = L.v[i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (std::uint32_t k = 0; k < n; ++k) sphereNode(S, sp, sx[k], su[k], sv[k], pass == 2, acc);
+        __syncthreads();
+        for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+            const std::uint32_t i = list[k];
+            const Q4<R> vq = sv[k];
+            const Q4<R> uq = su[k];
             if (pass == 1) {
-                const Q4<R> vq = L.v[i];
                 for (std::uint32_t p = 0; p < S.plane_count; ++p)
                     L.approach[p * L.N + i] = dot(xyz(vq), S.planes[p].normal);
-                const Q4<R> uq = L.u[i];
                 const V3<R> un = xyz(uq) + S.dt * xyz(vq);
                 L.u[i] = Q4<R>{un.x, un.y, un.z, uq.w};
+                L.v[i] = vq;
+            } else {
+                V3<R> vel = xyz(vq);
+                for (std::uint32_t p = 0; p < S.plane_count; ++p)
+                    if (L.engaged[p * L.N + i]) vel = supportVelocity(S.planes[p], vel, L.approach[p * L.N + i]);
+                L.u[i] = uq;
+                L.v[i] = Q4<R>{vel.x, vel.y, vel.z, vq.w};
             }
         }
+        __syncthreads();
     }
-    const R e1 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
-    acc.dissipated += static_cast<double>(e0 - e1);
-    if (pass == 2) {
-        for (std::uint32_t b = 0; b < L.blocks; ++b) {
-            const std::uint32_t n = L.cand_count[b];
-            for (std::uint32_t k = 0; k < n; ++k) {
-                const std::uint32_t i = L.cand_list[b * kCandidatesPerBlock + k];
-                for (std::uint32_t p = 0; p < S.plane_count; ++p) {
-                    if (!L.engaged[p * L.N + i]) continue;
-                    const Q4<R> vq = L.v[i];
-                    const V3<R> nv = supportVelocity(S.planes[p], xyz(vq), L.approach[p * L.N + i]);
-                    L.v[i] = Q4<R>{nv.x, nv.y, nv.z, vq.w};
-                }
-            }
-        }
+    if (threadIdx.x == 0) {
+        const R e1 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+        acc.dissipated += static_cast<double>(e0 - e1);
+        const R shift = length(sp.center - c0);
+        if (shift > R(acc.max_center_shift)) acc.max_center_shift = static_cast<double>(shift);
+        *L.sphere = sp;
+        L.ctl->contact = acc;
     }
-    const R shift = length(sp.center - c0);
-    if (shift > R(acc.max_center_shift)) acc.max_center_shift = static_cast<double>(shift);
-    *L.sphere = sp;
-    L.ctl->contact = acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -614,28 +650,39 @@ __global__ void __launch_bounds__(kThreads) kSupportVelocity(Dev<R> L, Settings<
 
 // ---------------------------------------------------------------------------
 // End-of-substep sample, plastic return and failure (LatticePhysics.hpp:1018-1114).
-// One thread per bond in schedule order. A bond is an event when it breaks,
-// flows, or raises its damage above the run's maximum; events are flagged in
-// one bit per bond and folded in bond order by kLedger.
+// One thread per bond in schedule order; a CTA is one "tile" of 256 bonds.
+// The reference folds its FP64 ledgers one bond at a time in bond order
+// (CpuLatticeBackend.cpp:446-478). Here every reduction has a fixed order that
+// depends on the bond order only, never on thread timing: plastic work is
+// summed per tile by a fixed shuffle tree and the tiles in index order; broken
+// bonds and damage-record candidates are flagged one bit per bond and listed
+// in bond order by kScanTiles/kEmitEvents.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned floatBits(float x) { return __float_as_uint(x); }
 
+// Sum over a warp in a fixed order (lane 0 holds the result).
+__device__ __forceinline__ double warpSumFixed(double x) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffU, x, o);
+    return x;
+}
+
 template <class R, bool Direct, bool Plastic>
 __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) {
-    __shared__ unsigned tile_count[kThreads / 32];
+    __shared__ unsigned tile_count[kThreads / 32], tile_dmg[kThreads / 32];
+    __shared__ double tile_work[kThreads / 32];
     __shared__ unsigned peak[4];
     if (L.ctl->stop) return;
     const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (threadIdx.x < 4) peak[threadIdx.x] = 0;
     __syncthreads();
-    bool event = false;
+    bool broke = false, dmg_candidate = false;
+    double plastic_work = 0.0;
     if (j < L.B) {
         const BondRec<R> rec = L.rec[j];
         if (!(rec.a & kDeadBit)) {
             const std::uint32_t a = rec.a, b = rec.b;
             const Q4<R> g = L.geo[j];
             const V3<R> edge{g.x, g.y, g.z};
-            double plastic_work = 0.0;
             float plastic_stretch = 0.0F;
             R pext = R(0);
             if (Plastic) {
@@ -685,7 +732,7 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
             }
             L.prev[j] = pv;
             const float dmg = static_cast<float>(pv.w);
-            const bool broke = pv.w >= R(1);
+            broke = pv.w >= R(1);
             if (broke) {
                 const R cc = g.w;
                 R energy = R(0);
@@ -698,12 +745,10 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
                 L.nbr[L.slot_b[j]].w = R(0);
                 L.ev_removed[j] = static_cast<double>(energy);
             }
-            event = broke || plastic_work != 0.0 || static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6;
-            if (event) {
-                L.ev_broke[j] = broke ? 1 : 0;
-                L.ev_plastic[j] = plastic_work;
-                L.ev_damage[j] = dmg;
-            }
+            // A bond can raise the run's damage maximum only if it exceeds the
+            // maximum as the substep began (CpuLatticeBackend.cpp:462-465).
+            dmg_candidate = static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6;
+            if (dmg_candidate) L.ev_damage[j] = dmg;
             // Peaks are non-negative, so their bit patterns order as the values do.
             atomicMax(&peak[0], floatBits(static_cast<float>(pt)));
             atomicMax(&peak[1], floatBits(static_cast<float>(pc)));
@@ -711,16 +756,31 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
             if (Plastic && S.yield_stretch > R(0)) atomicMax(&peak[3], floatBits(plastic_stretch));
         }
     }
-    const unsigned bits = __ballot_sync(0xffffffffU, event);
+    const unsigned bits = __ballot_sync(0xffffffffU, broke);
+    const unsigned dbits = __ballot_sync(0xffffffffU, dmg_candidate);
+    double work = 0.0;
+    if (Plastic) work = warpSumFixed(plastic_work);
     if ((threadIdx.x & 31) == 0) {
-        if (j / 32 < L.words_b) L.ev_bits[j / 32] = bits;
+        if (j / 32 < L.words_b) {
+            L.ev_bits[j / 32] = bits;
+            L.dmg_bits[j / 32] = dbits;
+        }
         tile_count[threadIdx.x / 32] = __popc(bits);
+        tile_dmg[threadIdx.x / 32] = __popc(dbits);
+        tile_work[threadIdx.x / 32] = work;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned total = 0;
-        for (int w = 0; w < kThreads / 32; ++w) total += tile_count[w];
+        unsigned total = 0, dtotal = 0;
+        double wsum = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) {
+            total += tile_count[w];
+            dtotal += tile_dmg[w];
+            wsum += tile_work[w];
+        }
         L.ev_tile[blockIdx.x] = total;
+        L.dmg_tile[blockIdx.x] = dtotal;
+        L.tile_plastic[blockIdx.x] = wsum;
         if (peak[0]) atomicMax(&L.ctl->max_t, peak[0]);
         if (peak[1]) atomicMax(&L.ctl->max_c, peak[1]);
         if (peak[2]) atomicMax(&L.ctl->max_s, peak[2]);
@@ -728,25 +788,15 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
     }
 }
 
-// Exclusive scan of the per-tile event counts, one CTA.
-template <class R>
-__global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L) {
-    if (L.ctl->stop) return;
-    __shared__ unsigned warp_sum[32];
-    __shared__ unsigned carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const unsigned T = L.tiles_b;
-    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
-    const unsigned first = threadIdx.x * per;
-    unsigned local = 0;
-    for (unsigned t = first; t < first + per && t < T; ++t) local += L.ev_tile[t];
-    unsigned x = local;
+// Block-wide exclusive scan helper for one value per thread (1024 threads).
+__device__ __forceinline__ unsigned blockExclusiveScan(unsigned x, unsigned *warp_sum, unsigned &total) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x / 32;
+    unsigned inc = x;
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
-        if ((threadIdx.x & 31) >= static_cast<unsigned>(o)) x += y;
+        const unsigned y = __shfl_up_sync(0xffffffffU, inc, o);
+        if (lane >= static_cast<unsigned>(o)) inc += y;
     }
-    if ((threadIdx.x & 31) == 31) warp_sum[threadIdx.x / 32] = x;
+    if (lane == 31) warp_sum[warp] = inc;
     __syncthreads();
     if (threadIdx.x < 32) {
         unsigned s = warp_sum[threadIdx.x];
@@ -757,46 +807,188 @@ __global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L) {
         warp_sum[threadIdx.x] = s;
     }
     __syncthreads();
-    unsigned run = x - local + (threadIdx.x >= 32 ? warp_sum[threadIdx.x / 32 - 1] : 0U);
-    for (unsigned t = first; t < first + per && t < T; ++t) {
-        const unsigned n = L.ev_tile[t];
-        L.ev_tile[t] = run;
-        run += n;
-    }
-    if (threadIdx.x == blockDim.x - 1) L.ctl->event_count = run;
+    total = warp_sum[31];
+    const unsigned before = (warp ? warp_sum[warp - 1] : 0U) + inc - x;
+    __syncthreads();
+    return before;
 }
 
-// Writes the event bond indices in bond order: one warp per end-sample tile.
+// One CTA: exclusive scans of the per-tile counts of broken bonds and of
+// damage candidates (turned into offsets in place), and the plastic work of
+// the substep summed over the tiles in a fixed order (each thread a contiguous
+// run of tiles, then a fixed tree over the threads).
+template <class R>
+__global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L, int plastic) {
+    __shared__ unsigned warp_sum[32];
+    __shared__ double partial[1024];
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    const unsigned T = L.tiles_b;
+    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
+    const unsigned first = threadIdx.x * per;
+    const unsigned last = first + per < T ? first + per : T;
+    unsigned nb = 0, nd = 0;
+    double work = 0.0;
+    for (unsigned t = first; t < last; ++t) {
+        nb += L.ev_tile[t];
+        nd += L.dmg_tile[t];
+        if (plastic) work += L.tile_plastic[t];
+    }
+    unsigned total_b = 0, total_d = 0;
+    unsigned run_b = blockExclusiveScan(nb, warp_sum, total_b);
+    unsigned run_d = blockExclusiveScan(nd, warp_sum, total_d);
+    for (unsigned t = first; t < last; ++t) {
+        const unsigned b = L.ev_tile[t], d = L.dmg_tile[t];
+        L.ev_tile[t] = run_b;
+        L.dmg_tile[t] = run_d;
+        run_b += b;
+        run_d += d;
+    }
+    partial[threadIdx.x] = work;
+    __syncthreads();
+    for (unsigned s = 512; s > 0; s >>= 1) {
+        if (threadIdx.x < s) partial[threadIdx.x] += partial[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        c.event_count = total_b;
+        c.dmg_count = total_d;
+        c.plastic_substep = plastic ? partial[0] : 0.0;
+        c.removed_substep = 0.0;
+        c.energy_gain = 0;
+        c.dirty_count = 0; // the restart of this substep has consumed the list
+    }
+}
+
+// One warp per end-sample tile: writes the tile's broken bonds in bond order
+// with their removed energy and its in-tile inclusive prefix (a fixed order:
+// sequential inside each 32-bond word, a shuffle scan across the words), the
+// tile's removed-energy total, and the tile's damage candidates in order.
 template <class R>
 __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
-    if (L.ctl->stop || L.ctl->event_count == 0) return;
+    const Ctl &c = *L.ctl;
+    if (c.stop || (c.event_count == 0 && c.dmg_count == 0)) return;
     const unsigned tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const unsigned lane = threadIdx.x & 31;
     if (tile >= L.tiles_b) return;
-    const unsigned base = L.ev_tile[tile];
-    const unsigned next = tile + 1 < L.tiles_b ? L.ev_tile[tile + 1] : L.ctl->event_count;
-    if (next == base) return;
     constexpr unsigned kWords = kThreads / 32;
     const unsigned w = tile * kWords + lane;
-    unsigned bits = (lane < kWords && w < L.words_b) ? L.ev_bits[w] : 0U;
-    unsigned n = __popc(bits), x = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
-        if (lane >= static_cast<unsigned>(o)) x += y;
+    const bool word = lane < kWords && w < L.words_b;
+    const unsigned base = L.ev_tile[tile];
+    const unsigned next = tile + 1 < L.tiles_b ? L.ev_tile[tile + 1] : c.event_count;
+    if (next != base) {
+        unsigned bits = word ? L.ev_bits[w] : 0U;
+        double own = 0.0;
+        for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[w * 32 + static_cast<unsigned>(__ffs(m) - 1)];
+        unsigned n = __popc(bits), x = n;
+        double inclusive = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
+            const double yb = __shfl_up_sync(0xffffffffU, inclusive, o);
+            if (lane >= static_cast<unsigned>(o)) { x += y; inclusive += yb; }
+        }
+        const double exclusive = __shfl_up_sync(0xffffffffU, inclusive, 1);
+        const double tile_total = __shfl_sync(0xffffffffU, inclusive, 31);
+        unsigned at = base + x - n;
+        double run = lane == 0 ? 0.0 : exclusive;
+        for (; bits; bits &= bits - 1) {
+            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(bits) - 1);
+            const double e = L.ev_removed[j];
+            run += e;
+            L.ev_list[at] = j;
+            L.ev_packed[at] = e;
+            L.ev_prefix[at] = run;
+            ++at;
+        }
+        if (lane == 0) L.tile_removed[tile] = tile_total;
+    } else if (lane == 0) {
+        L.tile_removed[tile] = 0.0;
     }
-    unsigned at = base + x - n;
-    while (bits) {
-        const int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        L.ev_list[at++] = w * 32 + static_cast<unsigned>(b);
+    const unsigned dbase = L.dmg_tile[tile];
+    const unsigned dnext = tile + 1 < L.tiles_b ? L.dmg_tile[tile + 1] : c.dmg_count;
+    if (dnext != dbase) {
+        unsigned bits = word ? L.dmg_bits[w] : 0U;
+        unsigned n = __popc(bits), x = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
+            if (lane >= static_cast<unsigned>(o)) x += y;
+        }
+        unsigned at = dbase + x - n;
+        for (; bits; bits &= bits - 1) {
+            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(bits) - 1);
+            L.dmg_list[at] = j;
+            L.dmg_value[at] = L.ev_damage[j];
+            ++at;
+        }
+    }
+}
+
+// One CTA: exclusive prefix of the tiles' removed energy in tile order (each
+// thread a contiguous run, a fixed tree over the threads), in place, and the
+// substep's total.
+template <class R>
+__global__ void __launch_bounds__(1024) kScanRemoved(Dev<R> L) {
+    __shared__ double part[1024];
+    Ctl &c = *L.ctl;
+    if (c.stop || c.event_count == 0) return;
+    const unsigned T = L.tiles_b;
+    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
+    const unsigned first = threadIdx.x * per;
+    const unsigned last = first + per < T ? first + per : T;
+    double own = 0.0;
+    for (unsigned t = first; t < last; ++t) own += L.tile_removed[t];
+    part[threadIdx.x] = own;
+    __syncthreads();
+    // Hillis-Steele inclusive scan over the 1024 partials: a fixed order.
+    for (unsigned o = 1; o < 1024; o <<= 1) {
+        const double y = threadIdx.x >= o ? part[threadIdx.x - o] : 0.0;
+        __syncthreads();
+        part[threadIdx.x] += y;
+        __syncthreads();
+    }
+    double run = part[threadIdx.x] - own;
+    for (unsigned t = first; t < last; ++t) {
+        const double e = L.tile_removed[t];
+        L.tile_removed[t] = run;
+        run += e;
+    }
+    if (threadIdx.x == 1023) c.removed_substep = part[1023];
+}
+
+// Parallel over this substep's broken bonds, in list order: the energy-gain
+// test of each bond against the running removed energy it would see
+// (CpuLatticeBackend.cpp:469-474), the first-failure list, and the dirty
+// marks and list of the next substep's restart (CpuLatticeBackend.cpp:476-477).
+template <class R>
+__global__ void __launch_bounds__(kThreads) kLedgerBroken(Dev<R> L) {
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    const unsigned n = c.event_count;
+    const bool first_round = c.broken_bonds == 0;
+    const double prior = c.removed_energy;
+    const double fraction = c.energy_flat_fraction;
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const std::uint32_t j = L.ev_list[e];
+        const double running = prior + (L.tile_removed[j / kThreads] + L.ev_prefix[e]);
+        const double removed = L.ev_packed[e];
+        if (removed > fraction * (running < 1.0e-12 ? 1.0e-12 : running)) atomicOr(&c.energy_gain, 1U);
+        if (first_round) L.ffb[e] = j;
+        const std::uint32_t ends[2] = {L.rec[j].a & ~kDeadBit, L.rec[j].b};
+        for (int q = 0; q < 2; ++q) {
+            const std::uint32_t node = ends[q];
+            unsigned *word = reinterpret_cast<unsigned *>(L.dirty + (node & ~3U));
+            const unsigned bit = 1U << (8 * (node & 3U));
+            if (!(atomicOr(word, bit) & bit)) L.dirty_list[atomicAdd(&c.dirty_count, 1U)] = node;
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
-// The serial tail of a substep, one thread: the external-load ledger, the FP64
-// failure and plastic ledgers in bond order (CpuLatticeBackend.cpp:441-488),
-// the sphere drift and support contact, the failure-round bookkeeping and the
-// exit rules (CpuLatticeBackend.cpp:279-298).
+// The serial tail of a substep, one thread: the external-load ledger (node
+// order), the substep's FP64 sums into the run totals, the damage-record scan
+// over its (few) candidates in bond order, the sphere drift and support
+// contact, the failure-round bookkeeping and the exit rules
+// (CpuLatticeBackend.cpp:279-298, 441-488).
 // ---------------------------------------------------------------------------
 template <class R>
 __global__ void kLedger(Dev<R> L, Settings<R> S) {
@@ -827,41 +1019,29 @@ __global__ void kLedger(Dev<R> L, Settings<R> S) {
         g.work = g.work + ch[6];
         c.loads_remaining -= 1;
     }
-    c.dirty_count = 0;
     c.full_restart = 0;
-    const bool first_round = c.broken_bonds == 0;
-    bool any = false;
-    for (unsigned e = 0; e < c.event_count; ++e) {
-        const std::uint32_t j = L.ev_list[e];
-        c.plastic_work += L.ev_plastic[j];
-        const float dmg = L.ev_damage[j];
+    c.plastic_work += c.plastic_substep;
+    for (unsigned e = 0; e < c.dmg_count; ++e) {
+        const float dmg = L.dmg_value[e];
         if (static_cast<double>(dmg) > c.max_damage + 1.0e-6) {
             c.max_damage = dmg;
             c.last_damage_gain_step = step;
         }
-        if (!L.ev_broke[j]) continue;
-        any = true;
-        if (first_round) L.ffb[c.ffb_count++] = j;
-        const double removed = L.ev_removed[j];
-        c.removed_energy += removed;
-        if (removed > c.energy_flat_fraction * (c.removed_energy < 1.0e-12 ? 1.0e-12 : c.removed_energy))
-            c.last_energy_gain_step = step;
-        ++c.broken_bonds;
-        const std::uint32_t ends[2] = {L.rec[j].a & ~kDeadBit, L.rec[j].b};
-        for (int q = 0; q < 2; ++q)
-            if (!L.dirty[ends[q]]) {
-                L.dirty[ends[q]] = 1;
-                L.dirty_list[c.dirty_count++] = ends[q];
-            }
     }
-    c.event_count = 0;
+    const unsigned broken = c.event_count;
+    if (broken) {
+        if (c.broken_bonds == 0) c.ffb_count = broken;
+        c.removed_energy += c.removed_substep;
+        if (c.energy_gain) c.last_energy_gain_step = step;
+        c.broken_bonds += broken;
+    }
     Sphere<R> sp = *L.sphere;
     if (!S.sphere_enabled) sp.velocity = sp.velocity + S.dt * S.gravity;
     sp.center = sp.center + S.dt * sp.velocity;
     sphereSupport(S, sp, c.contact);
     *L.sphere = sp;
     c.total_steps = step + 1;
-    if (any) {
+    if (broken) {
         if (c.first_failure_step == ~0ULL) c.first_failure_step = step;
         c.last_failure_step = step;
         ++c.failure_rounds;

@@ -58,7 +58,15 @@ def mismatches(expected: dict, actual: dict, keys) -> list[str]:
     return bad
 
 
-def status_mismatches(expected: dict, actual: dict, skip=()) -> list[str]:
+# The two FP64 ledgers the reference folds one bond at a time. The GPU sums
+# them in a fixed parallel order (deterministic, but not the serial order), so
+# against a serial runner they are held to the tolerance the reference gave its
+# own CUDA backend for them, 1e-12 relative (tests/fast_lattice_tests.cpp:517-521).
+LEDGERS = ("removed_energy_j", "plastic_work_j")
+LEDGER_RTOL = 1e-12
+
+
+def status_mismatches(expected: dict, actual: dict, skip=(), ledger_rtol: float = 0.0) -> list[str]:
     bad = []
     for name, i in STATUS_U64.items():
         if name not in skip and int(expected["status_u64"][i]) != int(actual["status_u64"][i]):
@@ -67,6 +75,10 @@ def status_mismatches(expected: dict, actual: dict, skip=()) -> list[str]:
         if name in skip:
             continue
         e, a = float(expected["status_f64"][i]), float(actual["status_f64"][i])
+        if name in LEDGERS and ledger_rtol > 0.0:
+            if abs(e - a) > ledger_rtol * max(abs(e), 1e-300):
+                bad.append(f"{name}: {e!r} != {a!r} beyond {ledger_rtol:g} relative")
+            continue
         if not (e == a or (np.isnan(e) and np.isnan(a))):
             bad.append(f"{name}: {e!r} != {a!r}")
     return bad

@@ -2,13 +2,16 @@
 
 Bar (the reference's own CUDA test, tests/fast_lattice_tests.cpp:480-524):
 positions, velocities, damage and every other state array bit for bit, the
-same bonds broken at the same substep, the same RunStatus. The FP64 ledgers are
-folded in bond order on the device, so they are held bit for bit as well.
+same bonds broken at the same substep, the same first-failure list and every
+RunStatus counter. The two FP64 ledgers the reference folds bond by bond
+(removed energy, plastic work) are summed on the device in a fixed parallel
+order -- deterministic run to run -- and held to 1e-12 relative, the bound the
+reference set for its own CUDA backend.
 """
 import numpy as np
 import pytest
 
-from _util import SCHEDULE_KEYS, STATE_KEYS, golden_names, load_golden, mismatches, status_mismatches
+from _util import LEDGER_RTOL, SCHEDULE_KEYS, STATE_KEYS, golden_names, load_golden, mismatches, status_mismatches
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +21,7 @@ def test_gpu_reproduces_reference_fixture(device, name):
     case, ref, precision = load_golden(name)
     out = device.run_case(case, precision=precision, per_substep=True)
     assert mismatches(ref, out, SCHEDULE_KEYS + STATE_KEYS + ["break_step"]) == []
-    assert status_mismatches(ref, out) == []
+    assert status_mismatches(ref, out, ledger_rtol=LEDGER_RTOL) == []
 
 
 def test_gpu_cantilever_full_run_matches_checker(device, port):
@@ -30,7 +33,7 @@ def test_gpu_cantilever_full_run_matches_checker(device, port):
     gpu = device.run_case(case)
     assert int(cpu["status_u64"][4]) > 0
     assert mismatches(cpu, gpu, STATE_KEYS) == []
-    assert status_mismatches(cpu, gpu) == []
+    assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
 
 
 def test_gpu_sliced_impact_matches_checker(device, port):
@@ -43,7 +46,7 @@ def test_gpu_sliced_impact_matches_checker(device, port):
     gpu = device.run_case(case, per_substep=True)
     assert int(cpu["status_u64"][4]) > 0 and int(cpu["status_u64"][9]) > 0
     assert mismatches(cpu, gpu, STATE_KEYS + ["break_step"]) == []
-    assert status_mismatches(cpu, gpu) == []
+    assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
 
 
 def test_gpu_double_lane_matches_checker(device, port):
@@ -53,7 +56,7 @@ def test_gpu_double_lane_matches_checker(device, port):
     cpu = port.run_port(case, precision="double", per_substep=True)
     gpu = device.run_case(case, precision="double", per_substep=True)
     assert mismatches(cpu, gpu, STATE_KEYS + ["break_step"]) == []
-    assert status_mismatches(cpu, gpu) == []
+    assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
 
 
 def test_gpu_runs_are_deterministic(device):
@@ -83,7 +86,7 @@ def test_status_accumulates_across_run_calls(device, port):
     be.download(state)
     assert np.array_equal(state.u, whole["u"]) and np.array_equal(state.alive, whole["alive"])
     assert st.broken_bonds == int(whole["status_u64"][4])
-    assert st.removed_energy_j == float(whole["status_f64"][0])
+    assert st.removed_energy_j == float(whole["status_f64"][0])  # same fixed order in both runs
 
 
 def _backend(device, case):
