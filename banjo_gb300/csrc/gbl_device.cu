@@ -47,8 +47,6 @@ private:
     std::vector<std::pair<void **, std::size_t>> offsets_;
 };
 
-constexpr std::uint32_t kChunk = 1024; // bonds per CTA in one projection launch
-
 } // namespace
 
 class BackendBase {
@@ -86,7 +84,6 @@ public:
         stream_ = own_stream_;
         check(cudaEventCreate(&ev0_), "event");
         check(cudaEventCreate(&ev1_), "event");
-        buildLevels();
     }
     ~Backend() override {
         dropGraph();
@@ -121,6 +118,7 @@ public:
         const std::uint32_t N = st.node_count, B = st.bond_count, D = st.max_degree;
         dropGraph();
         arena_.release();
+        buildLevels(st);
         Dev<R> d{};
         d.N = N; d.B = B; d.D = D; d.blocks = sched_.block_count;
         d.words_b = (B + 31) / 32;
@@ -138,6 +136,8 @@ public:
         arena_.reserve(d.thr2, B); arena_.reserve(d.plastic, B); arena_.reserve(d.lambda, B); arena_.reserve(d.mode, B);
         arena_.reserve(d.ev_bits, d.words_b + 1); arena_.reserve(d.ev_tile, d.tiles_b + 1); arena_.reserve(d.ev_list, B + 1);
         arena_.reserve(d.ev_removed, B); arena_.reserve(d.ev_packed, B + 1); arena_.reserve(d.ev_prefix, B + 1);
+        arena_.reserve(d.ev_ends, B); arena_.reserve(d.dev2sched, B);
+        arena_.reserve(d.isolated, isolated_.size() + 1);
         arena_.reserve(d.dmg_bits, d.words_b + 1); arena_.reserve(d.dmg_tile, d.tiles_b + 1);
         arena_.reserve(d.dmg_list, B + 1); arena_.reserve(d.ev_damage, B); arena_.reserve(d.dmg_value, B + 1);
         arena_.reserve(d.tile_plastic, d.tiles_b + 1); arena_.reserve(d.tile_removed, d.tiles_b + 1);
@@ -146,7 +146,6 @@ public:
         arena_.reserve(d.cand_count, sched_.block_count);
         arena_.reserve(d.dirty_list, N + 1); arena_.reserve(d.ffb, B + 1);
         arena_.reserve(d.sphere, 1); arena_.reserve(d.ctl, 1);
-        arena_.reserve(work_d_, work_h_.size() + 1);
         arena_.commit();
 
         // Nodes.
@@ -178,31 +177,40 @@ public:
                 nbr[s] = {R(st.nbr_rest[3 * s]), R(st.nbr_rest[3 * s + 1]), R(st.nbr_rest[3 * s + 2]),
                           (present && st.nbr_alive[s]) ? R(st.nbr_weight[s]) : R(0)};
                 other[s] = present ? st.nbr_other[s] : node;
-                bond[s] = st.nbr_bond[s];
+                bond[s] = present ? sched2dev_[st.nbr_bond[s]] : kNoBond;
             }
             copy(d.nbr, nbr); copy(d.nbr_other, other); copy(d.nbr_bond, bond);
         }
-        copyRaw(d.slot_a, st.bond_slot_a, B); copyRaw(d.slot_b, st.bond_slot_b, B);
-        // Bonds, schedule order.
+        // Bonds, level-major storage (storage index d holds schedule index j).
         {
             std::vector<BondRec<R>> rec(B);
             std::vector<Q4<R>> geo(B), prev(B), thr4(B);
             std::vector<Q2<R>> thr2(B), plastic(B);
+            std::vector<std::uint32_t> slot_a(B), slot_b(B);
+            std::vector<std::uint8_t> mode(B);
             plastic_state_ = false;
-            for (std::uint32_t j = 0; j < B; ++j) {
-                rec[j] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit), st.bond_b[j], R(st.rest_length_sq_minus[j]),
-                          R(st.rest_length[j])};
-                geo[j] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]), R(st.compliance[j])};
-                prev[j] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
+            for (std::uint32_t dd = 0; dd < B; ++dd) {
+                const std::uint32_t j = dev2sched_[dd];
+                rec[dd] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit) | (last_a_[dd] ? kLastABit : 0U),
+                           st.bond_b[j] | (last_b_[dd] ? kLastBBit : 0U), R(st.rest_length_sq_minus[j]),
+                           R(st.rest_length[j])};
+                geo[dd] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]),
+                           R(st.compliance[j])};
+                prev[dd] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
                 const double *t = st.threshold + 6 * static_cast<std::size_t>(j);
-                thr4[j] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
-                thr2[j] = {R(t[4]), R(t[5])};
-                plastic[j] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
-                plastic_state_ = plastic_state_ || plastic[j].x != R(0);
+                thr4[dd] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
+                thr2[dd] = {R(t[4]), R(t[5])};
+                plastic[dd] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
+                plastic_state_ = plastic_state_ || plastic[dd].x != R(0);
+                slot_a[dd] = st.bond_slot_a[j];
+                slot_b[dd] = st.bond_slot_b[j];
+                mode[dd] = st.failure_mode[j];
             }
             copy(d.rec, rec); copy(d.geo, geo); copy(d.prev, prev); copy(d.thr4, thr4); copy(d.thr2, thr2);
-            copy(d.plastic, plastic);
-            copyRaw(d.mode, st.failure_mode, B);
+            copy(d.plastic, plastic); copy(d.slot_a, slot_a); copy(d.slot_b, slot_b); copy(d.mode, mode);
+            copy(d.dev2sched, dev2sched_);
+            if (!isolated_.empty()) copy(d.isolated, isolated_);
+            d.isolated_count = static_cast<std::uint32_t>(isolated_.size());
         }
         zero(d.lambda, B);
         zero(d.ev_bits, d.words_b + 1);
@@ -211,7 +219,6 @@ public:
         zero(d.tile_removed, d.tiles_b + 1);
         copy(d.node_block_begin, sched_.node_block_begin);
         zero(d.cand_count, sched_.block_count);
-        copy(work_d_, work_h_);
         // Settings and sphere.
         S_ = convertSettings(set);
         plastic_ = plastic_state_ || S_.yield_stretch > R(0);
@@ -364,12 +371,14 @@ public:
         const auto rec = fetch(dev_.rec, B_);
         const auto prev = fetch(dev_.prev, B_);
         const auto pl = fetch(dev_.plastic, B_);
-        check(cudaMemcpy(st.failure_mode, dev_.mode, B_, cudaMemcpyDeviceToHost), "copy");
-        for (std::uint32_t j = 0; j < B_; ++j) {
-            st.alive[j] = (rec[j].a & kDeadBit) ? 0 : 1;
-            st.damage[j] = prev[j].w;
-            st.prev_tensile[j] = prev[j].x; st.prev_compressive[j] = prev[j].y; st.prev_shear[j] = prev[j].z;
-            st.plastic_extension[j] = pl[j].x; st.plastic_strain[j] = pl[j].y;
+        const auto mode = fetch(dev_.mode, B_);
+        for (std::uint32_t dd = 0; dd < B_; ++dd) {
+            const std::uint32_t j = dev2sched_[dd];
+            st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
+            st.failure_mode[j] = mode[dd];
+            st.damage[j] = prev[dd].w;
+            st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
+            st.plastic_extension[j] = pl[dd].x; st.plastic_strain[j] = pl[dd].y;
         }
         if (sphere) *sphere = fetchSphere();
     }
@@ -414,32 +423,66 @@ public:
     }
 
 private:
-    struct Level { std::uint32_t first_chunk, chunks; bool boundary; };
+    // Levels of the projection sweep. The reference sweeps bonds in one serial
+    // order: every slab's interior colours, then the boundary colours of even
+    // slabs, then of odd slabs (CpuLatticeBackend.cpp:336-348, 395-407). A
+    // bond's depth is one more than the deepest earlier bond at either of its
+    // nodes; bonds of equal depth share no node, and along every node the
+    // depths rise in the serial order, so running the levels in depth order,
+    // each level in any thread order, is the serial sweep exactly. Bonds are
+    // stored level-major (stable in the serial order), and each node's last
+    // bond of the sweep is flagged: its support projection follows that bond.
+    struct Level { std::uint32_t begin, end; };
 
-    // Levels: per colour, the union over the slabs that run together
-    // (CpuLatticeBackend.cpp:336-348, 395-407 sweep order). Every node's
-    // incident bonds keep their serial order: interior bonds of a slab only
-    // touch that slab; in the even and odd boundary passes each node meets
-    // bonds of a single owner slab.
-    void buildLevels() {
-        levels_.clear();
-        work_h_.clear();
-        const std::uint32_t C = sched_.color_count;
-        auto addLevel = [&](std::uint32_t boundary, std::uint32_t first_block, std::uint32_t step) {
+    void buildLevels(const gbl_state_view &st) {
+        const std::uint32_t N = st.node_count, B = st.bond_count, C = sched_.color_count;
+        std::vector<std::uint32_t> order;
+        order.reserve(B);
+        auto sweep = [&](std::uint32_t blk, std::uint32_t boundary) {
             for (std::uint32_t c = 0; c < C; ++c) {
-                const std::uint32_t start = static_cast<std::uint32_t>(work_h_.size());
-                for (std::uint32_t blk = first_block; blk < sched_.block_count; blk += step) {
-                    const std::size_t key = sched_.rangeKey(blk, boundary, c);
-                    for (std::uint32_t j = sched_.range_begin[key]; j < sched_.range_end[key]; j += kChunk)
-                        work_h_.push_back({j, std::min(j + kChunk, sched_.range_end[key])});
-                }
-                const std::uint32_t n = static_cast<std::uint32_t>(work_h_.size()) - start;
-                if (n) levels_.push_back({start, n, boundary != 0});
+                const std::size_t key = sched_.rangeKey(blk, boundary, c);
+                for (std::uint32_t j = sched_.range_begin[key]; j < sched_.range_end[key]; ++j) order.push_back(j);
             }
         };
-        addLevel(0, 0, 1);
-        addLevel(1, 0, 2);
-        addLevel(1, 1, 2);
+        for (std::uint32_t blk = 0; blk < sched_.block_count; ++blk) sweep(blk, 0);
+        for (std::uint32_t blk = 0; blk < sched_.block_count; blk += 2) sweep(blk, 1);
+        for (std::uint32_t blk = 1; blk < sched_.block_count; blk += 2) sweep(blk, 1);
+        if (order.size() != B) invalid("lattice schedule ranges do not cover every bond exactly once");
+        std::vector<std::uint32_t> depth(B), reached(N, 0), last(N, kNoBond);
+        std::uint32_t deepest = 0;
+        for (const std::uint32_t j : order) {
+            const std::uint32_t a = st.bond_a[j], b = st.bond_b[j];
+            if (a >= N || b >= N || a == b) invalid("lattice bond joins invalid nodes");
+            const std::uint32_t d = std::max(reached[a], reached[b]) + 1;
+            depth[j] = d;
+            reached[a] = reached[b] = d;
+            last[a] = last[b] = j;
+            deepest = std::max(deepest, d);
+        }
+        std::vector<std::uint32_t> first(deepest + 2, 0);
+        for (std::uint32_t j = 0; j < B; ++j) ++first[depth[j] + 1];
+        for (std::uint32_t d = 1; d <= deepest; ++d) first[d + 1] += first[d];
+        dev2sched_.assign(B, 0);
+        sched2dev_.assign(B, 0);
+        {
+            std::vector<std::uint32_t> fill(first.begin(), first.end());
+            for (const std::uint32_t j : order) dev2sched_[fill[depth[j]]++] = j;
+        }
+        for (std::uint32_t d = 0; d < B; ++d) sched2dev_[dev2sched_[d]] = d;
+        levels_.clear();
+        for (std::uint32_t d = 1; d <= deepest; ++d)
+            if (first[d + 1] > first[d]) levels_.push_back({first[d], first[d + 1]});
+        last_a_.assign(B, 0);
+        last_b_.assign(B, 0);
+        isolated_.clear();
+        for (std::uint32_t i = 0; i < N; ++i) {
+            if (last[i] == kNoBond) {
+                isolated_.push_back(i);
+                continue;
+            }
+            const std::uint32_t dd = sched2dev_[last[i]];
+            (st.bond_a[last[i]] == i ? last_a_ : last_b_)[dd] = 1;
+        }
     }
 
     static void validate(const gbl_state_view &st, const gbl_step_settings &s) {
@@ -454,7 +497,7 @@ private:
         for (std::uint32_t p = 0; p < s.plane_count; ++p)
             if (s.planes[p].footprint_count > kFootprints) invalid("at most four footprints per plane");
         if (!(s.dt > 0.0) || !std::isfinite(s.dt)) invalid("lattice step needs a finite positive timestep");
-        if (st.node_count >= kDeadBit) invalid("lattice exceeds 2^31 nodes");
+        if (st.node_count > kNodeMask) invalid("lattice exceeds 2^30 nodes");
     }
 
     Settings<R> convertSettings(const gbl_step_settings &s) const {
@@ -545,9 +588,10 @@ private:
         const auto prev = fetch(dev_.prev, B_);
         f.alive.resize(B_);
         f.damage.resize(B_);
-        for (std::uint32_t j = 0; j < B_; ++j) {
-            f.alive[j] = (rec[j].a & kDeadBit) ? 0 : 1;
-            f.damage[j] = static_cast<float>(prev[j].w);
+        for (std::uint32_t dd = 0; dd < B_; ++dd) {
+            const std::uint32_t j = dev2sched_[dd];
+            f.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
+            f.damage[j] = static_cast<float>(prev[dd].w);
         }
         f.sphere = fetchSphere();
         frames.push_back(std::move(f));
@@ -631,20 +675,18 @@ private:
         const unsigned I = S.iterations;
         for (unsigned it = 0; it < I; ++it) {
             const bool first = it == 0, last = it + 1 == I;
-            bool boundary_marked = false;
-            for (const Level &lv : levels_) {
-                if (lv.boundary && !boundary_marked) { mark(5); boundary_marked = true; }
-                launchSolve(lv, first, last);
-            }
-            mark(boundary_marked ? 6 : 5);
-            if (S.plane_count) kSupport<R><<<nodes, kThreads, 0, stream_>>>(L, S);
+            for (const Level &lv : levels_) launchSolve(lv, first, last);
+            mark(5);
+            if (S.plane_count && L.isolated_count)
+                kSupportIsolated<R><<<gridFor(L.isolated_count), kThreads, 0, stream_>>>(L, S);
             mark(7);
         }
         kVelocity<R><<<nodes, kThreads, 0, stream_>>>(L, S, S.damping_fraction <= R(0) ? 1 : 0);
         mark(8);
         if (S.damping_fraction > R(0)) {
             for (const Level &lv : levels_)
-                kDamp<R, kDirect><<<lv.chunks, kThreads, 0, stream_>>>(L, work_d_ + lv.first_chunk, S.damping_fraction);
+                kDamp<R, kDirect><<<gridFor(lv.end - lv.begin), kThreads, 0, stream_>>>(L, lv.begin, lv.end,
+                                                                                        S.damping_fraction);
             kSupportVelocity<R><<<nodes, kThreads, 0, stream_>>>(L, S);
             mark(9);
         }
@@ -665,19 +707,19 @@ private:
     }
 
     void launchSolve(const Level &lv, bool first, bool last) {
-        const Chunk *w = work_d_ + lv.first_chunk;
-        const R dt = S_.dt;
-#define GBL_SOLVE(F, La, P) kSolve<R, kDirect, F, La, P><<<lv.chunks, kThreads, 0, stream_>>>(dev_, w, dt)
-        if (plastic_) {
-            if (first && last) GBL_SOLVE(true, true, true);
-            else if (first) GBL_SOLVE(true, false, true);
-            else if (last) GBL_SOLVE(false, true, true);
-            else GBL_SOLVE(false, false, true);
-        } else {
-            if (first && last) GBL_SOLVE(true, true, false);
-            else if (first) GBL_SOLVE(true, false, false);
-            else if (last) GBL_SOLVE(false, true, false);
-            else GBL_SOLVE(false, false, false);
+        const unsigned grid = gridFor(lv.end - lv.begin);
+        const bool support = S_.plane_count != 0;
+        // One instantiation per (first, last, plastic, support) combination.
+        const int key = (first ? 8 : 0) | (last ? 4 : 0) | (plastic_ ? 2 : 0) | (support ? 1 : 0);
+#define GBL_SOLVE(K)                                                                                                \
+    case K:                                                                                                         \
+        kSolve<R, kDirect, ((K) & 8) != 0, ((K) & 4) != 0, ((K) & 2) != 0, ((K) & 1) != 0>                          \
+            <<<grid, kThreads, 0, stream_>>>(dev_, S_, lv.begin, lv.end);                                          \
+        break;
+        switch (key) {
+            GBL_SOLVE(0) GBL_SOLVE(1) GBL_SOLVE(2) GBL_SOLVE(3) GBL_SOLVE(4) GBL_SOLVE(5) GBL_SOLVE(6) GBL_SOLVE(7)
+            GBL_SOLVE(8) GBL_SOLVE(9) GBL_SOLVE(10) GBL_SOLVE(11) GBL_SOLVE(12) GBL_SOLVE(13) GBL_SOLVE(14)
+            GBL_SOLVE(15)
         }
 #undef GBL_SOLVE
     }
@@ -685,8 +727,8 @@ private:
     Schedule sched_;
     unsigned tpb_;
     std::vector<Level> levels_;
-    std::vector<Chunk> work_h_;
-    Chunk *work_d_{};
+    std::vector<std::uint32_t> dev2sched_, sched2dev_, isolated_;
+    std::vector<std::uint8_t> last_a_, last_b_;
     Arena arena_;
     Dev<R> dev_{};
     Settings<R> S_{};

@@ -6,14 +6,17 @@
 //          rinv   9 x N, unm 3 x N      (component-major, coalesced per node)
 //          nbr[k*N+i] = (rest.xyz, weight if the slot's bond is alive else 0)
 //          nbr_other[k*N+i] (i itself for a padded slot), nbr_bond[k*N+i]
-//   bonds  rec[j] = (a | dead bit, b, rest_length_sq_minus, rest_length)
-//          geo[j] = (rest_edge.xyz, compliance)
-//          prev[j] = (prev_tensile, prev_compressive, prev_shear, damage)
-//          plastic[j] = (extension, strain), thr4/thr2 = six damage thresholds
-// Bonds are stored in schedule order. The projection sweep runs one launch per
-// "level": the union, over the slabs that may run together, of one colour's
-// bond range (node-disjoint by construction), handed out to CTAs as
-// contiguous chunks.
+//   bonds  rec[d] = (a | dead | last-of-a, b | last-of-b, rest_length_sq_minus, rest_length)
+//          geo[d] = (rest_edge.xyz, compliance)
+//          prev[d] = (prev_tensile, prev_compressive, prev_shear, damage)
+//          plastic[d] = (extension, strain), thr4/thr2 = six damage thresholds
+// Bonds are stored level-major. A level is the set of bonds at one depth of
+// the reference's serial sweep order (CpuLatticeBackend.cpp:336-348, 395-407),
+// depth being one more than the deepest earlier bond at either end: a level
+// shares no node, and every node meets its bonds in the serial order, so any
+// thread mapping inside a level reproduces the serial sweep bit for bit.
+// dev2sched maps storage index d to schedule index j; everything a caller
+// sees (events, downloads, failure lists) is in schedule order.
 #pragma once
 
 #include "gbl_math.cuh"
@@ -26,6 +29,40 @@ namespace gbl {
 template <class R> struct BondRec;
 template <> struct alignas(16) BondRec<float> { std::uint32_t a, b; float rsm, rest; };
 template <> struct alignas(8) BondRec<double> { std::uint32_t a, b; double rsm, rest; };
+
+template <class R> __device__ __forceinline__ std::uint32_t endA(const BondRec<R> &r) { return r.a & kNodeMask; }
+template <class R> __device__ __forceinline__ std::uint32_t endB(const BondRec<R> &r) { return r.b & kNodeMask; }
+
+// Streaming loads for data read once per pass (bond records), so that they do
+// not evict the node arrays the gathers keep re-reading from L2.
+__device__ __forceinline__ BondRec<float> ldStream(const BondRec<float> *p) {
+    const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(p));
+    return {v.x, v.y, __uint_as_float(v.z), __uint_as_float(v.w)};
+}
+__device__ __forceinline__ BondRec<double> ldStream(const BondRec<double> *p) {
+    const uint2 ab = __ldcs(reinterpret_cast<const uint2 *>(p));
+    const double *d = reinterpret_cast<const double *>(p);
+    return {ab.x, ab.y, __ldcs(d + 1), __ldcs(d + 2)};
+}
+__device__ __forceinline__ Q4<float> ldStream(const Q4<float> *p) {
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Q4<double> ldStream(const Q4<double> *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 lo = __ldcs(q), hi = __ldcs(q + 1);
+    return {lo.x, lo.y, hi.x, hi.y};
+}
+// L2-only loads for node data gathered once per pass by a different thread.
+__device__ __forceinline__ Q4<float> ldShared(const Q4<float> *p) {
+    const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Q4<double> ldShared(const Q4<double> *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 lo = __ldcg(q), hi = __ldcg(q + 1);
+    return {lo.x, lo.y, hi.x, hi.y};
+}
 
 // Serial bookkeeping (ContactAccumulators, LatticePhysics.hpp:379-388).
 struct ContactAcc {
@@ -83,6 +120,10 @@ template <class R> struct Dev {
     // end-sample tile FP64 partials and their prefix.
     std::uint32_t *ev_bits, *ev_tile, *ev_list;
     double *ev_removed, *ev_packed, *ev_prefix;
+    uint2 *ev_ends;               // the two nodes of a broken bond, by schedule index
+    std::uint32_t *dev2sched;     // bond storage order (level-major) -> schedule index
+    std::uint32_t *isolated;      // nodes without bonds (their support projection has no sweep to ride on)
+    std::uint32_t isolated_count;
     std::uint32_t *dmg_bits, *dmg_tile, *dmg_list;
     float *ev_damage, *dmg_value;
     double *tile_plastic, *tile_removed;
@@ -230,7 +271,7 @@ __device__ __forceinline__ void startSample(const Dev<R> &L, std::uint32_t j) {
     if (rec.a & kDeadBit) return;
     const Q4<R> g = L.geo[j];
     R t, c, s;
-    sampleBond<R, Direct>(L, rec.a, rec.b, rec, V3<R>{g.x, g.y, g.z}, t, c, s);
+    sampleBond<R, Direct>(L, endA(rec), endB(rec), rec, V3<R>{g.x, g.y, g.z}, t, c, s);
     Q4<R> p = L.prev[j];
     p.x = maxR(R(0), t);
     p.y = maxR(R(0), c);
@@ -532,81 +573,19 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(Dev<R> L, Settings
 }
 
 // ---------------------------------------------------------------------------
-// XPBD projection of one level (LatticePhysics.hpp:1132-1168).
+// XPBD projection of one level (LatticePhysics.hpp:1132-1168), one bond per
+// thread over the level's contiguous storage range [begin, end).
+//
+// Support (LatticePhysics.hpp:1255-1261) rides on the sweep: the reference
+// projects every node out of the support planes after the whole sweep; here a
+// node is projected by the thread that ran its last bond of the sweep (the
+// record's last-of flags), right after that bond. Nothing later in the sweep
+// touches the node and the projection reads only the node itself, so the
+// result is the reference's, and the separate pass over the nodes is gone. A
+// broken or degenerate last bond still carries its nodes' projection.
 // ---------------------------------------------------------------------------
-struct Chunk { std::uint32_t begin, end; };
-
-template <class R, bool Direct, bool First, bool Last, bool Plastic>
-__global__ void __launch_bounds__(kThreads) kSolve(Dev<R> L, const Chunk *__restrict__ work, R dt) {
-    if (L.ctl->stop) return;
-    const Chunk ch = work[blockIdx.x];
-    const R dt2 = dt * dt;
-    for (std::uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += blockDim.x) {
-        const BondRec<R> rec = L.rec[j];
-        if (rec.a & kDeadBit) continue;
-        const std::uint32_t a = rec.a, b = rec.b;
-        const Q4<R> g = L.geo[j];
-        const Q4<R> qa = L.u[a], qb = L.u[b];
-        const V3<R> ua = xyz(qa), ub = xyz(qb), edge{g.x, g.y, g.z};
-        const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
-        const R cl = length(delta);
-        if (cl <= R(1.0e-12)) continue;
-        const R original = rec.rest;
-        const R plastic = Plastic ? L.plastic[j].x : R(0);
-        const R rest = Plastic ? original + plastic : original;
-        R constraint;
-        if (Direct) {
-            constraint = cl - rest;
-        } else {
-            const V3<R> du = ub - ua;
-            const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
-            constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
-        }
-        const V3<R> dir = delta / cl;
-        const R wa = qa.w, wb = qb.w;
-        const R alpha = g.w / dt2;
-        const R lambda = First ? R(0) : L.lambda[j];
-        const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
-        if (!Last) L.lambda[j] = lambda + dl;
-        const V3<R> na = ua - (wa * dl) * dir;
-        const V3<R> nb = ub + (wb * dl) * dir;
-        L.u[a] = Q4<R>{na.x, na.y, na.z, wa};
-        L.u[b] = Q4<R>{nb.x, nb.y, nb.z, wb};
-    }
-}
-
-// Radial pair damping of one level (LatticePhysics.hpp:1170-1184).
-template <class R, bool Direct>
-__global__ void __launch_bounds__(kThreads) kDamp(Dev<R> L, const Chunk *__restrict__ work, R fraction) {
-    if (L.ctl->stop) return;
-    const Chunk ch = work[blockIdx.x];
-    for (std::uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += blockDim.x) {
-        const BondRec<R> rec = L.rec[j];
-        if (rec.a & kDeadBit) continue;
-        const std::uint32_t a = rec.a, b = rec.b;
-        const Q4<R> va = L.v[a], vb = L.v[b];
-        const R ma = va.w, mb = vb.w;
-        if (ma <= R(0) || mb <= R(0)) continue;
-        const Q4<R> g = L.geo[j];
-        const V3<R> n = normalized(bondVector<R, Direct>(L, a, b, V3<R>{g.x, g.y, g.z}));
-        const R rel = dot(xyz(vb) - xyz(va), n);
-        const R im = R(1) / ma + R(1) / mb;
-        const R impulse = -fraction * rel / im;
-        const V3<R> na = xyz(va) - (impulse / ma) * n;
-        const V3<R> nb = xyz(vb) + (impulse / mb) * n;
-        L.v[a] = Q4<R>{na.x, na.y, na.z, ma};
-        L.v[b] = Q4<R>{nb.x, nb.y, nb.z, mb};
-    }
-}
-
-// Support projection after a sweep (LatticePhysics.hpp:1255-1261).
 template <class R>
-__global__ void __launch_bounds__(kThreads) kSupport(Dev<R> L, Settings<R> S) {
-    if (L.ctl->stop) return;
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= L.N) return;
-    const Q4<R> uq = L.u[i];
-    V3<R> u = xyz(uq);
+__device__ __forceinline__ bool supportProject(const Dev<R> &L, const Settings<R> &S, std::uint32_t i, V3<R> &u) {
     const V3<R> x0 = xyz(L.x0[i]);
     bool projected = false;
     for (std::uint32_t p = 0; p < S.plane_count; ++p) {
@@ -615,9 +594,109 @@ __global__ void __launch_bounds__(kThreads) kSupport(Dev<R> L, Settings<R> S) {
         if (depth > R(0)) L.engaged[p * L.N + i] = 1;
         projected = projected || here;
     }
+    return projected;
+}
+
+template <class R, bool Direct, bool First, bool Last, bool Plastic, bool Support>
+__global__ void __launch_bounds__(kThreads) kSolve(Dev<R> L, Settings<R> S, std::uint32_t begin, std::uint32_t end) {
+    if (L.ctl->stop) return;
+    const std::uint32_t d = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= end) return;
+    const BondRec<R> rec = ldStream(L.rec + d);
+    const std::uint32_t a = endA(rec), b = endB(rec);
+    Q4<R> qa, qb;
+    bool have = false, write_a = false, write_b = false;
+    if (!(rec.a & kDeadBit)) {
+        const Q4<R> g = ldStream(L.geo + d);
+        qa = ldShared(L.u + a);
+        qb = ldShared(L.u + b);
+        have = true;
+        const V3<R> ua = xyz(qa), ub = xyz(qb), edge{g.x, g.y, g.z};
+        const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
+        const R cl = length(delta);
+        if (cl > R(1.0e-12)) {
+            const R original = rec.rest;
+            const R plastic = Plastic ? L.plastic[d].x : R(0);
+            const R rest = Plastic ? original + plastic : original;
+            R constraint;
+            if (Direct) {
+                constraint = cl - rest;
+            } else {
+                const V3<R> du = ub - ua;
+                const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
+                constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
+            }
+            const V3<R> dir = delta / cl;
+            const R wa = qa.w, wb = qb.w;
+            const R alpha = g.w / (S.dt * S.dt);
+            const R lambda = First ? R(0) : __ldcs(L.lambda + d);
+            const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
+            if (!Last) __stcs(L.lambda + d, lambda + dl);
+            const V3<R> na = ua - (wa * dl) * dir;
+            const V3<R> nb = ub + (wb * dl) * dir;
+            qa = Q4<R>{na.x, na.y, na.z, wa};
+            qb = Q4<R>{nb.x, nb.y, nb.z, wb};
+            write_a = write_b = true;
+        }
+    }
+    if (Support) {
+        if (rec.a & kLastABit) {
+            if (!have) qa = L.u[a];
+            V3<R> u = xyz(qa);
+            if (supportProject(L, S, a, u)) {
+                qa = Q4<R>{u.x, u.y, u.z, qa.w};
+                write_a = true;
+            }
+        }
+        if (rec.b & kLastBBit) {
+            if (!have) qb = L.u[b];
+            V3<R> u = xyz(qb);
+            if (supportProject(L, S, b, u)) {
+                qb = Q4<R>{u.x, u.y, u.z, qb.w};
+                write_b = true;
+            }
+        }
+    }
+    if (write_a) L.u[a] = qa;
+    if (write_b) L.u[b] = qb;
+}
+
+// Radial pair damping of one level (LatticePhysics.hpp:1170-1184).
+template <class R, bool Direct>
+__global__ void __launch_bounds__(kThreads) kDamp(Dev<R> L, std::uint32_t begin, std::uint32_t end, R fraction) {
+    if (L.ctl->stop) return;
+    const std::uint32_t d = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= end) return;
+    const BondRec<R> rec = L.rec[d];
+    if (rec.a & kDeadBit) return;
+    const std::uint32_t a = endA(rec), b = endB(rec);
+    const Q4<R> va = L.v[a], vb = L.v[b];
+    const R ma = va.w, mb = vb.w;
+    if (ma <= R(0) || mb <= R(0)) return;
+    const Q4<R> g = L.geo[d];
+    const V3<R> n = normalized(bondVector<R, Direct>(L, a, b, V3<R>{g.x, g.y, g.z}));
+    const R rel = dot(xyz(vb) - xyz(va), n);
+    const R im = R(1) / ma + R(1) / mb;
+    const R impulse = -fraction * rel / im;
+    const V3<R> na = xyz(va) - (impulse / ma) * n;
+    const V3<R> nb = xyz(vb) + (impulse / mb) * n;
+    L.v[a] = Q4<R>{na.x, na.y, na.z, ma};
+    L.v[b] = Q4<R>{nb.x, nb.y, nb.z, mb};
+}
+
+// Support projection of the nodes that have no bond to carry it (isolated
+// nodes), after a sweep (LatticePhysics.hpp:1255-1261).
+template <class R>
+__global__ void __launch_bounds__(kThreads) kSupportIsolated(Dev<R> L, Settings<R> S) {
+    if (L.ctl->stop) return;
+    const std::uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L.isolated_count) return;
+    const std::uint32_t i = L.isolated[t];
+    const Q4<R> uq = L.u[i];
+    V3<R> u = xyz(uq);
     // Written back whenever a projection ran, even by a zero distance, so the
     // sign of a zero component is whatever the projection made it.
-    if (projected) L.u[i] = Q4<R>{u.x, u.y, u.z, uq.w};
+    if (supportProject(L, S, i, u)) L.u[i] = Q4<R>{u.x, u.y, u.z, uq.w};
 }
 
 // Velocity from accepted positions, then the support response of
@@ -668,19 +747,17 @@ __device__ __forceinline__ double warpSumFixed(double x) {
 
 template <class R, bool Direct, bool Plastic>
 __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) {
-    __shared__ unsigned tile_count[kThreads / 32], tile_dmg[kThreads / 32];
     __shared__ double tile_work[kThreads / 32];
     __shared__ unsigned peak[4];
     if (L.ctl->stop) return;
-    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; // storage index
     if (threadIdx.x < 4) peak[threadIdx.x] = 0;
     __syncthreads();
-    bool broke = false, dmg_candidate = false;
     double plastic_work = 0.0;
     if (j < L.B) {
         const BondRec<R> rec = L.rec[j];
         if (!(rec.a & kDeadBit)) {
-            const std::uint32_t a = rec.a, b = rec.b;
+            const std::uint32_t a = endA(rec), b = endB(rec);
             const Q4<R> g = L.geo[j];
             const V3<R> edge{g.x, g.y, g.z};
             float plastic_stretch = 0.0F;
@@ -732,23 +809,27 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
             }
             L.prev[j] = pv;
             const float dmg = static_cast<float>(pv.w);
-            broke = pv.w >= R(1);
-            if (broke) {
+            const std::uint32_t js = L.dev2sched[j];
+            if (pv.w >= R(1)) {
                 const R cc = g.w;
                 R energy = R(0);
                 if (!(cc <= R(0))) {
                     const R ext = length(bondVector<R, Direct>(L, a, b, edge)) - rec.rest - pext;
                     energy = R(0.5) * ext * ext / cc;
                 }
-                L.rec[j].a = a | kDeadBit;
+                L.rec[j].a = rec.a | kDeadBit;
                 L.nbr[L.slot_a[j]].w = R(0);
                 L.nbr[L.slot_b[j]].w = R(0);
-                L.ev_removed[j] = static_cast<double>(energy);
+                L.ev_removed[js] = static_cast<double>(energy);
+                L.ev_ends[js] = make_uint2(a, b);
+                atomicOr(L.ev_bits + (js >> 5), 1U << (js & 31U));
             }
             // A bond can raise the run's damage maximum only if it exceeds the
             // maximum as the substep began (CpuLatticeBackend.cpp:462-465).
-            dmg_candidate = static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6;
-            if (dmg_candidate) L.ev_damage[j] = dmg;
+            if (static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6) {
+                L.ev_damage[js] = dmg;
+                atomicOr(L.dmg_bits + (js >> 5), 1U << (js & 31U));
+            }
             // Peaks are non-negative, so their bit patterns order as the values do.
             atomicMax(&peak[0], floatBits(static_cast<float>(pt)));
             atomicMax(&peak[1], floatBits(static_cast<float>(pc)));
@@ -756,30 +837,13 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
             if (Plastic && S.yield_stretch > R(0)) atomicMax(&peak[3], floatBits(plastic_stretch));
         }
     }
-    const unsigned bits = __ballot_sync(0xffffffffU, broke);
-    const unsigned dbits = __ballot_sync(0xffffffffU, dmg_candidate);
     double work = 0.0;
     if (Plastic) work = warpSumFixed(plastic_work);
-    if ((threadIdx.x & 31) == 0) {
-        if (j / 32 < L.words_b) {
-            L.ev_bits[j / 32] = bits;
-            L.dmg_bits[j / 32] = dbits;
-        }
-        tile_count[threadIdx.x / 32] = __popc(bits);
-        tile_dmg[threadIdx.x / 32] = __popc(dbits);
-        tile_work[threadIdx.x / 32] = work;
-    }
+    if ((threadIdx.x & 31) == 0) tile_work[threadIdx.x / 32] = work;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned total = 0, dtotal = 0;
         double wsum = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) {
-            total += tile_count[w];
-            dtotal += tile_dmg[w];
-            wsum += tile_work[w];
-        }
-        L.ev_tile[blockIdx.x] = total;
-        L.dmg_tile[blockIdx.x] = dtotal;
+        for (int w = 0; w < kThreads / 32; ++w) wsum += tile_work[w];
         L.tile_plastic[blockIdx.x] = wsum;
         if (peak[0]) atomicMax(&L.ctl->max_t, peak[0]);
         if (peak[1]) atomicMax(&L.ctl->max_c, peak[1]);
@@ -827,11 +891,21 @@ __global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L, int plastic) {
     const unsigned per = (T + blockDim.x - 1) / blockDim.x;
     const unsigned first = threadIdx.x * per;
     const unsigned last = first + per < T ? first + per : T;
+    // Broken bonds and damage candidates per schedule-order tile of 256 bonds,
+    // counted from the bit words the end sample set.
+    constexpr unsigned kWords = kThreads / 32;
     unsigned nb = 0, nd = 0;
     double work = 0.0;
     for (unsigned t = first; t < last; ++t) {
-        nb += L.ev_tile[t];
-        nd += L.dmg_tile[t];
+        unsigned cb = 0, cd = 0;
+        for (unsigned w = t * kWords; w < (t + 1) * kWords && w < L.words_b; ++w) {
+            cb += __popc(L.ev_bits[w]);
+            cd += __popc(L.dmg_bits[w]);
+        }
+        L.ev_tile[t] = cb;
+        L.dmg_tile[t] = cd;
+        nb += cb;
+        nd += cd;
         if (plastic) work += L.tile_plastic[t];
     }
     unsigned total_b = 0, total_d = 0;
@@ -904,6 +978,7 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
     } else if (lane == 0) {
         L.tile_removed[tile] = 0.0;
     }
+    if (word) L.ev_bits[w] = 0; // the end sample sets bits with atomicOr: clear for the next substep
     const unsigned dbase = L.dmg_tile[tile];
     const unsigned dnext = tile + 1 < L.tiles_b ? L.dmg_tile[tile + 1] : c.dmg_count;
     if (dnext != dbase) {
@@ -921,6 +996,7 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
             ++at;
         }
     }
+    if (word) L.dmg_bits[w] = 0;
 }
 
 // One CTA: exclusive prefix of the tiles' removed energy in tile order (each
@@ -973,7 +1049,8 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(Dev<R> L) {
         const double removed = L.ev_packed[e];
         if (removed > fraction * (running < 1.0e-12 ? 1.0e-12 : running)) atomicOr(&c.energy_gain, 1U);
         if (first_round) L.ffb[e] = j;
-        const std::uint32_t ends[2] = {L.rec[j].a & ~kDeadBit, L.rec[j].b};
+        const uint2 e2 = L.ev_ends[j];
+        const std::uint32_t ends[2] = {e2.x, e2.y};
         for (int q = 0; q < 2; ++q) {
             const std::uint32_t node = ends[q];
             unsigned *word = reinterpret_cast<unsigned *>(L.dirty + (node & ~3U));

@@ -21,7 +21,14 @@
 namespace gbl {
 
 constexpr std::uint32_t kNoBond = 0xffffffffU;
-constexpr std::uint32_t kDeadBit = 0x80000000U;
+// Bond record flags, kept in the spare high bits of the two node indices
+// (nodes are limited to 2^30): a broken bond; the last bond of node a, and of
+// node b, in one sweep of the schedule (where that node's support projection
+// runs).
+constexpr std::uint32_t kDeadBit = 0x80000000U;  // in a
+constexpr std::uint32_t kLastABit = 0x40000000U; // in a
+constexpr std::uint32_t kLastBBit = 0x80000000U; // in b
+constexpr std::uint32_t kNodeMask = 0x3fffffffU;
 constexpr unsigned kPlanes = 2;
 constexpr unsigned kFootprints = 4;
 constexpr unsigned kCandidatesPerBlock = 1024;
