@@ -73,8 +73,8 @@ public:
 
 template <class R> class Backend final : public BackendBase {
     static constexpr bool kDirect = std::is_same<R, double>::value;
-    // x0, u, v of one slab's candidates, staged for the serial contact pass.
-    static constexpr unsigned kSphereSmem = 3 * kCandidatesPerBlock * sizeof(Q4<R>);
+    // One slab's candidates, staged for the serial contact pass.
+    static constexpr unsigned kSphereSmem = kCandidatesPerBlock * sizeof(Staged<R>);
 
 public:
     Backend(Schedule s, unsigned threads_per_block) : sched_(std::move(s)), tpb_(threads_per_block) {
@@ -141,6 +141,9 @@ public:
         arena_.reserve(d.dmg_bits, d.words_b + 1); arena_.reserve(d.dmg_tile, d.tiles_b + 1);
         arena_.reserve(d.dmg_list, B + 1); arena_.reserve(d.ev_damage, B); arena_.reserve(d.dmg_value, B + 1);
         arena_.reserve(d.tile_plastic, d.tiles_b + 1); arena_.reserve(d.tile_removed, d.tiles_b + 1);
+        const std::size_t scan_blocks = d.tiles_b / kScanBlock + 1;
+        arena_.reserve(d.blk_ev, scan_blocks); arena_.reserve(d.blk_dmg, scan_blocks);
+        arena_.reserve(d.blk_removed, scan_blocks); arena_.reserve(d.blk_plastic, scan_blocks);
         arena_.reserve(d.node_block_begin, sched_.block_count + 1);
         arena_.reserve(d.cand_list, static_cast<std::size_t>(sched_.block_count) * kCandidatesPerBlock);
         arena_.reserve(d.cand_count, sched_.block_count);
@@ -696,9 +699,12 @@ private:
         mark(11);
         if (plastic_) kEndSample<R, kDirect, true><<<std::max(1U, dev_.tiles_b), kThreads, 0, stream_>>>(L, S);
         else kEndSample<R, kDirect, false><<<std::max(1U, dev_.tiles_b), kThreads, 0, stream_>>>(L, S);
-        kScanTiles<R><<<1, 1024, 0, stream_>>>(L, plastic_ ? 1 : 0);
-        kEmitEvents<R><<<gridFor(dev_.tiles_b, kThreads / 32), kThreads, 0, stream_>>>(L);
-        kScanRemoved<R><<<1, 1024, 0, stream_>>>(L);
+        const unsigned tile_grid = gridFor(dev_.tiles_b, kThreads / 32);
+        const unsigned scan_blocks = gridFor(dev_.tiles_b, kScanBlock);
+        kTileCounts<R><<<tile_grid, kThreads, 0, stream_>>>(L);
+        kBlockScan<R><<<scan_blocks, kScanBlock, 0, stream_>>>(L, plastic_ ? 1 : 0);
+        kTopScan<R><<<1, kScanBlock, 0, stream_>>>(L, scan_blocks);
+        kEmitEvents<R><<<tile_grid, kThreads, 0, stream_>>>(L);
         kLedgerBroken<R><<<152U * 4U, kThreads, 0, stream_>>>(L);
         mark(12);
         kLedger<R><<<1, 1, 0, stream_>>>(L, S);

@@ -127,6 +127,8 @@ template <class R> struct Dev {
     std::uint32_t *dmg_bits, *dmg_tile, *dmg_list;
     float *ev_damage, *dmg_value;
     double *tile_plastic, *tile_removed;
+    std::uint32_t *blk_ev, *blk_dmg;   // per scan block of tiles: totals, then offsets
+    double *blk_removed, *blk_plastic;
     std::uint32_t *node_block_begin, *cand_list, *cand_count, *dirty_list, *ffb;
     Q4<R> *ext_force;     // applied force (backend precision), w != 0 marks a loaded node
     double *ext_req;      // requested force, 3 per node
@@ -433,48 +435,63 @@ __global__ void __launch_bounds__(1024) kCandidates(Dev<R> L) {
 }
 
 // ---------------------------------------------------------------------------
-// Sphere contact, one thread, candidates in slab then node order
-// (LatticePhysics.hpp:1322-1428).
+// Sphere contact (LatticePhysics.hpp:1322-1428): candidates in slab, then node
+// order, one contact at a time -- every contact moves the sphere the next one
+// sees, so that chain is serial by definition. It runs on one thread of one
+// CTA; everything that does not depend on the sphere's changing state is
+// computed by the whole CTA around it.
+//
+// A candidate's node data are staged in shared memory. In pass 1 the sphere
+// centre cannot move (only pass 2 corrects positions), so the offset r, its
+// length and unit normal, the gap, the inverse masses and the effective
+// inverse mass along the normal are computed in parallel before the chain,
+// with the reference's expressions; the chain then starts at the relative
+// velocity. In pass 2 the parallel part is the node's position and masses.
 // ---------------------------------------------------------------------------
-// One candidate against the sphere. The node's data arrive staged in shared
-// memory (x0, u, v with the mass in v.w) and are updated there.
+template <class R> struct Staged {
+    V3<R> p;       // position x0 + u (pass 2), or r = p - centre (pass 1)
+    V3<R> normal;  // pass 1: normalized(r)
+    R gap;         // pass 1: |r| - (sphere radius + node contact radius)
+    R eff_n;       // pass 1: effective inverse mass along the normal
+    R inm;         // 1 / mass
+    R before;      // the node's kinetic energy as the pass reaches it
+    Q4<R> u, v;    // u (w: inv_mass), v (w: mass)
+};
+
 template <class R>
-__device__ void sphereNode(const Settings<R> &S, Sphere<R> &sp, const Q4<R> &x0q, Q4<R> &uq_ref, Q4<R> &vq_ref,
-                           bool correct, ContactAcc &acc) {
-    const Q4<R> vq = vq_ref;
-    const R mass = vq.w;
-    if (mass <= R(0)) return;
+__device__ __forceinline__ void contactApply(V3<R> imp, V3<R> r, R inm, R ism, R iin, V3<R> &nv, Sphere<R> &sp,
+                                             ContactAcc &acc) {
+    nv = nv + inm * imp;
+    sp.velocity = sp.velocity - ism * imp;
+    const V3<R> ti = -cross(r, imp);
+    sp.angular = sp.angular + iin * ti;
+    acc.impulse_x += static_cast<double>(imp.x);
+    acc.impulse_y += static_cast<double>(imp.y);
+    acc.impulse_z += static_cast<double>(imp.z);
+}
+
+// The contact of one staged candidate, from its relative velocity on
+// (LatticePhysics.hpp:1338-1386). `max_pen` shadows acc.max_penetration in R:
+// the ledger only ever holds a widened R, so the comparison is the reference's.
+template <class R>
+__device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp, Staged<R> &c, V3<R> r, V3<R> normal,
+                                             R gap, R eff_n, R ism, R iin, bool correct, ContactAcc &acc, R &max_pen) {
     const R dt = S.dt;
-    const R ism = R(1) / sp.mass;
-    const R iin = R(1) / sp.inertia;
-    const R cr = sp.radius + S.c_node_radius;
-    const Q4<R> uq = uq_ref;
-    const V3<R> r = (xyz(x0q) + xyz(uq)) - sp.center;
-    const R distance = length(r);
-    const V3<R> normal = normalized(r);
-    const R gap = distance - cr;
-    V3<R> nv = xyz(vq);
+    V3<R> nv = xyz(c.v);
     const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
     const R vn = dot(rel, normal);
     if (gap > maxR(S.c_margin, -vn * dt)) return;
-    if (-gap > R(acc.max_penetration)) acc.max_penetration = static_cast<double>(-gap);
-    const R inm = R(1) / mass;
+    if (-gap > max_pen) {
+        max_pen = -gap;
+        acc.max_penetration = static_cast<double>(-gap);
+    }
+    const R inm = c.inm;
+    const R mass = c.v.w;
     const R restitution = -vn > S.c_threshold ? S.c_restitution : R(0);
     const R desired = gap > S.c_margin ? -gap / dt : -restitution * minR(vn, R(0));
-    const V3<R> rn = cross(r, normal);
-    const R ni = maxR(R(0), (desired - vn) / (inm + ism + iin * dot(rn, rn)));
+    const R ni = maxR(R(0), (desired - vn) / eff_n);
     if (ni > R(0)) {
-        const R before = R(0.5) * mass * dot(nv, nv);
-        auto apply = [&](V3<R> imp) {
-            nv = nv + inm * imp;
-            sp.velocity = sp.velocity - ism * imp;
-            const V3<R> ti = -cross(r, imp);
-            sp.angular = sp.angular + iin * ti;
-            acc.impulse_x += static_cast<double>(imp.x);
-            acc.impulse_y += static_cast<double>(imp.y);
-            acc.impulse_z += static_cast<double>(imp.z);
-        };
-        apply(ni * normal);
+        contactApply(ni * normal, r, inm, ism, iin, nv, sp, acc);
         const V3<R> after = nv - sp.velocity - cross(sp.angular, r);
         const V3<R> tangent = after - dot(after, normal) * normal;
         const R ts = length(tangent);
@@ -483,10 +500,10 @@ __device__ void sphereNode(const Settings<R> &S, Sphere<R> &sp, const Q4<R> &x0q
             const V3<R> rd = cross(r, d);
             const R stick = ts / (inm + ism + iin * dot(rd, rd));
             const R fi = stick <= S.c_static * ni ? stick : minR(stick, S.c_dynamic * ni);
-            apply(-fi * d);
+            contactApply(-fi * d, r, inm, ism, iin, nv, sp, acc);
         }
-        vq_ref = Q4<R>{nv.x, nv.y, nv.z, mass};
-        acc.dissipated += static_cast<double>(before - R(0.5) * mass * dot(nv, nv));
+        c.v = Q4<R>{nv.x, nv.y, nv.z, mass};
+        acc.dissipated += static_cast<double>(c.before - R(0.5) * mass * dot(nv, nv));
         ++acc.impulse_contacts;
     }
     if (correct && gap < -S.c_margin) {
@@ -494,58 +511,88 @@ __device__ void sphereNode(const Settings<R> &S, Sphere<R> &sp, const Q4<R> &x0q
         const R sum = inm + ism;
         const V3<R> ns = (corr * inm / sum) * normal;
         const V3<R> ss = -((corr * ism / sum) * normal);
-        const V3<R> un = xyz(uq) + ns;
-        uq_ref = Q4<R>{un.x, un.y, un.z, uq.w};
+        const V3<R> un = xyz(c.u) + ns;
+        c.u = Q4<R>{un.x, un.y, un.z, c.u.w};
         sp.center = sp.center + ss;
         if (corr > R(acc.max_correction)) acc.max_correction = static_cast<double>(corr);
     }
 }
 
-// The sequential contact pass (LatticePhysics.hpp:1389-1428), one CTA. The
-// candidates of a slab are staged into shared memory by the whole CTA, one
-// thread runs the contacts in list order -- the order is physics: every
-// contact moves the sphere the next one sees -- and the CTA writes the nodes
-// back. What the reference does per candidate after its contact (pass 1:
-// record the approach speed and predict; pass 2: the support velocity
-// response) touches that node alone, so it runs in the parallel write-back.
 constexpr unsigned kSphereThreads = 1024;
 
 template <class R>
 __global__ void __launch_bounds__(kSphereThreads) kSpherePass(Dev<R> L, Settings<R> S, int pass) {
     extern __shared__ __align__(16) unsigned char sphere_smem[];
-    Q4<R> *sx = reinterpret_cast<Q4<R> *>(sphere_smem);
-    Q4<R> *su = sx + kCandidatesPerBlock;
-    Q4<R> *sv = su + kCandidatesPerBlock;
+    Staged<R> *st = reinterpret_cast<Staged<R> *>(sphere_smem);
+    __shared__ Sphere<R> start;
     if (L.ctl->stop) return;
     Sphere<R> sp{};
     ContactAcc acc{};
     V3<R> c0{};
-    R e0 = R(0);
+    R e0 = R(0), max_pen = R(0);
     if (threadIdx.x == 0) {
         sp = *L.sphere;
         if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
         acc = L.ctl->contact;
+        max_pen = R(acc.max_penetration);
         c0 = sp.center;
         e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
+        start = sp;
     }
+    __syncthreads();
+    // Constant over the pass: the sphere's mass and inertia never change.
+    const R ism = R(1) / start.mass;
+    const R iin = R(1) / start.inertia;
+    const R cr = start.radius + S.c_node_radius;
     for (std::uint32_t b = 0; b < L.blocks; ++b) {
         const std::uint32_t n = L.cand_count[b];
         if (n == 0) continue;
         const std::uint32_t *list = L.cand_list + b * kCandidatesPerBlock;
         for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
             const std::uint32_t i = list[k];
-            sx[k] = L.x0[i];
-            su[k] = L.u[i];
-            sv[k] = L.v[i];
+            Staged<R> c;
+            c.u = L.u[i];
+            c.v = L.v[i];
+            const R mass = c.v.w;
+            const V3<R> p = xyz(L.x0[i]) + xyz(c.u);
+            c.inm = R(1) / mass;
+            c.before = R(0.5) * mass * dot(xyz(c.v), xyz(c.v));
+            if (pass == 1) {
+                const V3<R> r = p - start.center;
+                const R distance = length(r);
+                const V3<R> normal = normalized(r);
+                const V3<R> rn = cross(r, normal);
+                c.p = r;
+                c.normal = normal;
+                c.gap = distance - cr;
+                c.eff_n = c.inm + ism + iin * dot(rn, rn);
+            } else {
+                c.p = p;
+            }
+            st[k] = c;
         }
         __syncthreads();
-        if (threadIdx.x == 0)
-            for (std::uint32_t k = 0; k < n; ++k) sphereNode(S, sp, sx[k], su[k], sv[k], pass == 2, acc);
+        if (threadIdx.x == 0) {
+            for (std::uint32_t k = 0; k < n; ++k) {
+                Staged<R> &c = st[k];
+                if (c.v.w <= R(0)) continue;
+                if (pass == 1) {
+                    contactChain(S, sp, c, c.p, c.normal, c.gap, c.eff_n, ism, iin, false, acc, max_pen);
+                } else {
+                    const V3<R> r = c.p - sp.center;
+                    const R distance = length(r);
+                    const V3<R> normal = normalized(r);
+                    const V3<R> rn = cross(r, normal);
+                    const R eff_n = c.inm + ism + iin * dot(rn, rn);
+                    contactChain(S, sp, c, r, normal, distance - cr, eff_n, ism, iin, true, acc, max_pen);
+                }
+            }
+        }
         __syncthreads();
         for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
             const std::uint32_t i = list[k];
-            const Q4<R> vq = sv[k];
-            const Q4<R> uq = su[k];
+            const Q4<R> vq = st[k].v;
+            const Q4<R> uq = st[k].u;
             if (pass == 1) {
                 for (std::uint32_t p = 0; p < S.plane_count; ++p)
                     L.approach[p * L.N + i] = dot(xyz(vq), S.planes[p].normal);
@@ -735,7 +782,7 @@ __global__ void __launch_bounds__(kThreads) kSupportVelocity(Dev<R> L, Settings<
 // depends on the bond order only, never on thread timing: plastic work is
 // summed per tile by a fixed shuffle tree and the tiles in index order; broken
 // bonds and damage-record candidates are flagged one bit per bond and listed
-// in bond order by kScanTiles/kEmitEvents.
+// in bond order by kTileCounts/kBlockScan/kTopScan/kEmitEvents.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned floatBits(float x) { return __float_as_uint(x); }
 
@@ -852,92 +899,181 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
     }
 }
 
-// Block-wide exclusive scan helper for one value per thread (1024 threads).
-__device__ __forceinline__ unsigned blockExclusiveScan(unsigned x, unsigned *warp_sum, unsigned &total) {
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x / 32;
-    unsigned inc = x;
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffU, inc, o);
-        if (lane >= static_cast<unsigned>(o)) inc += y;
+// ---------------------------------------------------------------------------
+// The substep ledger's ordered lists and FP64 sums, fully parallel and in a
+// fixed order. A "tile" is 256 bonds of schedule order (8 bit words); a scan
+// block is kScanBlock tiles. Every sum below is formed in an order fixed by the
+// bond order alone: sequential inside a 32-bond word, a Hillis-Steele scan
+// across the words of a tile, across the tiles of a block, across the blocks.
+// ---------------------------------------------------------------------------
+constexpr unsigned kScanBlock = 1024;
+
+// Hillis-Steele inclusive scan of one double per thread across a 1024-thread
+// CTA (a fixed order); `buf` is 1024 doubles of shared memory.
+__device__ __forceinline__ double blockInclusiveScan(double x, double *buf) {
+    buf[threadIdx.x] = x;
+    __syncthreads();
+    for (unsigned o = 1; o < blockDim.x; o <<= 1) {
+        const double y = threadIdx.x >= o ? buf[threadIdx.x - o] : 0.0;
+        __syncthreads();
+        if (threadIdx.x >= o) buf[threadIdx.x] += y;
+        __syncthreads();
     }
-    if (lane == 31) warp_sum[warp] = inc;
+    const double r = buf[threadIdx.x];
     __syncthreads();
-    if (threadIdx.x < 32) {
-        unsigned s = warp_sum[threadIdx.x];
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffU, s, o);
-            if (threadIdx.x >= static_cast<unsigned>(o)) s += y;
-        }
-        warp_sum[threadIdx.x] = s;
-    }
-    __syncthreads();
-    total = warp_sum[31];
-    const unsigned before = (warp ? warp_sum[warp - 1] : 0U) + inc - x;
-    __syncthreads();
-    return before;
+    return r;
 }
 
-// One CTA: exclusive scans of the per-tile counts of broken bonds and of
-// damage candidates (turned into offsets in place), and the plastic work of
-// the substep summed over the tiles in a fixed order (each thread a contiguous
-// run of tiles, then a fixed tree over the threads).
+__device__ __forceinline__ unsigned blockExclusiveScanU(unsigned x, unsigned *buf, unsigned &total) {
+    buf[threadIdx.x] = x;
+    __syncthreads();
+    for (unsigned o = 1; o < blockDim.x; o <<= 1) {
+        const unsigned y = threadIdx.x >= o ? buf[threadIdx.x - o] : 0U;
+        __syncthreads();
+        if (threadIdx.x >= o) buf[threadIdx.x] += y;
+        __syncthreads();
+    }
+    const unsigned inclusive = buf[threadIdx.x];
+    total = buf[blockDim.x - 1];
+    __syncthreads();
+    return inclusive - x;
+}
+
+// Removed energy of a tile's broken bonds: per word, in bit order; across the
+// tile's words by an inclusive shuffle scan. Returns this lane's inclusive sum
+// (lane 7, or the last word of the tile, holds the tile's total).
+__device__ __forceinline__ double tileRemovedScan(double own) {
+    const unsigned lane = threadIdx.x & 31;
+    double inclusive = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffU, inclusive, o);
+        if (lane >= static_cast<unsigned>(o)) inclusive += y;
+    }
+    return inclusive;
+}
+
+// One warp per tile: broken-bond and damage-candidate counts and the tile's
+// removed energy.
 template <class R>
-__global__ void __launch_bounds__(1024) kScanTiles(Dev<R> L, int plastic) {
-    __shared__ unsigned warp_sum[32];
-    __shared__ double partial[1024];
+__global__ void __launch_bounds__(kThreads) kTileCounts(Dev<R> L) {
+    if (L.ctl->stop) return;
+    const unsigned tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const unsigned lane = threadIdx.x & 31;
+    if (tile >= L.tiles_b) return;
+    constexpr unsigned kWords = kThreads / 32;
+    const unsigned w = tile * kWords + lane;
+    const bool word = lane < kWords && w < L.words_b;
+    const unsigned bits = word ? L.ev_bits[w] : 0U;
+    const unsigned dbits = word ? L.dmg_bits[w] : 0U;
+    double own = 0.0;
+    for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[w * 32 + static_cast<unsigned>(__ffs(m) - 1)];
+    unsigned nb = __popc(bits), nd = __popc(dbits);
+    for (int o = 16; o > 0; o >>= 1) {
+        nb += __shfl_down_sync(0xffffffffU, nb, o);
+        nd += __shfl_down_sync(0xffffffffU, nd, o);
+    }
+    const double total = __shfl_sync(0xffffffffU, tileRemovedScan(own), 31);
+    if (lane == 0) {
+        L.ev_tile[tile] = nb;
+        L.dmg_tile[tile] = nd;
+        L.tile_removed[tile] = total;
+    }
+}
+
+// One CTA per scan block: exclusive offsets of the tiles inside the block (in
+// place) and the block's totals; the plastic work of the end-sample tiles of
+// the same index range is reduced by a fixed tree.
+template <class R>
+__global__ void __launch_bounds__(kScanBlock) kBlockScan(Dev<R> L, int plastic) {
+    __shared__ double dbuf[kScanBlock];
+    __shared__ unsigned ubuf[kScanBlock];
+    if (L.ctl->stop) return;
+    const unsigned t = blockIdx.x * kScanBlock + threadIdx.x;
+    const bool in = t < L.tiles_b;
+    unsigned tb = 0, td = 0;
+    const unsigned ob = blockExclusiveScanU(in ? L.ev_tile[t] : 0U, ubuf, tb);
+    const unsigned od = blockExclusiveScanU(in ? L.dmg_tile[t] : 0U, ubuf, td);
+    // The inclusive scan leaves dbuf holding every thread's inclusive sum.
+    (void)blockInclusiveScan(in ? L.tile_removed[t] : 0.0, dbuf);
+    const double exclusive = threadIdx.x ? dbuf[threadIdx.x - 1] : 0.0;
+    const double removed_total = dbuf[kScanBlock - 1];
+    __syncthreads();
+    if (in) {
+        L.ev_tile[t] = ob;
+        L.dmg_tile[t] = od;
+        L.tile_removed[t] = exclusive;
+    }
+    double work = 0.0;
+    if (plastic) {
+        dbuf[threadIdx.x] = in ? L.tile_plastic[t] : 0.0;
+        __syncthreads();
+        for (unsigned s = kScanBlock / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) dbuf[threadIdx.x] += dbuf[threadIdx.x + s];
+            __syncthreads();
+        }
+        work = dbuf[0];
+    }
+    if (threadIdx.x == 0) {
+        L.blk_ev[blockIdx.x] = tb;
+        L.blk_dmg[blockIdx.x] = td;
+        L.blk_removed[blockIdx.x] = removed_total;
+        L.blk_plastic[blockIdx.x] = work;
+    }
+}
+
+// One CTA: exclusive offsets of the blocks (rounds of 1024 blocks with a
+// carry), and the substep's totals.
+template <class R>
+__global__ void __launch_bounds__(kScanBlock) kTopScan(Dev<R> L, unsigned blocks) {
+    __shared__ double dbuf[kScanBlock];
+    __shared__ unsigned ubuf[kScanBlock];
+    __shared__ double plastic_carry;
     Ctl &c = *L.ctl;
     if (c.stop) return;
-    const unsigned T = L.tiles_b;
-    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
-    const unsigned first = threadIdx.x * per;
-    const unsigned last = first + per < T ? first + per : T;
-    // Broken bonds and damage candidates per schedule-order tile of 256 bonds,
-    // counted from the bit words the end sample set.
-    constexpr unsigned kWords = kThreads / 32;
-    unsigned nb = 0, nd = 0;
-    double work = 0.0;
-    for (unsigned t = first; t < last; ++t) {
-        unsigned cb = 0, cd = 0;
-        for (unsigned w = t * kWords; w < (t + 1) * kWords && w < L.words_b; ++w) {
-            cb += __popc(L.ev_bits[w]);
-            cd += __popc(L.dmg_bits[w]);
+    unsigned carry_b = 0, carry_d = 0;
+    double carry_r = 0.0;
+    if (threadIdx.x == 0) plastic_carry = 0.0;
+    for (unsigned base = 0; base < blocks; base += kScanBlock) {
+        const unsigned k = base + threadIdx.x;
+        const bool in = k < blocks;
+        unsigned tb = 0, td = 0;
+        const unsigned ob = blockExclusiveScanU(in ? L.blk_ev[k] : 0U, ubuf, tb);
+        const unsigned od = blockExclusiveScanU(in ? L.blk_dmg[k] : 0U, ubuf, td);
+        (void)blockInclusiveScan(in ? L.blk_removed[k] : 0.0, dbuf);
+        const double before = threadIdx.x ? dbuf[threadIdx.x - 1] : 0.0;
+        const double round_total = dbuf[kScanBlock - 1];
+        __syncthreads();
+        dbuf[threadIdx.x] = in ? L.blk_plastic[k] : 0.0;
+        __syncthreads();
+        for (unsigned s = kScanBlock / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) dbuf[threadIdx.x] += dbuf[threadIdx.x + s];
+            __syncthreads();
         }
-        L.ev_tile[t] = cb;
-        L.dmg_tile[t] = cd;
-        nb += cb;
-        nd += cd;
-        if (plastic) work += L.tile_plastic[t];
-    }
-    unsigned total_b = 0, total_d = 0;
-    unsigned run_b = blockExclusiveScan(nb, warp_sum, total_b);
-    unsigned run_d = blockExclusiveScan(nd, warp_sum, total_d);
-    for (unsigned t = first; t < last; ++t) {
-        const unsigned b = L.ev_tile[t], d = L.dmg_tile[t];
-        L.ev_tile[t] = run_b;
-        L.dmg_tile[t] = run_d;
-        run_b += b;
-        run_d += d;
-    }
-    partial[threadIdx.x] = work;
-    __syncthreads();
-    for (unsigned s = 512; s > 0; s >>= 1) {
-        if (threadIdx.x < s) partial[threadIdx.x] += partial[threadIdx.x + s];
+        if (in) {
+            L.blk_ev[k] = carry_b + ob;
+            L.blk_dmg[k] = carry_d + od;
+            L.blk_removed[k] = carry_r + before;
+        }
+        if (threadIdx.x == 0) plastic_carry += dbuf[0];
+        carry_b += tb;
+        carry_d += td;
+        carry_r += round_total;
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        c.event_count = total_b;
-        c.dmg_count = total_d;
-        c.plastic_substep = plastic ? partial[0] : 0.0;
-        c.removed_substep = 0.0;
+        c.event_count = carry_b;
+        c.dmg_count = carry_d;
+        c.removed_substep = carry_r;
+        c.plastic_substep = plastic_carry;
         c.energy_gain = 0;
         c.dirty_count = 0; // the restart of this substep has consumed the list
     }
 }
 
-// One warp per end-sample tile: writes the tile's broken bonds in bond order
-// with their removed energy and its in-tile inclusive prefix (a fixed order:
-// sequential inside each 32-bond word, a shuffle scan across the words), the
-// tile's removed-energy total, and the tile's damage candidates in order.
+// One warp per tile: the tile's broken bonds in bond order with their removed
+// energy and their prefix of the substep's removed energy (block offset, tile
+// offset, in-tile inclusive scan: the same orders as the counts), and its
+// damage candidates in order. The bit words are cleared for the next substep.
 template <class R>
 __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
     const Ctl &c = *L.ctl;
@@ -948,22 +1084,20 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
     constexpr unsigned kWords = kThreads / 32;
     const unsigned w = tile * kWords + lane;
     const bool word = lane < kWords && w < L.words_b;
-    const unsigned base = L.ev_tile[tile];
-    const unsigned next = tile + 1 < L.tiles_b ? L.ev_tile[tile + 1] : c.event_count;
-    if (next != base) {
-        unsigned bits = word ? L.ev_bits[w] : 0U;
+    const unsigned blk = tile / kScanBlock;
+    unsigned bits = word ? L.ev_bits[w] : 0U;
+    if (__any_sync(0xffffffffU, bits != 0)) {
         double own = 0.0;
         for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[w * 32 + static_cast<unsigned>(__ffs(m) - 1)];
+        const double inclusive = tileRemovedScan(own);
+        const double exclusive = __shfl_up_sync(0xffffffffU, inclusive, 1);
         unsigned n = __popc(bits), x = n;
-        double inclusive = own;
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
-            const double yb = __shfl_up_sync(0xffffffffU, inclusive, o);
-            if (lane >= static_cast<unsigned>(o)) { x += y; inclusive += yb; }
+            if (lane >= static_cast<unsigned>(o)) x += y;
         }
-        const double exclusive = __shfl_up_sync(0xffffffffU, inclusive, 1);
-        const double tile_total = __shfl_sync(0xffffffffU, inclusive, 31);
-        unsigned at = base + x - n;
+        unsigned at = L.blk_ev[blk] + L.ev_tile[tile] + x - n;
+        const double offset = L.blk_removed[blk] + L.tile_removed[tile];
         double run = lane == 0 ? 0.0 : exclusive;
         for (; bits; bits &= bits - 1) {
             const unsigned j = w * 32 + static_cast<unsigned>(__ffs(bits) - 1);
@@ -971,64 +1105,27 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
             run += e;
             L.ev_list[at] = j;
             L.ev_packed[at] = e;
-            L.ev_prefix[at] = run;
+            L.ev_prefix[at] = offset + run;
             ++at;
         }
-        if (lane == 0) L.tile_removed[tile] = tile_total;
-    } else if (lane == 0) {
-        L.tile_removed[tile] = 0.0;
+        if (word) L.ev_bits[w] = 0; // the end sample sets bits with atomicOr
     }
-    if (word) L.ev_bits[w] = 0; // the end sample sets bits with atomicOr: clear for the next substep
-    const unsigned dbase = L.dmg_tile[tile];
-    const unsigned dnext = tile + 1 < L.tiles_b ? L.dmg_tile[tile + 1] : c.dmg_count;
-    if (dnext != dbase) {
-        unsigned bits = word ? L.dmg_bits[w] : 0U;
-        unsigned n = __popc(bits), x = n;
+    unsigned dbits = word ? L.dmg_bits[w] : 0U;
+    if (__any_sync(0xffffffffU, dbits != 0)) {
+        unsigned n = __popc(dbits), x = n;
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffU, x, o);
             if (lane >= static_cast<unsigned>(o)) x += y;
         }
-        unsigned at = dbase + x - n;
-        for (; bits; bits &= bits - 1) {
-            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(bits) - 1);
+        unsigned at = L.blk_dmg[blk] + L.dmg_tile[tile] + x - n;
+        for (; dbits; dbits &= dbits - 1) {
+            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(dbits) - 1);
             L.dmg_list[at] = j;
             L.dmg_value[at] = L.ev_damage[j];
             ++at;
         }
+        if (word) L.dmg_bits[w] = 0;
     }
-    if (word) L.dmg_bits[w] = 0;
-}
-
-// One CTA: exclusive prefix of the tiles' removed energy in tile order (each
-// thread a contiguous run, a fixed tree over the threads), in place, and the
-// substep's total.
-template <class R>
-__global__ void __launch_bounds__(1024) kScanRemoved(Dev<R> L) {
-    __shared__ double part[1024];
-    Ctl &c = *L.ctl;
-    if (c.stop || c.event_count == 0) return;
-    const unsigned T = L.tiles_b;
-    const unsigned per = (T + blockDim.x - 1) / blockDim.x;
-    const unsigned first = threadIdx.x * per;
-    const unsigned last = first + per < T ? first + per : T;
-    double own = 0.0;
-    for (unsigned t = first; t < last; ++t) own += L.tile_removed[t];
-    part[threadIdx.x] = own;
-    __syncthreads();
-    // Hillis-Steele inclusive scan over the 1024 partials: a fixed order.
-    for (unsigned o = 1; o < 1024; o <<= 1) {
-        const double y = threadIdx.x >= o ? part[threadIdx.x - o] : 0.0;
-        __syncthreads();
-        part[threadIdx.x] += y;
-        __syncthreads();
-    }
-    double run = part[threadIdx.x] - own;
-    for (unsigned t = first; t < last; ++t) {
-        const double e = L.tile_removed[t];
-        L.tile_removed[t] = run;
-        run += e;
-    }
-    if (threadIdx.x == 1023) c.removed_substep = part[1023];
 }
 
 // Parallel over this substep's broken bonds, in list order: the energy-gain
@@ -1045,7 +1142,7 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(Dev<R> L) {
     const double fraction = c.energy_flat_fraction;
     for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const std::uint32_t j = L.ev_list[e];
-        const double running = prior + (L.tile_removed[j / kThreads] + L.ev_prefix[e]);
+        const double running = prior + L.ev_prefix[e];
         const double removed = L.ev_packed[e];
         if (removed > fraction * (running < 1.0e-12 ? 1.0e-12 : running)) atomicOr(&c.energy_gain, 1U);
         if (first_round) L.ffb[e] = j;
