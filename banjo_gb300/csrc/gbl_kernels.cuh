@@ -137,9 +137,46 @@ template <class R> struct Dev {
     double origin[3];
     Sphere<R> *sphere;
     Ctl *ctl;
+    unsigned *running; // lattices of the engine still running this call; a lattice that stops takes itself off
 };
 
 constexpr int kThreads = 256;
+
+// One CTA's share of a launch: a range of one lattice's nodes, bonds, tiles or
+// scan blocks (what the range indexes is the kernel's).
+struct Work {
+    std::uint32_t lattice, begin, end;
+};
+
+// What a launch covers. With many lattices (Many = true) every CTA reads its
+// item from `list` and its lattice's descriptor from `table`, so one launch
+// advances any number of independent lattices. A launch over one lattice
+// (Many = false) carries that lattice's descriptor in `one`, in the kernel's
+// parameter space, and CTA b covers [base + b*per, min(base + (b+1)*per, end)):
+// no dependent loads before the work itself.
+template <class R> struct Grid {
+    const Dev<R> *table;
+    const Work *list;
+    std::uint32_t base, end, per;
+    Dev<R> one;
+};
+
+template <bool Many, class R> __device__ __forceinline__ Work item(const Grid<R> &g) {
+    if (Many) return g.list[blockIdx.x];
+    const std::uint32_t b = g.base + blockIdx.x * g.per;
+    return Work{0U, b, b + g.per < g.end ? b + g.per : g.end};
+}
+
+// Items of a launch split into parts: {lattice, part, parts}.
+template <bool Many, class R> __device__ __forceinline__ Work part(const Grid<R> &g) {
+    if (Many) return g.list[blockIdx.x];
+    return Work{0U, blockIdx.x, gridDim.x};
+}
+
+template <class R, bool Many> __device__ __forceinline__ Dev<R> descriptor(const Grid<R> &g, const Work &w) {
+    if (Many) return g.table[w.lattice];
+    return g.one;
+}
 
 template <class R> __device__ __forceinline__ V3<R> pos(const Dev<R> &L, std::uint32_t i) {
     return xyz(L.x0[i]) + xyz(L.u[i]);
@@ -204,24 +241,29 @@ __device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
     L.strain[2 * i + 1] = Q4<R>{e[4], e[5], R(1), R(0)};
 }
 
-template <class R, bool Direct>
-__global__ void __launch_bounds__(kThreads) kStrainAll(Dev<R> L) {
+template <class R, bool Many, bool Direct>
+__global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < L.N) nodeStrain<R, Direct>(L, i);
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i < w.end) nodeStrain<R, Direct>(L, i);
 }
 
 // The start-of-substep restart after an upload (every node) or after a failure
 // round (the dirty nodes only: every other node's strain is unchanged, since
 // positions have not moved since the end sample and its bonds are the same;
 // src/fastlattice/ParallelCpuLatticeBackend.cpp:1718-1757 relies on the same fact).
-template <class R, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartStrain(Dev<R> L) {
+template <class R, bool Many, bool Direct>
+__global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const bool full = L.ctl->full_restart != 0;
-    const std::uint32_t count = full ? L.N : L.ctl->dirty_count;
-    for (std::uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x)
-        nodeStrain<R, Direct>(L, full ? t : L.dirty_list[t]);
+    // Items cover the node index range; a dirty list is never longer.
+    const std::uint32_t t = w.begin + threadIdx.x;
+    if (t >= w.end) return;
+    if (L.ctl->full_restart) nodeStrain<R, Direct>(L, t);
+    else if (t < L.ctl->dirty_count) nodeStrain<R, Direct>(L, L.dirty_list[t]);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,22 +323,30 @@ __device__ __forceinline__ void startSample(const Dev<R> &L, std::uint32_t j) {
     L.prev[j] = p;
 }
 
-template <class R, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartBonds(Dev<R> L) {
-    if (L.ctl->stop) return;
-    if (L.ctl->full_restart) {
-        for (std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < L.B; j += gridDim.x * blockDim.x)
-            startSample<R, Direct>(L, j);
-        return;
-    }
-    // Live bonds at a dirty node: one thread per (dirty node, neighbour slot).
-    // A bond with both ends dirty is sampled twice to the same values.
-    const std::uint64_t count = static_cast<std::uint64_t>(L.ctl->dirty_count) * L.D;
-    for (std::uint64_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        const std::uint32_t node = L.dirty_list[t / L.D];
-        const std::uint32_t k = static_cast<std::uint32_t>(t % L.D);
-        const std::uint32_t j = L.nbr_bond[static_cast<std::size_t>(k) * L.N + node];
-        if (j != kNoBond) startSample<R, Direct>(L, j);
+// Every live bond, after an upload: items cover the bond storage range.
+template <class R, bool Many, bool Direct>
+__global__ void __launch_bounds__(kThreads) kRestartBondsAll(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop || !L.ctl->full_restart) return;
+    const std::uint32_t d = w.begin + threadIdx.x;
+    if (d < w.end) startSample<R, Direct>(L, d);
+}
+
+// The live bonds at each dirty node, after a failure round: items cover the
+// node index range (one thread per dirty-list entry, over its neighbour
+// slots). A bond with both ends dirty is sampled twice to the same values.
+template <class R, bool Many, bool Direct>
+__global__ void __launch_bounds__(kThreads) kRestartBondsDirty(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop || L.ctl->full_restart) return;
+    const std::uint32_t t = w.begin + threadIdx.x;
+    if (t >= w.end || t >= L.ctl->dirty_count) return;
+    const std::uint32_t node = L.dirty_list[t];
+    for (std::uint32_t k = 0; k < L.D; ++k) {
+        const std::uint32_t d = L.nbr_bond[static_cast<std::size_t>(k) * L.N + node];
+        if (d != kNoBond) startSample<R, Direct>(L, d);
     }
 }
 
@@ -315,12 +365,14 @@ __device__ __forceinline__ bool sphereCandidate(const Settings<R> &S, const Sphe
     return gap <= reach;
 }
 
-template <class R>
-__global__ void __launch_bounds__(kThreads) kKick(Dev<R> L, Settings<R> S) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kKick(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const std::uint32_t i = w.begin + threadIdx.x; // items start on multiples of 256: warps cover whole bit words
     bool cand = false;
-    if (i < L.N) {
+    if (i < w.end) {
         Q4<R> vq = L.v[i];
         const Q4<R> uq = L.u[i];
         V3<R> vel = xyz(vq);
@@ -338,19 +390,19 @@ __global__ void __launch_bounds__(kThreads) kKick(Dev<R> L, Settings<R> S) {
                     const double n[3] = {double(after.x), double(after.y), double(after.z)};
                     const double imp[3] = {m * (n[0] - o[0]), m * (n[1] - o[1]), m * (n[2] - o[2])};
                     const V3<R> p = xyz(L.x0[i]) + xyz(uq);
-                    const double w[3] = {L.origin[0] + double(p.x), L.origin[1] + double(p.y), L.origin[2] + double(p.z)};
+                    const double wp[3] = {L.origin[0] + double(p.x), L.origin[1] + double(p.y), L.origin[2] + double(p.z)};
                     const double dt = static_cast<double>(S.dt);
                     const double rq[3] = {dt * L.ext_req[3 * i], dt * L.ext_req[3 * i + 1], dt * L.ext_req[3 * i + 2]};
                     double *c = L.ext_contrib + 13 * static_cast<std::size_t>(i);
                     c[0] = imp[0]; c[1] = imp[1]; c[2] = imp[2];
-                    c[3] = w[1] * imp[2] - w[2] * imp[1];
-                    c[4] = w[2] * imp[0] - w[0] * imp[2];
-                    c[5] = w[0] * imp[1] - w[1] * imp[0];
+                    c[3] = wp[1] * imp[2] - wp[2] * imp[1];
+                    c[4] = wp[2] * imp[0] - wp[0] * imp[2];
+                    c[5] = wp[0] * imp[1] - wp[1] * imp[0];
                     c[6] = imp[0] * (.5 * (o[0] + n[0])) + imp[1] * (.5 * (o[1] + n[1])) + imp[2] * (.5 * (o[2] + n[2]));
                     c[7] = rq[0]; c[8] = rq[1]; c[9] = rq[2];
-                    c[10] = w[1] * rq[2] - w[2] * rq[1];
-                    c[11] = w[2] * rq[0] - w[0] * rq[2];
-                    c[12] = w[0] * rq[1] - w[1] * rq[0];
+                    c[10] = wp[1] * rq[2] - wp[2] * rq[1];
+                    c[11] = wp[2] * rq[0] - wp[0] * rq[2];
+                    c[12] = wp[0] * rq[1] - wp[1] * rq[0];
                 }
             }
         }
@@ -379,22 +431,24 @@ __global__ void __launch_bounds__(kThreads) kKick(Dev<R> L, Settings<R> S) {
 
 // Ordered candidate lists per slab, capped at 1024 (CpuLatticeBackend.cpp:375-386):
 // one CTA per slab scans its bit words in node order.
-template <class R>
-__global__ void __launch_bounds__(1024) kCandidates(Dev<R> L) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(1024) kCandidates(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
     __shared__ std::uint32_t warp_total[32];
     __shared__ std::uint32_t carry;
-    const std::uint32_t blk = blockIdx.x;
+    const std::uint32_t blk = w.begin; // one item per (lattice, slab)
     const std::uint32_t nb = L.node_block_begin[blk], ne = L.node_block_begin[blk + 1];
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const std::uint32_t w0 = nb / 32, w1 = ne == nb ? w0 : (ne - 1) / 32 + 1;
     for (std::uint32_t base = w0; base < w1; base += blockDim.x) {
-        const std::uint32_t w = base + threadIdx.x;
+        const std::uint32_t word = base + threadIdx.x;
         std::uint32_t bits = 0;
-        if (w < w1) {
-            bits = L.cand_bits[w];
-            const std::uint32_t lo = w * 32, hi = lo + 32;
+        if (word < w1) {
+            bits = L.cand_bits[word];
+            const std::uint32_t lo = word * 32, hi = lo + 32;
             if (nb > lo) bits &= ~0U << (nb - lo);
             if (ne < hi) bits &= (ne - lo) >= 32 ? ~0U : ((1U << (ne - lo)) - 1U);
         }
@@ -420,7 +474,7 @@ __global__ void __launch_bounds__(1024) kCandidates(Dev<R> L) {
         while (bits) {
             const int b = __ffs(bits) - 1;
             bits &= bits - 1;
-            if (before < kCandidatesPerBlock) L.cand_list[blk * kCandidatesPerBlock + before] = w * 32 + b;
+            if (before < kCandidatesPerBlock) L.cand_list[blk * kCandidatesPerBlock + before] = word * 32 + b;
             ++before;
         }
         __syncthreads();
@@ -520,8 +574,10 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
 
 constexpr unsigned kSphereThreads = 1024;
 
-template <class R>
-__global__ void __launch_bounds__(kSphereThreads) kSpherePass(Dev<R> L, Settings<R> S, int pass) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> launch, Settings<R> S, int pass) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     extern __shared__ __align__(16) unsigned char sphere_smem[];
     Staged<R> *st = reinterpret_cast<Staged<R> *>(sphere_smem);
     __shared__ Sphere<R> start;
@@ -644,11 +700,13 @@ __device__ __forceinline__ bool supportProject(const Dev<R> &L, const Settings<R
     return projected;
 }
 
-template <class R, bool Direct, bool First, bool Last, bool Plastic, bool Support>
-__global__ void __launch_bounds__(kThreads) kSolve(Dev<R> L, Settings<R> S, std::uint32_t begin, std::uint32_t end) {
+template <class R, bool Many, bool Direct, bool First, bool Last, bool Plastic, bool Support>
+__global__ void __launch_bounds__(kThreads) kSolve(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t d = begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= end) return;
+    const std::uint32_t d = w.begin + threadIdx.x;
+    if (d >= w.end) return;
     const BondRec<R> rec = ldStream(L.rec + d);
     const std::uint32_t a = endA(rec), b = endB(rec);
     Q4<R> qa, qb;
@@ -709,11 +767,13 @@ __global__ void __launch_bounds__(kThreads) kSolve(Dev<R> L, Settings<R> S, std:
 }
 
 // Radial pair damping of one level (LatticePhysics.hpp:1170-1184).
-template <class R, bool Direct>
-__global__ void __launch_bounds__(kThreads) kDamp(Dev<R> L, std::uint32_t begin, std::uint32_t end, R fraction) {
+template <class R, bool Many, bool Direct>
+__global__ void __launch_bounds__(kThreads) kDamp(const Grid<R> launch, R fraction) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t d = begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= end) return;
+    const std::uint32_t d = w.begin + threadIdx.x;
+    if (d >= w.end) return;
     const BondRec<R> rec = L.rec[d];
     if (rec.a & kDeadBit) return;
     const std::uint32_t a = endA(rec), b = endB(rec);
@@ -733,11 +793,13 @@ __global__ void __launch_bounds__(kThreads) kDamp(Dev<R> L, std::uint32_t begin,
 
 // Support projection of the nodes that have no bond to carry it (isolated
 // nodes), after a sweep (LatticePhysics.hpp:1255-1261).
-template <class R>
-__global__ void __launch_bounds__(kThreads) kSupportIsolated(Dev<R> L, Settings<R> S) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kSupportIsolated(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= L.isolated_count) return;
+    const std::uint32_t t = w.begin + threadIdx.x;
+    if (t >= w.end) return;
     const std::uint32_t i = L.isolated[t];
     const Q4<R> uq = L.u[i];
     V3<R> u = xyz(uq);
@@ -748,11 +810,13 @@ __global__ void __launch_bounds__(kThreads) kSupportIsolated(Dev<R> L, Settings<
 
 // Velocity from accepted positions, then the support response of
 // non-candidates when no damping sweep follows (LatticePhysics.hpp:1725-1730).
-template <class R>
-__global__ void __launch_bounds__(kThreads) kVelocity(Dev<R> L, Settings<R> S, int respond) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kVelocity(const Grid<R> launch, Settings<R> S, int respond) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= L.N) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i >= w.end) return;
     const Q4<R> vq = L.v[i];
     V3<R> vel = (xyz(L.u[i]) - xyz(L.up[i])) / S.dt;
     if (respond && !L.candidate[i])
@@ -762,11 +826,13 @@ __global__ void __launch_bounds__(kThreads) kVelocity(Dev<R> L, Settings<R> S, i
 }
 
 // Support response of non-candidates after the damping sweep (CpuLatticeBackend.cpp:414-415).
-template <class R>
-__global__ void __launch_bounds__(kThreads) kSupportVelocity(Dev<R> L, Settings<R> S) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kSupportVelocity(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= L.N || L.candidate[i]) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i >= w.end || L.candidate[i]) return;
     const Q4<R> vq = L.v[i];
     V3<R> vel = xyz(vq);
     for (std::uint32_t p = 0; p < S.plane_count; ++p)
@@ -792,16 +858,18 @@ __device__ __forceinline__ double warpSumFixed(double x) {
     return x;
 }
 
-template <class R, bool Direct, bool Plastic>
-__global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) {
+template <class R, bool Many, bool Direct, bool Plastic>
+__global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     __shared__ double tile_work[kThreads / 32];
     __shared__ unsigned peak[4];
     if (L.ctl->stop) return;
-    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; // storage index
+    const std::uint32_t j = w.begin + threadIdx.x; // storage index; items start on multiples of 256
     if (threadIdx.x < 4) peak[threadIdx.x] = 0;
     __syncthreads();
     double plastic_work = 0.0;
-    if (j < L.B) {
+    if (j < w.end) {
         const BondRec<R> rec = L.rec[j];
         if (!(rec.a & kDeadBit)) {
             const std::uint32_t a = endA(rec), b = endB(rec);
@@ -884,14 +952,14 @@ __global__ void __launch_bounds__(kThreads) kEndSample(Dev<R> L, Settings<R> S) 
             if (Plastic && S.yield_stretch > R(0)) atomicMax(&peak[3], floatBits(plastic_stretch));
         }
     }
-    double work = 0.0;
-    if (Plastic) work = warpSumFixed(plastic_work);
-    if ((threadIdx.x & 31) == 0) tile_work[threadIdx.x / 32] = work;
+    double warp_work = 0.0;
+    if (Plastic) warp_work = warpSumFixed(plastic_work);
+    if ((threadIdx.x & 31) == 0) tile_work[threadIdx.x / 32] = warp_work;
     __syncthreads();
     if (threadIdx.x == 0) {
         double wsum = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) wsum += tile_work[w];
-        L.tile_plastic[blockIdx.x] = wsum;
+        for (int q = 0; q < kThreads / 32; ++q) wsum += tile_work[q];
+        L.tile_plastic[w.begin / kThreads] = wsum;
         if (peak[0]) atomicMax(&L.ctl->max_t, peak[0]);
         if (peak[1]) atomicMax(&L.ctl->max_c, peak[1]);
         if (peak[2]) atomicMax(&L.ctl->max_s, peak[2]);
@@ -954,19 +1022,21 @@ __device__ __forceinline__ double tileRemovedScan(double own) {
 
 // One warp per tile: broken-bond and damage-candidate counts and the tile's
 // removed energy.
-template <class R>
-__global__ void __launch_bounds__(kThreads) kTileCounts(Dev<R> L) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kTileCounts(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const unsigned tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const unsigned tile = w.begin + threadIdx.x / 32; // items: up to 8 tiles of one lattice
     const unsigned lane = threadIdx.x & 31;
-    if (tile >= L.tiles_b) return;
+    if (tile >= w.end) return;
     constexpr unsigned kWords = kThreads / 32;
-    const unsigned w = tile * kWords + lane;
-    const bool word = lane < kWords && w < L.words_b;
-    const unsigned bits = word ? L.ev_bits[w] : 0U;
-    const unsigned dbits = word ? L.dmg_bits[w] : 0U;
+    const unsigned wd = tile * kWords + lane;
+    const bool word = lane < kWords && wd < L.words_b;
+    const unsigned bits = word ? L.ev_bits[wd] : 0U;
+    const unsigned dbits = word ? L.dmg_bits[wd] : 0U;
     double own = 0.0;
-    for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[w * 32 + static_cast<unsigned>(__ffs(m) - 1)];
+    for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[wd * 32 + static_cast<unsigned>(__ffs(m) - 1)];
     unsigned nb = __popc(bits), nd = __popc(dbits);
     for (int o = 16; o > 0; o >>= 1) {
         nb += __shfl_down_sync(0xffffffffU, nb, o);
@@ -983,12 +1053,15 @@ __global__ void __launch_bounds__(kThreads) kTileCounts(Dev<R> L) {
 // One CTA per scan block: exclusive offsets of the tiles inside the block (in
 // place) and the block's totals; the plastic work of the end-sample tiles of
 // the same index range is reduced by a fixed tree.
-template <class R>
-__global__ void __launch_bounds__(kScanBlock) kBlockScan(Dev<R> L, int plastic) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kScanBlock) kBlockScan(const Grid<R> launch, int plastic) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     __shared__ double dbuf[kScanBlock];
     __shared__ unsigned ubuf[kScanBlock];
     if (L.ctl->stop) return;
-    const unsigned t = blockIdx.x * kScanBlock + threadIdx.x;
+    const unsigned blk = w.begin; // one item per (lattice, scan block)
+    const unsigned t = blk * kScanBlock + threadIdx.x;
     const bool in = t < L.tiles_b;
     unsigned tb = 0, td = 0;
     const unsigned ob = blockExclusiveScanU(in ? L.ev_tile[t] : 0U, ubuf, tb);
@@ -1003,7 +1076,7 @@ __global__ void __launch_bounds__(kScanBlock) kBlockScan(Dev<R> L, int plastic) 
         L.dmg_tile[t] = od;
         L.tile_removed[t] = exclusive;
     }
-    double work = 0.0;
+    double block_work = 0.0;
     if (plastic) {
         dbuf[threadIdx.x] = in ? L.tile_plastic[t] : 0.0;
         __syncthreads();
@@ -1011,20 +1084,23 @@ __global__ void __launch_bounds__(kScanBlock) kBlockScan(Dev<R> L, int plastic) 
             if (threadIdx.x < s) dbuf[threadIdx.x] += dbuf[threadIdx.x + s];
             __syncthreads();
         }
-        work = dbuf[0];
+        block_work = dbuf[0];
     }
     if (threadIdx.x == 0) {
-        L.blk_ev[blockIdx.x] = tb;
-        L.blk_dmg[blockIdx.x] = td;
-        L.blk_removed[blockIdx.x] = removed_total;
-        L.blk_plastic[blockIdx.x] = work;
+        L.blk_ev[blk] = tb;
+        L.blk_dmg[blk] = td;
+        L.blk_removed[blk] = removed_total;
+        L.blk_plastic[blk] = block_work;
     }
 }
 
 // One CTA: exclusive offsets of the blocks (rounds of 1024 blocks with a
 // carry), and the substep's totals.
-template <class R>
-__global__ void __launch_bounds__(kScanBlock) kTopScan(Dev<R> L, unsigned blocks) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kScanBlock) kTopScan(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    const unsigned blocks = L.tiles_b / kScanBlock + 1; // one item per lattice
     __shared__ double dbuf[kScanBlock];
     __shared__ unsigned ubuf[kScanBlock];
     __shared__ double plastic_carry;
@@ -1074,21 +1150,23 @@ __global__ void __launch_bounds__(kScanBlock) kTopScan(Dev<R> L, unsigned blocks
 // energy and their prefix of the substep's removed energy (block offset, tile
 // offset, in-tile inclusive scan: the same orders as the counts), and its
 // damage candidates in order. The bit words are cleared for the next substep.
-template <class R>
-__global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kEmitEvents(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     const Ctl &c = *L.ctl;
     if (c.stop || (c.event_count == 0 && c.dmg_count == 0)) return;
-    const unsigned tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const unsigned tile = w.begin + threadIdx.x / 32;
     const unsigned lane = threadIdx.x & 31;
-    if (tile >= L.tiles_b) return;
+    if (tile >= w.end) return;
     constexpr unsigned kWords = kThreads / 32;
-    const unsigned w = tile * kWords + lane;
-    const bool word = lane < kWords && w < L.words_b;
+    const unsigned wd = tile * kWords + lane;
+    const bool word = lane < kWords && wd < L.words_b;
     const unsigned blk = tile / kScanBlock;
-    unsigned bits = word ? L.ev_bits[w] : 0U;
+    unsigned bits = word ? L.ev_bits[wd] : 0U;
     if (__any_sync(0xffffffffU, bits != 0)) {
         double own = 0.0;
-        for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[w * 32 + static_cast<unsigned>(__ffs(m) - 1)];
+        for (unsigned m = bits; m; m &= m - 1) own += L.ev_removed[wd * 32 + static_cast<unsigned>(__ffs(m) - 1)];
         const double inclusive = tileRemovedScan(own);
         const double exclusive = __shfl_up_sync(0xffffffffU, inclusive, 1);
         unsigned n = __popc(bits), x = n;
@@ -1100,7 +1178,7 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
         const double offset = L.blk_removed[blk] + L.tile_removed[tile];
         double run = lane == 0 ? 0.0 : exclusive;
         for (; bits; bits &= bits - 1) {
-            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(bits) - 1);
+            const unsigned j = wd * 32 + static_cast<unsigned>(__ffs(bits) - 1);
             const double e = L.ev_removed[j];
             run += e;
             L.ev_list[at] = j;
@@ -1108,9 +1186,9 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
             L.ev_prefix[at] = offset + run;
             ++at;
         }
-        if (word) L.ev_bits[w] = 0; // the end sample sets bits with atomicOr
+        if (word) L.ev_bits[wd] = 0; // the end sample sets bits with atomicOr
     }
-    unsigned dbits = word ? L.dmg_bits[w] : 0U;
+    unsigned dbits = word ? L.dmg_bits[wd] : 0U;
     if (__any_sync(0xffffffffU, dbits != 0)) {
         unsigned n = __popc(dbits), x = n;
         for (int o = 1; o < 32; o <<= 1) {
@@ -1119,12 +1197,12 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
         }
         unsigned at = L.blk_dmg[blk] + L.dmg_tile[tile] + x - n;
         for (; dbits; dbits &= dbits - 1) {
-            const unsigned j = w * 32 + static_cast<unsigned>(__ffs(dbits) - 1);
+            const unsigned j = wd * 32 + static_cast<unsigned>(__ffs(dbits) - 1);
             L.dmg_list[at] = j;
             L.dmg_value[at] = L.ev_damage[j];
             ++at;
         }
-        if (word) L.dmg_bits[w] = 0;
+        if (word) L.dmg_bits[wd] = 0;
     }
 }
 
@@ -1132,15 +1210,18 @@ __global__ void __launch_bounds__(kThreads) kEmitEvents(Dev<R> L) {
 // test of each bond against the running removed energy it would see
 // (CpuLatticeBackend.cpp:469-474), the first-failure list, and the dirty
 // marks and list of the next substep's restart (CpuLatticeBackend.cpp:476-477).
-template <class R>
-__global__ void __launch_bounds__(kThreads) kLedgerBroken(Dev<R> L) {
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kLedgerBroken(const Grid<R> launch) {
+    const Work w = part<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     Ctl &c = *L.ctl;
     if (c.stop) return;
     const unsigned n = c.event_count;
     const bool first_round = c.broken_bonds == 0;
     const double prior = c.removed_energy;
     const double fraction = c.energy_flat_fraction;
-    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    // Items: part `begin` of `end` parts of this lattice's event list.
+    for (unsigned e = w.begin * blockDim.x + threadIdx.x; e < n; e += w.end * blockDim.x) {
         const std::uint32_t j = L.ev_list[e];
         const double running = prior + L.ev_prefix[e];
         const double removed = L.ev_packed[e];
@@ -1164,13 +1245,16 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(Dev<R> L) {
 // contact, the failure-round bookkeeping and the exit rules
 // (CpuLatticeBackend.cpp:279-298, 441-488).
 // ---------------------------------------------------------------------------
-template <class R>
-__global__ void kLedger(Dev<R> L, Settings<R> S) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+template <class R, bool Many>
+__global__ void kLedger(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (threadIdx.x != 0) return;
     Ctl &c = *L.ctl;
     if (c.stop) return;
     if (c.error) {
         c.stop = 1;
+        atomicSub(L.running, 1U);
         return;
     }
     const unsigned long long step = c.total_steps;
@@ -1226,7 +1310,10 @@ __global__ void kLedger(Dev<R> L, Settings<R> S) {
         : exitReason(c.total_steps, c.broken_bonds, c.last_failure_step, c.quiet_steps, c.min_steps, c.no_failure_steps,
                      c.energy_flat_steps, c.last_energy_gain_step, c.calm_steps, c.last_damage_gain_step, c.max_damage,
                      c.calm_damage_margin, c.removed_energy, c.removable_energy > 0 ? available : 0.0);
-    if (c.exit_reason != 0) c.stop = 1;
+    if (c.exit_reason != 0) {
+        c.stop = 1;
+        atomicSub(L.running, 1U);
+    }
 }
 
 } // namespace gbl

@@ -170,6 +170,19 @@ def library() -> C.CDLL:
         "gbl_build_state": ([C.POINTER(MatterView), vp, f64p, C.POINTER(vp)], C.c_int),
         "gbl_state_view_of": ([vp, C.POINTER(StateView)], C.c_int), "gbl_state_pin": ([vp, u8p], C.c_int),
         "gbl_state_free": ([vp], None),
+        "gbl_batch_create": ([C.c_int, C.POINTER(vp)], C.c_int), "gbl_batch_destroy": ([vp], None),
+        "gbl_batch_add": ([vp, C.POINTER(ScheduleView), C.POINTER(StateView), C.POINTER(Sphere),
+                           C.POINTER(C.c_uint32)], C.c_int),
+        "gbl_batch_settle": ([vp, C.POINTER(StepSettings)], C.c_int),
+        "gbl_batch_set_external_forces": ([vp, C.c_uint32, f64p, C.c_uint64, C.c_uint64], C.c_int),
+        "gbl_batch_run": ([vp, C.POINTER(RunControlC)], C.c_int),
+        "gbl_batch_size": ([vp, C.POINTER(C.c_uint32)], C.c_int),
+        "gbl_batch_status": ([vp, C.c_uint32, C.POINTER(RunStatus)], C.c_int),
+        "gbl_batch_download": ([vp, C.c_uint32, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
+        "gbl_batch_first_failure_bonds": ([vp, C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_batch_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
+        "gbl_batch_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_batch_set_stream": ([vp, vp], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -502,6 +515,82 @@ def make_gb300_lattice_backend(schedule: Schedule, precision: str = "float", thr
     return Backend(schedule, precision, threads_per_block)
 
 
+class Batch:
+    """Independent lattices stepped together on the device, sharing step
+    settings; each lattice's results equal the same lattice run alone. Replaces
+    the reference's one-backend-per-trial loop (TileImpactScene.cpp:345-351, 777)."""
+
+    def __init__(self, precision: str = "float"):
+        self._h = None
+        h = C.c_void_p()
+        _call(library().gbl_batch_create, 1 if precision == "double" else 0, C.byref(h))
+        self._h = h
+        self.precision = precision
+        self._keep = []  # schedules stay alive while the batch refers to their lattices
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_batch_destroy(self._h)
+            self._h = None
+
+    def add(self, schedule: Schedule, state: State, sphere: Sphere) -> int:
+        k = C.c_uint32()
+        _call(library().gbl_batch_add, self._h, C.byref(schedule.view), C.byref(state.view), C.byref(sphere),
+              C.byref(k))
+        self._keep.append(schedule)
+        return int(k.value)
+
+    def settle(self, settings: StepSettings) -> None:
+        _call(library().gbl_batch_settle, self._h, C.byref(settings))
+
+    def __len__(self) -> int:
+        n = C.c_uint32()
+        _call(library().gbl_batch_size, self._h, C.byref(n))
+        return int(n.value)
+
+    def set_external_forces(self, index: int, forces, substeps: int) -> None:
+        if forces is None or len(forces) == 0:
+            _call(library().gbl_batch_set_external_forces, self._h, index, None, 0, int(substeps))
+            return
+        f = np.ascontiguousarray(forces, dtype=np.float64).reshape(-1)
+        _call(library().gbl_batch_set_external_forces, self._h, index, _ptr(f, C.c_double), f.size // 3,
+              int(substeps))
+
+    def run(self, control: RunControl) -> None:
+        ctl = control.c()
+        _call(library().gbl_batch_run, self._h, C.byref(ctl))
+
+    def status(self, index: int) -> RunStatus:
+        st = RunStatus()
+        _call(library().gbl_batch_status, self._h, index, C.byref(st))
+        return st
+
+    def download(self, index: int, state: State) -> Sphere:
+        sp = Sphere()
+        _call(library().gbl_batch_download, self._h, index, C.byref(state.view), C.byref(sp))
+        return sp
+
+    def first_failure_bonds(self, index: int) -> np.ndarray:
+        n = C.c_uint64()
+        _call(library().gbl_batch_first_failure_bonds, self._h, index, None, 0, C.byref(n))
+        out = np.zeros(n.value, dtype=np.uint32)
+        _call(library().gbl_batch_first_failure_bonds, self._h, index, _ptr(out, C.c_uint32), n.value, C.byref(n))
+        return out
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _call(library().gbl_batch_set_stream, self._h, C.c_void_p(stream_ptr) if stream_ptr else None)
+
+    def kernels_per_substep(self) -> int:
+        n = C.c_uint64()
+        _call(library().gbl_batch_kernels_per_substep, self._h, C.byref(n))
+        return int(n.value)
+
+    def profile_phases(self, substeps: int) -> dict:
+        out = np.zeros(16, dtype=np.float64)
+        _call(library().gbl_batch_profile_phases, self._h, int(substeps), _ptr(out, C.c_double))
+        return {PHASE_NAMES[k]: float(out[k]) for k in range(16)}
+
+
 def status_arrays(st: RunStatus) -> dict:
     """RunStatus packed as the case files pack it (oracle/case_layout.hpp)."""
     u = np.zeros(13, dtype=np.uint64)
@@ -566,3 +655,44 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
     if per_substep:
         out["break_step"] = break_step
     return out
+
+
+def _outputs(state: State, sp: Sphere, ffb: np.ndarray, st: RunStatus) -> dict:
+    out = {"u": state.u.copy(), "u_prev": state.u_prev.copy(), "v": state.v.copy(), "alive": state.alive.copy(),
+           "failure_mode": state.failure_mode.copy(), "damage": state.damage.copy(),
+           "plastic_extension": state.plastic_extension.copy(), "plastic_strain": state.plastic_strain.copy(),
+           "prev_tensile": state.prev_tensile.copy(), "prev_compressive": state.prev_compressive.copy(),
+           "prev_shear": state.prev_shear.copy(), "sphere_out": pack_sphere(sp), "first_failure_bonds": ffb}
+    out.update(status_arrays(st))
+    return out
+
+
+def run_batch(cases: list, precision: str = "float", control: RunControl | None = None) -> list:
+    """Runs scene cases as one batch (they must share step settings) and
+    returns one output dict per case: the state and status keys of run_case.
+    Every case runs `control` (default: the longest case's substep count);
+    exit rules stop each case on its own."""
+    for c in cases[1:]:
+        if not np.array_equal(c["settings"], cases[0]["settings"]):
+            raise ValueError("the cases of one batch share their step settings")
+    batch = Batch(precision)
+    settings = step_settings(cases[0]["settings"])
+    settings.direct_arithmetic = 1 if precision == "double" else 0
+    states = []
+    for c in cases:
+        n = int(c["node_count"][0])
+        sched = build_lattice_schedule(n, c["bond_a"], c["bond_b"], c["node_block_begin"])
+        state = build_lattice_state(c, sched)
+        batch.add(sched, state, sphere_state(c["sphere"]))
+        states.append(state)
+    batch.settle(settings)
+    for k, c in enumerate(cases):
+        if c.get("forces") is not None and "force_ramp_steps" not in c:
+            batch.set_external_forces(k, c["forces"], int(c["force_substeps"][0]))
+    steps = max(int(c["steps"][0]) for c in cases)
+    batch.run(control if control is not None else RunControl(max_steps=steps))
+    outs = []
+    for k, state in enumerate(states):
+        sp = batch.download(k, state)
+        outs.append(_outputs(state, sp, batch.first_failure_bonds(k), batch.status(k)))
+    return outs

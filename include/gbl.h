@@ -279,6 +279,41 @@ gbl_result gbl_kernels_per_substep(gbl_backend *backend, uint64_t *count);
  * gbl_run with max_steps = substeps and exit rules off. */
 gbl_result gbl_profile_phases(gbl_backend *backend, uint64_t substeps, double *phase_ms);
 
+/* ---- The batch: many independent lattices advanced together. ----
+ * The reference runs a batch of trials as one backend per trial
+ * (runTileImpact, src/fastlattice/TileImpactScene.cpp:777; makeBackend
+ * :345-351); these calls replace that loop with one device-resident set of
+ * lattices stepped by shared launches, one substep per launch sequence for
+ * every lattice at once. Each lattice keeps its own state, control block,
+ * ledgers and exit rules: its results are bit for bit those of the same
+ * lattice run alone by gbl_run. The lattices share the step settings.
+ *
+ * Order: gbl_batch_create, gbl_batch_add per lattice (uploads it),
+ * gbl_batch_settle (settings; resets every lattice's RunStatus), then any
+ * number of gbl_batch_run; loads, status and downloads per lattice index.
+ * A lattice that meets an exit rule stops; the others go on. gbl_batch_run
+ * returns when every lattice has stopped or after max_steps substeps. */
+typedef struct gbl_batch gbl_batch;
+gbl_result gbl_batch_create(int precision, gbl_batch **out);
+void gbl_batch_destroy(gbl_batch *batch);
+/* Uploads one lattice (schedule and state as for gbl_create/gbl_upload);
+ * `index` receives its position in the batch. */
+gbl_result gbl_batch_add(gbl_batch *batch, const gbl_schedule_view *schedule, const gbl_state_view *state,
+                         const gbl_sphere *sphere, uint32_t *index);
+gbl_result gbl_batch_settle(gbl_batch *batch, const gbl_step_settings *settings);
+gbl_result gbl_batch_set_external_forces(gbl_batch *batch, uint32_t index, const double *forces_world_n,
+                                         uint64_t count, uint64_t substeps);
+gbl_result gbl_batch_run(gbl_batch *batch, const gbl_run_control *control);
+gbl_result gbl_batch_size(const gbl_batch *batch, uint32_t *count);
+gbl_result gbl_batch_status(gbl_batch *batch, uint32_t index, gbl_run_status *status_out);
+gbl_result gbl_batch_download(gbl_batch *batch, uint32_t index, gbl_state_view *state, gbl_sphere *sphere);
+gbl_result gbl_batch_first_failure_bonds(gbl_batch *batch, uint32_t index, uint32_t *out, uint64_t capacity,
+                                         uint64_t *count);
+/* As gbl_profile_phases, over every lattice of the batch. */
+gbl_result gbl_batch_profile_phases(gbl_batch *batch, uint64_t substeps, double *phase_ms);
+gbl_result gbl_batch_kernels_per_substep(gbl_batch *batch, uint64_t *count);
+gbl_result gbl_batch_set_stream(gbl_batch *batch, void *cuda_stream);
+
 /* The bonds that broke between two aliveness snapshots (one byte per bond,
  * schedule order, non-zero = alive), listed in schedule order -- without
  * allocating anything. This entry point has no counterpart in the reference.
