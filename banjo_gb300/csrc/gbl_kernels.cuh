@@ -491,9 +491,9 @@ __global__ void __launch_bounds__(1024) kCandidates(const Grid<R> launch) {
 // ---------------------------------------------------------------------------
 // Sphere contact (LatticePhysics.hpp:1322-1428): candidates in slab, then node
 // order, one contact at a time -- every contact moves the sphere the next one
-// sees, so that chain is serial by definition. It runs on one thread of one
-// CTA; everything that does not depend on the sphere's changing state is
-// computed by the whole CTA around it.
+// sees, so that chain is serial by definition. It runs on one warp of one
+// CTA per lattice; everything that does not depend on the sphere's changing
+// state is computed by the whole CTA around it.
 //
 // A candidate's node data are staged in shared memory. In pass 1 the sphere
 // centre cannot move (only pass 2 corrects positions), so the offset r, its
@@ -522,6 +522,17 @@ __device__ __forceinline__ void contactApply(V3<R> imp, V3<R> r, R inm, R ism, R
     acc.impulse_x += static_cast<double>(imp.x);
     acc.impulse_y += static_cast<double>(imp.y);
     acc.impulse_z += static_cast<double>(imp.z);
+}
+
+// The contact gate: a candidate whose gap exceeds both the contact margin and
+// what its approach along the normal closes in one substep is left alone and
+// changes nothing (LatticePhysics.hpp:1338-1342).
+template <class R>
+__device__ __forceinline__ bool contactGate(const Settings<R> &S, const Sphere<R> &sp, V3<R> nv, V3<R> r, V3<R> normal,
+                                            R gap) {
+    const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
+    const R vn = dot(rel, normal);
+    return !(gap > maxR(S.c_margin, -vn * S.dt));
 }
 
 // The contact of one staged candidate, from its relative velocity on
@@ -572,8 +583,14 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
     }
 }
 
-constexpr unsigned kSphereThreads = 1024;
+constexpr unsigned kSphereThreads = 256;
 
+// The chain runs on warp 0, with every lane holding the same sphere state and
+// ledgers. Only a candidate that passes the contact gate changes anything, so
+// the lanes test the next 32 candidates against the current state at once; the
+// first that passes is applied (by every lane, identically) and the scan
+// resumes after it. The candidates skipped were tested against exactly the
+// state the serial order shows them, so the result is the serial chain's.
 template <class R, bool Many>
 __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> launch, Settings<R> S, int pass) {
     const Work w = item<Many>(launch);
@@ -582,18 +599,20 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
     Staged<R> *st = reinterpret_cast<Staged<R> *>(sphere_smem);
     __shared__ Sphere<R> start;
     if (L.ctl->stop) return;
+    const unsigned lane = threadIdx.x & 31U;
+    const bool chain = threadIdx.x < 32;
     Sphere<R> sp{};
     ContactAcc acc{};
     V3<R> c0{};
     R e0 = R(0), max_pen = R(0);
-    if (threadIdx.x == 0) {
+    if (chain) {
         sp = *L.sphere;
         if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
         acc = L.ctl->contact;
         max_pen = R(acc.max_penetration);
         c0 = sp.center;
         e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
-        start = sp;
+        if (threadIdx.x == 0) start = sp;
     }
     __syncthreads();
     // Constant over the pass: the sphere's mass and inertia never change.
@@ -628,10 +647,29 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             st[k] = c;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (std::uint32_t k = 0; k < n; ++k) {
-                Staged<R> &c = st[k];
-                if (c.v.w <= R(0)) continue;
+        if (chain) {
+            std::uint32_t k0 = 0;
+            while (k0 < n) {
+                const std::uint32_t k = k0 + lane;
+                bool hit = false;
+                if (k < n) {
+                    const Staged<R> &c = st[k];
+                    if (c.v.w > R(0)) {
+                        if (pass == 1) {
+                            hit = contactGate(S, sp, xyz(c.v), c.p, c.normal, c.gap);
+                        } else {
+                            const V3<R> r = c.p - sp.center;
+                            hit = contactGate(S, sp, xyz(c.v), r, normalized(r), length(r) - cr);
+                        }
+                    }
+                }
+                const unsigned mask = __ballot_sync(0xffffffffU, hit);
+                if (mask == 0) {
+                    k0 += 32;
+                    continue;
+                }
+                const std::uint32_t j = k0 + static_cast<std::uint32_t>(__ffs(mask) - 1);
+                Staged<R> c = st[j];
                 if (pass == 1) {
                     contactChain(S, sp, c, c.p, c.normal, c.gap, c.eff_n, ism, iin, false, acc, max_pen);
                 } else {
@@ -642,6 +680,9 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
                     const R eff_n = c.inm + ism + iin * dot(rn, rn);
                     contactChain(S, sp, c, r, normal, distance - cr, eff_n, ism, iin, true, acc, max_pen);
                 }
+                __syncwarp();
+                if (lane == 0) st[j] = c;
+                k0 = j + 1;
             }
         }
         __syncthreads();
