@@ -15,6 +15,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -181,6 +183,48 @@ template <class R> struct Resident {
         }
     }
 
+    // The device arrays of one lattice, in one allocation.
+    static void reserve(Arena &a, Dev<R> &d, std::uint32_t N, std::uint32_t B, std::uint32_t D, std::uint32_t blocks,
+                        std::size_t isolated) {
+        const std::size_t P = static_cast<std::size_t>(D) * N;
+        a.reserve(d.u, N); a.reserve(d.v, N); a.reserve(d.x0, N); a.reserve(d.up, N);
+        a.reserve(d.strain, 2 * static_cast<std::size_t>(N));
+        a.reserve(d.rinv, 9 * static_cast<std::size_t>(N)); a.reserve(d.unm, 3 * static_cast<std::size_t>(N));
+        a.reserve(d.approach, kPlanes * static_cast<std::size_t>(N));
+        a.reserve(d.dirty, N + 4); a.reserve(d.engaged, kPlanes * static_cast<std::size_t>(N));
+        a.reserve(d.candidate, N); a.reserve(d.cand_bits, (N + 31) / 32 + 1);
+        a.reserve(d.nbr, P); a.reserve(d.nbr_other, P); a.reserve(d.nbr_bond, P);
+        a.reserve(d.slot_a, B); a.reserve(d.slot_b, B);
+        a.reserve(d.rec, B); a.reserve(d.geo, B); a.reserve(d.prev, B); a.reserve(d.thr4, B);
+        a.reserve(d.thr2, B); a.reserve(d.plastic, B); a.reserve(d.lambda, B); a.reserve(d.mode, B);
+        a.reserve(d.ev_bits, d.words_b + 1); a.reserve(d.ev_tile, d.tiles_b + 1); a.reserve(d.ev_list, B + 1);
+        a.reserve(d.ev_removed, B); a.reserve(d.ev_packed, B + 1); a.reserve(d.ev_prefix, B + 1);
+        a.reserve(d.ev_ends, B); a.reserve(d.dev2sched, B);
+        a.reserve(d.isolated, isolated + 1);
+        a.reserve(d.dmg_bits, d.words_b + 1); a.reserve(d.dmg_tile, d.tiles_b + 1);
+        a.reserve(d.dmg_list, B + 1); a.reserve(d.ev_damage, B); a.reserve(d.dmg_value, B + 1);
+        a.reserve(d.tile_plastic, d.tiles_b + 1); a.reserve(d.tile_removed, d.tiles_b + 1);
+        const std::size_t scan_blocks = d.tiles_b / kScanBlock + 1;
+        a.reserve(d.blk_ev, scan_blocks); a.reserve(d.blk_dmg, scan_blocks);
+        a.reserve(d.blk_removed, scan_blocks); a.reserve(d.blk_plastic, scan_blocks);
+        a.reserve(d.node_block_begin, blocks + 1);
+        a.reserve(d.cand_list, static_cast<std::size_t>(blocks) * kCandidatesPerBlock);
+        a.reserve(d.cand_count, blocks);
+        a.reserve(d.dirty_list, N + 1); a.reserve(d.ffb, B + 1);
+        a.reserve(d.sphere, 1);
+    }
+
+    // Device bytes a lattice of these counts takes (its isolated nodes at
+    // most N; external load buffers included): what admission charges.
+    static std::size_t footprint(std::uint32_t N, std::uint32_t B, std::uint32_t D, std::uint32_t blocks) {
+        Arena a;
+        Dev<R> d{};
+        d.words_b = (B + 31) / 32;
+        d.tiles_b = (B + kThreads - 1) / kThreads;
+        reserve(a, d, N, B, D, blocks, N);
+        return a.bytes() + static_cast<std::size_t>(N) * (sizeof(Q4<R>) + 16 * sizeof(double) + sizeof(std::uint32_t));
+    }
+
     // upload (FastLattice.hpp:267-268; WorkingLattice::fromState, LatticeWorking.hpp:53-124)
     void upload(const gbl_state_view &st, const gbl_sphere &sphere, cudaStream_t stream) {
         N = st.node_count;
@@ -193,34 +237,10 @@ template <class R> struct Resident {
         d.N = N; d.B = B; d.D = D; d.blocks = sched.block_count;
         d.words_b = (B + 31) / 32;
         d.tiles_b = (B + kThreads - 1) / kThreads;
-        const std::size_t P = static_cast<std::size_t>(D) * N;
         arena.release();
-        arena.reserve(d.u, N); arena.reserve(d.v, N); arena.reserve(d.x0, N); arena.reserve(d.up, N);
-        arena.reserve(d.strain, 2 * static_cast<std::size_t>(N));
-        arena.reserve(d.rinv, 9 * static_cast<std::size_t>(N)); arena.reserve(d.unm, 3 * static_cast<std::size_t>(N));
-        arena.reserve(d.approach, kPlanes * static_cast<std::size_t>(N));
-        arena.reserve(d.dirty, N + 4); arena.reserve(d.engaged, kPlanes * static_cast<std::size_t>(N));
-        arena.reserve(d.candidate, N); arena.reserve(d.cand_bits, (N + 31) / 32 + 1);
-        arena.reserve(d.nbr, P); arena.reserve(d.nbr_other, P); arena.reserve(d.nbr_bond, P);
-        arena.reserve(d.slot_a, B); arena.reserve(d.slot_b, B);
-        arena.reserve(d.rec, B); arena.reserve(d.geo, B); arena.reserve(d.prev, B); arena.reserve(d.thr4, B);
-        arena.reserve(d.thr2, B); arena.reserve(d.plastic, B); arena.reserve(d.lambda, B); arena.reserve(d.mode, B);
-        arena.reserve(d.ev_bits, d.words_b + 1); arena.reserve(d.ev_tile, d.tiles_b + 1); arena.reserve(d.ev_list, B + 1);
-        arena.reserve(d.ev_removed, B); arena.reserve(d.ev_packed, B + 1); arena.reserve(d.ev_prefix, B + 1);
-        arena.reserve(d.ev_ends, B); arena.reserve(d.dev2sched, B);
-        arena.reserve(d.isolated, isolated.size() + 1);
-        arena.reserve(d.dmg_bits, d.words_b + 1); arena.reserve(d.dmg_tile, d.tiles_b + 1);
-        arena.reserve(d.dmg_list, B + 1); arena.reserve(d.ev_damage, B); arena.reserve(d.dmg_value, B + 1);
-        arena.reserve(d.tile_plastic, d.tiles_b + 1); arena.reserve(d.tile_removed, d.tiles_b + 1);
-        const std::size_t scan_blocks = d.tiles_b / kScanBlock + 1;
-        arena.reserve(d.blk_ev, scan_blocks); arena.reserve(d.blk_dmg, scan_blocks);
-        arena.reserve(d.blk_removed, scan_blocks); arena.reserve(d.blk_plastic, scan_blocks);
-        arena.reserve(d.node_block_begin, sched.block_count + 1);
-        arena.reserve(d.cand_list, static_cast<std::size_t>(sched.block_count) * kCandidatesPerBlock);
-        arena.reserve(d.cand_count, sched.block_count);
-        arena.reserve(d.dirty_list, N + 1); arena.reserve(d.ffb, B + 1);
-        arena.reserve(d.sphere, 1);
+        reserve(arena, d, N, B, D, sched.block_count, isolated.size());
         arena.commit();
+        const std::size_t P = static_cast<std::size_t>(D) * N;
 
         std::vector<Q4<R>> u(N), v(N), x0(N), up(N);
         mass.resize(N);
@@ -450,7 +470,12 @@ template <class R> struct Resident {
     }
 };
 
-// K lattices advanced together, one launch per phase and per sweep level.
+// Lattices advanced together, one launch per phase and per sweep level.
+//
+// Lattices live in slots: a slot's control block, descriptor and work items
+// are its own, and lattices enter (admit) and leave (retire) between substeps
+// without touching the others, which is what continuous batching needs. The
+// work lists and the captured substep graph are rebuilt when the set changes.
 template <class R> class Engine {
     static constexpr bool kDirect = std::is_same<R, double>::value;
     static constexpr unsigned kSphereSmem = kCandidatesPerBlock * sizeof(Staged<R>);
@@ -466,24 +491,34 @@ public:
         check(cudaEventCreate(&ev0_), "event");
         check(cudaEventCreate(&ev1_), "event");
         check(cudaMallocHost(&running_host_, sizeof(unsigned)), "pinned allocation");
+        check(cudaMalloc(&running_, sizeof(unsigned)), "device allocation");
     }
     Engine(const Engine &) = delete;
     Engine &operator=(const Engine &) = delete;
     ~Engine() {
         dropGraph();
-        release();
+        slots_.clear();
+        if (ctl_) cudaFree(ctl_);
+        if (table_) cudaFree(table_);
+        if (work_) cudaFree(work_);
+        if (running_) cudaFree(running_);
         if (running_host_) cudaFreeHost(running_host_);
         cudaEventDestroy(ev0_);
         cudaEventDestroy(ev1_);
         cudaStreamDestroy(own_stream_);
     }
 
-    [[nodiscard]] std::size_t size() const { return lattices_.size(); }
+    // Slots in use, and the largest slot index + 1.
+    [[nodiscard]] std::size_t size() const { return active_.size(); }
+    [[nodiscard]] std::size_t slots() const { return slots_.size(); }
+    [[nodiscard]] bool occupied(std::size_t k) const { return k < slots_.size() && slots_[k] != nullptr; }
     Resident<R> &lattice(std::size_t k) {
-        if (k >= lattices_.size()) invalid("lattice index out of range");
-        return *lattices_[k];
+        if (!occupied(k)) invalid("lattice index out of range");
+        return *slots_[k];
     }
+    [[nodiscard]] const Ctl &control(std::size_t k) const { return ctl_host_.at(k); }
     [[nodiscard]] cudaStream_t stream() const { return stream_; }
+    [[nodiscard]] bool settled() const { return ready_; }
     void setStream(cudaStream_t s) {
         stream_ = s ? s : own_stream_;
         dropGraph();
@@ -491,50 +526,74 @@ public:
 
     void clear() {
         dropGraph();
-        lattices_.clear();
+        slots_.clear();
+        active_.clear();
         ready_ = false;
+        dirty_ = true;
     }
 
-    // Upload one lattice (its arrays); settle() makes the set runnable.
-    std::size_t add(const Schedule &sched, const gbl_state_view &st, const gbl_sphere &sphere) {
+    // Upload one lattice into the first free slot. Before settle() this only
+    // uploads; after it the lattice is admitted: a fresh control block (a new
+    // RunStatus) with `step_limit` substeps to run (0: no limit).
+    std::size_t add(const Schedule &sched, const gbl_state_view &st, const gbl_sphere &sphere,
+                    std::uint64_t step_limit = 0) {
         auto r = std::make_unique<Resident<R>>(sched);
         r->upload(st, sphere, stream_);
-        lattices_.push_back(std::move(r));
-        ready_ = false;
-        return lattices_.size() - 1;
+        std::size_t k = 0;
+        while (k < slots_.size() && slots_[k]) ++k;
+        if (k == slots_.size()) slots_.emplace_back();
+        slots_[k] = std::move(r);
+        listActive();
+        dirty_ = true;
+        if (ready_) {
+            growControl(slots_.size());
+            if (slots_[k]->plastic_state && !plastic_) {
+                plastic_ = true;
+                dropGraph();
+            }
+            initControl(k, step_limit);
+            pushDescriptor(k);
+            check(cudaStreamSynchronize(stream_), "admit");
+        }
+        return k;
     }
 
-    // The settings every lattice shares, the control blocks (reset: a fresh
-    // RunStatus per lattice), the descriptor table and the work lists.
+    // Take a lattice out (its device memory is freed); the others go on.
+    void retire(std::size_t k) {
+        if (!occupied(k)) invalid("lattice index out of range");
+        check(cudaStreamSynchronize(stream_), "retire");
+        slots_[k].reset();
+        while (!slots_.empty() && !slots_.back()) slots_.pop_back();
+        listActive();
+        dirty_ = true;
+    }
+
+    // The settings every lattice shares, and a fresh control block (reset:
+    // a new RunStatus) for every lattice present.
     void settle(const gbl_step_settings &set) {
         validate(set);
-        if (lattices_.empty()) invalid("the batch holds no lattice");
+        if (active_.empty()) invalid("the batch holds no lattice");
         dropGraph();
         S_ = convertSettings(set);
         plastic_ = S_.yield_stretch > R(0);
-        for (auto &l : lattices_) plastic_ = plastic_ || l->plastic_state;
-        const std::size_t K = lattices_.size();
-        release();
-        check(cudaMalloc(&ctl_, sizeof(Ctl) * std::max<std::size_t>(K, 1)), "device allocation");
-        check(cudaMalloc(&running_, sizeof(unsigned)), "device allocation");
-        check(cudaMalloc(&table_, sizeof(Dev<R>) * std::max<std::size_t>(K, 1)), "device allocation");
-        ctl_host_.assign(K, Ctl{});
-        for (std::size_t k = 0; k < K; ++k) {
-            Ctl &c = ctl_host_[k];
-            c.first_failure_step = c.last_failure_step = c.last_energy_gain_step = ~0ULL;
-            c.full_restart = 1;
-            c.energy_flat_fraction = 1.0e-3;
-            c.calm_damage_margin = 0.5;
-            lattices_[k]->dev.ctl = ctl_ + k;
-            lattices_[k]->dev.running = running_;
-            lattices_[k]->ext_count = 0;
-            lattices_[k]->ext_remaining = 0;
-        }
-        if (K) upload(ctl_, ctl_host_, stream_);
-        pushTable();
-        buildWork();
+        for (auto k : active_) plastic_ = plastic_ || slots_[k]->plastic_state;
+        growControl(slots_.size());
+        for (auto k : active_) initControl(k, 0);
+        for (auto k : active_) pushDescriptor(k);
         check(cudaStreamSynchronize(stream_), "settle");
         ready_ = true;
+        dirty_ = true;
+    }
+
+    // A settle() without lattices: the settings of a server that admits later.
+    void configure(const gbl_step_settings &set) {
+        validate(set);
+        dropGraph();
+        S_ = convertSettings(set);
+        plastic_ = S_.yield_stretch > R(0);
+        for (auto k : active_) plastic_ = plastic_ || slots_[k]->plastic_state;
+        ready_ = true;
+        dirty_ = true;
     }
 
     void setExternalForces(std::size_t k, const double *forces, std::uint64_t count, std::uint64_t substeps) {
@@ -543,23 +602,28 @@ public:
         const bool had = l.ext_force != nullptr;
         l.setExternalForces(forces, count, substeps, stream_);
         if (!had && l.ext_force) {
-            pushTable(); // the descriptor now points at the load buffers
-            dropGraph(); // a single lattice's launches carry the descriptor itself
+            pushDescriptor(k); // the descriptor now points at the load buffers
+            check(cudaStreamSynchronize(stream_), "descriptor");
+            dropGraph();       // a single lattice's launches carry the descriptor itself
         }
     }
 
-    // run (CpuLatticeBackend.cpp:255-304) for every lattice with one control.
+    // run (CpuLatticeBackend.cpp:255-304) for every lattice with one control;
+    // a lattice whose step limit is spent stays stopped.
     void run(const gbl_run_control &control) {
         requireReady();
         const auto start = std::chrono::steady_clock::now();
-        const std::size_t K = lattices_.size();
-        if (K == 0) return;
-        pullCtl();
-        for (std::size_t k = 0; k < K; ++k) {
+        if (active_.empty()) return;
+        pullControl();
+        unsigned running = 0;
+        for (auto k : active_) {
             Ctl &c = ctl_host_[k];
-            Resident<R> &l = *lattices_[k];
-            c.stop = 0;
-            c.exit_reason = 0;
+            Resident<R> &l = *slots_[k];
+            const bool spent = c.step_limit != 0 && c.total_steps >= c.step_limit;
+            c.stop = spent ? 1U : 0U;
+            if (spent) c.exit_reason = 3;
+            else c.exit_reason = 0;
+            running += spent ? 0U : 1U;
             c.quiet_steps = control.quiet_steps; c.min_steps = control.min_steps;
             c.no_failure_steps = control.no_failure_steps; c.energy_flat_steps = control.energy_flat_steps;
             c.calm_steps = control.calm_steps; c.energy_flat_fraction = control.energy_flat_fraction;
@@ -570,28 +634,28 @@ public:
                 l.ext_dirty = false;
             }
         }
-        upload(ctl_, ctl_host_, stream_);
-        *running_host_ = static_cast<unsigned>(K);
+        pushControl();
+        *running_host_ = running;
         check(cudaMemcpyAsync(running_, running_host_, sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "copy");
-        std::vector<std::uint64_t> before(K);
-        for (std::size_t k = 0; k < K; ++k) before[k] = ctl_host_[k].total_steps;
-        ensureGraph();
+        std::vector<std::uint64_t> before(slots_.size(), 0);
+        for (auto k : active_) before[k] = ctl_host_[k].total_steps;
+        prepare();
         std::uint64_t chunk = control.steps_per_launch ? control.steps_per_launch : control.max_steps;
         if (control.abandon && chunk > 64) chunk = 64;
         const bool capture = control.capture_stride != 0;
         std::uint64_t launched = 0;
         bool abandoned = false;
         check(cudaEventRecord(ev0_, stream_), "event");
-        while (launched < control.max_steps) {
+        while (running && launched < control.max_steps) {
             if (control.abandon && *control.abandon) { abandoned = true; break; }
             const std::uint64_t n = std::min(chunk, control.max_steps - launched);
             bool halted = false;
             for (std::uint64_t s = 0; s < n; ++s) {
                 if (capture) {
                     bool synced = false;
-                    for (std::size_t k = 0; k < K; ++k) {
+                    for (auto k : active_) {
                         const std::uint64_t step = before[k] + launched + s;
-                        Resident<R> &l = *lattices_[k];
+                        Resident<R> &l = *slots_[k];
                         if (step % control.capture_stride != 0 || l.status.frames_captured >= control.max_frames) continue;
                         if (!synced) {
                             if (allStopped()) { halted = true; break; }
@@ -604,18 +668,18 @@ public:
                 check(cudaGraphLaunch(exec_, stream_), "graph launch");
             }
             launched += n;
-            for (auto &l : lattices_) ++l->status.launches;
+            for (auto k : active_) ++slots_[k]->status.launches;
             if (halted || allStopped()) break;
         }
         check(cudaEventRecord(ev1_, stream_), "event");
         check(cudaStreamSynchronize(stream_), "lattice run");
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0_, ev1_);
-        pullCtl();
+        pullControl();
         bool overflowed = false;
-        for (std::size_t k = 0; k < K; ++k) {
+        for (auto k : active_) {
             Ctl &c = ctl_host_[k];
-            Resident<R> &l = *lattices_[k];
+            Resident<R> &l = *slots_[k];
             l.status.kernel_seconds += ms * 1e-3;
             if (c.error & kErrExternalOverflow) {
                 c.error = 0;
@@ -633,12 +697,12 @@ public:
             }
         }
         if (overflowed) {
-            upload(ctl_, ctl_host_, stream_);
+            pushControl();
             check(cudaStreamSynchronize(stream_), "status");
             overflow("external force kick exceeds backend precision");
         }
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
-        for (auto &l : lattices_) l->status.wall_seconds += wall;
+        for (auto k : active_) slots_[k]->status.wall_seconds += wall;
     }
 
     // Per-phase device time: the substep enqueued outside the graph, with an
@@ -646,24 +710,28 @@ public:
     void profile(std::uint64_t substeps, double *phase_ms) {
         requireReady();
         for (unsigned p = 0; p < GBL_PHASE_COUNT; ++p) phase_ms[p] = 0.0;
-        const std::size_t K = lattices_.size();
-        if (K == 0) return;
-        pullCtl();
-        for (auto &c : ctl_host_) {
-            c.stop = 0;
-            c.exit_reason = 0;
+        if (active_.empty()) return;
+        pullControl();
+        unsigned running = 0;
+        for (auto k : active_) {
+            Ctl &c = ctl_host_[k];
+            const bool spent = c.step_limit != 0 && c.total_steps >= c.step_limit;
+            c.stop = spent ? 1U : 0U;
+            c.exit_reason = spent ? 3U : 0U;
+            running += spent ? 0U : 1U;
             c.quiet_steps = c.min_steps = c.no_failure_steps = c.energy_flat_steps = c.calm_steps = 0;
             c.removable_energy = 0;
-        }
-        for (std::size_t k = 0; k < K; ++k)
-            if (lattices_[k]->ext_dirty) {
-                ctl_host_[k].ext_count = lattices_[k]->ext_count;
-                ctl_host_[k].loads_remaining = lattices_[k]->ext_remaining;
-                lattices_[k]->ext_dirty = false;
+            Resident<R> &l = *slots_[k];
+            if (l.ext_dirty) {
+                c.ext_count = l.ext_count;
+                c.loads_remaining = l.ext_remaining;
+                l.ext_dirty = false;
             }
-        upload(ctl_, ctl_host_, stream_);
-        *running_host_ = static_cast<unsigned>(K);
+        }
+        pushControl();
+        *running_host_ = running;
         check(cudaMemcpyAsync(running_, running_host_, sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "copy");
+        prepare();
         std::vector<cudaEvent_t> evs;
         std::vector<unsigned> ids;
         auto mark = [&](unsigned phase) {
@@ -684,17 +752,18 @@ public:
             phase_ms[ids[k + 1]] += ms;
         }
         for (auto e : evs) cudaEventDestroy(e);
-        pullCtl();
-        for (std::size_t k = 0; k < K; ++k) {
-            lattices_[k]->ext_remaining = ctl_host_[k].loads_remaining;
-            lattices_[k]->fillStatus(ctl_host_[k]);
-            for (unsigned p = 0; p < GBL_PHASE_COUNT; ++p) lattices_[k]->status.phase_seconds[p] += phase_ms[p] * 1e-3;
+        pullControl();
+        for (auto k : active_) {
+            slots_[k]->ext_remaining = ctl_host_[k].loads_remaining;
+            slots_[k]->fillStatus(ctl_host_[k]);
+            for (unsigned p = 0; p < GBL_PHASE_COUNT; ++p) slots_[k]->status.phase_seconds[p] += phase_ms[p] * 1e-3;
         }
     }
 
     std::uint64_t kernelsPerSubstep() {
         requireReady();
-        ensureGraph();
+        if (active_.empty()) return 0;
+        prepare();
         std::size_t n = 0;
         check(cudaGraphGetNodes(graph_, nullptr, &n), "graph nodes");
         return n;
@@ -757,27 +826,78 @@ private:
         return o;
     }
 
-    void release() {
-        if (ctl_) cudaFree(ctl_);
-        if (running_) cudaFree(running_);
-        if (table_) cudaFree(table_);
-        if (work_) cudaFree(work_);
-        ctl_ = nullptr;
-        running_ = nullptr;
-        table_ = nullptr;
-        work_ = nullptr;
+    void listActive() {
+        active_.clear();
+        for (std::size_t k = 0; k < slots_.size(); ++k)
+            if (slots_[k]) active_.push_back(static_cast<std::uint32_t>(k));
     }
 
-    void pushTable() {
-        std::vector<Dev<R>> table(lattices_.size());
-        for (std::size_t k = 0; k < lattices_.size(); ++k) table[k] = lattices_[k]->dev;
-        upload(table_, table, stream_);
-        check(cudaStreamSynchronize(stream_), "table");
+    // Control blocks and descriptors for `need` slots, kept across growth.
+    void growControl(std::size_t need) {
+        if (need <= cap_) return;
+        std::size_t cap = std::max<std::size_t>(cap_ ? cap_ * 2 : 1, need);
+        Ctl *ctl = nullptr;
+        Dev<R> *table = nullptr;
+        check(cudaMalloc(&ctl, sizeof(Ctl) * cap), "device allocation");
+        check(cudaMalloc(&table, sizeof(Dev<R>) * cap), "device allocation");
+        if (ctl_) {
+            check(cudaMemcpyAsync(ctl, ctl_, sizeof(Ctl) * cap_, cudaMemcpyDeviceToDevice, stream_), "copy");
+            check(cudaStreamSynchronize(stream_), "copy");
+            cudaFree(ctl_);
+            cudaFree(table_);
+        }
+        ctl_ = ctl;
+        table_ = table;
+        cap_ = cap;
+        ctl_host_.resize(cap);
+        // Every descriptor points at its control block: all move.
+        for (auto k : active_)
+            if (k < cap_) {
+                slots_[k]->dev.ctl = ctl_ + k;
+                pushDescriptor(k);
+            }
+        check(cudaStreamSynchronize(stream_), "descriptors");
+        dropGraph();
+        dirty_ = true;
     }
 
-    void pullCtl() {
-        if (ctl_host_.empty()) return;
-        check(cudaMemcpyAsync(ctl_host_.data(), ctl_, sizeof(Ctl) * ctl_host_.size(), cudaMemcpyDeviceToHost, stream_),
+    void initControl(std::size_t k, std::uint64_t step_limit) {
+        Ctl c{};
+        c.first_failure_step = c.last_failure_step = c.last_energy_gain_step = ~0ULL;
+        c.full_restart = 1;
+        c.energy_flat_fraction = 1.0e-3;
+        c.calm_damage_margin = 0.5;
+        c.step_limit = step_limit;
+        ctl_host_[k] = c;
+        Resident<R> &l = *slots_[k];
+        l.dev.ctl = ctl_ + k;
+        l.dev.running = running_;
+        l.ext_count = 0;
+        l.ext_remaining = 0;
+        l.ext_dirty = false;
+        l.status = gbl_run_status{};
+        l.status.first_failure_step = l.status.last_failure_step = l.status.last_energy_gain_step = ~0ULL;
+        l.first_failure.clear();
+        l.frames.clear();
+        check(cudaMemcpyAsync(ctl_ + k, &ctl_host_[k], sizeof(Ctl), cudaMemcpyHostToDevice, stream_), "copy");
+        check(cudaStreamSynchronize(stream_), "copy");
+    }
+
+    void pushDescriptor(std::size_t k) {
+        check(cudaMemcpyAsync(table_ + k, &slots_[k]->dev, sizeof(Dev<R>), cudaMemcpyHostToDevice, stream_), "copy");
+    }
+
+    // Control blocks of the slots, between the host mirror and the device, in
+    // one copy (a free slot's block is read by no kernel).
+    void pullControl() {
+        if (slots_.empty()) return;
+        check(cudaMemcpyAsync(ctl_host_.data(), ctl_, sizeof(Ctl) * slots_.size(), cudaMemcpyDeviceToHost, stream_),
+              "copy");
+        check(cudaStreamSynchronize(stream_), "status");
+    }
+    void pushControl() {
+        if (slots_.empty()) return;
+        check(cudaMemcpyAsync(ctl_, ctl_host_.data(), sizeof(Ctl) * slots_.size(), cudaMemcpyHostToDevice, stream_),
               "copy");
         check(cudaStreamSynchronize(stream_), "status");
     }
@@ -788,14 +908,28 @@ private:
         return *running_host_ == 0;
     }
 
+    // Work lists and graph for the lattices present.
+    void prepare() {
+        if (dirty_) {
+            buildWork();
+            dropGraph();
+            dirty_ = false;
+        }
+        if (!exec_) {
+            check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
+            enqueueSubstep([](unsigned) {});
+            check(cudaStreamEndCapture(stream_, &graph_), "graph capture");
+            check(cudaGraphInstantiate(&exec_, graph_, 0), "graph instantiate");
+        }
+    }
+
     // A launch's items: [first, first + count) of the work array; for a
     // single lattice, the same items as (base, end, per).
     struct Span { std::uint32_t first, count, base, end, per; };
 
-    // Work lists of every phase, one item per CTA, lattices in order.
+    // Work lists of every phase, one item per CTA, lattices in slot order.
     void buildWork() {
         std::vector<Work> all;
-        const std::uint32_t K = static_cast<std::uint32_t>(lattices_.size());
         auto ranges = [&](std::uint32_t k, std::uint32_t begin, std::uint32_t end, std::uint32_t per) {
             for (std::uint32_t b = begin; b < end; b += per) all.push_back({k, b, std::min(end, b + per)});
         };
@@ -803,50 +937,50 @@ private:
         auto span = [&](auto &&bounds, std::uint32_t per) {
             const std::uint32_t first = static_cast<std::uint32_t>(all.size());
             std::uint32_t b0 = 0, e0 = 0;
-            for (std::uint32_t k = 0; k < K; ++k) {
+            bool lead = true;
+            for (auto k : active_) {
                 std::uint32_t b = 0, e = 0;
-                bounds(k, b, e);
-                if (k == 0) { b0 = b; e0 = e; }
+                bounds(*slots_[k], b, e);
+                if (lead) { b0 = b; e0 = e; lead = false; }
                 ranges(k, b, e, per);
             }
             return Span{first, static_cast<std::uint32_t>(all.size()) - first, b0, e0, per};
         };
-        nodes_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) { b = 0; e = lattices_[k]->N; }, kThreads);
-        bonds_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) { b = 0; e = lattices_[k]->B; }, kThreads);
-        tiles_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) { b = 0; e = lattices_[k]->dev.tiles_b; },
-                      kThreads / 32);
-        blocks_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) {
-            b = 0;
-            e = lattices_[k]->dev.tiles_b / kScanBlock + 1;
-        }, 1);
-        each_ = span([&](std::uint32_t, std::uint32_t &b, std::uint32_t &e) { b = 0; e = 1; }, 1);
-        slabs_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) { b = 0; e = lattices_[k]->sched.block_count; },
-                      1);
-        isolated_ = span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) {
-            b = 0;
-            e = static_cast<std::uint32_t>(lattices_[k]->isolated.size());
-        }, kThreads);
+        using Res = Resident<R>;
+        using U = std::uint32_t;
+        nodes_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.N; }, kThreads);
+        bonds_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.B; }, kThreads);
+        tiles_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.dev.tiles_b; }, kThreads / 32);
+        blocks_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.dev.tiles_b / kScanBlock + 1; }, 1);
+        each_ = span([](const Res &, U &b, U &e) { b = 0; e = 1; }, 1);
+        slabs_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.sched.block_count; }, 1);
+        isolated_ = span([](const Res &l, U &b, U &e) { b = 0; e = static_cast<U>(l.isolated.size()); }, kThreads);
         {
-            const std::uint32_t first = static_cast<std::uint32_t>(all.size());
-            for (std::uint32_t k = 0; k < K; ++k) {
-                const std::uint32_t parts = std::max(1U, std::min(608U, lattices_[k]->B / 65536U));
-                for (std::uint32_t q = 0; q < parts; ++q) all.push_back({k, q, parts});
+            const U first = static_cast<U>(all.size());
+            for (auto k : active_) {
+                const U parts = std::max(1U, std::min(608U, slots_[k]->B / 65536U));
+                for (U q = 0; q < parts; ++q) all.push_back({k, q, parts});
             }
-            const std::uint32_t count = static_cast<std::uint32_t>(all.size()) - first;
+            const U count = static_cast<U>(all.size()) - first;
             broken_ = Span{first, count, 0, count, 1};
         }
         std::size_t deepest = 0;
-        for (auto &l : lattices_) deepest = std::max(deepest, l->levels.size());
+        for (auto k : active_) deepest = std::max(deepest, slots_[k]->levels.size());
         levels_.clear();
         for (std::size_t d = 0; d < deepest; ++d)
-            levels_.push_back(span([&](std::uint32_t k, std::uint32_t &b, std::uint32_t &e) {
-                const auto &lv = lattices_[k]->levels;
-                b = d < lv.size() ? lv[d].begin : 0;
-                e = d < lv.size() ? lv[d].end : 0;
+            levels_.push_back(span([d](const Res &l, U &b, U &e) {
+                b = d < l.levels.size() ? l.levels[d].begin : 0;
+                e = d < l.levels.size() ? l.levels[d].end : 0;
             }, kThreads));
-        check(cudaMalloc(&work_, sizeof(Work) * std::max<std::size_t>(all.size(), 1)), "device allocation");
+        if (all.size() > work_cap_) {
+            if (work_) cudaFree(work_);
+            work_cap_ = std::max<std::size_t>(all.size(), 2 * work_cap_);
+            check(cudaMalloc(&work_, sizeof(Work) * work_cap_), "device allocation");
+        }
         upload(work_, all, stream_);
-        many_ = K > 1;
+        check(cudaStreamSynchronize(stream_), "work lists");
+        many_ = active_.size() > 1;
+        one_ = active_.empty() ? 0 : active_.front();
     }
 
     void dropGraph() {
@@ -854,14 +988,6 @@ private:
         if (graph_) cudaGraphDestroy(graph_);
         exec_ = nullptr;
         graph_ = nullptr;
-    }
-
-    void ensureGraph() {
-        if (exec_) return;
-        check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
-        enqueueSubstep([](unsigned) {});
-        check(cudaStreamEndCapture(stream_, &graph_), "graph capture");
-        check(cudaGraphInstantiate(&exec_, graph_, 0), "graph instantiate");
     }
 
     // The launch form of a span: the work list and descriptor table for many
@@ -875,7 +1001,7 @@ private:
             g.base = s.base;
             g.end = s.end;
             g.per = s.per;
-            g.one = lattices_[0]->dev;
+            g.one = slots_[one_]->dev;
         }
         return g;
     }
@@ -954,10 +1080,13 @@ private:
 #undef GBL_SOLVE
     }
 
-    std::vector<std::unique_ptr<Resident<R>>> lattices_;
+    std::vector<std::unique_ptr<Resident<R>>> slots_;
+    std::vector<std::uint32_t> active_;
     Settings<R> S_{};
-    bool plastic_{false}, ready_{false}, many_{false};
+    bool plastic_{false}, ready_{false}, many_{false}, dirty_{true};
+    std::uint32_t one_{0};
     Ctl *ctl_{};
+    std::size_t cap_{0}, work_cap_{0};
     std::vector<Ctl> ctl_host_;
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
@@ -1072,6 +1201,230 @@ private:
     Engine<R> engine_;
 };
 
+// The served form: requests (one lattice each, with a substep count) arrive at
+// any time; they are admitted in arrival order while their device footprint
+// fits the HBM budget, run together one chunk of substeps at a time with every
+// other admitted request, and leave as soon as their own count is done, which
+// frees their memory for the next in line. Each request's result is the one it
+// would get alone: lattices never interact, and each keeps its own control
+// block and ledgers.
+struct ResultBuffers {
+    std::vector<double> u, u_prev, v, damage, prev_t, prev_c, prev_s, plastic_e, plastic_s;
+    std::vector<std::uint8_t> alive, mode;
+    gbl_state_view view(std::uint32_t n, std::uint32_t b) {
+        u.resize(3 * static_cast<std::size_t>(n)); u_prev.resize(u.size()); v.resize(u.size());
+        damage.resize(b); prev_t.resize(b); prev_c.resize(b); prev_s.resize(b); plastic_e.resize(b);
+        plastic_s.resize(b); alive.resize(b); mode.resize(b);
+        gbl_state_view w{};
+        w.node_count = n;
+        w.bond_count = b;
+        w.u = u.data(); w.u_prev = u_prev.data(); w.v = v.data();
+        w.alive = alive.data(); w.failure_mode = mode.data(); w.damage = damage.data();
+        w.prev_tensile = prev_t.data(); w.prev_compressive = prev_c.data(); w.prev_shear = prev_s.data();
+        w.plastic_extension = plastic_e.data(); w.plastic_strain = plastic_s.data();
+        return w;
+    }
+    void copyTo(gbl_state_view &out) const {
+        auto put = [](auto *dst, const auto &src) {
+            if (dst && !src.empty()) std::memcpy(dst, src.data(), sizeof(src[0]) * src.size());
+        };
+        put(out.u, u); put(out.u_prev, u_prev); put(out.v, v); put(out.alive, alive); put(out.failure_mode, mode);
+        put(out.damage, damage); put(out.prev_tensile, prev_t); put(out.prev_compressive, prev_c);
+        put(out.prev_shear, prev_s); put(out.plastic_extension, plastic_e); put(out.plastic_strain, plastic_s);
+    }
+};
+
+class ServerBase {
+public:
+    virtual ~ServerBase() = default;
+    virtual std::uint64_t submit(const gbl_schedule_view &s, const gbl_state_view &st, const gbl_sphere &sp,
+                                 std::uint64_t substeps) = 0;
+    virtual void step(std::uint64_t substeps, gbl_server_stats *stats) = 0;
+    virtual void poll(std::uint64_t ticket, gbl_request_info &info) = 0;
+    virtual void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) = 0;
+    virtual void cancel(std::uint64_t ticket) = 0;
+    virtual void stats(gbl_server_stats &out) = 0;
+};
+
+template <class R> class Server final : public ServerBase {
+public:
+    Server(const gbl_step_settings &settings, std::uint64_t budget) : budget_(budget), t0_(clock()) {
+        engine_.configure(settings);
+    }
+
+    std::uint64_t submit(const gbl_schedule_view &sv, const gbl_state_view &st, const gbl_sphere &sp,
+                         std::uint64_t substeps) override {
+        if (substeps == 0) invalid("a served request needs at least one substep");
+        if (sv.node_count != st.node_count || sv.bond_count != st.bond_count)
+            invalid("lattice schedule does not match the lattice");
+        const std::uint64_t bytes =
+            Resident<R>::footprint(st.node_count, st.bond_count, st.max_degree, sv.block_count);
+        if (bytes > budget_) invalid("request exceeds the device memory budget on its own");
+        Request q;
+        q.ticket = ++last_ticket_;
+        q.sched = Schedule::fromView(sv);
+        q.view = st;
+        q.sphere = sp;
+        q.substeps = substeps;
+        q.bytes = bytes;
+        q.submitted = clock() - t0_;
+        const std::uint64_t t = q.ticket;
+        requests_.emplace(t, std::move(q));
+        queue_.push_back(t);
+        ++queued_;
+        return t;
+    }
+
+    void step(std::uint64_t substeps, gbl_server_stats *out) override {
+        admit();
+        if (engine_.size() > 0 && substeps > 0) {
+            gbl_run_control c{}; // RunControl's defaults (FastLattice.hpp:79-128), exit rules off
+            c.energy_flat_fraction = 1.0e-3;
+            c.calm_damage_margin = 0.5;
+            c.max_steps = substeps;
+            const double before = kernelSeconds();
+            engine_.run(c);
+            device_seconds_ += kernelSeconds() - before;
+            substeps_run_ += substeps;
+            retireFinished();
+            admit(); // memory freed this step goes to the next in line now
+        }
+        if (out) stats(*out);
+    }
+
+    void poll(std::uint64_t ticket, gbl_request_info &info) override {
+        const Request &q = find(ticket);
+        info = gbl_request_info{};
+        info.phase = q.phase;
+        info.slot = q.phase == GBL_REQUEST_RUNNING ? static_cast<std::uint32_t>(q.slot) : ~0U;
+        info.substeps = q.substeps;
+        info.substeps_done = q.phase == GBL_REQUEST_RUNNING ? engine_.control(q.slot).total_steps : q.done_steps;
+        info.device_bytes = q.bytes;
+        info.submitted_s = q.submitted;
+        info.admitted_s = q.admitted;
+        info.finished_s = q.finished;
+    }
+
+    void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) override {
+        Request &q = find(ticket);
+        if (q.phase != GBL_REQUEST_DONE) invalid("the request has not finished");
+        if (st) {
+            if (st->node_count != q.view.node_count || st->bond_count != q.view.bond_count)
+                invalid("result state does not match the request's lattice");
+            q.result.copyTo(*st);
+        }
+        if (sp) *sp = q.sphere;
+        if (status) *status = q.status;
+        requests_.erase(ticket);
+        --done_;
+    }
+
+    void cancel(std::uint64_t ticket) override {
+        Request &q = find(ticket);
+        if (q.phase == GBL_REQUEST_QUEUED) {
+            queue_.erase(std::find(queue_.begin(), queue_.end(), ticket));
+            --queued_;
+        } else if (q.phase == GBL_REQUEST_RUNNING) {
+            engine_.retire(q.slot);
+            used_ -= q.bytes;
+            --running_;
+        } else {
+            if (q.phase == GBL_REQUEST_DONE) --done_;
+        }
+        requests_.erase(ticket);
+    }
+
+    void stats(gbl_server_stats &o) override {
+        o = gbl_server_stats{};
+        o.queued = queued_;
+        o.running = running_;
+        o.done = done_;
+        o.bytes_in_use = used_;
+        o.budget_bytes = budget_;
+        o.substeps_run = substeps_run_;
+        o.device_seconds = device_seconds_;
+        o.clock_s = clock() - t0_;
+    }
+
+private:
+    struct Request {
+        std::uint64_t ticket{}, substeps{}, bytes{}, done_steps{};
+        Schedule sched;
+        gbl_state_view view{};
+        gbl_sphere sphere{};
+        int phase{GBL_REQUEST_QUEUED};
+        std::size_t slot{};
+        double submitted{-1}, admitted{-1}, finished{-1};
+        gbl_run_status status{};
+        ResultBuffers result;
+    };
+
+    static double clock() {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    }
+
+    Request &find(std::uint64_t ticket) {
+        auto it = requests_.find(ticket);
+        if (it == requests_.end()) invalid("unknown request ticket");
+        return it->second;
+    }
+
+    double kernelSeconds() {
+        double s = 0;
+        for (std::size_t k = 0; k < engine_.slots(); ++k)
+            if (engine_.occupied(k)) s = std::max(s, engine_.lattice(k).status.kernel_seconds);
+        return s;
+    }
+
+    // Arrival order, while the next request fits what is left of the budget.
+    void admit() {
+        while (!queue_.empty()) {
+            Request &q = requests_.at(queue_.front());
+            if (used_ + q.bytes > budget_) break;
+            q.slot = engine_.add(q.sched, q.view, q.sphere, q.substeps);
+            q.phase = GBL_REQUEST_RUNNING;
+            q.admitted = clock() - t0_;
+            used_ += q.bytes;
+            slot_ticket_.resize(std::max(slot_ticket_.size(), q.slot + 1));
+            slot_ticket_[q.slot] = q.ticket;
+            queue_.pop_front();
+            --queued_;
+            ++running_;
+        }
+    }
+
+    void retireFinished() {
+        for (std::size_t k = 0; k < engine_.slots(); ++k) {
+            if (!engine_.occupied(k)) continue;
+            const Ctl &c = engine_.control(k);
+            if (!(c.step_limit != 0 && c.total_steps >= c.step_limit) && c.exit_reason == 0) continue;
+            Request &q = requests_.at(slot_ticket_[k]);
+            Resident<R> &l = engine_.lattice(k);
+            gbl_state_view out = q.result.view(l.N, l.B);
+            engine_.download(k, out, &q.sphere);
+            q.status = l.status;
+            q.status.exit_reason = c.exit_reason;
+            q.done_steps = c.total_steps;
+            engine_.retire(k);
+            used_ -= q.bytes;
+            q.phase = GBL_REQUEST_DONE;
+            q.finished = clock() - t0_;
+            q.sched = Schedule{};
+            --running_;
+            ++done_;
+        }
+    }
+
+    Engine<R> engine_;
+    std::uint64_t budget_, used_{0}, last_ticket_{0};
+    std::uint64_t queued_{0}, running_{0}, done_{0}, substeps_run_{0};
+    double device_seconds_{0};
+    double t0_;
+    std::map<std::uint64_t, Request> requests_;
+    std::deque<std::uint64_t> queue_;
+    std::vector<std::uint64_t> slot_ticket_;
+};
+
 } // namespace gbl
 
 struct gbl_backend {
@@ -1079,6 +1432,9 @@ struct gbl_backend {
 };
 struct gbl_batch {
     std::unique_ptr<gbl::BatchBase> impl;
+};
+struct gbl_server {
+    std::unique_ptr<gbl::ServerBase> impl;
 };
 
 extern "C" {
@@ -1336,6 +1692,76 @@ gbl_result gbl_batch_set_stream(gbl_batch *batch, void *cuda_stream) {
     return gbl::guard([&] {
         if (!batch) gbl::invalid("null batch");
         batch->impl->setStream(static_cast<cudaStream_t>(cuda_stream));
+    });
+}
+
+gbl_result gbl_serve_create(int precision, const gbl_step_settings *settings, uint64_t budget_bytes, gbl_server **out) {
+    return gbl::guard([&] {
+        if (!settings || !out) gbl::invalid("null argument");
+        if (!gbl_available()) gbl::runtime("no CUDA device is available for the lattice backend");
+        auto s = std::make_unique<gbl_server>();
+        if (precision == GBL_PRECISION_DOUBLE) s->impl = std::make_unique<gbl::Server<double>>(*settings, budget_bytes);
+        else if (precision == GBL_PRECISION_FLOAT) s->impl = std::make_unique<gbl::Server<float>>(*settings, budget_bytes);
+        else gbl::invalid("unknown precision");
+        *out = s.release();
+    });
+}
+
+void gbl_serve_destroy(gbl_server *server) { delete server; }
+
+gbl_result gbl_serve_submit(gbl_server *server, const gbl_schedule_view *schedule, const gbl_state_view *state,
+                            const gbl_sphere *sphere, uint64_t substeps, uint64_t *ticket) {
+    return gbl::guard([&] {
+        if (!server || !schedule || !state || !sphere || !ticket) gbl::invalid("null argument");
+        *ticket = server->impl->submit(*schedule, *state, *sphere, substeps);
+    });
+}
+
+gbl_result gbl_serve_step(gbl_server *server, uint64_t substeps, gbl_server_stats *stats) {
+    return gbl::guard([&] {
+        if (!server) gbl::invalid("null server");
+        server->impl->step(substeps, stats);
+    });
+}
+
+gbl_result gbl_serve_poll(gbl_server *server, uint64_t ticket, gbl_request_info *info) {
+    return gbl::guard([&] {
+        if (!server || !info) gbl::invalid("null argument");
+        server->impl->poll(ticket, *info);
+    });
+}
+
+gbl_result gbl_serve_take(gbl_server *server, uint64_t ticket, gbl_state_view *state, gbl_sphere *sphere,
+                          gbl_run_status *status) {
+    return gbl::guard([&] {
+        if (!server) gbl::invalid("null server");
+        server->impl->take(ticket, state, sphere, status);
+    });
+}
+
+gbl_result gbl_serve_cancel(gbl_server *server, uint64_t ticket) {
+    return gbl::guard([&] {
+        if (!server) gbl::invalid("null server");
+        server->impl->cancel(ticket);
+    });
+}
+
+gbl_result gbl_serve_stats(gbl_server *server, gbl_server_stats *stats) {
+    return gbl::guard([&] {
+        if (!server || !stats) gbl::invalid("null argument");
+        server->impl->stats(*stats);
+    });
+}
+
+gbl_result gbl_serve_footprint(int precision, uint32_t node_count, uint32_t bond_count, uint32_t max_degree,
+                               uint32_t block_count, uint64_t *bytes) {
+    return gbl::guard([&] {
+        if (!bytes) gbl::invalid("null argument");
+        if (precision == GBL_PRECISION_DOUBLE)
+            *bytes = gbl::Resident<double>::footprint(node_count, bond_count, max_degree, block_count);
+        else if (precision == GBL_PRECISION_FLOAT)
+            *bytes = gbl::Resident<float>::footprint(node_count, bond_count, max_degree, block_count);
+        else gbl::invalid("unknown precision");
     });
 }
 

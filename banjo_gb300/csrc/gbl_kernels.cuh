@@ -90,6 +90,7 @@ struct Ctl {
     unsigned long long quiet_steps, min_steps, no_failure_steps, energy_flat_steps, calm_steps;
     double energy_flat_fraction, calm_damage_margin, removable_energy;
     unsigned long long loads_remaining;
+    unsigned long long step_limit; // a served lattice's substep count (0: none); reaching it is exit 3 (max steps)
     // transient
     unsigned full_restart, dirty_count, ffb_count, loads_kicked;
     unsigned event_count, ext_count; // broken bonds this substep; loaded nodes (set between runs)
@@ -1351,6 +1352,7 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
         : exitReason(c.total_steps, c.broken_bonds, c.last_failure_step, c.quiet_steps, c.min_steps, c.no_failure_steps,
                      c.energy_flat_steps, c.last_energy_gain_step, c.calm_steps, c.last_damage_gain_step, c.max_damage,
                      c.calm_damage_margin, c.removed_energy, c.removable_energy > 0 ? available : 0.0);
+    if (c.exit_reason == 0 && c.step_limit != 0 && c.total_steps >= c.step_limit) c.exit_reason = 3U;
     if (c.exit_reason != 0) {
         c.stop = 1;
         atomicSub(L.running, 1U);

@@ -118,6 +118,21 @@ class LoadLedger(C.Structure):
                 ("angular_impulse_kg_m2_s", C.c_double * 3), ("work_j", C.c_double)]
 
 
+class RequestInfo(C.Structure):
+    _fields_ = [("phase", C.c_int32), ("slot", C.c_uint32), ("substeps", C.c_uint64), ("substeps_done", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("submitted_s", C.c_double), ("admitted_s", C.c_double),
+                ("finished_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_uint64), ("running", C.c_uint64), ("done", C.c_uint64), ("bytes_in_use", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("substeps_run", C.c_uint64), ("device_seconds", C.c_double),
+                ("clock_s", C.c_double)]
+
+
+REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE = 0, 1, 2
+
+
 class RunStatus(C.Structure):
     _fields_ = [("total_steps", C.c_uint64), ("first_failure_step", C.c_uint64), ("last_failure_step", C.c_uint64),
                 ("failure_rounds", C.c_uint32), ("broken_bonds", C.c_uint32), ("removed_energy_j", C.c_double),
@@ -183,6 +198,17 @@ def library() -> C.CDLL:
         "gbl_batch_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
         "gbl_batch_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_set_stream": ([vp, vp], C.c_int),
+        "gbl_serve_create": ([C.c_int, C.POINTER(StepSettings), C.c_uint64, C.POINTER(vp)], C.c_int),
+        "gbl_serve_destroy": ([vp], None),
+        "gbl_serve_submit": ([vp, C.POINTER(ScheduleView), C.POINTER(StateView), C.POINTER(Sphere), C.c_uint64,
+                              C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_serve_step": ([vp, C.c_uint64, C.POINTER(ServerStats)], C.c_int),
+        "gbl_serve_poll": ([vp, C.c_uint64, C.POINTER(RequestInfo)], C.c_int),
+        "gbl_serve_take": ([vp, C.c_uint64, C.POINTER(StateView), C.POINTER(Sphere), C.POINTER(RunStatus)], C.c_int),
+        "gbl_serve_cancel": ([vp, C.c_uint64], C.c_int),
+        "gbl_serve_stats": ([vp, C.POINTER(ServerStats)], C.c_int),
+        "gbl_serve_footprint": ([C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64)],
+                                C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -191,7 +217,8 @@ def library() -> C.CDLL:
     for name, cls in [("gbl_schedule_view", ScheduleView), ("gbl_state_view", StateView),
                       ("gbl_matter_view", MatterView), ("gbl_support_plane", SupportPlane),
                       ("gbl_step_settings", StepSettings), ("gbl_sphere", Sphere),
-                      ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus)]:
+                      ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
+                      ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -589,6 +616,66 @@ class Batch:
         out = np.zeros(16, dtype=np.float64)
         _call(library().gbl_batch_profile_phases, self._h, int(substeps), _ptr(out, C.c_double))
         return {PHASE_NAMES[k]: float(out[k]) for k in range(16)}
+
+
+class Server:
+    """Continuous batching of lattice requests under a device memory budget
+    (the served form of the step; the reference has no counterpart)."""
+
+    def __init__(self, settings: StepSettings, budget_bytes: int, precision: str = "float"):
+        self._h = None
+        h = C.c_void_p()
+        _call(library().gbl_serve_create, 1 if precision == "double" else 0, C.byref(settings), int(budget_bytes),
+              C.byref(h))
+        self._h = h
+        self._held = {}  # ticket -> (schedule, state): the views stay valid until admission
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_serve_destroy(self._h)
+            self._h = None
+
+    def submit(self, schedule: Schedule, state: State, sphere: Sphere, substeps: int) -> int:
+        t = C.c_uint64()
+        _call(library().gbl_serve_submit, self._h, C.byref(schedule.view), C.byref(state.view), C.byref(sphere),
+              int(substeps), C.byref(t))
+        self._held[t.value] = (schedule, state)
+        return int(t.value)
+
+    def step(self, substeps: int) -> ServerStats:
+        st = ServerStats()
+        _call(library().gbl_serve_step, self._h, int(substeps), C.byref(st))
+        return st
+
+    def poll(self, ticket: int) -> RequestInfo:
+        info = RequestInfo()
+        _call(library().gbl_serve_poll, self._h, int(ticket), C.byref(info))
+        if info.phase != REQUEST_QUEUED:
+            self._held.pop(ticket, None)
+        return info
+
+    def take(self, ticket: int, state: State) -> tuple:
+        sp = Sphere()
+        st = RunStatus()
+        _call(library().gbl_serve_take, self._h, int(ticket), C.byref(state.view), C.byref(sp), C.byref(st))
+        self._held.pop(ticket, None)
+        return sp, st
+
+    def cancel(self, ticket: int) -> None:
+        _call(library().gbl_serve_cancel, self._h, int(ticket))
+        self._held.pop(ticket, None)
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _call(library().gbl_serve_stats, self._h, C.byref(st))
+        return st
+
+
+def footprint(node_count: int, bond_count: int, max_degree: int, block_count: int, precision: str = "float") -> int:
+    n = C.c_uint64()
+    _call(library().gbl_serve_footprint, 1 if precision == "double" else 0, node_count, bond_count, max_degree,
+          block_count, C.byref(n))
+    return int(n.value)
 
 
 def status_arrays(st: RunStatus) -> dict:

@@ -314,6 +314,60 @@ gbl_result gbl_batch_profile_phases(gbl_batch *batch, uint64_t substeps, double 
 gbl_result gbl_batch_kernels_per_substep(gbl_batch *batch, uint64_t *count);
 gbl_result gbl_batch_set_stream(gbl_batch *batch, void *cuda_stream);
 
+/* ---- The server: continuous batching of lattice requests. ----
+ * The reference serves no requests (its callers build one backend per trial,
+ * TileImpactScene.cpp:345-351); this is the served form of the same step. A
+ * request is one lattice and a substep count. Requests queue in arrival order
+ * and are admitted while their device footprint (gbl_serve_footprint) fits
+ * what is left of the budget; admitted requests advance together, a chunk of
+ * substeps per gbl_serve_step, each stopping at its own count, and leave at
+ * once, freeing their memory for the next in line (admission is re-checked in
+ * the same call). Every request's result is the one it gets alone.
+ *
+ * The schedule and state views given to gbl_serve_submit must stay valid
+ * until the request is admitted (phase RUNNING) or cancelled; the result is
+ * kept by the server until gbl_serve_take. Times are seconds on the server's
+ * steady clock since its creation, -1 before the event. */
+typedef struct gbl_server gbl_server;
+enum { GBL_REQUEST_QUEUED = 0, GBL_REQUEST_RUNNING = 1, GBL_REQUEST_DONE = 2 };
+typedef struct gbl_request_info {
+    int32_t phase;
+    uint32_t slot;          /* while RUNNING */
+    uint64_t substeps;      /* requested */
+    uint64_t substeps_done;
+    uint64_t device_bytes;  /* charged against the budget while RUNNING */
+    double submitted_s;
+    double admitted_s;
+    double finished_s;
+} gbl_request_info;
+typedef struct gbl_server_stats {
+    uint64_t queued;
+    uint64_t running;
+    uint64_t done;          /* finished, not yet taken */
+    uint64_t bytes_in_use;
+    uint64_t budget_bytes;
+    uint64_t substeps_run;  /* chunks stepped, in substeps */
+    double device_seconds;  /* device time of the steps */
+    double clock_s;
+} gbl_server_stats;
+gbl_result gbl_serve_create(int precision, const gbl_step_settings *settings, uint64_t budget_bytes, gbl_server **out);
+void gbl_serve_destroy(gbl_server *server);
+gbl_result gbl_serve_submit(gbl_server *server, const gbl_schedule_view *schedule, const gbl_state_view *state,
+                            const gbl_sphere *sphere, uint64_t substeps, uint64_t *ticket);
+/* Admits what fits, advances every admitted request by up to `substeps`
+ * substeps, retires the finished, admits again. */
+gbl_result gbl_serve_step(gbl_server *server, uint64_t substeps, gbl_server_stats *stats);
+gbl_result gbl_serve_poll(gbl_server *server, uint64_t ticket, gbl_request_info *info);
+/* The finished request's state (arrays gbl_download writes), sphere and
+ * RunStatus; the request is then forgotten. */
+gbl_result gbl_serve_take(gbl_server *server, uint64_t ticket, gbl_state_view *state, gbl_sphere *sphere,
+                          gbl_run_status *status);
+gbl_result gbl_serve_cancel(gbl_server *server, uint64_t ticket);
+gbl_result gbl_serve_stats(gbl_server *server, gbl_server_stats *stats);
+/* Device bytes a lattice of these counts is charged on admission. */
+gbl_result gbl_serve_footprint(int precision, uint32_t node_count, uint32_t bond_count, uint32_t max_degree,
+                               uint32_t block_count, uint64_t *bytes);
+
 /* The bonds that broke between two aliveness snapshots (one byte per bond,
  * schedule order, non-zero = alive), listed in schedule order -- without
  * allocating anything. This entry point has no counterpart in the reference.
