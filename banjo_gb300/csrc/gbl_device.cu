@@ -12,13 +12,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -30,7 +34,11 @@ void check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) runtime(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// One device allocation per lattice, carved into aligned arrays.
+// One allocation per lattice, carved into aligned arrays. The layout is
+// recorded once (reserve) and bound to a base: a host image while the
+// lattice is prepared, then its device allocation (stream-ordered, from the
+// device's memory pool: admitting and retiring lattices does not synchronise
+// the device).
 class Arena {
 public:
     Arena() = default;
@@ -38,23 +46,28 @@ public:
     Arena &operator=(const Arena &) = delete;
     ~Arena() { release(); }
     void release() {
-        if (base_) cudaFree(base_);
+        if (base_) cudaFreeAsync(base_, stream_);
         base_ = nullptr;
-        bytes_ = 0;
     }
     template <class T> void reserve(T *&p, std::size_t count) {
         offsets_.push_back({reinterpret_cast<void **>(&p), bytes_});
         bytes_ += (count * sizeof(T) + 255) & ~static_cast<std::size_t>(255);
     }
-    void commit() {
-        check(cudaMalloc(&base_, bytes_ ? bytes_ : 256), "device allocation");
-        for (auto &o : offsets_) *o.first = static_cast<char *>(base_) + o.second;
-        offsets_.clear();
+    void bind(void *base) {
+        for (auto &o : offsets_) *o.first = static_cast<char *>(base) + o.second;
+    }
+    void allocate(cudaStream_t stream) {
+        release();
+        stream_ = stream;
+        check(cudaMallocAsync(&base_, bytes_ ? bytes_ : 256, stream), "device allocation");
+        bind(base_);
     }
     [[nodiscard]] std::size_t bytes() const { return bytes_; }
+    [[nodiscard]] void *base() const { return base_; }
 
 private:
     void *base_{};
+    cudaStream_t stream_{};
     std::size_t bytes_{};
     std::vector<std::pair<void **, std::size_t>> offsets_;
 };
@@ -74,7 +87,23 @@ template <class T> std::vector<T> fetch(const T *src, std::size_t n) {
     return out;
 }
 
-unsigned chunks(std::size_t n, unsigned per) { return static_cast<unsigned>((n + per - 1) / per); }
+// A static split of [0, n) over host threads, for the O(N + B) conversion
+// loops of upload and download (f(begin, end) on disjoint ranges; f must not
+// throw). Small ranges stay on the calling thread.
+template <class F> void parallelFor(std::size_t n, F &&f) {
+    constexpr std::size_t kGrain = std::size_t(1) << 16;
+    const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
+    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 32), (n + kGrain - 1) / kGrain);
+    if (T <= 1) {
+        f(std::size_t(0), n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(T - 1);
+    for (std::size_t t = 1; t < T; ++t) pool.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T); });
+    f(std::size_t(0), n / T);
+    for (auto &th : pool) th.join();
+}
 
 } // namespace
 
@@ -111,6 +140,12 @@ template <class R> struct Resident {
     gbl_run_status status{};
     std::vector<std::uint32_t> first_failure;
     std::vector<Frame> frames;
+    // The prepared host image of the filled part of the allocation.
+    struct FreeImage {
+        void operator()(unsigned char *p) const { std::free(p); }
+    };
+    std::unique_ptr<unsigned char, FreeImage> image_;
+    std::size_t filled_{};
 
     explicit Resident(Schedule s) : sched(std::move(s)) {}
     Resident(const Resident &) = delete;
@@ -183,35 +218,41 @@ template <class R> struct Resident {
         }
     }
 
-    // The device arrays of one lattice, in one allocation.
-    static void reserve(Arena &a, Dev<R> &d, std::uint32_t N, std::uint32_t B, std::uint32_t D, std::uint32_t blocks,
-                        std::size_t isolated) {
+    // The device arrays of one lattice, in one allocation: first the arrays an
+    // upload fills from the state, then the ones that start at zero. Returns
+    // the size of the first part.
+    static std::size_t reserve(Arena &a, Dev<R> &d, std::uint32_t N, std::uint32_t B, std::uint32_t D,
+                               std::uint32_t blocks, std::size_t isolated) {
         const std::size_t P = static_cast<std::size_t>(D) * N;
         a.reserve(d.u, N); a.reserve(d.v, N); a.reserve(d.x0, N); a.reserve(d.up, N);
-        a.reserve(d.strain, 2 * static_cast<std::size_t>(N));
-        a.reserve(d.rinv, 9 * static_cast<std::size_t>(N)); a.reserve(d.unm, 3 * static_cast<std::size_t>(N));
-        a.reserve(d.approach, kPlanes * static_cast<std::size_t>(N));
-        a.reserve(d.dirty, N + 4); a.reserve(d.engaged, kPlanes * static_cast<std::size_t>(N));
-        a.reserve(d.candidate, N); a.reserve(d.cand_bits, (N + 31) / 32 + 1);
         a.reserve(d.nbr, P); a.reserve(d.nbr_other, P); a.reserve(d.nbr_bond, P);
         a.reserve(d.slot_a, B); a.reserve(d.slot_b, B);
         a.reserve(d.rec, B); a.reserve(d.geo, B); a.reserve(d.prev, B); a.reserve(d.thr4, B);
-        a.reserve(d.thr2, B); a.reserve(d.plastic, B); a.reserve(d.lambda, B); a.reserve(d.mode, B);
+        a.reserve(d.thr2, B); a.reserve(d.plastic, B); a.reserve(d.mode, B);
+        a.reserve(d.dev2sched, B); a.reserve(d.isolated, isolated + 1);
+        a.reserve(d.node_block_begin, blocks + 1);
+        a.reserve(d.sphere, 1);
+        a.reserve(d.dirty, N + 4);
+        const std::size_t filled = a.bytes();
+        a.reserve(d.strain, 2 * static_cast<std::size_t>(N));
+        a.reserve(d.rinv, 9 * static_cast<std::size_t>(N)); a.reserve(d.unm, 3 * static_cast<std::size_t>(N));
+        a.reserve(d.approach, kPlanes * static_cast<std::size_t>(N));
+        a.reserve(d.engaged, kPlanes * static_cast<std::size_t>(N));
+        a.reserve(d.candidate, N); a.reserve(d.cand_bits, (N + 31) / 32 + 1);
+        a.reserve(d.lambda, B);
         a.reserve(d.ev_bits, d.words_b + 1); a.reserve(d.ev_tile, d.tiles_b + 1); a.reserve(d.ev_list, B + 1);
         a.reserve(d.ev_removed, B); a.reserve(d.ev_packed, B + 1); a.reserve(d.ev_prefix, B + 1);
-        a.reserve(d.ev_ends, B); a.reserve(d.dev2sched, B);
-        a.reserve(d.isolated, isolated + 1);
+        a.reserve(d.ev_ends, B);
         a.reserve(d.dmg_bits, d.words_b + 1); a.reserve(d.dmg_tile, d.tiles_b + 1);
         a.reserve(d.dmg_list, B + 1); a.reserve(d.ev_damage, B); a.reserve(d.dmg_value, B + 1);
         a.reserve(d.tile_plastic, d.tiles_b + 1); a.reserve(d.tile_removed, d.tiles_b + 1);
         const std::size_t scan_blocks = d.tiles_b / kScanBlock + 1;
         a.reserve(d.blk_ev, scan_blocks); a.reserve(d.blk_dmg, scan_blocks);
         a.reserve(d.blk_removed, scan_blocks); a.reserve(d.blk_plastic, scan_blocks);
-        a.reserve(d.node_block_begin, blocks + 1);
         a.reserve(d.cand_list, static_cast<std::size_t>(blocks) * kCandidatesPerBlock);
         a.reserve(d.cand_count, blocks);
         a.reserve(d.dirty_list, N + 1); a.reserve(d.ffb, B + 1);
-        a.reserve(d.sphere, 1);
+        return filled;
     }
 
     // Device bytes a lattice of these counts takes (its isolated nodes at
@@ -225,109 +266,115 @@ template <class R> struct Resident {
         return a.bytes() + static_cast<std::size_t>(N) * (sizeof(Q4<R>) + 16 * sizeof(double) + sizeof(std::uint32_t));
     }
 
-    // upload (FastLattice.hpp:267-268; WorkingLattice::fromState, LatticeWorking.hpp:53-124)
-    void upload(const gbl_state_view &st, const gbl_sphere &sphere, cudaStream_t stream) {
+    // upload, host half (FastLattice.hpp:267-268; WorkingLattice::fromState,
+    // LatticeWorking.hpp:53-124): the device layout of the state, written into
+    // a host image of the allocation. No CUDA call: lattices can be prepared
+    // on several threads at once.
+    void prepare(const gbl_state_view &st, const gbl_sphere &sphere) {
         N = st.node_count;
         B = st.bond_count;
         if (N > kNodeMask) invalid("lattice exceeds 2^30 nodes");
         if (sched.bond_count != B || sched.node_count != N) invalid("lattice schedule does not match the lattice");
         const std::uint32_t D = st.max_degree;
         buildLevels(st);
-        Dev<R> d{};
+        Dev<R> &d = dev;
+        d = Dev<R>{};
         d.N = N; d.B = B; d.D = D; d.blocks = sched.block_count;
         d.words_b = (B + 31) / 32;
         d.tiles_b = (B + kThreads - 1) / kThreads;
-        arena.release();
-        reserve(arena, d, N, B, D, sched.block_count, isolated.size());
-        arena.commit();
-        const std::size_t P = static_cast<std::size_t>(D) * N;
-
-        std::vector<Q4<R>> u(N), v(N), x0(N), up(N);
+        filled_ = reserve(arena, d, N, B, D, sched.block_count, isolated.size());
+        image_.reset(static_cast<unsigned char *>(std::aligned_alloc(256, filled_ ? filled_ : 256)));
+        if (!image_) throw std::bad_alloc();
+        arena.bind(image_.get());
         mass.resize(N);
         inv_mass.resize(N);
-        for (std::uint32_t i = 0; i < N; ++i) {
-            u[i] = {R(st.u[3 * i]), R(st.u[3 * i + 1]), R(st.u[3 * i + 2]), R(st.inv_mass[i])};
-            v[i] = {R(st.v[3 * i]), R(st.v[3 * i + 1]), R(st.v[3 * i + 2]), R(st.mass[i])};
-            x0[i] = {R(st.x0[3 * i]), R(st.x0[3 * i + 1]), R(st.x0[3 * i + 2]), R(0)};
-            up[i] = {R(st.u_prev[3 * i]), R(st.u_prev[3 * i + 1]), R(st.u_prev[3 * i + 2]), R(0)};
-            mass[i] = R(st.mass[i]);
-            inv_mass[i] = R(st.inv_mass[i]);
-        }
-        gbl::upload(d.u, u, stream); gbl::upload(d.v, v, stream); gbl::upload(d.x0, x0, stream);
-        gbl::upload(d.up, up, stream);
-        zero(d.strain, 2 * static_cast<std::size_t>(N), stream); zero(d.rinv, 9 * static_cast<std::size_t>(N), stream);
-        zero(d.unm, 3 * static_cast<std::size_t>(N), stream);
-        zero(d.approach, kPlanes * static_cast<std::size_t>(N), stream);
-        zero(d.engaged, kPlanes * static_cast<std::size_t>(N), stream); zero(d.candidate, N, stream);
-        zero(d.cand_bits, (N + 31) / 32 + 1, stream);
-        zero(d.dirty, N + 4, stream);
-        check(cudaMemsetAsync(d.dirty, 1, N, stream), "memset");
+        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t i = lo; i < hi; ++i) {
+                d.u[i] = {R(st.u[3 * i]), R(st.u[3 * i + 1]), R(st.u[3 * i + 2]), R(st.inv_mass[i])};
+                d.v[i] = {R(st.v[3 * i]), R(st.v[3 * i + 1]), R(st.v[3 * i + 2]), R(st.mass[i])};
+                d.x0[i] = {R(st.x0[3 * i]), R(st.x0[3 * i + 1]), R(st.x0[3 * i + 2]), R(0)};
+                d.up[i] = {R(st.u_prev[3 * i]), R(st.u_prev[3 * i + 1]), R(st.u_prev[3 * i + 2]), R(0)};
+                mass[i] = R(st.mass[i]);
+                inv_mass[i] = R(st.inv_mass[i]);
+            }
+        });
+        // Every node starts dirty: the first substep restarts in full.
+        std::memset(d.dirty, 1, N);
+        std::memset(d.dirty + N, 0, 4);
         // Neighbour slots: (rest, weight if alive), the other node (itself when padded).
-        std::vector<Q4<R>> nbr(P);
-        std::vector<std::uint32_t> other(P), bond(P);
-        for (std::size_t s = 0; s < P; ++s) {
-            const bool present = st.nbr_bond[s] != kNoBond;
-            const std::uint32_t node = static_cast<std::uint32_t>(s % N);
-            nbr[s] = {R(st.nbr_rest[3 * s]), R(st.nbr_rest[3 * s + 1]), R(st.nbr_rest[3 * s + 2]),
-                      (present && st.nbr_alive[s]) ? R(st.nbr_weight[s]) : R(0)};
-            other[s] = present ? st.nbr_other[s] : node;
-            bond[s] = present ? sched2dev[st.nbr_bond[s]] : kNoBond;
-        }
-        gbl::upload(d.nbr, nbr, stream); gbl::upload(d.nbr_other, other, stream); gbl::upload(d.nbr_bond, bond, stream);
+        const std::size_t P = static_cast<std::size_t>(D) * N;
+        parallelFor(P, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t s = lo; s < hi; ++s) {
+                const bool present = st.nbr_bond[s] != kNoBond;
+                const std::uint32_t node = static_cast<std::uint32_t>(s % N);
+                d.nbr[s] = {R(st.nbr_rest[3 * s]), R(st.nbr_rest[3 * s + 1]), R(st.nbr_rest[3 * s + 2]),
+                            (present && st.nbr_alive[s]) ? R(st.nbr_weight[s]) : R(0)};
+                d.nbr_other[s] = present ? st.nbr_other[s] : node;
+                d.nbr_bond[s] = present ? sched2dev[st.nbr_bond[s]] : kNoBond;
+            }
+        });
         // Bonds, level-major storage (storage index dd holds schedule index j).
-        std::vector<BondRec<R>> rec(B);
-        std::vector<Q4<R>> geo(B), prev(B), thr4(B);
-        std::vector<Q2<R>> thr2(B), plastic(B);
-        std::vector<std::uint32_t> slot_a(B), slot_b(B);
-        std::vector<std::uint8_t> mode(B);
-        plastic_state = false;
-        for (std::uint32_t dd = 0; dd < B; ++dd) {
-            const std::uint32_t j = dev2sched[dd];
-            rec[dd] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit) | (last_a[dd] ? kLastABit : 0U),
-                       st.bond_b[j] | (last_b[dd] ? kLastBBit : 0U), R(st.rest_length_sq_minus[j]), R(st.rest_length[j])};
-            geo[dd] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]), R(st.compliance[j])};
-            prev[dd] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
-            const double *t = st.threshold + 6 * static_cast<std::size_t>(j);
-            thr4[dd] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
-            thr2[dd] = {R(t[4]), R(t[5])};
-            plastic[dd] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
-            plastic_state = plastic_state || plastic[dd].x != R(0);
-            slot_a[dd] = st.bond_slot_a[j];
-            slot_b[dd] = st.bond_slot_b[j];
-            mode[dd] = st.failure_mode[j];
-        }
-        gbl::upload(d.rec, rec, stream); gbl::upload(d.geo, geo, stream); gbl::upload(d.prev, prev, stream);
-        gbl::upload(d.thr4, thr4, stream); gbl::upload(d.thr2, thr2, stream); gbl::upload(d.plastic, plastic, stream);
-        gbl::upload(d.slot_a, slot_a, stream); gbl::upload(d.slot_b, slot_b, stream); gbl::upload(d.mode, mode, stream);
-        gbl::upload(d.dev2sched, dev2sched, stream);
-        gbl::upload(d.isolated, isolated, stream);
+        std::atomic<bool> plastic_any{false};
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            bool any = false;
+            for (std::size_t dd = lo; dd < hi; ++dd) {
+                const std::uint32_t j = dev2sched[dd];
+                d.rec[dd] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit) | (last_a[dd] ? kLastABit : 0U),
+                             st.bond_b[j] | (last_b[dd] ? kLastBBit : 0U), R(st.rest_length_sq_minus[j]),
+                             R(st.rest_length[j])};
+                d.geo[dd] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]),
+                             R(st.compliance[j])};
+                d.prev[dd] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
+                const double *t = st.threshold + 6 * static_cast<std::size_t>(j);
+                d.thr4[dd] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
+                d.thr2[dd] = {R(t[4]), R(t[5])};
+                d.plastic[dd] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
+                any = any || d.plastic[dd].x != R(0);
+                d.slot_a[dd] = st.bond_slot_a[j];
+                d.slot_b[dd] = st.bond_slot_b[j];
+                d.mode[dd] = st.failure_mode[j];
+            }
+            if (any) plastic_any.store(true);
+        });
+        plastic_state = plastic_any.load();
+        std::memcpy(d.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B);
+        if (!isolated.empty()) std::memcpy(d.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size());
         d.isolated_count = static_cast<std::uint32_t>(isolated.size());
-        zero(d.lambda, B, stream);
-        zero(d.ev_bits, d.words_b + 1, stream);
-        zero(d.dmg_bits, d.words_b + 1, stream);
-        zero(d.tile_plastic, d.tiles_b + 1, stream);
-        zero(d.tile_removed, d.tiles_b + 1, stream);
-        gbl::upload(d.node_block_begin, sched.node_block_begin, stream);
-        zero(d.cand_count, sched.block_count, stream);
+        std::memcpy(d.node_block_begin, sched.node_block_begin.data(), sizeof(std::uint32_t) * (sched.block_count + 1));
         sphere0.center = {R(sphere.center[0]), R(sphere.center[1]), R(sphere.center[2])};
         sphere0.velocity = {R(sphere.velocity[0]), R(sphere.velocity[1]), R(sphere.velocity[2])};
         sphere0.angular = {R(sphere.angular_velocity[0]), R(sphere.angular_velocity[1]), R(sphere.angular_velocity[2])};
         sphere0.radius = R(sphere.radius);
         sphere0.mass = R(sphere.mass);
         sphere0.inertia = R(sphere.inertia);
-        uploadRaw(d.sphere, &sphere0, 1, stream);
+        *d.sphere = sphere0;
         std::memcpy(d.origin, st.origin, sizeof(d.origin));
         // Loads do not survive an upload (ExternalLoads.hpp:26 reset).
-        d.ext_force = ext_force; d.ext_req = ext_req; d.ext_contrib = ext_contrib; d.ext_nodes = ext_nodes;
         ext_count = 0;
         ext_remaining = 0;
-        dev = d;
-        // Synchronize: the host staging vectors die with this scope.
-        check(cudaStreamSynchronize(stream), "upload");
         status = gbl_run_status{};
         status.first_failure_step = status.last_failure_step = status.last_energy_gain_step = ~0ULL;
         first_failure.clear();
         frames.clear();
+    }
+
+    // upload, device half: one allocation, the prepared image copied in, the
+    // rest cleared. The host image is released.
+    void commit(cudaStream_t stream) {
+        if (!image_) logic("lattice committed before it was prepared");
+        arena.allocate(stream);
+        check(cudaMemcpyAsync(arena.base(), image_.get(), filled_, cudaMemcpyHostToDevice, stream), "copy");
+        if (arena.bytes() > filled_)
+            check(cudaMemsetAsync(static_cast<char *>(arena.base()) + filled_, 0, arena.bytes() - filled_, stream),
+                  "memset");
+        dev.ext_force = ext_force; dev.ext_req = ext_req; dev.ext_contrib = ext_contrib; dev.ext_nodes = ext_nodes;
+        check(cudaStreamSynchronize(stream), "upload");
+        image_.reset();
+    }
+
+    void upload(const gbl_state_view &st, const gbl_sphere &sphere, cudaStream_t stream) {
+        prepare(st, sphere);
+        commit(stream);
     }
 
     // setExternalForces (ExternalLoads.hpp:28-50): validated in full before
@@ -376,23 +423,27 @@ template <class R> struct Resident {
     void download(gbl_state_view &st, gbl_sphere *sphere) {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
         const auto u = fetch(dev.u, N), up = fetch(dev.up, N), v = fetch(dev.v, N);
-        for (std::uint32_t i = 0; i < N; ++i) {
-            st.u[3 * i] = u[i].x; st.u[3 * i + 1] = u[i].y; st.u[3 * i + 2] = u[i].z;
-            st.u_prev[3 * i] = up[i].x; st.u_prev[3 * i + 1] = up[i].y; st.u_prev[3 * i + 2] = up[i].z;
-            st.v[3 * i] = v[i].x; st.v[3 * i + 1] = v[i].y; st.v[3 * i + 2] = v[i].z;
-        }
+        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t i = lo; i < hi; ++i) {
+                st.u[3 * i] = u[i].x; st.u[3 * i + 1] = u[i].y; st.u[3 * i + 2] = u[i].z;
+                st.u_prev[3 * i] = up[i].x; st.u_prev[3 * i + 1] = up[i].y; st.u_prev[3 * i + 2] = up[i].z;
+                st.v[3 * i] = v[i].x; st.v[3 * i + 1] = v[i].y; st.v[3 * i + 2] = v[i].z;
+            }
+        });
         const auto rec = fetch(dev.rec, B);
         const auto prev = fetch(dev.prev, B);
         const auto pl = fetch(dev.plastic, B);
         const auto mode = fetch(dev.mode, B);
-        for (std::uint32_t dd = 0; dd < B; ++dd) {
-            const std::uint32_t j = dev2sched[dd];
-            st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
-            st.failure_mode[j] = mode[dd];
-            st.damage[j] = prev[dd].w;
-            st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
-            st.plastic_extension[j] = pl[dd].x; st.plastic_strain[j] = pl[dd].y;
-        }
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t dd = lo; dd < hi; ++dd) {
+                const std::uint32_t j = dev2sched[dd];
+                st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
+                st.failure_mode[j] = mode[dd];
+                st.damage[j] = prev[dd].w;
+                st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
+                st.plastic_extension[j] = pl[dd].x; st.plastic_strain[j] = pl[dd].y;
+            }
+        });
         if (sphere) *sphere = fetchSphere();
     }
 
@@ -537,8 +588,22 @@ public:
     // RunStatus) with `step_limit` substeps to run (0: no limit).
     std::size_t add(const Schedule &sched, const gbl_state_view &st, const gbl_sphere &sphere,
                     std::uint64_t step_limit = 0) {
+        return place(prepare(sched, st, sphere), step_limit);
+    }
+
+    // The host half of add: no CUDA call and no engine state, so any number
+    // of threads may prepare lattices while the engine runs.
+    static std::unique_ptr<Resident<R>> prepare(const Schedule &sched, const gbl_state_view &st,
+                                                const gbl_sphere &sphere) {
         auto r = std::make_unique<Resident<R>>(sched);
-        r->upload(st, sphere, stream_);
+        r->prepare(st, sphere);
+        return r;
+    }
+
+    // The device half of add: a prepared lattice takes the first free slot.
+    std::size_t place(std::unique_ptr<Resident<R>> r, std::uint64_t step_limit = 0) {
+        std::lock_guard<std::mutex> lock(place_mutex_);
+        r->commit(stream_);
         std::size_t k = 0;
         while (k < slots_.size() && slots_[k]) ++k;
         if (k == slots_.size()) slots_.emplace_back();
@@ -1082,6 +1147,7 @@ private:
 
     std::vector<std::unique_ptr<Resident<R>>> slots_;
     std::vector<std::uint32_t> active_;
+    std::mutex place_mutex_;
     Settings<R> S_{};
     bool plastic_{false}, ready_{false}, many_{false}, dirty_{true};
     std::uint32_t one_{0};
@@ -1261,13 +1327,17 @@ public:
             Resident<R>::footprint(st.node_count, st.bond_count, st.max_degree, sv.block_count);
         if (bytes > budget_) invalid("request exceeds the device memory budget on its own");
         Request q;
-        q.ticket = ++last_ticket_;
-        q.sched = Schedule::fromView(sv);
-        q.view = st;
+        q.submitted = clock() - t0_;
+        // The device image is prepared here, on the caller's thread, outside
+        // the lock: a step may be running meanwhile.
+        q.prepared = Engine<R>::prepare(Schedule::fromView(sv), st, sp);
+        q.nodes = st.node_count;
+        q.bonds = st.bond_count;
         q.sphere = sp;
         q.substeps = substeps;
         q.bytes = bytes;
-        q.submitted = clock() - t0_;
+        std::lock_guard<std::mutex> lock(mutex_);
+        q.ticket = ++last_ticket_;
         const std::uint64_t t = q.ticket;
         requests_.emplace(t, std::move(q));
         queue_.push_back(t);
@@ -1276,6 +1346,7 @@ public:
     }
 
     void step(std::uint64_t substeps, gbl_server_stats *out) override {
+        std::lock_guard<std::mutex> lock(mutex_);
         admit();
         if (engine_.size() > 0 && substeps > 0) {
             gbl_run_control c{}; // RunControl's defaults (FastLattice.hpp:79-128), exit rules off
@@ -1289,10 +1360,11 @@ public:
             retireFinished();
             admit(); // memory freed this step goes to the next in line now
         }
-        if (out) stats(*out);
+        if (out) fillStats(*out);
     }
 
     void poll(std::uint64_t ticket, gbl_request_info &info) override {
+        std::lock_guard<std::mutex> lock(mutex_);
         const Request &q = find(ticket);
         info = gbl_request_info{};
         info.phase = q.phase;
@@ -1306,10 +1378,11 @@ public:
     }
 
     void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) override {
+        std::lock_guard<std::mutex> lock(mutex_);
         Request &q = find(ticket);
         if (q.phase != GBL_REQUEST_DONE) invalid("the request has not finished");
         if (st) {
-            if (st->node_count != q.view.node_count || st->bond_count != q.view.bond_count)
+            if (st->node_count != q.nodes || st->bond_count != q.bonds)
                 invalid("result state does not match the request's lattice");
             q.result.copyTo(*st);
         }
@@ -1320,6 +1393,7 @@ public:
     }
 
     void cancel(std::uint64_t ticket) override {
+        std::lock_guard<std::mutex> lock(mutex_);
         Request &q = find(ticket);
         if (q.phase == GBL_REQUEST_QUEUED) {
             queue_.erase(std::find(queue_.begin(), queue_.end(), ticket));
@@ -1335,6 +1409,12 @@ public:
     }
 
     void stats(gbl_server_stats &o) override {
+        std::lock_guard<std::mutex> lock(mutex_);
+        fillStats(o);
+    }
+
+private:
+    void fillStats(gbl_server_stats &o) {
         o = gbl_server_stats{};
         o.queued = queued_;
         o.running = running_;
@@ -1346,11 +1426,10 @@ public:
         o.clock_s = clock() - t0_;
     }
 
-private:
     struct Request {
         std::uint64_t ticket{}, substeps{}, bytes{}, done_steps{};
-        Schedule sched;
-        gbl_state_view view{};
+        std::uint32_t nodes{}, bonds{};
+        std::unique_ptr<Resident<R>> prepared;
         gbl_sphere sphere{};
         int phase{GBL_REQUEST_QUEUED};
         std::size_t slot{};
@@ -1381,7 +1460,7 @@ private:
         while (!queue_.empty()) {
             Request &q = requests_.at(queue_.front());
             if (used_ + q.bytes > budget_) break;
-            q.slot = engine_.add(q.sched, q.view, q.sphere, q.substeps);
+            q.slot = engine_.place(std::move(q.prepared), q.substeps);
             q.phase = GBL_REQUEST_RUNNING;
             q.admitted = clock() - t0_;
             used_ += q.bytes;
@@ -1409,7 +1488,6 @@ private:
             used_ -= q.bytes;
             q.phase = GBL_REQUEST_DONE;
             q.finished = clock() - t0_;
-            q.sched = Schedule{};
             --running_;
             ++done_;
         }
@@ -1423,6 +1501,7 @@ private:
     std::map<std::uint64_t, Request> requests_;
     std::deque<std::uint64_t> queue_;
     std::vector<std::uint64_t> slot_ticket_;
+    std::mutex mutex_;
 };
 
 } // namespace gbl

@@ -11,6 +11,7 @@
 #include "gbl_internal.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -265,6 +266,7 @@ size_t gbl_struct_size(const char *name) {
     GBL_SIZE(gbl_contact_settings) GBL_SIZE(gbl_node_contact_settings) GBL_SIZE(gbl_step_settings)
     GBL_SIZE(gbl_sphere) GBL_SIZE(gbl_run_control) GBL_SIZE(gbl_contact_accumulators) GBL_SIZE(gbl_load_ledger)
     GBL_SIZE(gbl_run_status) GBL_SIZE(gbl_matter_view) GBL_SIZE(gbl_request_info) GBL_SIZE(gbl_server_stats)
+    GBL_SIZE(gbl_box_spec)
 #undef GBL_SIZE
     return 0;
 }
@@ -312,5 +314,127 @@ gbl_result gbl_state_pin(gbl_state *state, const uint8_t *pinned) {
 }
 
 void gbl_state_free(gbl_state *state) { delete state; }
+
+} // extern "C"
+
+// ---- Box lattices (the input generator of the reference's box scenes) ----
+
+namespace gbl {
+
+// generateBoxTileLattice's walk (src/matter/BoxLattice.cpp:117-155): nodes at
+// cell centres, index x + nx*(y + ny*z) (BoxLattice.hpp:22-26, positions
+// BoxLattice.cpp:82-86); for each node in index order, each integer offset of
+// the positive half-space in dz, dy, dx order over [-h, h]
+// (src/matter/Lattice.cpp:49-52) whose neighbour lies inside makes a bond
+// (node, neighbour) of rest length spacing*|o|. The offset rule is the
+// horizon |o| <= h, or |o|^2 <= max_offset_sq when that is set. Slabs:
+// boxLatticeSlabs, BoxLattice.cpp:175-195.
+struct Box {
+    std::uint32_t node_count{}, bond_count{};
+    std::vector<double> ref, pos, vel, mass, rest, compliance, threshold;
+    std::vector<std::uint32_t> a, b, slabs;
+};
+
+Box buildBox(const gbl_box_spec &sp) {
+    if (sp.nx == 0 || sp.ny == 0 || sp.nz == 0) invalid("box lattice needs at least one cell per axis");
+    const std::uint64_t n64 = static_cast<std::uint64_t>(sp.nx) * sp.ny * sp.nz;
+    if (n64 > kNodeLimit) invalid("box lattice exceeds 2^30 nodes");
+    const int h = static_cast<int>(sp.horizon ? sp.horizon : 1);
+    struct Offset { int dx, dy, dz, d2; };
+    std::vector<Offset> offs;
+    for (int dz = -h; dz <= h; ++dz)
+        for (int dy = -h; dy <= h; ++dy)
+            for (int dx = -h; dx <= h; ++dx) {
+                if (!(dz > 0 || (dz == 0 && dy > 0) || (dz == 0 && dy == 0 && dx > 0))) continue;
+                const int d2 = dx * dx + dy * dy + dz * dz;
+                if (sp.max_offset_sq ? d2 > static_cast<int>(sp.max_offset_sq) : std::sqrt(double(d2)) > h + 1e-9) continue;
+                offs.push_back({dx, dy, dz, d2});
+            }
+    Box bx;
+    const std::uint32_t nx = sp.nx, ny = sp.ny, nz = sp.nz;
+    const std::uint32_t n = static_cast<std::uint32_t>(n64);
+    bx.node_count = n;
+    bx.ref.resize(3 * static_cast<std::size_t>(n));
+    for (std::uint32_t i = 0; i < n; ++i) {
+        const std::uint32_t x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
+        bx.ref[3 * i] = ((double(x) + 0.5) - 0.5 * nx) * sp.spacing + sp.center[0];
+        bx.ref[3 * i + 1] = ((double(y) + 0.5) - 0.5 * ny) * sp.spacing + sp.center[1];
+        bx.ref[3 * i + 2] = ((double(z) + 0.5) - 0.5 * nz) * sp.spacing + sp.center[2];
+    }
+    bx.pos = bx.ref;
+    bx.vel.assign(bx.ref.size(), 0.0);
+    bx.mass.assign(n, sp.node_mass);
+    bx.a.reserve(static_cast<std::size_t>(n) * offs.size());
+    bx.b.reserve(bx.a.capacity());
+    std::vector<double> rest_of(offs.size());
+    for (std::size_t k = 0; k < offs.size(); ++k) rest_of[k] = std::sqrt(double(offs[k].d2)) * sp.spacing;
+    for (std::uint32_t i = 0; i < n; ++i) {
+        const int x = static_cast<int>(i % nx), y = static_cast<int>((i / nx) % ny), z = static_cast<int>(i / (nx * ny));
+        for (std::size_t k = 0; k < offs.size(); ++k) {
+            const int X = x + offs[k].dx, Y = y + offs[k].dy, Z = z + offs[k].dz;
+            if (X < 0 || Y < 0 || Z < 0 || X >= static_cast<int>(nx) || Y >= static_cast<int>(ny) ||
+                Z >= static_cast<int>(nz))
+                continue;
+            bx.a.push_back(i);
+            bx.b.push_back(static_cast<std::uint32_t>(X) + nx * (static_cast<std::uint32_t>(Y) + ny * Z));
+            bx.rest.push_back(rest_of[k]);
+        }
+    }
+    const std::size_t B = bx.a.size();
+    if (B > 0xffffffffULL) invalid("box lattice has more than 2^32 - 1 bonds");
+    bx.bond_count = static_cast<std::uint32_t>(B);
+    bx.compliance.assign(B, sp.compliance);
+    bx.threshold.resize(6 * B);
+    for (std::size_t q = 0; q < B; ++q)
+        for (int t = 0; t < 6; ++t) bx.threshold[6 * q + t] = sp.threshold[t];
+    std::uint32_t blocks = std::max(1U, sp.slabs);
+    blocks = std::min(blocks, std::max(1U, nz));
+    const std::uint32_t layer = nx * ny;
+    bx.slabs.resize(blocks + 1);
+    for (std::uint32_t k = 0; k <= blocks; ++k)
+        bx.slabs[k] = static_cast<std::uint32_t>((static_cast<std::uint64_t>(nz) * k / blocks) * layer);
+    bx.slabs[blocks] = layer * nz;
+    return bx;
+}
+
+} // namespace gbl
+
+struct gbl_box {
+    gbl::Box b;
+};
+
+extern "C" {
+
+gbl_result gbl_build_box(const gbl_box_spec *spec, gbl_box **out) {
+    return gbl::guard([&] {
+        if (!spec || !out) gbl::invalid("null argument");
+        *out = new gbl_box{gbl::buildBox(*spec)};
+    });
+}
+
+gbl_result gbl_box_view_of(const gbl_box *box, gbl_matter_view *matter, const uint32_t **node_block_begin,
+                           uint32_t *block_count) {
+    return gbl::guard([&] {
+        if (!box || !matter) gbl::invalid("null argument");
+        const gbl::Box &b = box->b;
+        gbl_matter_view m{};
+        m.node_count = b.node_count;
+        m.bond_count = b.bond_count;
+        m.reference_position = b.ref.data();
+        m.position = b.pos.data();
+        m.velocity = b.vel.data();
+        m.mass = b.mass.data();
+        m.bond_a = b.a.data();
+        m.bond_b = b.b.data();
+        m.rest_length = b.rest.data();
+        m.compliance = b.compliance.data();
+        m.threshold = b.threshold.data();
+        *matter = m;
+        if (node_block_begin) *node_block_begin = b.slabs.data();
+        if (block_count) *block_count = static_cast<uint32_t>(b.slabs.size() - 1);
+    });
+}
+
+void gbl_box_free(gbl_box *box) { delete box; }
 
 } // extern "C"

@@ -10,6 +10,8 @@
 
 namespace gbl {
 
+constexpr std::uint64_t kNodeLimit = 1ULL << 30; // node indices keep two flag bits free
+
 // Exceptions carry the gbl_result the C ABI returns for them; the names follow
 // the reference's exception types (FastLattice.hpp:263-358).
 struct Error : std::runtime_error {

@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libgbl.so")
 
 u8p, u32p, f64p, f32p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_float)
 NO_BOND = 0xFFFFFFFF
+INF_F = float("inf")
 
 
 class ScheduleView(C.Structure):
@@ -118,6 +119,13 @@ class LoadLedger(C.Structure):
                 ("angular_impulse_kg_m2_s", C.c_double * 3), ("work_j", C.c_double)]
 
 
+class BoxSpec(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("horizon", C.c_uint32),
+                ("max_offset_sq", C.c_uint32), ("slabs", C.c_uint32), ("spacing", C.c_double),
+                ("center", C.c_double * 3), ("node_mass", C.c_double), ("compliance", C.c_double),
+                ("threshold", C.c_double * 6)]
+
+
 class RequestInfo(C.Structure):
     _fields_ = [("phase", C.c_int32), ("slot", C.c_uint32), ("substeps", C.c_uint64), ("substeps_done", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("submitted_s", C.c_double), ("admitted_s", C.c_double),
@@ -198,6 +206,9 @@ def library() -> C.CDLL:
         "gbl_batch_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
         "gbl_batch_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_set_stream": ([vp, vp], C.c_int),
+        "gbl_build_box": ([C.POINTER(BoxSpec), C.POINTER(vp)], C.c_int),
+        "gbl_box_view_of": ([vp, C.POINTER(MatterView), C.POINTER(u32p), C.POINTER(C.c_uint32)], C.c_int),
+        "gbl_box_free": ([vp], None),
         "gbl_serve_create": ([C.c_int, C.POINTER(StepSettings), C.c_uint64, C.POINTER(vp)], C.c_int),
         "gbl_serve_destroy": ([vp], None),
         "gbl_serve_submit": ([vp, C.POINTER(ScheduleView), C.POINTER(StateView), C.POINTER(Sphere), C.c_uint64,
@@ -218,7 +229,8 @@ def library() -> C.CDLL:
                       ("gbl_matter_view", MatterView), ("gbl_support_plane", SupportPlane),
                       ("gbl_step_settings", StepSettings), ("gbl_sphere", Sphere),
                       ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
-                      ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats)]:
+                      ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats),
+                      ("gbl_box_spec", BoxSpec)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -382,6 +394,61 @@ def build_lattice_state(case: dict, schedule: Schedule) -> State:
     if "pinned" in case:
         st.pin(case["pinned"])
     return st
+
+
+class Box:
+    """A box lattice built by the library (generateBoxTileLattice's walk,
+    src/matter/BoxLattice.cpp:49-195, uniform bonds)."""
+
+    def __init__(self, spec: BoxSpec):
+        self._h = None
+        h = C.c_void_p()
+        _call(library().gbl_build_box, C.byref(spec), C.byref(h))
+        self._h = h
+        self.matter = MatterView()
+        slabs = u32p()
+        count = C.c_uint32()
+        _call(library().gbl_box_view_of, self._h, C.byref(self.matter), C.byref(slabs), C.byref(count))
+        self.node_count = int(self.matter.node_count)
+        self.bond_count = int(self.matter.bond_count)
+        self.node_block_begin = np.ctypeslib.as_array(slabs, shape=(count.value + 1,)).copy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            library().gbl_box_free(self._h)
+            self._h = None
+
+    def array(self, name: str) -> np.ndarray:
+        """A copy of one matter array: ref_pos, pos, vel, mass, bond_a, bond_b, rest_length, compliance, threshold."""
+        m = self.matter
+        n, b = self.node_count, self.bond_count
+        field, count = {"ref_pos": ("reference_position", 3 * n), "pos": ("position", 3 * n),
+                        "vel": ("velocity", 3 * n), "mass": ("mass", n), "bond_a": ("bond_a", b),
+                        "bond_b": ("bond_b", b), "rest_length": ("rest_length", b), "compliance": ("compliance", b),
+                        "threshold": ("threshold", 6 * b)}[name]
+        return np.ctypeslib.as_array(getattr(m, field), shape=(count,)).copy() if count else np.zeros(0)
+
+
+def build_box(nx, ny, nz, spacing, center=(0.0, 0.0, 0.0), compliance=1e-7, threshold=(INF_F,) * 6,
+              node_mass=1e-3, horizon=1, max_offset_sq=2, slabs=1) -> Box:
+    spec = BoxSpec(nx, ny, nz, horizon, max_offset_sq, slabs, spacing, (C.c_double * 3)(*center), node_mass,
+                   compliance, (C.c_double * 6)(*threshold))
+    return Box(spec)
+
+
+def box_schedule(box: Box) -> Schedule:
+    h = C.c_void_p()
+    blocks = box.node_block_begin.size - 1
+    _call(library().gbl_build_schedule, box.node_count, box.bond_count, box.matter.bond_a, box.matter.bond_b,
+          _ptr(box.node_block_begin, C.c_uint32), blocks, C.byref(h))
+    return Schedule(h)
+
+
+def box_state(box: Box, schedule: Schedule, origin=(0.0, 0.0, 0.0)) -> State:
+    o = np.asarray(origin, dtype=np.float64)
+    h = C.c_void_p()
+    _call(library().gbl_build_state, C.byref(box.matter), schedule._h, _ptr(o, C.c_double), C.byref(h))
+    return State(h)
 
 
 def step_settings(packed: np.ndarray) -> StepSettings:
@@ -628,7 +695,6 @@ class Server:
         _call(library().gbl_serve_create, 1 if precision == "double" else 0, C.byref(settings), int(budget_bytes),
               C.byref(h))
         self._h = h
-        self._held = {}  # ticket -> (schedule, state): the views stay valid until admission
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -639,7 +705,6 @@ class Server:
         t = C.c_uint64()
         _call(library().gbl_serve_submit, self._h, C.byref(schedule.view), C.byref(state.view), C.byref(sphere),
               int(substeps), C.byref(t))
-        self._held[t.value] = (schedule, state)
         return int(t.value)
 
     def step(self, substeps: int) -> ServerStats:
@@ -650,20 +715,18 @@ class Server:
     def poll(self, ticket: int) -> RequestInfo:
         info = RequestInfo()
         _call(library().gbl_serve_poll, self._h, int(ticket), C.byref(info))
-        if info.phase != REQUEST_QUEUED:
-            self._held.pop(ticket, None)
         return info
 
-    def take(self, ticket: int, state: State) -> tuple:
+    def take(self, ticket: int, state: State | None) -> tuple:
+        """The result into `state` (None: the state is dropped), with the sphere and RunStatus."""
         sp = Sphere()
         st = RunStatus()
-        _call(library().gbl_serve_take, self._h, int(ticket), C.byref(state.view), C.byref(sp), C.byref(st))
-        self._held.pop(ticket, None)
+        _call(library().gbl_serve_take, self._h, int(ticket), C.byref(state.view) if state is not None else None,
+              C.byref(sp), C.byref(st))
         return sp, st
 
     def cancel(self, ticket: int) -> None:
         _call(library().gbl_serve_cancel, self._h, int(ticket))
-        self._held.pop(ticket, None)
 
     def stats(self) -> ServerStats:
         st = ServerStats()

@@ -149,6 +149,171 @@ def cpu_baseline(case: dict, threads: int, substeps: int = 3) -> dict:
                       f"(restart) substep excluded; {float(np.sum(secs)):.2f} s timed"}
 
 
+# ---------------------------------------------------------------------------
+# Batched and served trials: drop trials of uneven sizes (edges uniform on
+# 8..48 per axis, compliance log-uniform 1e-8..1e-5, break strain uniform
+# 1e-3..5e-3, drop height uniform 0.1..1 m onto a ground plane; the seeded
+# draws of banjo_gb300.scenes.trial_parameters), built by the library's box
+# builder on host threads.
+# ---------------------------------------------------------------------------
+TRIAL_SPACING = 0.01
+
+
+def trial_specs(count: int, seed: int = 3) -> list:
+    from banjo_gb300 import scenes
+
+    edges, comp, strain, height = scenes.trial_parameters(count=count, seed=seed)
+    return [(int(e[0]), int(e[1]), int(e[2]), float(c), float(s), float(h))
+            for e, c, s, h in zip(edges, comp, strain, height)]
+
+
+def build_trial(lattice, spec):
+    nx, ny, nz, comp, strain, height = spec
+    inf = float("inf")
+    lift = height + 0.5 * ny * TRIAL_SPACING
+    box = lattice.build_box(nx, ny, nz, TRIAL_SPACING, center=(0.0, lift, 0.0), compliance=comp,
+                            threshold=(strain, strain, inf, inf, inf, inf))
+    sched = lattice.box_schedule(box)
+    return sched, lattice.box_state(box, sched)
+
+
+def trial_settings(lattice):
+    from banjo_gb300 import scenes
+
+    return lattice.step_settings(scenes.settings(planes=[scenes.plane((0.0, 0.0, 0.0),
+                                                                      node_radius=0.5 * TRIAL_SPACING)]))
+
+
+def host_threads() -> int:
+    return max(1, min(32, os.cpu_count() or 1))
+
+
+def batched_leg(args, lattice) -> dict:
+    """Config-3 trials in one batch against the same trials run one lattice at
+    a time through the single-lattice backend ("plain")."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    specs = trial_specs(args.trials)
+    settings = trial_settings(lattice)
+    batch = lattice.Batch()
+    t0 = time.perf_counter()
+
+    def add(spec):
+        sched, state = build_trial(lattice, spec)
+        batch.add(sched, state, lattice.Sphere())  # prepared on this thread, placed under the batch's lock
+        return state.node_count, state.bond_count
+
+    with ThreadPoolExecutor(host_threads()) as ex:
+        sizes = list(ex.map(add, specs))
+    build_s = time.perf_counter() - t0
+    batch.settle(settings)
+    nodes = sum(n for n, _ in sizes)
+    bonds = sum(b for _, b in sizes)
+    w, k = args.warmup * SUBSTEPS_PER_STEP, args.steps * SUBSTEPS_PER_STEP
+    batch.run(lattice.RunControl(max_steps=w))
+    before = [batch.status(i) for i in range(len(specs))]
+    batch.run(lattice.RunControl(max_steps=k))
+    after = [batch.status(i) for i in range(len(specs))]
+    device_s = after[0].kernel_seconds - before[0].kernel_seconds
+    live = sum(b - a.broken_bonds for (_, b), a in zip(sizes, after))
+    value = ITERATIONS * live * k / device_s
+    launches = batch.kernels_per_substep()
+    del batch
+
+    # Plain: the first trials of the same draw, one backend at a time.
+    plain_n = min(args.plain_trials, len(specs))
+    plain_proj, plain_s = 0.0, 0.0
+    for spec in specs[:plain_n]:
+        sched, state = build_trial(lattice, spec)
+        be = lattice.make_gb300_lattice_backend(sched)
+        be.upload(state, settings, lattice.Sphere())
+        be.run(lattice.RunControl(max_steps=w))
+        st0 = be.status()
+        st1 = be.run(lattice.RunControl(max_steps=k))
+        plain_s += st1.kernel_seconds - st0.kernel_seconds
+        plain_proj += ITERATIONS * (state.bond_count - st1.broken_bonds) * k
+    plain = plain_proj / plain_s
+    return {"value": value, "unit": "projections/s", "trials": len(specs), "nodes": nodes, "bonds": bonds,
+            "ms_per_step": device_s / args.steps * 1e3, "gpu_launches_per_substep": launches,
+            "host_build_s": build_s, "host_threads": host_threads(),
+            "plain": {"value": plain, "unit": "projections/s", "trials": plain_n,
+                      "note": "the first trials of the same draw, each alone through the single-lattice backend "
+                              "(its own captured substep graph), device time summed"},
+            "speedup_vs_plain": value / plain,
+            "workload": f"{len(specs)} drop trials, edges 8..48 per axis (seeded), one batch; step = "
+                        f"{SUBSTEPS_PER_STEP} substeps, I={ITERATIONS}; device time of {args.steps} steps"}
+
+
+def served_leg(args, lattice) -> dict:
+    """Config-4 requests: Poisson arrivals, 90% config-3 trials and 10% 128^3
+    lattices, admitted against a device memory budget, stepped together."""
+    import threading
+
+    rng = np.random.default_rng(11)
+    small = trial_specs(args.served_pool)
+    large_specs = [(128, 128, 128, s[3], s[4], s[5]) for s in trial_specs(2, seed=5)]
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(host_threads()) as ex:
+        pool_small = list(ex.map(lambda sp: build_trial(lattice, sp), small))
+        pool_large = list(ex.map(lambda sp: build_trial(lattice, sp), large_specs))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.served_rate, size=int(args.served_rate * args.served_window * 3)))
+    arrivals = arrivals[arrivals < args.served_window]
+    kinds = rng.random(arrivals.size) < 0.1
+    picks = [(pool_large[int(rng.integers(len(pool_large)))] if big else pool_small[int(rng.integers(len(pool_small)))])
+             for big in kinds]
+    horizon = args.served_substeps
+    server = lattice.Server(trial_settings(lattice), int(args.served_budget_gb * (1 << 30)))
+    sphere = lattice.Sphere()
+    tickets = [None] * arrivals.size
+    start = time.perf_counter()
+
+    def produce():
+        for i, t in enumerate(arrivals):
+            delay = start + float(t) - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            sched, state = picks[i]
+            tickets[i] = server.submit(sched, state, sphere, horizon)
+
+    producer = threading.Thread(target=produce)
+    producer.start()
+    done, latency, wait, proj = set(), {}, {}, 0.0
+    sizes = {}
+    while len(done) < arrivals.size:
+        st = server.step(args.served_chunk)
+        if st.running == 0 and st.queued == 0:
+            time.sleep(0.0005)  # nothing admitted yet: wait for the next arrival
+        for i, t in enumerate(tickets):
+            if t is None or i in done:
+                continue
+            info = server.poll(t)
+            if info.phase == lattice.REQUEST_DONE:
+                _, st = server.take(t, None)
+                finished = time.perf_counter() - start
+                latency[i] = finished - float(arrivals[i])
+                wait[i] = info.admitted_s - info.submitted_s
+                b = picks[i][1].bond_count
+                proj += ITERATIONS * (b - st.broken_bonds) * horizon
+                done.add(i)
+        if not producer.is_alive() and all(t is not None for t in tickets) and len(done) == arrivals.size:
+            break
+    producer.join()
+    wall = time.perf_counter() - start
+    stats = server.stats()
+    lat = np.array([latency[i] for i in range(arrivals.size)])
+    wq = np.array([wait[i] for i in range(arrivals.size)])
+    return {"value": proj / wall, "unit": "projections/s", "requests": int(arrivals.size),
+            "large_requests": int(kinds.sum()), "substeps_per_request": horizon,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "p50_admission_wait_s": float(np.percentile(wq, 50)), "p99_admission_wait_s": float(np.percentile(wq, 99)),
+            "wall_s": wall, "device_s": stats.device_seconds, "budget_gb": args.served_budget_gb,
+            "chunk_substeps": args.served_chunk,
+            "workload": f"Poisson arrivals at {args.served_rate:g}/s for {args.served_window:g} s; 90% drawn from "
+                        f"{len(pool_small)} config-3 trials, 10% 128^3 lattices; {horizon} substeps each (a bounded "
+                        f"horizon: the full 2400 would hold the GPU for hours at this arrival rate); latency = "
+                        "finish - scheduled arrival, wall clock"}
+
+
 def distributed():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -287,6 +452,11 @@ def run_gb300(args) -> None:
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, os.cpu_count() or 1)
+    del backend, e2e_backend, state, e2e_state, case
+    if args.trials > 0:
+        line["batched"] = batched_leg(args, lattice)
+    if args.served_window > 0:
+        line["served"] = served_leg(args, lattice)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -343,6 +513,14 @@ def main() -> None:
     p.add_argument("--workload", default="impact", choices=["impact", "impact_mid", "cantilever"])
     p.add_argument("--profile-substeps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--trials", type=int, default=4096, help="batched leg: trials in one batch (0: skip)")
+    p.add_argument("--plain-trials", type=int, default=64, help="batched leg: trials timed one at a time")
+    p.add_argument("--served-window", type=float, default=0.25, help="served leg: seconds of arrivals (0: skip)")
+    p.add_argument("--served-rate", type=float, default=2000.0)
+    p.add_argument("--served-substeps", type=int, default=40)
+    p.add_argument("--served-chunk", type=int, default=10)
+    p.add_argument("--served-pool", type=int, default=256)
+    p.add_argument("--served-budget-gb", type=float, default=80.0)
     args = p.parse_args()
     if args.warmup < 3:
         raise SystemExit("warm-up must be at least 3 steps")

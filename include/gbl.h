@@ -324,10 +324,11 @@ gbl_result gbl_batch_set_stream(gbl_batch *batch, void *cuda_stream);
  * once, freeing their memory for the next in line (admission is re-checked in
  * the same call). Every request's result is the one it gets alone.
  *
- * The schedule and state views given to gbl_serve_submit must stay valid
- * until the request is admitted (phase RUNNING) or cancelled; the result is
- * kept by the server until gbl_serve_take. Times are seconds on the server's
- * steady clock since its creation, -1 before the event. */
+ * gbl_serve_submit prepares the request's device image from the views on the
+ * calling thread, outside the server's lock (so submissions from other threads
+ * overlap a running gbl_serve_step); the views may be freed when it returns.
+ * The result is kept by the server until gbl_serve_take. Times are seconds on
+ * the server's steady clock since its creation, -1 before the event. */
 typedef struct gbl_server gbl_server;
 enum { GBL_REQUEST_QUEUED = 0, GBL_REQUEST_RUNNING = 1, GBL_REQUEST_DONE = 2 };
 typedef struct gbl_request_info {
@@ -431,6 +432,32 @@ gbl_result gbl_state_view_of(gbl_state *state, gbl_state_view *view);
 /* Sets inv_mass of the flagged nodes to 0 (a pinned node keeps its mass). */
 gbl_result gbl_state_pin(gbl_state *state, const uint8_t *pinned);
 void gbl_state_free(gbl_state *state);
+
+/* A box lattice, the input generator of the reference's box scenes
+ * (generateBoxTileLattice, src/matter/BoxLattice.cpp:49-173, and
+ * boxLatticeSlabs :175-195), restated for uniform bonds: cell-centre nodes of
+ * one mass, node index x + nx*(y + ny*z), bonds (node, neighbour) for every
+ * integer offset of the positive half-space in the generator's walk order,
+ * rest length spacing*|offset|, one compliance and one threshold record for
+ * every bond. Feed its matter view to gbl_build_schedule/gbl_build_state. */
+typedef struct gbl_box_spec {
+    uint32_t nx, ny, nz;
+    uint32_t horizon;       /* offsets within `horizon` cells on each axis (0 means 1) */
+    uint32_t max_offset_sq; /* 0: the generator's rule |o| <= horizon; else |o|^2 <= max_offset_sq */
+    uint32_t slabs;         /* z-slabs requested */
+    double spacing;
+    double center[3];
+    double node_mass;
+    double compliance;
+    double threshold[6];    /* ds, de, cs, ce, ss, se */
+} gbl_box_spec;
+typedef struct gbl_box gbl_box;
+gbl_result gbl_build_box(const gbl_box_spec *spec, gbl_box **out);
+/* Views into the box (valid until gbl_box_free): its matter, and its
+ * block_count + 1 slab node offsets. */
+gbl_result gbl_box_view_of(const gbl_box *box, gbl_matter_view *matter, const uint32_t **node_block_begin,
+                           uint32_t *block_count);
+void gbl_box_free(gbl_box *box);
 
 #ifdef __cplusplus
 }
