@@ -1036,7 +1036,7 @@ private:
             levels_.push_back(span([d](const Res &l, U &b, U &e) {
                 b = d < l.levels.size() ? l.levels[d].begin : 0;
                 e = d < l.levels.size() ? l.levels[d].end : 0;
-            }, kThreads));
+            }, kThreads * kSolvePer));
         if (all.size() > work_cap_) {
             if (work_) cudaFree(work_);
             work_cap_ = std::max<std::size_t>(all.size(), 2 * work_cap_);

@@ -742,70 +742,96 @@ __device__ __forceinline__ bool supportProject(const Dev<R> &L, const Settings<R
     return projected;
 }
 
+// Bonds per thread of the sweep: a thread issues the record loads of all its
+// bonds, then all their gathers, then solves them, so each thread keeps
+// several independent memory chains in flight. A level's bonds share no node,
+// so the order among them is free.
+constexpr int kSolvePer = 2;
+
 template <class R, bool Many, bool Direct, bool First, bool Last, bool Plastic, bool Support>
-__global__ void __launch_bounds__(kThreads) kSolve(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kThreads, 4) kSolve(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
+    BondRec<R> rec[kSolvePer];
+    std::uint32_t at[kSolvePer];
+#pragma unroll
+    for (int k = 0; k < kSolvePer; ++k) {
+        at[k] = w.begin + threadIdx.x + static_cast<std::uint32_t>(k) * kThreads;
+        if (at[k] < w.end) rec[k] = ldStream(L.rec + at[k]);
+    }
+    // The records are on their way before the stop flag is read.
     if (L.ctl->stop) return;
-    const std::uint32_t d = w.begin + threadIdx.x;
-    if (d >= w.end) return;
-    const BondRec<R> rec = ldStream(L.rec + d);
-    const std::uint32_t a = endA(rec), b = endB(rec);
-    Q4<R> qa, qb;
-    bool have = false, write_a = false, write_b = false;
-    if (!(rec.a & kDeadBit)) {
-        const Q4<R> g = ldStream(L.geo + d);
-        qa = ldShared(L.u + a);
-        qb = ldShared(L.u + b);
-        have = true;
-        const V3<R> ua = xyz(qa), ub = xyz(qb), edge{g.x, g.y, g.z};
-        const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
-        const R cl = length(delta);
-        if (cl > R(1.0e-12)) {
-            const R original = rec.rest;
-            const R plastic = Plastic ? L.plastic[d].x : R(0);
-            const R rest = Plastic ? original + plastic : original;
-            R constraint;
-            if (Direct) {
-                constraint = cl - rest;
-            } else {
-                const V3<R> du = ub - ua;
-                const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
-                constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
-            }
-            const V3<R> dir = delta / cl;
-            const R wa = qa.w, wb = qb.w;
-            const R alpha = g.w / (S.dt * S.dt);
-            const R lambda = First ? R(0) : __ldcs(L.lambda + d);
-            const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
-            if (!Last) __stcs(L.lambda + d, lambda + dl);
-            const V3<R> na = ua - (wa * dl) * dir;
-            const V3<R> nb = ub + (wb * dl) * dir;
-            qa = Q4<R>{na.x, na.y, na.z, wa};
-            qb = Q4<R>{nb.x, nb.y, nb.z, wb};
-            write_a = write_b = true;
+    Q4<R> geo[kSolvePer], qa[kSolvePer], qb[kSolvePer];
+    R lam[kSolvePer], pl[kSolvePer];
+    bool live[kSolvePer];
+#pragma unroll
+    for (int k = 0; k < kSolvePer; ++k) {
+        live[k] = at[k] < w.end && !(rec[k].a & kDeadBit);
+        if (live[k]) {
+            geo[k] = ldStream(L.geo + at[k]);
+            qa[k] = ldShared(L.u + endA(rec[k]));
+            qb[k] = ldShared(L.u + endB(rec[k]));
+            lam[k] = First ? R(0) : __ldcs(L.lambda + at[k]);
+            pl[k] = Plastic ? L.plastic[at[k]].x : R(0);
         }
     }
-    if (Support) {
-        if (rec.a & kLastABit) {
-            if (!have) qa = L.u[a];
-            V3<R> u = xyz(qa);
-            if (supportProject(L, S, a, u)) {
-                qa = Q4<R>{u.x, u.y, u.z, qa.w};
-                write_a = true;
+#pragma unroll
+    for (int k = 0; k < kSolvePer; ++k) {
+        if (at[k] >= w.end) continue;
+        const std::uint32_t d = at[k];
+        const std::uint32_t a = endA(rec[k]), b = endB(rec[k]);
+        bool write_a = false, write_b = false;
+        if (live[k]) {
+            const Q4<R> g = geo[k];
+            const V3<R> ua = xyz(qa[k]), ub = xyz(qb[k]), edge{g.x, g.y, g.z};
+            const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
+            const R cl = length(delta);
+            if (cl > R(1.0e-12)) {
+                const R original = rec[k].rest;
+                const R plastic = pl[k];
+                const R rest = Plastic ? original + plastic : original;
+                R constraint;
+                if (Direct) {
+                    constraint = cl - rest;
+                } else {
+                    const V3<R> du = ub - ua;
+                    const R num = rec[k].rsm + R(2) * dot(edge, du) + dot(du, du);
+                    constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
+                }
+                const V3<R> dir = delta / cl;
+                const R wa = qa[k].w, wb = qb[k].w;
+                const R alpha = g.w / (S.dt * S.dt);
+                const R lambda = lam[k];
+                const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
+                if (!Last) __stcs(L.lambda + d, lambda + dl);
+                const V3<R> na = ua - (wa * dl) * dir;
+                const V3<R> nb = ub + (wb * dl) * dir;
+                qa[k] = Q4<R>{na.x, na.y, na.z, wa};
+                qb[k] = Q4<R>{nb.x, nb.y, nb.z, wb};
+                write_a = write_b = true;
             }
         }
-        if (rec.b & kLastBBit) {
-            if (!have) qb = L.u[b];
-            V3<R> u = xyz(qb);
-            if (supportProject(L, S, b, u)) {
-                qb = Q4<R>{u.x, u.y, u.z, qb.w};
-                write_b = true;
+        if (Support) {
+            if (rec[k].a & kLastABit) {
+                if (!live[k]) qa[k] = L.u[a];
+                V3<R> u = xyz(qa[k]);
+                if (supportProject(L, S, a, u)) {
+                    qa[k] = Q4<R>{u.x, u.y, u.z, qa[k].w};
+                    write_a = true;
+                }
+            }
+            if (rec[k].b & kLastBBit) {
+                if (!live[k]) qb[k] = L.u[b];
+                V3<R> u = xyz(qb[k]);
+                if (supportProject(L, S, b, u)) {
+                    qb[k] = Q4<R>{u.x, u.y, u.z, qb[k].w};
+                    write_b = true;
+                }
             }
         }
+        if (write_a) L.u[a] = qa[k];
+        if (write_b) L.u[b] = qb[k];
     }
-    if (write_a) L.u[a] = qa;
-    if (write_b) L.u[b] = qb;
 }
 
 // Radial pair damping of one level (LatticePhysics.hpp:1170-1184).
@@ -814,23 +840,24 @@ __global__ void __launch_bounds__(kThreads) kDamp(const Grid<R> launch, R fracti
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
-    const std::uint32_t d = w.begin + threadIdx.x;
-    if (d >= w.end) return;
-    const BondRec<R> rec = L.rec[d];
-    if (rec.a & kDeadBit) return;
-    const std::uint32_t a = endA(rec), b = endB(rec);
-    const Q4<R> va = L.v[a], vb = L.v[b];
-    const R ma = va.w, mb = vb.w;
-    if (ma <= R(0) || mb <= R(0)) return;
-    const Q4<R> g = L.geo[d];
-    const V3<R> n = normalized(bondVector<R, Direct>(L, a, b, V3<R>{g.x, g.y, g.z}));
-    const R rel = dot(xyz(vb) - xyz(va), n);
-    const R im = R(1) / ma + R(1) / mb;
-    const R impulse = -fraction * rel / im;
-    const V3<R> na = xyz(va) - (impulse / ma) * n;
-    const V3<R> nb = xyz(vb) + (impulse / mb) * n;
-    L.v[a] = Q4<R>{na.x, na.y, na.z, ma};
-    L.v[b] = Q4<R>{nb.x, nb.y, nb.z, mb};
+    // Items are sweep levels' ranges: any length, strided over the CTA.
+    for (std::uint32_t d = w.begin + threadIdx.x; d < w.end; d += blockDim.x) {
+        const BondRec<R> rec = L.rec[d];
+        if (rec.a & kDeadBit) continue;
+        const std::uint32_t a = endA(rec), b = endB(rec);
+        const Q4<R> va = L.v[a], vb = L.v[b];
+        const R ma = va.w, mb = vb.w;
+        if (ma <= R(0) || mb <= R(0)) continue;
+        const Q4<R> g = L.geo[d];
+        const V3<R> n = normalized(bondVector<R, Direct>(L, a, b, V3<R>{g.x, g.y, g.z}));
+        const R rel = dot(xyz(vb) - xyz(va), n);
+        const R im = R(1) / ma + R(1) / mb;
+        const R impulse = -fraction * rel / im;
+        const V3<R> na = xyz(va) - (impulse / ma) * n;
+        const V3<R> nb = xyz(vb) + (impulse / mb) * n;
+        L.v[a] = Q4<R>{na.x, na.y, na.z, ma};
+        L.v[b] = Q4<R>{nb.x, nb.y, nb.z, mb};
+    }
 }
 
 // Support projection of the nodes that have no bond to carry it (isolated

@@ -267,13 +267,21 @@ def served_leg(args, lattice) -> dict:
     tickets = [None] * arrivals.size
     start = time.perf_counter()
 
+    # Clients submit from a pool of host threads (submission prepares the
+    # request's device image on the submitting thread), each at its arrival.
+    clients = ThreadPoolExecutor(max(1, host_threads() - 2))
+
+    def submit(i):
+        sched, state = picks[i]
+        tickets[i] = server.submit(sched, state, sphere, horizon)
+
     def produce():
         for i, t in enumerate(arrivals):
             delay = start + float(t) - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
-            sched, state = picks[i]
-            tickets[i] = server.submit(sched, state, sphere, horizon)
+            clients.submit(submit, i)
+        clients.shutdown(wait=True)
 
     producer = threading.Thread(target=produce)
     producer.start()
