@@ -1128,14 +1128,39 @@ private:
         check(cudaGetLastError(), "kernel launch");
     }
 
+    // A launch that may start while the previous kernel of the stream still
+    // runs (programmatic dependent launch); the kernel waits for it itself.
+    // Only between sweep levels of two or more levels per iteration: a level
+    // reads the multipliers its own range wrote one iteration earlier, which
+    // must be complete -- with a single level that writer would be the very
+    // kernel it overlaps.
+    template <class... P, class... A>
+    void launchOverlapped(void (*kernel)(P...), unsigned blocks, unsigned threads, A &&...args) {
+        if (levels_.size() < 2) {
+            kernel<<<blocks, threads, 0, stream_>>>(std::forward<A>(args)...);
+            return;
+        }
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = stream_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        check(cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...), "kernel launch");
+    }
+
     template <bool M> void launchSolve(const Span &lv, bool first, bool last) {
         if (!lv.count) return;
         const bool support = S_.plane_count != 0;
         const int key = (first ? 8 : 0) | (last ? 4 : 0) | (plastic_ ? 2 : 0) | (support ? 1 : 0);
 #define GBL_SOLVE(K)                                                                                                \
     case K:                                                                                                         \
-        kSolve<R, M, kDirect, ((K) & 8) != 0, ((K) & 4) != 0, ((K) & 2) != 0, ((K) & 1) != 0>                       \
-            <<<lv.count, kThreads, 0, stream_>>>(grid(lv), S_);                                                     \
+        launchOverlapped(kSolve<R, M, kDirect, ((K) & 8) != 0, ((K) & 4) != 0, ((K) & 2) != 0, ((K) & 1) != 0>,     \
+                         lv.count, kThreads, grid(lv), S_);                                                         \
         break;
         switch (key) {
             GBL_SOLVE(0) GBL_SOLVE(1) GBL_SOLVE(2) GBL_SOLVE(3) GBL_SOLVE(4) GBL_SOLVE(5) GBL_SOLVE(6) GBL_SOLVE(7)

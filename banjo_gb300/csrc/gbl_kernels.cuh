@@ -748,31 +748,46 @@ __device__ __forceinline__ bool supportProject(const Dev<R> &L, const Settings<R
 // so the order among them is free.
 constexpr int kSolvePer = 2;
 
+// Programmatic dependent launch (sm_90+): a sweep level is launched while the
+// previous one still runs; its CTAs load what no earlier kernel of the substep
+// writes (records, geometry, multipliers, plastic extension, the stop flag),
+// then wait for the previous grid to finish and its writes to be visible
+// before they touch the nodes. A level lets the next one launch only after its
+// own wait, so at most two levels overlap and everything before the previous
+// level is complete when a level starts.
+__device__ __forceinline__ void waitPreviousGrid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allowNextGrid() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <class R, bool Many, bool Direct, bool First, bool Last, bool Plastic, bool Support>
 __global__ void __launch_bounds__(kThreads, 4) kSolve(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     BondRec<R> rec[kSolvePer];
+    Q4<R> geo[kSolvePer], qa[kSolvePer], qb[kSolvePer];
+    R lam[kSolvePer], pl[kSolvePer];
     std::uint32_t at[kSolvePer];
+    // Everything that no kernel since the last end sample has written.
 #pragma unroll
     for (int k = 0; k < kSolvePer; ++k) {
         at[k] = w.begin + threadIdx.x + static_cast<std::uint32_t>(k) * kThreads;
-        if (at[k] < w.end) rec[k] = ldStream(L.rec + at[k]);
+        if (at[k] < w.end) {
+            rec[k] = ldStream(L.rec + at[k]);
+            geo[k] = ldStream(L.geo + at[k]);
+            lam[k] = First ? R(0) : __ldcs(L.lambda + at[k]);
+            pl[k] = Plastic ? L.plastic[at[k]].x : R(0);
+        }
     }
-    // The records are on their way before the stop flag is read.
-    if (L.ctl->stop) return;
-    Q4<R> geo[kSolvePer], qa[kSolvePer], qb[kSolvePer];
-    R lam[kSolvePer], pl[kSolvePer];
+    const unsigned stop = L.ctl->stop;
+    waitPreviousGrid();
+    allowNextGrid();
+    if (stop) return;
     bool live[kSolvePer];
 #pragma unroll
     for (int k = 0; k < kSolvePer; ++k) {
         live[k] = at[k] < w.end && !(rec[k].a & kDeadBit);
         if (live[k]) {
-            geo[k] = ldStream(L.geo + at[k]);
             qa[k] = ldShared(L.u + endA(rec[k]));
             qb[k] = ldShared(L.u + endB(rec[k]));
-            lam[k] = First ? R(0) : __ldcs(L.lambda + at[k]);
-            pl[k] = Plastic ? L.plastic[at[k]].x : R(0);
         }
     }
 #pragma unroll
