@@ -307,3 +307,131 @@ def trial_parameters(count=4096, seed=3, edge_lo=8, edge_hi=48):
     strain = 1e-3 + 4e-3 * u[:, 4]
     height = 0.1 + 0.9 * u[:, 5]
     return edges, compliance, strain, height
+
+
+# ---------------------------------------------------------------------------
+# The notched bar: an energy-scaled brittle material with plastic flow.
+# ---------------------------------------------------------------------------
+# Material constants of the bar: density (kg/m^3), Young's modulus (Pa),
+# Poisson ratio, tensile strength (Pa), yield strength (Pa), hardening ratio,
+# fracture energy (J/m^2).
+BAR_MATERIAL = (2500.0, 70.0e9, 0.22, 45.0e6, 36.0e6, 0.0, 8.0)
+
+
+def compile_energy_scaled(material=BAR_MATERIAL, cell=0.01, horizon=2) -> dict:
+    """The reference's material compile for the energy-scaled law with plastic
+    flow, in FP64: withPlasticFlow(withEnergyScaledFailure(
+    compileElasticLatticeReference(m, cell, horizon), m, cell, horizon), m)
+    (src/material/MaterialCompiler.cpp:44-66, 68-108, 110-125, 127-214), with
+    the default solver calibration (damage x1, break x2; src/material/Material.hpp:30-35)
+    and no declared compressive or shear strength (disabled ramps)."""
+    density, young, _nu, tensile, yield_, hardening, gc = material
+    damage_mult, break_mult = 1.0, 2.0
+    compliance = 1.0 / (young * (cell * cell) / (cell * float(horizon)))
+
+    def failure_strain(strain, mult, minimum=1.0e-5):
+        return INF if strain <= 0.0 else max(minimum, strain * mult)
+
+    tensile_strain = tensile / young
+    start = failure_strain(tensile_strain, damage_mult)
+    strength_end = max(start * 1.01, failure_strain(tensile_strain, break_mult))
+    crossings = 0.0
+    for dz in range(-horizon, horizon + 1):
+        for dy in range(-horizon, horizon + 1):
+            for dx in range(-horizon, horizon + 1):
+                if not (dz > 0 or (dz == 0 and dy > 0) or (dz == 0 and dy == 0 and dx > 0)):
+                    continue
+                if math.sqrt(float(dx * dx + dy * dy + dz * dz)) > float(horizon) + 1.0e-9:
+                    continue
+                crossings += abs(float(dx))
+    energy = math.sqrt(2.0 * float(horizon) * gc / (crossings * young * cell))
+    bounded = max(1.0e-5, min(energy, strength_end))
+    fraction = min(max(damage_mult / break_mult, 0.0), 1.0)
+    ds = max(1.0e-5, bounded * fraction)
+    de = max(ds * 1.01, bounded)
+    return {"bond_compliance": compliance, "damage_start": ds, "damage_end": de, "energy_scaled_stretch": energy,
+            "strength_bound_active": strength_end < energy,
+            "yield_stretch": yield_ / young if yield_ > 0.0 else 0.0,
+            "hardening": hardening if yield_ > 0.0 else 0.0, "density": density}
+
+
+def notched_bar(nx=128, ny=32, nz=32, h=0.01, horizon=2, material=BAR_MATERIAL, ramp_steps=10000, load_factor=2.0,
+                steps=10000, substeps=10, blocks=1, notch=True):
+    """A bar along x with a one-cell-wide slot at mid-length through the lower
+    half of its depth (cells x = nx/2, y < ny/2, every z, removed before
+    bonding). Bonds follow the box generator's horizon walk
+    (src/matter/BoxLattice.cpp:117-155) between the cells present, node
+    indices in x + nx*(y + ny*z) order with the slot cells skipped; per-bond
+    compliance is bond_compliance / horizon weight, weight 1/max(1, |o|^2)
+    (:139-142); thresholds are the compiled ones (strength variation 0); node
+    mass is density * h^3. The x = 0 face is pinned; the x = nx-1 face carries
+    tension along +x, ramped linearly from 0 to load_factor x (tensile
+    strength x cross-section) over ramp_steps rigid steps, the load re-set
+    every step for that step's substeps. No gravity.
+    """
+    comp = compile_energy_scaled(material, h, horizon)
+    n_all = nx * ny * nz
+    idx = np.arange(n_all, dtype=np.int64)
+    gx, gy, gz = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    keep = np.ones(n_all, dtype=bool)
+    if notch:
+        keep &= ~((gx == nx // 2) & (gy < ny // 2))
+    new_index = np.full(n_all, -1, dtype=np.int64)
+    new_index[keep] = np.arange(int(keep.sum()))
+    n = int(keep.sum())
+    offs = half_offsets(horizon, None)
+    a_list, b_list, comp_list = [], [], []
+    other = np.full((n_all, len(offs)), -1, dtype=np.int64)
+    for k, (dx, dy, dz, _) in enumerate(offs):
+        ox, oy, oz = gx + dx, gy + dy, gz + dz
+        inside = (ox >= 0) & (oy >= 0) & (oz >= 0) & (ox < nx) & (oy < ny) & (oz < nz)
+        o = np.where(inside, ox + nx * (oy + ny * oz), 0)
+        ok = inside & keep & keep[o]
+        other[ok, k] = new_index[o[ok]]
+    mask = other >= 0
+    src = np.nonzero(mask)
+    a = new_index[src[0]].astype(np.uint32)
+    b = other[mask].astype(np.uint32)
+    d2 = np.asarray([o[3] for o in offs], dtype=np.float64)[src[1]]
+    dist = np.sqrt(d2)
+    rest = dist * h
+    weight = 1.0 / np.maximum(1.0, dist * dist)
+    compliance = comp["bond_compliance"] / weight
+    nb = a.size
+    thr = np.empty((nb, 6), dtype=np.float64)
+    thr[:, 0], thr[:, 1] = comp["damage_start"], comp["damage_end"]
+    thr[:, 2:] = INF
+    ref = box_nodes(nx, ny, nz, h).reshape(-1, 3)[keep].reshape(-1)
+    mass = comp["density"] * (h * h * h)
+    kx = gx[keep]
+    pinned = (kx == 0).astype(np.uint8)
+    loaded = kx == nx - 1
+    forces = np.zeros((n, 3), dtype=np.float64)
+    forces[loaded, 0] = material[3] * (ny * h) * (nz * h) / float(loaded.sum())
+    layer = nx * ny
+    slab_begin = [int(keep[: (nz * k // blocks) * layer].sum()) for k in range(blocks + 1)]
+    slab_begin[-1] = n
+    s = settings(gravity=(0.0, 0.0, 0.0), yield_stretch=comp["yield_stretch"], hardening=comp["hardening"])
+    return {
+        "node_count": np.array([n], dtype=np.uint32),
+        "bond_count": np.array([nb], dtype=np.uint32),
+        "ref_pos": ref,
+        "pos": ref.copy(),
+        "vel": np.zeros(3 * n, dtype=np.float64),
+        "mass": np.full(n, mass, dtype=np.float64),
+        "bond_a": a,
+        "bond_b": b,
+        "rest_length": rest,
+        "compliance": compliance,
+        "threshold": thr.reshape(-1),
+        "node_block_begin": np.asarray(slab_begin, dtype=np.uint32),
+        "origin": np.zeros(3, dtype=np.float64),
+        "sphere": sphere(),
+        "pinned": pinned,
+        "forces": forces.reshape(-1),
+        "force_ramp_steps": np.array([ramp_steps], dtype=np.uint64),
+        "force_ramp_scale": np.array([load_factor], dtype=np.float64),
+        "settings": s,
+        "steps": np.array([steps * substeps], dtype=np.uint64),
+        "substeps_per_step": np.array([substeps], dtype=np.uint64),
+    }

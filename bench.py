@@ -322,6 +322,60 @@ def served_leg(args, lattice) -> dict:
                         "finish - scheduled arrival, wall clock"}
 
 
+def fp64_error(case: dict, gpu: dict, cpu64: dict) -> dict:
+    """FP32 device run against the FP64 CPU restatement on the same case:
+    position error over the lattice extent, ledger relative errors, and the
+    bonds whose broken state differs."""
+    ref = case["ref_pos"].reshape(-1, 3)
+    extent = float(np.max(ref.max(axis=0) - ref.min(axis=0)))
+    du = np.abs(gpu["u"].astype(np.float64) - cpu64["u"]).max()
+    rel = lambda a, b: abs(a - b) / max(abs(b), 1e-300)  # noqa: E731
+    return {"max_position_error_over_extent": float(du / extent),
+            "removed_energy_rel_error": rel(float(gpu["status_f64"][0]), float(cpu64["status_f64"][0])),
+            "plastic_work_rel_error": rel(float(gpu["status_f64"][2]), float(cpu64["status_f64"][2])),
+            "broken_bonds_fp32": int(gpu["status_u64"][4]), "broken_bonds_fp64": int(cpu64["status_u64"][4]),
+            "broken_state_differs": int(np.count_nonzero(gpu["alive"] != cpu64["alive"]))}
+
+
+def cascade_leg(args, lattice) -> dict:
+    """Config 5: the notched bar (energy-scaled law, plastic flow, horizon 2)
+    under its ramped end load on the device, and its error against the FP64
+    CPU restatement over the first steps."""
+    import oracle
+    from banjo_gb300 import scenes
+
+    case = scenes.notched_bar(steps=args.cascade_steps)
+    n, b = int(case["node_count"][0]), int(case["bond_count"][0])
+    sched = lattice.build_lattice_schedule(n, case["bond_a"], case["bond_b"], case["node_block_begin"])
+    state = lattice.build_lattice_state(case, sched)
+    be = lattice.make_gb300_lattice_backend(sched)
+    be.upload(state, lattice.step_settings(case["settings"]), lattice.Sphere())
+    base = case["forces"]
+    per = SUBSTEPS_PER_STEP
+    proj, device_s = 0.0, 0.0
+    for step in range(args.cascade_steps):
+        scale = float(case["force_ramp_scale"][0]) * step / float(case["force_ramp_steps"][0])
+        be.set_external_forces(scale * base, per)
+        before = be.status()
+        st = be.run(lattice.RunControl(max_steps=per))
+        device_s += st.kernel_seconds - before.kernel_seconds
+        proj += ITERATIONS * (b - st.broken_bonds) * per
+    out = {"value": proj / device_s, "unit": "projections/s", "nodes": n, "bonds": b,
+           "steps": args.cascade_steps, "broken_bonds": int(st.broken_bonds),
+           "removed_energy_j": st.removed_energy_j, "plastic_work_j": st.plastic_work_j,
+           "max_plastic_stretch": st.max_plastic_stretch,
+           "workload": f"notched bar 128x32x32 (slot at mid-length, lower half), horizon 2, energy-scaled law + "
+                       f"plastic flow compiled in FP64; end load ramped 0 -> 2x(45 MPa x 0.1024 m^2) over 10000 "
+                       f"steps, the first {args.cascade_steps} steps run; device time"}
+    if args.cascade_fp64_steps > 0:
+        short = scenes.notched_bar(steps=args.cascade_fp64_steps)
+        gpu = lattice.run_case(short)
+        cpu64 = oracle.run_port(short, precision="double", threads=os.cpu_count() or 1)
+        out["fp64_check"] = dict(fp64_error(short, gpu, cpu64), steps=args.cascade_fp64_steps,
+                                 note="device FP32 vs the CPU restatement in FP64 (direct arithmetic), same case")
+    return out
+
+
 def distributed():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -465,6 +519,8 @@ def run_gb300(args) -> None:
         line["batched"] = batched_leg(args, lattice)
     if args.served_window > 0:
         line["served"] = served_leg(args, lattice)
+    if args.cascade_steps > 0:
+        line["cascade"] = cascade_leg(args, lattice)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -529,6 +585,8 @@ def main() -> None:
     p.add_argument("--served-chunk", type=int, default=10)
     p.add_argument("--served-pool", type=int, default=256)
     p.add_argument("--served-budget-gb", type=float, default=80.0)
+    p.add_argument("--cascade-steps", type=int, default=200, help="notched-bar leg: ramp steps run (0: skip)")
+    p.add_argument("--cascade-fp64-steps", type=int, default=10, help="notched-bar leg: steps of the FP64 check")
     args = p.parse_args()
     if args.warmup < 3:
         raise SystemExit("warm-up must be at least 3 steps")

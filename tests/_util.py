@@ -25,7 +25,9 @@ STATUS_F64 = {"removed_energy_j": 0, "max_damage": 1, "plastic_work_j": 2, "max_
 
 
 def golden_names() -> list[str]:
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The lattice-run fixtures (material_*.npz hold material compiles)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("material_"))
 
 
 def load_golden(name: str):

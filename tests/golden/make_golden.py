@@ -49,12 +49,30 @@ def cases() -> dict:
                          footprints=((-0.04, 0.0, 0.02, 0.06), (0.04, 0.0, 0.02, 0.06)))
     damped["settings"] = scenes.settings(damping_fraction=0.05, planes=[ledge, ground])
     out["damped_ledge"] = (damped, "float")
+    # The notched bar (energy-scaled law, plastic flow, horizon 2, pinned end,
+    # ramped end load), small, through its first failure rounds.
+    out["bar_small"] = (scenes.notched_bar(24, 8, 8, ramp_steps=800, steps=20), "float")
+    out["bar_small_double"] = (scenes.notched_bar(16, 6, 6, ramp_steps=800, steps=6), "double")
     return out
+
+
+def material() -> None:
+    """The reference's own compile of the bar material (MaterialCompiler.cpp), for
+    the restatement in banjo_gb300.scenes.compile_energy_scaled."""
+    m = list(scenes.BAR_MATERIAL) + [0.01, 2.0]  # + cell, horizon
+    ref = oracle.run_reference({"material": np.asarray(m, dtype=np.float64)})
+    path = os.path.join(HERE, "material_bar.npz")
+    np.savez_compressed(path, material=np.asarray(m), compiled=ref["compiled"])
+    print("material_bar:", ref["compiled"])
 
 
 def main() -> None:
     oracle.build_reference()
+    material()
+    only = set(sys.argv[1:])
     for name, (case, precision) in cases().items():
+        if only and name not in only:
+            continue
         ref = oracle.run_reference(case, precision=precision, per_substep=True)
         data = {"case__" + k: np.asarray(v) for k, v in case.items()}
         for k, v in ref.items():
