@@ -231,6 +231,7 @@ template <class R> struct Resident {
         a.reserve(d.thr2, B); a.reserve(d.plastic, B); a.reserve(d.mode, B);
         a.reserve(d.dev2sched, B); a.reserve(d.isolated, isolated + 1);
         a.reserve(d.node_block_begin, blocks + 1);
+        a.reserve(d.level_begin, kMaxFusedLevels + 1);
         a.reserve(d.sphere, 1);
         a.reserve(d.dirty, N + 4);
         const std::size_t filled = a.bytes();
@@ -341,6 +342,10 @@ template <class R> struct Resident {
         if (!isolated.empty()) std::memcpy(d.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size());
         d.isolated_count = static_cast<std::uint32_t>(isolated.size());
         std::memcpy(d.node_block_begin, sched.node_block_begin.data(), sizeof(std::uint32_t) * (sched.block_count + 1));
+        // Level boundaries for the one-CTA sweep, when the levels fit its table.
+        d.level_count = levels.size() <= kMaxFusedLevels ? static_cast<std::uint32_t>(levels.size()) : 0U;
+        for (std::uint32_t k = 0; k < d.level_count; ++k) d.level_begin[k] = levels[k].begin;
+        d.level_begin[d.level_count] = d.level_count ? levels[d.level_count - 1].end : 0U;
         sphere0.center = {R(sphere.center[0]), R(sphere.center[1]), R(sphere.center[2])};
         sphere0.velocity = {R(sphere.velocity[0]), R(sphere.velocity[1]), R(sphere.velocity[2])};
         sphere0.angular = {R(sphere.angular_velocity[0]), R(sphere.angular_velocity[1]), R(sphere.angular_velocity[2])};
@@ -529,13 +534,20 @@ template <class R> struct Resident {
 // work lists and the captured substep graph are rebuilt when the set changes.
 template <class R> class Engine {
     static constexpr bool kDirect = std::is_same<R, double>::value;
-    static constexpr unsigned kSphereSmem = kCandidatesPerBlock * sizeof(Staged<R>);
+    static constexpr unsigned kSphereSlab = kCandidatesPerBlock * sizeof(Staged<R>);
 
 public:
     Engine() {
-        check(cudaFuncSetAttribute(kSpherePass<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSphereSmem),
+        // Two staging buffers for the contact pass where the device's shared
+        // memory per block holds them, else one.
+        int device = 0, optin = 0;
+        check(cudaGetDevice(&device), "device");
+        check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "device attribute");
+        sphere_buffers_ = 2U * kSphereSlab + 1024U <= static_cast<unsigned>(optin) ? 2U : 1U;
+        const int smem = static_cast<int>(sphere_buffers_ * kSphereSlab);
+        check(cudaFuncSetAttribute(kSpherePass<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
               "contact pass shared memory");
-        check(cudaFuncSetAttribute(kSpherePass<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSphereSmem),
+        check(cudaFuncSetAttribute(kSpherePass<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
               "contact pass shared memory");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "stream");
         stream_ = own_stream_;
@@ -992,8 +1004,15 @@ private:
     // single lattice, the same items as (base, end, per).
     struct Span { std::uint32_t first, count, base, end, per; };
 
+    // A lattice of a batch swept by one CTA (kSweepLattice): small enough to
+    // keep its nodes in L2 across its levels, with levels that fit the table.
+    static bool sweptWhole(const Resident<R> &l) {
+        return l.B > 0 && l.B <= kMaxFusedBonds && l.dev.level_count == l.levels.size();
+    }
+
     // Work lists of every phase, one item per CTA, lattices in slot order.
     void buildWork() {
+        many_ = active_.size() > 1;
         std::vector<Work> all;
         auto ranges = [&](std::uint32_t k, std::uint32_t begin, std::uint32_t end, std::uint32_t per) {
             for (std::uint32_t b = begin; b < end; b += per) all.push_back({k, b, std::min(end, b + per)});
@@ -1019,7 +1038,24 @@ private:
         blocks_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.dev.tiles_b / kScanBlock + 1; }, 1);
         each_ = span([](const Res &, U &b, U &e) { b = 0; e = 1; }, 1);
         slabs_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.sched.block_count; }, 1);
-        isolated_ = span([](const Res &l, U &b, U &e) { b = 0; e = static_cast<U>(l.isolated.size()); }, kThreads);
+        // With many lattices, the small ones sweep in one CTA each (largest first);
+        // the level launches and the isolated-node launch cover the others.
+        auto leveled = [this](const Res &l) { return !many_ || !sweptWhole(l); };
+        isolated_ = span([&](const Res &l, U &b, U &e) {
+            b = 0;
+            e = leveled(l) ? static_cast<U>(l.isolated.size()) : 0U;
+        }, kThreads);
+        {
+            std::vector<std::uint32_t> whole;
+            if (many_)
+                for (auto k : active_)
+                    if (sweptWhole(*slots_[k])) whole.push_back(k);
+            std::stable_sort(whole.begin(), whole.end(),
+                             [this](std::uint32_t x, std::uint32_t y) { return slots_[x]->B > slots_[y]->B; });
+            const U first = static_cast<U>(all.size());
+            for (auto k : whole) all.push_back({k, 0, 1});
+            whole_ = Span{first, static_cast<U>(whole.size()), 0, 1, 1};
+        }
         {
             const U first = static_cast<U>(all.size());
             for (auto k : active_) {
@@ -1030,12 +1066,14 @@ private:
             broken_ = Span{first, count, 0, count, 1};
         }
         std::size_t deepest = 0;
-        for (auto k : active_) deepest = std::max(deepest, slots_[k]->levels.size());
+        for (auto k : active_)
+            if (leveled(*slots_[k])) deepest = std::max(deepest, slots_[k]->levels.size());
         levels_.clear();
         for (std::size_t d = 0; d < deepest; ++d)
-            levels_.push_back(span([d](const Res &l, U &b, U &e) {
-                b = d < l.levels.size() ? l.levels[d].begin : 0;
-                e = d < l.levels.size() ? l.levels[d].end : 0;
+            levels_.push_back(span([&](const Res &l, U &b, U &e) {
+                const bool in = leveled(l) && d < l.levels.size();
+                b = in ? l.levels[d].begin : 0;
+                e = in ? l.levels[d].end : 0;
             }, kThreads * kSolvePer));
         if (all.size() > work_cap_) {
             if (work_) cudaFree(work_);
@@ -1044,7 +1082,6 @@ private:
         }
         upload(work_, all, stream_);
         check(cudaStreamSynchronize(stream_), "work lists");
-        many_ = active_.size() > 1;
         one_ = active_.empty() ? 0 : active_.front();
     }
 
@@ -1089,8 +1126,11 @@ private:
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
         if (S.sphere_enabled && slabs_.count) kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
         mark(3);
-        if (S.sphere_enabled) kSpherePass<R, M><<<each_.count, kSphereThreads, kSphereSmem, st>>>(grid(each_), S, 1);
+        if (S.sphere_enabled)
+            kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 1,
+                                                                                               sphere_buffers_);
         mark(4);
+        if (M && whole_.count) launchSweepWhole(whole_);
         const unsigned I = S.iterations;
         for (unsigned it = 0; it < I; ++it) {
             const bool first = it == 0, last = it + 1 == I;
@@ -1109,7 +1149,9 @@ private:
             if (nodes_.count) kSupportVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
             mark(9);
         }
-        if (S.sphere_enabled) kSpherePass<R, M><<<each_.count, kSphereThreads, kSphereSmem, st>>>(grid(each_), S, 2);
+        if (S.sphere_enabled)
+            kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 2,
+                                                                                               sphere_buffers_);
         mark(10);
         if (nodes_.count) kStrainAll<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
         mark(11);
@@ -1153,6 +1195,19 @@ private:
         check(cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...), "kernel launch");
     }
 
+    void launchSweepWhole(const Span &span) {
+        const bool support = S_.plane_count != 0;
+        const int key = (plastic_ ? 2 : 0) | (support ? 1 : 0);
+        const Grid<R> g = grid(span);
+        const unsigned smem = 0;
+        switch (key) {
+        case 0: kSweepLattice<R, kDirect, false, false><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
+        case 1: kSweepLattice<R, kDirect, false, true><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
+        case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
+        default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
+        }
+    }
+
     template <bool M> void launchSolve(const Span &lv, bool first, bool last) {
         if (!lv.count) return;
         const bool support = S_.plane_count != 0;
@@ -1175,6 +1230,7 @@ private:
     std::mutex place_mutex_;
     Settings<R> S_{};
     bool plastic_{false}, ready_{false}, many_{false}, dirty_{true};
+    unsigned sphere_buffers_{1};
     std::uint32_t one_{0};
     Ctl *ctl_{};
     std::size_t cap_{0}, work_cap_{0};
@@ -1182,7 +1238,7 @@ private:
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
     Work *work_{};
-    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, isolated_{}, broken_{};
+    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, isolated_{}, broken_{}, whole_{};
     std::vector<Span> levels_;
     cudaStream_t own_stream_{}, stream_{};
     cudaEvent_t ev0_{}, ev1_{};

@@ -125,6 +125,8 @@ template <class R> struct Dev {
     std::uint32_t *dev2sched;     // bond storage order (level-major) -> schedule index
     std::uint32_t *isolated;      // nodes without bonds (their support projection has no sweep to ride on)
     std::uint32_t isolated_count;
+    std::uint32_t *level_begin;   // sweep level boundaries in storage order (level_count + 1), when level_count fits
+    std::uint32_t level_count;
     std::uint32_t *dmg_bits, *dmg_tile, *dmg_list;
     float *ev_damage, *dmg_value;
     double *tile_plastic, *tile_removed;
@@ -536,6 +538,20 @@ __device__ __forceinline__ bool contactGate(const Settings<R> &S, const Sphere<R
     return !(gap > maxR(S.c_margin, -vn * S.dt));
 }
 
+// Whether a candidate past the gate changes any state: a positive normal
+// impulse (which moves the node and the sphere), or in pass 2 a position
+// correction; the same expressions as contactChain.
+template <class R>
+__device__ __forceinline__ bool contactChanges(const Settings<R> &S, const Sphere<R> &sp, V3<R> nv, V3<R> r,
+                                               V3<R> normal, R gap, R eff_n, bool correct) {
+    const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
+    const R vn = dot(rel, normal);
+    const R restitution = -vn > S.c_threshold ? S.c_restitution : R(0);
+    const R desired = gap > S.c_margin ? -gap / S.dt : -restitution * minR(vn, R(0));
+    const R ni = maxR(R(0), (desired - vn) / eff_n);
+    return ni > R(0) || (correct && gap < -S.c_margin);
+}
+
 // The contact of one staged candidate, from its relative velocity on
 // (LatticePhysics.hpp:1338-1386). `max_pen` shadows acc.max_penetration in R:
 // the ledger only ever holds a widened R, so the comparison is the reference's.
@@ -585,6 +601,12 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
 }
 
 constexpr unsigned kSphereThreads = 256;
+// Staging buffers of the contact pass: with two, the chain of one slab runs on
+// warp 0 while the other warps write back the slab before it from the other
+// buffer and then stage the slab after it into that buffer (a thread writes
+// back and stages the same buffer slots, so no barrier is needed between);
+// with one (when two do not fit the device's shared memory), one slab at a
+// time.
 
 // The chain runs on warp 0, with every lane holding the same sphere state and
 // ledgers. Only a candidate that passes the contact gate changes anything, so
@@ -592,12 +614,15 @@ constexpr unsigned kSphereThreads = 256;
 // first that passes is applied (by every lane, identically) and the scan
 // resumes after it. The candidates skipped were tested against exactly the
 // state the serial order shows them, so the result is the serial chain's.
+// Slabs are disjoint sets of nodes: staging one slab's candidates, running
+// another's chain and writing back a third's touch different nodes.
 template <class R, bool Many>
-__global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> launch, Settings<R> S, int pass) {
+__global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> launch, Settings<R> S, int pass,
+                                                              unsigned buffers) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     extern __shared__ __align__(16) unsigned char sphere_smem[];
-    Staged<R> *st = reinterpret_cast<Staged<R> *>(sphere_smem);
+    Staged<R> *stage_base = reinterpret_cast<Staged<R> *>(sphere_smem);
     __shared__ Sphere<R> start;
     if (L.ctl->stop) return;
     const unsigned lane = threadIdx.x & 31U;
@@ -620,11 +645,12 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
     const R ism = R(1) / start.mass;
     const R iin = R(1) / start.inertia;
     const R cr = start.radius + S.c_node_radius;
-    for (std::uint32_t b = 0; b < L.blocks; ++b) {
+
+    // A slab's candidates into a buffer, by threads [t0, t0 + nt).
+    auto stageSlab = [&](std::uint32_t b, Staged<R> *st, unsigned t0, unsigned nt) {
         const std::uint32_t n = L.cand_count[b];
-        if (n == 0) continue;
         const std::uint32_t *list = L.cand_list + b * kCandidatesPerBlock;
-        for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        for (std::uint32_t k = threadIdx.x - t0; k < n; k += nt) {
             const std::uint32_t i = list[k];
             Staged<R> c;
             c.u = L.u[i];
@@ -647,47 +673,12 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             }
             st[k] = c;
         }
-        __syncthreads();
-        if (chain) {
-            std::uint32_t k0 = 0;
-            while (k0 < n) {
-                const std::uint32_t k = k0 + lane;
-                bool hit = false;
-                if (k < n) {
-                    const Staged<R> &c = st[k];
-                    if (c.v.w > R(0)) {
-                        if (pass == 1) {
-                            hit = contactGate(S, sp, xyz(c.v), c.p, c.normal, c.gap);
-                        } else {
-                            const V3<R> r = c.p - sp.center;
-                            hit = contactGate(S, sp, xyz(c.v), r, normalized(r), length(r) - cr);
-                        }
-                    }
-                }
-                const unsigned mask = __ballot_sync(0xffffffffU, hit);
-                if (mask == 0) {
-                    k0 += 32;
-                    continue;
-                }
-                const std::uint32_t j = k0 + static_cast<std::uint32_t>(__ffs(mask) - 1);
-                Staged<R> c = st[j];
-                if (pass == 1) {
-                    contactChain(S, sp, c, c.p, c.normal, c.gap, c.eff_n, ism, iin, false, acc, max_pen);
-                } else {
-                    const V3<R> r = c.p - sp.center;
-                    const R distance = length(r);
-                    const V3<R> normal = normalized(r);
-                    const V3<R> rn = cross(r, normal);
-                    const R eff_n = c.inm + ism + iin * dot(rn, rn);
-                    contactChain(S, sp, c, r, normal, distance - cr, eff_n, ism, iin, true, acc, max_pen);
-                }
-                __syncwarp();
-                if (lane == 0) st[j] = c;
-                k0 = j + 1;
-            }
-        }
-        __syncthreads();
-        for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    };
+    // A slab's candidates back to the node arrays, by threads [t0, t0 + nt).
+    auto writeBack = [&](std::uint32_t b, const Staged<R> *st, unsigned t0, unsigned nt) {
+        const std::uint32_t n = L.cand_count[b];
+        const std::uint32_t *list = L.cand_list + b * kCandidatesPerBlock;
+        for (std::uint32_t k = threadIdx.x - t0; k < n; k += nt) {
             const std::uint32_t i = list[k];
             const Q4<R> vq = st[k].v;
             const Q4<R> uq = st[k].u;
@@ -705,7 +696,123 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
                 L.v[i] = Q4<R>{vel.x, vel.y, vel.z, vq.w};
             }
         }
+    };
+    // The serial chain over a staged slab, on warp 0.
+    auto runChain = [&](std::uint32_t n, Staged<R> *st) {
+        std::uint32_t k0 = 0;
+        while (k0 < n) {
+            const std::uint32_t k = k0 + lane;
+            // hit: the contact changes the sphere or the node (an impulse, or
+            // a position correction in pass 2). graze: it passes the gate but
+            // only raises the penetration record, a maximum that any order
+            // forms alike.
+            bool hit = false, graze = false;
+            R pen = R(0);
+            V3<R> r{}, normal{};
+            R gap = R(0), eff_n = R(0);
+            if (k < n) {
+                const Staged<R> &c = st[k];
+                if (c.v.w > R(0)) {
+                    if (pass == 1) {
+                        r = c.p;
+                        normal = c.normal;
+                        gap = c.gap;
+                        eff_n = c.eff_n;
+                    } else {
+                        r = c.p - sp.center;
+                        const R distance = length(r);
+                        normal = normalized(r);
+                        const V3<R> rn = cross(r, normal);
+                        eff_n = c.inm + ism + iin * dot(rn, rn);
+                        gap = distance - cr;
+                    }
+                    if (contactGate(S, sp, xyz(c.v), r, normal, gap)) {
+                        hit = contactChanges(S, sp, xyz(c.v), r, normal, gap, eff_n, pass == 2);
+                        graze = !hit;
+                        pen = -gap;
+                    }
+                }
+            }
+            const unsigned mask = __ballot_sync(0xffffffffU, hit);
+            const unsigned limit = mask ? static_cast<unsigned>(__ffs(mask) - 1) : 32U;
+            // The grazes before the first hit raise the record as the serial
+            // chain would have, one after another.
+            const bool raises = graze && lane < limit && pen > max_pen;
+            if (__any_sync(0xffffffffU, raises)) {
+                R best = raises ? pen : max_pen;
+                if constexpr (std::is_same<R, float>::value) {
+                    // The record starts at zero and only grows, so a raising
+                    // value is positive and its bits order as its value.
+                    best = __uint_as_float(__reduce_max_sync(0xffffffffU, __float_as_uint(best)));
+                } else {
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const R other = __shfl_xor_sync(0xffffffffU, best, o);
+                        best = other > best ? other : best;
+                    }
+                }
+                if (best > max_pen) {
+                    max_pen = best;
+                    acc.max_penetration = static_cast<double>(best);
+                }
+            }
+            if (mask == 0) {
+                k0 += 32;
+                continue;
+            }
+            const std::uint32_t j = k0 + limit;
+            Staged<R> c = st[j];
+            // The hit lane's geometry, computed in the scan against the state
+            // the chain is in, to every lane.
+            const int src = static_cast<int>(limit);
+            const V3<R> hr{__shfl_sync(0xffffffffU, r.x, src), __shfl_sync(0xffffffffU, r.y, src),
+                           __shfl_sync(0xffffffffU, r.z, src)};
+            const V3<R> hn{__shfl_sync(0xffffffffU, normal.x, src), __shfl_sync(0xffffffffU, normal.y, src),
+                           __shfl_sync(0xffffffffU, normal.z, src)};
+            const R hgap = __shfl_sync(0xffffffffU, gap, src);
+            const R heff = __shfl_sync(0xffffffffU, eff_n, src);
+            contactChain(S, sp, c, hr, hn, hgap, heff, ism, iin, pass == 2, acc, max_pen);
+            __syncwarp();
+            if (lane == 0) st[j] = c;
+            k0 = j + 1;
+        }
+    };
+    // The next slab with candidates after b (L.blocks: none).
+    auto nextSlab = [&](std::uint32_t b) {
+        while (b < L.blocks && L.cand_count[b] == 0) ++b;
+        return b;
+    };
+
+    if (buffers == 2) {
+        std::uint32_t cur = nextSlab(0);
+        if (cur < L.blocks) stageSlab(cur, stage_base, 0, blockDim.x);
         __syncthreads();
+        std::uint32_t prev = L.blocks;
+        unsigned cb = 0;
+        while (cur < L.blocks) {
+            const std::uint32_t nxt = nextSlab(cur + 1);
+            const unsigned ob = cb ^ 1U;
+            if (chain) {
+                runChain(L.cand_count[cur], stage_base + cb * kCandidatesPerBlock);
+            } else {
+                Staged<R> *other = stage_base + ob * kCandidatesPerBlock;
+                if (prev < L.blocks) writeBack(prev, other, 32, blockDim.x - 32);
+                if (nxt < L.blocks) stageSlab(nxt, other, 32, blockDim.x - 32);
+            }
+            __syncthreads();
+            prev = cur;
+            cur = nxt;
+            cb = ob;
+        }
+        if (prev < L.blocks) writeBack(prev, stage_base + (cb ^ 1U) * kCandidatesPerBlock, 0, blockDim.x);
+    } else {
+        for (std::uint32_t b = nextSlab(0); b < L.blocks; b = nextSlab(b + 1)) {
+            stageSlab(b, stage_base, 0, blockDim.x);
+            __syncthreads();
+            if (chain) runChain(L.cand_count[b], stage_base);
+            __syncthreads();
+            writeBack(b, stage_base, 0, blockDim.x);
+            __syncthreads();
+        }
     }
     if (threadIdx.x == 0) {
         const R e1 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
@@ -742,11 +849,20 @@ __device__ __forceinline__ bool supportProject(const Dev<R> &L, const Settings<R
     return projected;
 }
 
-// Bonds per thread of the sweep: a thread issues the record loads of all its
-// bonds, then all their gathers, then solves them, so each thread keeps
-// several independent memory chains in flight. A level's bonds share no node,
-// so the order among them is free.
-constexpr int kSolvePer = 2;
+// Bonds per thread of the sweep and the sweep CTAs an SM keeps resident: a
+// thread issues the record loads of all its bonds, then all their gathers,
+// then solves them. A level's bonds share no node, so the order among them is
+// free. Measured on GB300 (impact 256x128x128, sweep ms per substep): one bond
+// per thread with six 256-thread CTAs per SM 2.50; two bonds, four CTAs 2.66;
+// one bond, eight CTAs (spilling at 32 registers) 2.76; two bonds, five CTAs
+// 2.93.
+#ifndef GBL_SOLVE_PER
+#define GBL_SOLVE_PER 1
+#endif
+#ifndef GBL_SOLVE_MIN_BLOCKS
+#define GBL_SOLVE_MIN_BLOCKS 6
+#endif
+constexpr int kSolvePer = GBL_SOLVE_PER;
 
 // Programmatic dependent launch (sm_90+): a sweep level is launched while the
 // previous one still runs; its CTAs load what no earlier kernel of the substep
@@ -758,8 +874,71 @@ constexpr int kSolvePer = 2;
 __device__ __forceinline__ void waitPreviousGrid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void allowNextGrid() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// The projection of one live bond (LatticePhysics.hpp:1132-1168) from its
+// record, geometry, multiplier and plastic extension and its gathered nodes;
+// the multiplier is stored unless this is the last iteration. Returns whether
+// the nodes moved (a degenerate bond leaves them).
+template <class R, bool Direct, bool Plastic>
+__device__ __forceinline__ bool projectBond(const Dev<R> &L, const Settings<R> &S, std::uint32_t d,
+                                            const BondRec<R> &rec, const Q4<R> &g, R lambda, R plastic, bool last,
+                                            Q4<R> &qa, Q4<R> &qb) {
+    const std::uint32_t a = endA(rec), b = endB(rec);
+    const V3<R> ua = xyz(qa), ub = xyz(qb), edge{g.x, g.y, g.z};
+    const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
+    const R cl = length(delta);
+    if (!(cl > R(1.0e-12))) return false;
+    const R original = rec.rest;
+    const R rest = Plastic ? original + plastic : original;
+    R constraint;
+    if (Direct) {
+        constraint = cl - rest;
+    } else {
+        const V3<R> du = ub - ua;
+        const R num = rec.rsm + R(2) * dot(edge, du) + dot(du, du);
+        constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
+    }
+    const V3<R> dir = delta / cl;
+    const R wa = qa.w, wb = qb.w;
+    const R alpha = g.w / (S.dt * S.dt);
+    const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
+    if (!last) __stcs(L.lambda + d, lambda + dl);
+    const V3<R> na = ua - (wa * dl) * dir;
+    const V3<R> nb = ub + (wb * dl) * dir;
+    qa = Q4<R>{na.x, na.y, na.z, wa};
+    qb = Q4<R>{nb.x, nb.y, nb.z, wb};
+    return true;
+}
+
+// The support projection of a node after its last bond of the sweep.
+template <class R>
+__device__ __forceinline__ void supportLast(const Dev<R> &L, const Settings<R> &S, std::uint32_t i, bool have,
+                                            Q4<R> &q, bool &write) {
+    if (!have) q = L.u[i];
+    V3<R> u = xyz(q);
+    if (supportProject(L, S, i, u)) {
+        q = Q4<R>{u.x, u.y, u.z, q.w};
+        write = true;
+    }
+}
+// A bond's projection, then the support projection of the nodes whose last
+// bond of the sweep it is, then the write-back of what moved.
+template <class R, bool Direct, bool Plastic, bool Support>
+__device__ __forceinline__ void finishBond(const Dev<R> &L, const Settings<R> &S, std::uint32_t d,
+                                           const BondRec<R> &rec, bool live, const Q4<R> &g, R lambda, R plastic,
+                                           bool last, Q4<R> qa, Q4<R> qb) {
+    const std::uint32_t a = endA(rec), b = endB(rec);
+    bool write_a = false, write_b = false;
+    if (live) write_a = write_b = projectBond<R, Direct, Plastic>(L, S, d, rec, g, lambda, plastic, last, qa, qb);
+    if (Support) {
+        if (rec.a & kLastABit) supportLast(L, S, a, live, qa, write_a);
+        if (rec.b & kLastBBit) supportLast(L, S, b, live, qb, write_b);
+    }
+    if (write_a) L.u[a] = qa;
+    if (write_b) L.u[b] = qb;
+}
+
 template <class R, bool Many, bool Direct, bool First, bool Last, bool Plastic, bool Support>
-__global__ void __launch_bounds__(kThreads, 4) kSolve(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kThreads, GBL_SOLVE_MIN_BLOCKS) kSolve(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     BondRec<R> rec[kSolvePer];
@@ -791,61 +970,89 @@ __global__ void __launch_bounds__(kThreads, 4) kSolve(const Grid<R> launch, Sett
         }
     }
 #pragma unroll
-    for (int k = 0; k < kSolvePer; ++k) {
-        if (at[k] >= w.end) continue;
-        const std::uint32_t d = at[k];
-        const std::uint32_t a = endA(rec[k]), b = endB(rec[k]);
-        bool write_a = false, write_b = false;
-        if (live[k]) {
-            const Q4<R> g = geo[k];
-            const V3<R> ua = xyz(qa[k]), ub = xyz(qb[k]), edge{g.x, g.y, g.z};
-            const V3<R> delta = Direct ? (xyz(L.x0[b]) + ub) - (xyz(L.x0[a]) + ua) : edge + (ub - ua);
-            const R cl = length(delta);
-            if (cl > R(1.0e-12)) {
-                const R original = rec[k].rest;
-                const R plastic = pl[k];
-                const R rest = Plastic ? original + plastic : original;
-                R constraint;
-                if (Direct) {
-                    constraint = cl - rest;
-                } else {
-                    const V3<R> du = ub - ua;
-                    const R num = rec[k].rsm + R(2) * dot(edge, du) + dot(du, du);
-                    constraint = (Plastic ? num - plastic * (rest + original) : num) / (cl + rest);
+    for (int k = 0; k < kSolvePer; ++k)
+        if (at[k] < w.end)
+            finishBond<R, Direct, Plastic, Support>(L, S, at[k], rec[k], live[k], geo[k], lam[k], pl[k], Last, qa[k],
+                                                    qb[k]);
+}
+
+// The whole sweep of one lattice in one CTA: every iteration, every level in
+// order with a barrier between levels, then the isolated nodes' support. A
+// lattice of a batch small enough for one CTA runs here, so its nodes stay in
+// L2 (and the SM's L1) across all its levels instead of being streamed from
+// HBM again at every level launch; the arithmetic and the per-node order are
+// those of the level launches.
+constexpr unsigned kSweepThreads = 512;
+constexpr unsigned kSweepSlots = kSweepThreads * kSolvePer;
+constexpr std::uint32_t kMaxFusedLevels = 1024;
+constexpr std::uint32_t kMaxFusedBonds = 1U << 21;
+
+template <class R, bool Support>
+__device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Settings<R> &S) {
+    if (!Support || !L.isolated_count) return;
+    __syncthreads();
+    for (std::uint32_t t = threadIdx.x; t < L.isolated_count; t += blockDim.x) {
+        const std::uint32_t i = L.isolated[t];
+        const Q4<R> uq = L.u[i];
+        V3<R> u = xyz(uq);
+        if (supportProject(L, S, i, u)) L.u[i] = Q4<R>{u.x, u.y, u.z, uq.w};
+    }
+}
+
+template <class R, bool Direct, bool Plastic, bool Support>
+__global__ void __launch_bounds__(kSweepThreads, 2) kSweepLattice(const Grid<R> launch, Settings<R> S) {
+    // The lattice's descriptor, copied once into shared memory: its fields
+    // are read throughout the sweep, and shared memory is never written by
+    // the sweep's global stores, so the compiler may keep them as it likes.
+    __shared__ __align__(16) unsigned char desc[sizeof(Dev<R>)];
+    {
+        const Work w = item<true>(launch);
+        const unsigned *src = reinterpret_cast<const unsigned *>(launch.table + w.lattice);
+        unsigned *dst = reinterpret_cast<unsigned *>(desc);
+        for (unsigned k = threadIdx.x; k < sizeof(Dev<R>) / sizeof(unsigned); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    const Dev<R> &L = *reinterpret_cast<const Dev<R> *>(desc);
+    if (L.ctl->stop) return;
+    const unsigned I = S.iterations;
+    for (unsigned it = 0; it < I; ++it) {
+        const bool first = it == 0, last = it + 1 == I;
+        for (std::uint32_t lv = 0; lv < L.level_count; ++lv) {
+            const std::uint32_t end = L.level_begin[lv + 1];
+            for (std::uint32_t base = L.level_begin[lv]; base < end; base += kSweepSlots) {
+                BondRec<R> rec[kSolvePer];
+                Q4<R> geo[kSolvePer], qa[kSolvePer], qb[kSolvePer];
+                R lam[kSolvePer], pl[kSolvePer];
+                std::uint32_t at[kSolvePer];
+                bool live[kSolvePer];
+#pragma unroll
+                for (int k = 0; k < kSolvePer; ++k) {
+                    at[k] = base + threadIdx.x + static_cast<std::uint32_t>(k) * kSweepThreads;
+                    if (at[k] < end) {
+                        rec[k] = ldStream(L.rec + at[k]);
+                        geo[k] = ldStream(L.geo + at[k]);
+                        lam[k] = first ? R(0) : __ldcs(L.lambda + at[k]);
+                        pl[k] = Plastic ? L.plastic[at[k]].x : R(0);
+                    }
                 }
-                const V3<R> dir = delta / cl;
-                const R wa = qa[k].w, wb = qb[k].w;
-                const R alpha = g.w / (S.dt * S.dt);
-                const R lambda = lam[k];
-                const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
-                if (!Last) __stcs(L.lambda + d, lambda + dl);
-                const V3<R> na = ua - (wa * dl) * dir;
-                const V3<R> nb = ub + (wb * dl) * dir;
-                qa[k] = Q4<R>{na.x, na.y, na.z, wa};
-                qb[k] = Q4<R>{nb.x, nb.y, nb.z, wb};
-                write_a = write_b = true;
+#pragma unroll
+                for (int k = 0; k < kSolvePer; ++k) {
+                    live[k] = at[k] < end && !(rec[k].a & kDeadBit);
+                    if (live[k]) {
+                        qa[k] = ldShared(L.u + endA(rec[k]));
+                        qb[k] = ldShared(L.u + endB(rec[k]));
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kSolvePer; ++k)
+                    if (at[k] < end)
+                        finishBond<R, Direct, Plastic, Support>(L, S, at[k], rec[k], live[k], geo[k], lam[k],
+                                                                pl[k], last, qa[k], qb[k]);
             }
+            __syncthreads();
         }
-        if (Support) {
-            if (rec[k].a & kLastABit) {
-                if (!live[k]) qa[k] = L.u[a];
-                V3<R> u = xyz(qa[k]);
-                if (supportProject(L, S, a, u)) {
-                    qa[k] = Q4<R>{u.x, u.y, u.z, qa[k].w};
-                    write_a = true;
-                }
-            }
-            if (rec[k].b & kLastBBit) {
-                if (!live[k]) qb[k] = L.u[b];
-                V3<R> u = xyz(qb[k]);
-                if (supportProject(L, S, b, u)) {
-                    qb[k] = Q4<R>{u.x, u.y, u.z, qb[k].w};
-                    write_b = true;
-                }
-            }
-        }
-        if (write_a) L.u[a] = qa[k];
-        if (write_b) L.u[b] = qb[k];
+        supportIsolatedInCta<R, Support>(L, S);
+        __syncthreads();
     }
 }
 

@@ -218,6 +218,7 @@ def batched_leg(args, lattice) -> dict:
     live = sum(b - a.broken_bonds for (_, b), a in zip(sizes, after))
     value = ITERATIONS * live * k / device_s
     launches = batch.kernels_per_substep()
+    phases = batch.profile_phases(1)
     del batch
 
     # Plain: the first trials of the same draw, one backend at a time.
@@ -240,6 +241,7 @@ def batched_leg(args, lattice) -> dict:
                       "note": "the first trials of the same draw, each alone through the single-lattice backend "
                               "(its own captured substep graph), device time summed"},
             "speedup_vs_plain": value / plain,
+            "phase_ms_per_substep": {name: v for name, v in phases.items() if v > 0},
             "workload": f"{len(specs)} drop trials, edges 8..48 per axis (seeded), one batch; step = "
                         f"{SUBSTEPS_PER_STEP} substeps, I={ITERATIONS}; device time of {args.steps} steps"}
 
