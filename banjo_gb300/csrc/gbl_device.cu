@@ -253,6 +253,7 @@ template <class R> struct Resident {
         a.reserve(d.cand_list, static_cast<std::size_t>(blocks) * kCandidatesPerBlock);
         a.reserve(d.cand_count, blocks);
         a.reserve(d.dirty_list, N + 1); a.reserve(d.ffb, B + 1);
+        a.reserve(d.halo_stamp, N); a.reserve(d.late_tile_stamp, d.tiles_b + 1);
         return filled;
     }
 
@@ -550,6 +551,9 @@ public:
         check(cudaFuncSetAttribute(kSpherePass<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
               "contact pass shared memory");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "stream");
+        check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream");
+        check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming), "event");
         stream_ = own_stream_;
         check(cudaEventCreate(&ev0_), "event");
         check(cudaEventCreate(&ev1_), "event");
@@ -568,6 +572,9 @@ public:
         if (running_host_) cudaFreeHost(running_host_);
         cudaEventDestroy(ev0_);
         cudaEventDestroy(ev1_);
+        cudaEventDestroy(fork_);
+        cudaEventDestroy(join_);
+        cudaStreamDestroy(side_);
         cudaStreamDestroy(own_stream_);
     }
 
@@ -1124,7 +1131,10 @@ private:
         if (nodes_.count) kRestartBondsDirty<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
         mark(2);
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
-        if (S.sphere_enabled && slabs_.count) kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
+        if (S.sphere_enabled && slabs_.count) {
+            kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
+            kMarkHalo<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
+        }
         mark(3);
         if (S.sphere_enabled)
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 1,
@@ -1149,16 +1159,21 @@ private:
             if (nodes_.count) kSupportVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
             mark(9);
         }
-        if (S.sphere_enabled)
+        // With a sphere, the strain and end sample outside the contact halo
+        // run on a second stream beside the second contact pass; the halo's
+        // follow it.
+        const bool split = S.sphere_enabled != 0;
+        if (split) {
+            check(cudaEventRecord(fork_, st), "event");
+            check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
+            endPhase<M>(side_, 1);
+            check(cudaEventRecord(join_, side_), "event");
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 2,
                                                                                                sphere_buffers_);
-        mark(10);
-        if (nodes_.count) kStrainAll<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
-        mark(11);
-        if (bonds_.count) {
-            if (plastic_) kEndSample<R, M, kDirect, true><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), S);
-            else kEndSample<R, M, kDirect, false><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), S);
         }
+        mark(10);
+        if (split) check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
+        endPhase<M>(st, split ? 2 : 0, mark);
         if (tiles_.count) kTileCounts<R, M><<<tiles_.count, kThreads, 0, st>>>(grid(tiles_));
         kBlockScan<R, M><<<blocks_.count, kScanBlock, 0, st>>>(grid(blocks_), plastic_ ? 1 : 0);
         kTopScan<R, M><<<each_.count, kScanBlock, 0, st>>>(grid(each_));
@@ -1208,6 +1223,18 @@ private:
         }
     }
 
+    // Strain of the nodes, then the end sample of the bonds, of one part
+    // (0 all, 1 outside the contact halo, 2 inside it).
+    template <bool M, class Mark = void (*)(unsigned)>
+    void endPhase(cudaStream_t st, int part, Mark &&mark = [](unsigned) {}) {
+        if (nodes_.count) kStrainAll<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), part);
+        mark(11);
+        if (bonds_.count) {
+            if (plastic_) kEndSample<R, M, kDirect, true><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), S_, part);
+            else kEndSample<R, M, kDirect, false><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), S_, part);
+        }
+    }
+
     template <bool M> void launchSolve(const Span &lv, bool first, bool last) {
         if (!lv.count) return;
         const bool support = S_.plane_count != 0;
@@ -1240,8 +1267,8 @@ private:
     Work *work_{};
     Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, isolated_{}, broken_{}, whole_{};
     std::vector<Span> levels_;
-    cudaStream_t own_stream_{}, stream_{};
-    cudaEvent_t ev0_{}, ev1_{};
+    cudaStream_t own_stream_{}, stream_{}, side_{};
+    cudaEvent_t ev0_{}, ev1_{}, fork_{}, join_{};
     cudaGraph_t graph_{};
     cudaGraphExec_t exec_{};
 };

@@ -133,6 +133,11 @@ template <class R> struct Dev {
     std::uint32_t *blk_ev, *blk_dmg;   // per scan block of tiles: totals, then offsets
     double *blk_removed, *blk_plastic;
     std::uint32_t *node_block_begin, *cand_list, *cand_count, *dirty_list, *ffb;
+    // Contact halo of the substep (stamped with the substep's number + 1): the
+    // listed sphere candidates and their neighbours, and the end-sample tiles
+    // holding a bond at one of them. Everything outside it is final before the
+    // second contact pass, so its strain and end sample run beside that pass.
+    std::uint32_t *halo_stamp, *late_tile_stamp;
     Q4<R> *ext_force;     // applied force (backend precision), w != 0 marks a loaded node
     double *ext_req;      // requested force, 3 per node
     double *ext_contrib;  // 13 per node: impulse 3, angular 3, work, requested 3, requested angular 3
@@ -244,13 +249,24 @@ __device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
     L.strain[2 * i + 1] = Q4<R>{e[4], e[5], R(1), R(0)};
 }
 
+// The stamp of the running substep in the halo marks (never 0, the cleared value).
+template <class R> __device__ __forceinline__ std::uint32_t substepStamp(const Dev<R> &L) {
+    return static_cast<std::uint32_t>(L.ctl->total_steps) + 1U;
+}
+
 template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch) {
+__global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int part) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
     const std::uint32_t i = w.begin + threadIdx.x;
-    if (i < w.end) nodeStrain<R, Direct>(L, i);
+    if (i >= w.end) return;
+    // part 0: every node; 1: the nodes outside the contact halo; 2: inside it.
+    if (part != 0) {
+        const bool halo = L.halo_stamp[i] == substepStamp(L);
+        if (halo != (part == 2)) return;
+    }
+    nodeStrain<R, Direct>(L, i);
 }
 
 // The start-of-substep restart after an upload (every node) or after a failure
@@ -488,6 +504,32 @@ __global__ void __launch_bounds__(1024) kCandidates(const Grid<R> launch) {
         const std::uint32_t total = carry;
         L.cand_count[blk] = total < kCandidatesPerBlock ? total : kCandidatesPerBlock;
         if (total > kCandidatesPerBlock) L.ctl->contact.candidate_overflow += total - kCandidatesPerBlock;
+    }
+}
+
+// The contact halo of the substep: per (lattice, slab) item, its listed
+// candidates, their neighbours, and the end-sample tiles of every bond at one
+// of those nodes. Threads that mark the same entry write the same stamp.
+template <class R, bool Many>
+__global__ void __launch_bounds__(1024) kMarkHalo(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop) return;
+    const std::uint32_t stamp = substepStamp(L);
+    const std::uint32_t n = L.cand_count[w.begin];
+    const std::uint32_t *list = L.cand_list + w.begin * kCandidatesPerBlock;
+    for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const std::uint32_t c = list[k];
+        L.halo_stamp[c] = stamp;
+        for (std::uint32_t q = 0; q < L.D; ++q) {
+            const std::size_t slot = static_cast<std::size_t>(q) * L.N + c;
+            const std::uint32_t o = L.nbr_other[slot];
+            L.halo_stamp[o] = stamp;
+            for (std::uint32_t r = 0; r < L.D; ++r) {
+                const std::uint32_t bd = L.nbr_bond[static_cast<std::size_t>(r) * L.N + o];
+                if (bd != kNoBond) L.late_tile_stamp[bd / kThreads] = stamp;
+            }
+        }
     }
 }
 
@@ -1150,12 +1192,17 @@ __device__ __forceinline__ double warpSumFixed(double x) {
 }
 
 template <class R, bool Many, bool Direct, bool Plastic>
-__global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Settings<R> S, int part) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     __shared__ double tile_work[kThreads / 32];
     __shared__ unsigned peak[4];
     if (L.ctl->stop) return;
+    // part 0: every tile; 1: the tiles outside the contact halo; 2: inside it.
+    if (part != 0) {
+        const bool late = L.late_tile_stamp[w.begin / kThreads] == substepStamp(L);
+        if (late != (part == 2)) return;
+    }
     const std::uint32_t j = w.begin + threadIdx.x; // storage index; items start on multiples of 256
     if (threadIdx.x < 4) peak[threadIdx.x] = 0;
     __syncthreads();
