@@ -1125,20 +1125,26 @@ private:
     template <bool M, class Mark> void enqueueSubstepAs(Mark &&mark) {
         const Settings<R> &S = S_;
         cudaStream_t st = stream_;
-        if (nodes_.count) kRestartStrain<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
-        mark(1);
-        if (bonds_.count) kRestartBondsAll<R, M, kDirect><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_));
-        if (nodes_.count) kRestartBondsDirty<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
-        mark(2);
+        // With a sphere, the restart runs beside the first contact pass (on
+        // the second stream, from the starting positions the kick keeps);
+        // without, before the kick.
+        const bool side_restart = S.sphere_enabled != 0;
+        if (!side_restart) restartPhase<M>(st, 0, mark);
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
         if (S.sphere_enabled && slabs_.count) {
             kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
             kMarkHalo<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
         }
         mark(3);
-        if (S.sphere_enabled)
+        if (side_restart) {
+            check(cudaEventRecord(fork_, st), "event");
+            check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
+            restartPhase<M>(side_, 1);
+            check(cudaEventRecord(join_, side_), "event");
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 1,
                                                                                                sphere_buffers_);
+            check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
+        }
         mark(4);
         if (M && whole_.count) launchSweepWhole(whole_);
         const unsigned I = S.iterations;
@@ -1221,6 +1227,19 @@ private:
         case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
         default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
         }
+    }
+
+    // The start-of-substep restart: strain of the dirty (or all) nodes, then
+    // the start samples of their bonds.
+    template <bool M, class Mark = void (*)(unsigned)>
+    void restartPhase(cudaStream_t st, int after_kick, Mark &&mark = [](unsigned) {}) {
+        if (nodes_.count) kRestartStrain<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), after_kick);
+        mark(1);
+        if (bonds_.count)
+            kRestartBondsAll<R, M, kDirect><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), after_kick);
+        if (nodes_.count)
+            kRestartBondsDirty<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), after_kick);
+        mark(2);
     }
 
     // Strain of the nodes, then the end sample of the bonds, of one part

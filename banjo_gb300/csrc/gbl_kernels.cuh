@@ -273,10 +273,13 @@ __global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int
 // round (the dirty nodes only: every other node's strain is unchanged, since
 // positions have not moved since the end sample and its bonds are the same;
 // src/fastlattice/ParallelCpuLatticeBackend.cpp:1718-1757 relies on the same fact).
+// It reads the substep's starting positions: before the kick from u, or after
+// it (beside the first contact pass) from u_prev, where the kick copied them.
 template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch) {
+__global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch, int after_kick) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Dev<R> L = descriptor<R, Many>(launch, w);
+    if (after_kick) L.u = L.up; // the kick kept the substep's starting positions there
     if (L.ctl->stop) return;
     // Items cover the node index range; a dirty list is never longer.
     const std::uint32_t t = w.begin + threadIdx.x;
@@ -344,9 +347,10 @@ __device__ __forceinline__ void startSample(const Dev<R> &L, std::uint32_t j) {
 
 // Every live bond, after an upload: items cover the bond storage range.
 template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartBondsAll(const Grid<R> launch) {
+__global__ void __launch_bounds__(kThreads) kRestartBondsAll(const Grid<R> launch, int after_kick) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Dev<R> L = descriptor<R, Many>(launch, w);
+    if (after_kick) L.u = L.up;
     if (L.ctl->stop || !L.ctl->full_restart) return;
     const std::uint32_t d = w.begin + threadIdx.x;
     if (d < w.end) startSample<R, Direct>(L, d);
@@ -356,9 +360,10 @@ __global__ void __launch_bounds__(kThreads) kRestartBondsAll(const Grid<R> launc
 // node index range (one thread per dirty-list entry, over its neighbour
 // slots). A bond with both ends dirty is sampled twice to the same values.
 template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartBondsDirty(const Grid<R> launch) {
+__global__ void __launch_bounds__(kThreads) kRestartBondsDirty(const Grid<R> launch, int after_kick) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Dev<R> L = descriptor<R, Many>(launch, w);
+    if (after_kick) L.u = L.up;
     if (L.ctl->stop || L.ctl->full_restart) return;
     const std::uint32_t t = w.begin + threadIdx.x;
     if (t >= w.end || t >= L.ctl->dirty_count) return;
