@@ -81,19 +81,57 @@ template <class T> void uploadRaw(T *dst, const T *src, std::size_t n, cudaStrea
 template <class T> void zero(T *dst, std::size_t n, cudaStream_t s) {
     if (n) check(cudaMemsetAsync(dst, 0, sizeof(T) * n, s), "memset");
 }
-template <class T> std::vector<T> fetch(const T *src, std::size_t n) {
-    std::vector<T> out(n);
-    if (n) check(cudaMemcpy(out.data(), src, sizeof(T) * n, cudaMemcpyDeviceToHost), "copy");
+// A large copy between pageable host memory and the device, split into chunks
+// copied by several host threads at once (each on its own stream): the
+// staging of pageable memory is host-bound, one thread at a time.
+void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind kind) {
+    constexpr std::size_t kChunk = std::size_t(64) << 20;
+    const std::size_t chunks = (bytes + kChunk - 1) / kChunk;
+    if (chunks <= 1) {
+        if (bytes) check(cudaMemcpy(dst, src, bytes, kind), "copy");
+        return;
+    }
+    std::atomic<int> failed{static_cast<int>(cudaSuccess)};
+    const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
+    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 16), chunks);
+    std::vector<std::thread> pool;
+    auto note = [&](cudaError_t e) {
+        int ok = static_cast<int>(cudaSuccess);
+        if (e != cudaSuccess) failed.compare_exchange_strong(ok, static_cast<int>(e));
+    };
+    auto work = [&](std::size_t t) {
+        cudaStream_t s = nullptr;
+        const cudaError_t made = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (made != cudaSuccess) {
+            note(made);
+            return;
+        }
+        for (std::size_t c = t; c < chunks; c += T) {
+            const std::size_t off = c * kChunk, n = std::min(kChunk, bytes - off);
+            note(cudaMemcpyAsync(static_cast<char *>(dst) + off, static_cast<const char *>(src) + off, n, kind, s));
+        }
+        note(cudaStreamSynchronize(s));
+        cudaStreamDestroy(s);
+    };
+    for (std::size_t t = 1; t < T; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+    check(static_cast<cudaError_t>(failed.load()), "copy");
+}
+
+// Device array to host, into uninitialised storage (no zero fill).
+template <class T> std::unique_ptr<T[]> fetch(const T *src, std::size_t n) {
+    std::unique_ptr<T[]> out(new T[n ? n : 1]);
+    copyParallel(out.get(), src, sizeof(T) * n, cudaMemcpyDeviceToHost);
     return out;
 }
 
 // A static split of [0, n) over host threads, for the O(N + B) conversion
 // loops of upload and download (f(begin, end) on disjoint ranges; f must not
 // throw). Small ranges stay on the calling thread.
-template <class F> void parallelFor(std::size_t n, F &&f) {
-    constexpr std::size_t kGrain = std::size_t(1) << 16;
+template <class F> void parallelFor(std::size_t n, F &&f, std::size_t grain = std::size_t(1) << 16) {
     const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
-    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 32), (n + kGrain - 1) / kGrain);
+    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 32), (n + grain - 1) / grain);
     if (T <= 1) {
         f(std::size_t(0), n);
         return;
@@ -168,54 +206,148 @@ template <class R> struct Resident {
     // each node's last bond of the sweep is flagged: its support projection
     // follows that bond.
     void buildLevels(const gbl_state_view &st) {
-        const std::uint32_t C = sched.color_count;
-        std::vector<std::uint32_t> order;
-        order.reserve(B);
-        auto sweep = [&](std::uint32_t blk, std::uint32_t boundary) {
+        const std::uint32_t C = sched.color_count, K = sched.block_count;
+        const std::uint32_t *nbb = sched.node_block_begin.data();
+        // The serial order as segments: every slab's interior colours, then
+        // the boundary colours of even slabs, then of odd slabs.
+        struct Seg { std::uint32_t slab, phase, begin, end; };
+        std::vector<Seg> segs;
+        std::uint32_t total = 0;
+        auto add = [&](std::uint32_t blk, std::uint32_t boundary, std::uint32_t phase) {
             for (std::uint32_t c = 0; c < C; ++c) {
                 const std::size_t key = sched.rangeKey(blk, boundary, c);
-                for (std::uint32_t j = sched.range_begin[key]; j < sched.range_end[key]; ++j) order.push_back(j);
+                const std::uint32_t n = sched.range_end[key] - sched.range_begin[key];
+                if (n) segs.push_back({blk, phase, sched.range_begin[key], sched.range_begin[key] + n});
+                total += n;
             }
         };
-        for (std::uint32_t blk = 0; blk < sched.block_count; ++blk) sweep(blk, 0);
-        for (std::uint32_t blk = 0; blk < sched.block_count; blk += 2) sweep(blk, 1);
-        for (std::uint32_t blk = 1; blk < sched.block_count; blk += 2) sweep(blk, 1);
-        if (order.size() != B) invalid("lattice schedule ranges do not cover every bond exactly once");
-        std::vector<std::uint32_t> depth(B), reached(N, 0), last(N, kNoBond);
-        std::uint32_t deepest = 0;
-        for (const std::uint32_t j : order) {
-            const std::uint32_t a = st.bond_a[j], b = st.bond_b[j];
-            if (a >= N || b >= N || a == b) invalid("lattice bond joins invalid nodes");
-            const std::uint32_t d = std::max(reached[a], reached[b]) + 1;
-            depth[j] = d;
-            reached[a] = reached[b] = d;
-            last[a] = last[b] = j;
-            deepest = std::max(deepest, d);
+        for (std::uint32_t blk = 0; blk < K; ++blk) add(blk, 0, 0);
+        for (std::uint32_t blk = 0; blk < K; blk += 2) add(blk, 1, 1);
+        for (std::uint32_t blk = 1; blk < K; blk += 2) add(blk, 1, 2);
+        if (total != B) invalid("lattice schedule ranges do not cover every bond exactly once");
+        // Segments grouped by (phase, slab), in serial order.
+        struct Task { std::uint32_t phase, slab, seg_begin, seg_end; };
+        std::vector<Task> tasks;
+        for (std::uint32_t k = 0; k < segs.size(); ++k) {
+            if (tasks.empty() || tasks.back().phase != segs[k].phase || tasks.back().slab != segs[k].slab)
+                tasks.push_back({segs[k].phase, segs[k].slab, k, k});
+            tasks.back().seg_end = k + 1;
         }
-        std::vector<std::uint32_t> first(deepest + 2, 0);
-        for (std::uint32_t j = 0; j < B; ++j) ++first[depth[j] + 1];
-        for (std::uint32_t d = 1; d <= deepest; ++d) first[d + 1] += first[d];
+        // Within a phase the slabs touch disjoint nodes when every interior
+        // bond stays in its slab and every boundary bond in its slab and the
+        // next; then the slabs of a phase run in parallel (the per-node order
+        // of the serial walk is kept exactly), else the walk is serial.
+        std::atomic<bool> bad{false}, local{true};
+        parallelFor(tasks.size(), [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t t = lo; t < hi; ++t) {
+                const Task &task = tasks[t];
+                const std::uint32_t n0 = nbb[task.slab];
+                const std::uint32_t n1 = nbb[std::min<std::uint32_t>(task.slab + (task.phase == 0 ? 1U : 2U), K)];
+                for (std::uint32_t k = task.seg_begin; k < task.seg_end; ++k)
+                    for (std::uint32_t j = segs[k].begin; j < segs[k].end; ++j) {
+                        const std::uint32_t a = st.bond_a[j], b = st.bond_b[j];
+                        if (a >= N || b >= N || a == b) bad.store(true);
+                        else if (a < n0 || a >= n1 || b < n0 || b >= n1) local.store(false);
+                    }
+            }
+        }, 1);
+        if (bad.load()) invalid("lattice bond joins invalid nodes");
+        std::vector<std::uint32_t> depth(B), reached(N, 0), last(N, kNoBond);
+        auto walk = [&](const Task &task) {
+            std::uint32_t deepest = 0;
+            for (std::uint32_t k = task.seg_begin; k < task.seg_end; ++k)
+                for (std::uint32_t j = segs[k].begin; j < segs[k].end; ++j) {
+                    const std::uint32_t a = st.bond_a[j], b = st.bond_b[j];
+                    const std::uint32_t d = std::max(reached[a], reached[b]) + 1;
+                    depth[j] = d;
+                    reached[a] = reached[b] = d;
+                    last[a] = last[b] = j;
+                    deepest = std::max(deepest, d);
+                }
+            return deepest;
+        };
+        std::uint32_t deepest = 0;
+        if (local.load()) {
+            std::mutex m;
+            for (std::uint32_t phase = 0; phase < 3; ++phase) {
+                std::vector<std::uint32_t> ids;
+                for (std::uint32_t t = 0; t < tasks.size(); ++t)
+                    if (tasks[t].phase == phase) ids.push_back(t);
+                parallelFor(ids.size(), [&](std::size_t lo, std::size_t hi) {
+                    std::uint32_t dmax = 0;
+                    for (std::size_t q = lo; q < hi; ++q) dmax = std::max(dmax, walk(tasks[ids[q]]));
+                    std::lock_guard<std::mutex> lock(m);
+                    deepest = std::max(deepest, dmax);
+                }, 1);
+            }
+        } else {
+            for (const Task &task : tasks) deepest = std::max(deepest, walk(task));
+        }
+        // Storage order: by depth, stable in the serial order (a parallel
+        // counting sort over chunks of the serial walk).
+        std::vector<std::uint32_t> order(B);
+        {
+            std::vector<std::uint32_t> at(segs.size() + 1, 0);
+            for (std::size_t k = 0; k < segs.size(); ++k) at[k + 1] = at[k] + (segs[k].end - segs[k].begin);
+            parallelFor(segs.size(), [&](std::size_t lo, std::size_t hi) {
+                for (std::size_t k = lo; k < hi; ++k)
+                    for (std::uint32_t j = segs[k].begin, o = at[k]; j < segs[k].end; ++j, ++o) order[o] = j;
+            }, 1);
+        }
+        const std::uint32_t D1 = deepest + 2;
+        const std::size_t chunk = std::max<std::size_t>(std::size_t(1) << 16, (B + 63) / 64);
+        const std::size_t nchunks = (B + chunk - 1) / chunk;
+        std::vector<std::uint32_t> counts(nchunks * D1, 0);
+        parallelFor(nchunks, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t c = lo; c < hi; ++c) {
+                std::uint32_t *h = counts.data() + c * D1;
+                for (std::size_t o = c * chunk; o < std::min<std::size_t>(B, (c + 1) * chunk); ++o) ++h[depth[order[o]]];
+            }
+        }, 1);
+        std::vector<std::uint32_t> first(D1 + 1, 0);
+        for (std::uint32_t d = 0; d < D1; ++d) {
+            std::uint32_t sum = 0;
+            for (std::size_t c = 0; c < nchunks; ++c) sum += counts[c * D1 + d];
+            first[d + 1] = first[d] + sum;
+        }
+        // counts becomes each chunk's starting offset within each depth.
+        for (std::uint32_t d = 0; d < D1; ++d) {
+            std::uint32_t run = first[d];
+            for (std::size_t c = 0; c < nchunks; ++c) {
+                const std::uint32_t n = counts[c * D1 + d];
+                counts[c * D1 + d] = run;
+                run += n;
+            }
+        }
         dev2sched.assign(B, 0);
         sched2dev.assign(B, 0);
-        {
-            std::vector<std::uint32_t> fill(first.begin(), first.end());
-            for (const std::uint32_t j : order) dev2sched[fill[depth[j]]++] = j;
-        }
-        for (std::uint32_t d = 0; d < B; ++d) sched2dev[dev2sched[d]] = d;
+        parallelFor(nchunks, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t c = lo; c < hi; ++c) {
+                std::uint32_t *fill = counts.data() + c * D1;
+                for (std::size_t o = c * chunk; o < std::min<std::size_t>(B, (c + 1) * chunk); ++o) {
+                    const std::uint32_t j = order[o];
+                    dev2sched[fill[depth[j]]++] = j;
+                }
+            }
+        }, 1);
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t d = lo; d < hi; ++d) sched2dev[dev2sched[d]] = static_cast<std::uint32_t>(d);
+        });
         levels.clear();
         for (std::uint32_t d = 1; d <= deepest; ++d)
             if (first[d + 1] > first[d]) levels.push_back({first[d], first[d + 1]});
         last_a.assign(B, 0);
         last_b.assign(B, 0);
-        isolated.clear();
-        for (std::uint32_t i = 0; i < N; ++i) {
-            if (last[i] == kNoBond) {
-                isolated.push_back(i);
-                continue;
+        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t i = lo; i < hi; ++i) {
+                if (last[i] == kNoBond) continue;
+                const std::uint32_t dd = sched2dev[last[i]];
+                (st.bond_a[last[i]] == i ? last_a : last_b)[dd] = 1;
             }
-            const std::uint32_t dd = sched2dev[last[i]];
-            (st.bond_a[last[i]] == i ? last_a : last_b)[dd] = 1;
-        }
+        });
+        isolated.clear();
+        for (std::uint32_t i = 0; i < N; ++i)
+            if (last[i] == kNoBond) isolated.push_back(i);
     }
 
     // The device arrays of one lattice, in one allocation: first the arrays an
@@ -369,7 +501,8 @@ template <class R> struct Resident {
     void commit(cudaStream_t stream) {
         if (!image_) logic("lattice committed before it was prepared");
         arena.allocate(stream);
-        check(cudaMemcpyAsync(arena.base(), image_.get(), filled_, cudaMemcpyHostToDevice, stream), "copy");
+        check(cudaStreamSynchronize(stream), "device allocation");
+        copyParallel(arena.base(), image_.get(), filled_, cudaMemcpyHostToDevice);
         if (arena.bytes() > filled_)
             check(cudaMemsetAsync(static_cast<char *>(arena.base()) + filled_, 0, arena.bytes() - filled_, stream),
                   "memset");

@@ -475,9 +475,12 @@ def run_gb300(args) -> None:
     e2e_backend = lattice.make_gb300_lattice_backend(sched)
     t0 = time.perf_counter()
     e2e_backend.upload(e2e_state, settings, sphere)
+    t1 = time.perf_counter()
     e2e_st = e2e_backend.run(lattice.RunControl(max_steps=substeps_k))
+    t2 = time.perf_counter()
     e2e_backend.download(e2e_state)
     e2e_s = time.perf_counter() - t0
+    e2e_parts = {"upload_s": t1 - t0, "run_s": t2 - t1, "download_s": e2e_s - (t2 - t0)}
     e2e_proj = ITERATIONS * (b - e2e_st.broken_bonds) * substeps_k
     e2e_s_max = max_over_ranks(e2e_s, dist, torch)
     e2e_total = sum_over_ranks(float(e2e_proj), dist, torch)
@@ -504,7 +507,7 @@ def run_gb300(args) -> None:
                    "live_bonds_end": live_end, "broken_in_window": st.broken_bonds - before.broken_bonds},
         "e2e": {"value": e2e_total / e2e_s_max, "unit": "projections/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps,
-                "note": "one upload of the host LatticeState, K steps, one download; wall clock"},
+                "note": "one upload of the host LatticeState, K steps, one download; wall clock", **e2e_parts},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind, "kernel": "kSolve (projection sweep)",
                      "sweep_ms_per_substep": sweep_ms, "whole_substep_gbs": total_gbs,
