@@ -467,6 +467,11 @@ def run_gb300(args) -> None:
     algo = bytes_per_substep(n, b, plastic)
     peak, peak_kind = peaks()
     achieved = algo["sweep"] / (sweep_ms * 1e-3) / 1e9
+    # DRAM bytes of one substep's sweep (its 116 level launches), measured by
+    # ncu (dram__bytes_read.sum + dram__bytes_write.sum, warm caches) on the
+    # impact workload at 128x64x64 (4,616,704 bonds): 759.26 MB, scaled here by
+    # bonds (the traffic grows with the bonds processed).
+    traffic = 759.26e6 * b / 4616704.0 if args.workload.startswith("impact") else None
     sub_per_s = substeps_k / device_s
     total_gbs = algo["total"] * sub_per_s / 1e9
 
@@ -509,7 +514,9 @@ def run_gb300(args) -> None:
                 "d2h_bytes_per_step": d2h // args.steps,
                 "note": "one upload of the host LatticeState, K steps, one download; wall clock", **e2e_parts},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "kSolve (projection sweep)",
+                     "traffic": traffic, "traffic_per": "substep sweep (bytes)",
+                     "algorithmic_bytes_per_substep_sweep": algo["sweep"],
+                     "peak_kind": peak_kind, "kernel": "kSolve (projection sweep)",
                      "sweep_ms_per_substep": sweep_ms, "whole_substep_gbs": total_gbs,
                      "whole_substep_frac": total_gbs / peak},
         "gpu_launches": launches * substeps_k,
