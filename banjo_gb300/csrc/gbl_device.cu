@@ -1279,11 +1279,20 @@ private:
             check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
         }
         mark(4);
-        if (M && whole_.count) launchSweepWhole(whole_);
+        // The small lattices of a batch sweep whole, one CTA each, on the
+        // second stream beside the level launches of the others.
+        const bool whole = M && whole_.count;
+        if (whole) {
+            check(cudaEventRecord(fork_, st), "event");
+            check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
+            launchSweepWhole(whole_, side_);
+            check(cudaEventRecord(join_, side_), "event");
+        }
         const unsigned I = S.iterations;
         for (unsigned it = 0; it < I; ++it) {
             const bool first = it == 0, last = it + 1 == I;
             for (const Span &lv : levels_) launchSolve<M>(lv, first, last);
+            if (whole && it + 1 == I) check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
             mark(5);
             if (S.plane_count && isolated_.count)
                 kSupportIsolated<R, M><<<isolated_.count, kThreads, 0, st>>>(grid(isolated_), S);
@@ -1349,16 +1358,16 @@ private:
         check(cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...), "kernel launch");
     }
 
-    void launchSweepWhole(const Span &span) {
+    void launchSweepWhole(const Span &span, cudaStream_t st) {
         const bool support = S_.plane_count != 0;
         const int key = (plastic_ ? 2 : 0) | (support ? 1 : 0);
         const Grid<R> g = grid(span);
         const unsigned smem = 0;
         switch (key) {
-        case 0: kSweepLattice<R, kDirect, false, false><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
-        case 1: kSweepLattice<R, kDirect, false, true><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
-        case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
-        default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, stream_>>>(g, S_); break;
+        case 0: kSweepLattice<R, kDirect, false, false><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
+        case 1: kSweepLattice<R, kDirect, false, true><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
+        case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
+        default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
         }
     }
 

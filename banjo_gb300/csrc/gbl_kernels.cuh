@@ -1029,10 +1029,20 @@ __global__ void __launch_bounds__(kThreads, GBL_SOLVE_MIN_BLOCKS) kSolve(const G
 // L2 (and the SM's L1) across all its levels instead of being streamed from
 // HBM again at every level launch; the arithmetic and the per-node order are
 // those of the level launches.
-constexpr unsigned kSweepThreads = 512;
+#ifndef GBL_SWEEP_THREADS
+#define GBL_SWEEP_THREADS 512
+#endif
+#ifndef GBL_SWEEP_MIN_BLOCKS
+#define GBL_SWEEP_MIN_BLOCKS 2
+#endif
+constexpr unsigned kSweepThreads = GBL_SWEEP_THREADS;
 constexpr unsigned kSweepSlots = kSweepThreads * kSolvePer;
 constexpr std::uint32_t kMaxFusedLevels = 1024;
-constexpr std::uint32_t kMaxFusedBonds = 1U << 21;
+// A lattice's one-CTA sweep takes as long as its bonds over one CTA's rate, so
+// only lattices small enough to finish well within the batch's level launches
+// are swept whole (measured: a 48^3 trial alone in one CTA bounded the whole
+// batch's sweep).
+constexpr std::uint32_t kMaxFusedBonds = 1U << 18;
 
 template <class R, bool Support>
 __device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Settings<R> &S) {
@@ -1047,7 +1057,7 @@ __device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Sett
 }
 
 template <class R, bool Direct, bool Plastic, bool Support>
-__global__ void __launch_bounds__(kSweepThreads, 2) kSweepLattice(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kSweepThreads, GBL_SWEEP_MIN_BLOCKS) kSweepLattice(const Grid<R> launch, Settings<R> S) {
     // The lattice's descriptor, copied once into shared memory: its fields
     // are read throughout the sweep, and shared memory is never written by
     // the sweep's global stores, so the compiler may keep them as it likes.
@@ -1062,44 +1072,76 @@ __global__ void __launch_bounds__(kSweepThreads, 2) kSweepLattice(const Grid<R> 
     const Dev<R> &L = *reinterpret_cast<const Dev<R> *>(desc);
     if (L.ctl->stop) return;
     const unsigned I = S.iterations;
-    for (unsigned it = 0; it < I; ++it) {
-        const bool first = it == 0, last = it + 1 == I;
-        for (std::uint32_t lv = 0; lv < L.level_count; ++lv) {
-            const std::uint32_t end = L.level_begin[lv + 1];
-            for (std::uint32_t base = L.level_begin[lv]; base < end; base += kSweepSlots) {
-                BondRec<R> rec[kSolvePer];
-                Q4<R> geo[kSolvePer], qa[kSolvePer], qb[kSolvePer];
-                R lam[kSolvePer], pl[kSolvePer];
-                std::uint32_t at[kSolvePer];
-                bool live[kSolvePer];
-#pragma unroll
-                for (int k = 0; k < kSolvePer; ++k) {
-                    at[k] = base + threadIdx.x + static_cast<std::uint32_t>(k) * kSweepThreads;
-                    if (at[k] < end) {
-                        rec[k] = ldStream(L.rec + at[k]);
-                        geo[k] = ldStream(L.geo + at[k]);
-                        lam[k] = first ? R(0) : __ldcs(L.lambda + at[k]);
-                        pl[k] = Plastic ? L.plastic[at[k]].x : R(0);
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < kSolvePer; ++k) {
-                    live[k] = at[k] < end && !(rec[k].a & kDeadBit);
-                    if (live[k]) {
-                        qa[k] = ldShared(L.u + endA(rec[k]));
-                        qb[k] = ldShared(L.u + endB(rec[k]));
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < kSolvePer; ++k)
-                    if (at[k] < end)
-                        finishBond<R, Direct, Plastic, Support>(L, S, at[k], rec[k], live[k], geo[k], lam[k],
-                                                                pl[k], last, qa[k], qb[k]);
-            }
-            __syncthreads();
+    // One bond per thread per round; the rounds of the whole sweep in order
+    // (iteration, level, base). The next round's streamed data (record,
+    // geometry, multiplier, plastic extension: nothing the node updates
+    // touch) is loaded before the current round's node gathers, so two
+    // rounds' memory traffic is in flight. A round's multipliers are written
+    // one iteration before the round reads them, except in a sweep of one
+    // round per iteration, whose next round is itself: there they are loaded
+    // after the write.
+    struct Round {
+        unsigned it;
+        std::uint32_t lv, base;
+    };
+    struct Streamed {
+        BondRec<R> rec;
+        Q4<R> geo;
+        R lam, pl;
+    };
+    auto advance = [&](Round &r) {
+        r.base += kSweepThreads;
+        if (r.base < L.level_begin[r.lv + 1]) return true;
+        if (++r.lv == L.level_count) {
+            r.lv = 0;
+            if (++r.it == I) return false;
         }
-        supportIsolatedInCta<R, Support>(L, S);
-        __syncthreads();
+        r.base = L.level_begin[r.lv];
+        return true;
+    };
+    const bool self_next = L.level_count == 1 && L.level_begin[1] - L.level_begin[0] <= kSweepThreads;
+    auto load = [&](const Round &r, Streamed &x) {
+        const std::uint32_t d = r.base + threadIdx.x;
+        if (d < L.level_begin[r.lv + 1]) {
+            x.rec = ldStream(L.rec + d);
+            x.geo = ldStream(L.geo + d);
+            x.lam = (r.it == 0 || self_next) ? R(0) : __ldcs(L.lambda + d);
+            x.pl = Plastic ? L.plastic[d].x : R(0);
+        }
+    };
+    Round cur{0, 0, L.level_begin[0]};
+    Streamed now{}, next{};
+    load(cur, now);
+    for (;;) {
+        Round nxt = cur;
+        const bool more = advance(nxt);
+        if (more) load(nxt, next);
+        const std::uint32_t end = L.level_begin[cur.lv + 1];
+        const std::uint32_t d = cur.base + threadIdx.x;
+        if (d < end) {
+            if (self_next && cur.it != 0) now.lam = __ldcs(L.lambda + d);
+            const bool live = !(now.rec.a & kDeadBit);
+            Q4<R> qa{}, qb{};
+            if (live) {
+                qa = ldShared(L.u + endA(now.rec));
+                qb = ldShared(L.u + endB(now.rec));
+            }
+            finishBond<R, Direct, Plastic, Support>(L, S, d, now.rec, live, now.geo, now.lam, now.pl,
+                                                    cur.it + 1 == I, qa, qb);
+        }
+        if (!more) {
+            supportIsolatedInCta<R, Support>(L, S);
+            break;
+        }
+        if (nxt.lv != cur.lv || nxt.it != cur.it) {
+            __syncthreads();
+            if (nxt.it != cur.it) {
+                supportIsolatedInCta<R, Support>(L, S);
+                __syncthreads();
+            }
+        }
+        cur = nxt;
+        now = next;
     }
 }
 
