@@ -299,9 +299,7 @@ __device__ __forceinline__ V3<R> bondVector(const Dev<R> &L, std::uint32_t a, st
 
 template <class R, bool Direct>
 __device__ void sampleBond(const Dev<R> &L, std::uint32_t a, std::uint32_t b, const BondRec<R> &rec, V3<R> edge,
-                           R &t, R &c, R &s) {
-    const V3<R> delta = bondVector<R, Direct>(L, a, b, edge);
-    const R len = length(delta);
+                           R len, R &t, R &c, R &s) {
     const R rest = rec.rest;
     R stretch;
     if (Direct) {
@@ -337,7 +335,9 @@ __device__ __forceinline__ void startSample(const Dev<R> &L, std::uint32_t j) {
     if (rec.a & kDeadBit) return;
     const Q4<R> g = L.geo[j];
     R t, c, s;
-    sampleBond<R, Direct>(L, endA(rec), endB(rec), rec, V3<R>{g.x, g.y, g.z}, t, c, s);
+    const V3<R> edge{g.x, g.y, g.z};
+    const R len = length(bondVector<R, Direct>(L, endA(rec), endB(rec), edge));
+    sampleBond<R, Direct>(L, endA(rec), endB(rec), rec, edge, len, t, c, s);
     Q4<R> p = L.prev[j];
     p.x = maxR(R(0), t);
     p.y = maxR(R(0), c);
@@ -1251,7 +1251,16 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
         if (late != (part == 2)) return;
     }
     const std::uint32_t j = w.begin + threadIdx.x; // storage index; items start on multiples of 256
+    // A bond can raise the run's damage maximum only if it exceeds the maximum
+    // as the substep began (CpuLatticeBackend.cpp:462-465); the bound is formed
+    // once per CTA.
+    __shared__ double damage_floor;
+    __shared__ int any_work;
     if (threadIdx.x < 4) peak[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        damage_floor = L.ctl->max_damage + 1.0e-6;
+        any_work = 0;
+    }
     __syncthreads();
     double plastic_work = 0.0;
     if (j < w.end) {
@@ -1262,11 +1271,14 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
             const V3<R> edge{g.x, g.y, g.z};
             float plastic_stretch = 0.0F;
             R pext = R(0);
+            // The bond's current length, used by the plastic return, the
+            // sample and the stored energy of a failure alike.
+            const R len = length(bondVector<R, Direct>(L, a, b, edge));
             if (Plastic) {
                 Q2<R> pl = L.plastic[j];
                 pext = pl.x;
                 if (S.yield_stretch > R(0)) {
-                    const R elastic = length(bondVector<R, Direct>(L, a, b, edge)) - rec.rest - pl.x;
+                    const R elastic = len - rec.rest - pl.x;
                     const R magnitude = absR(elastic);
                     const R h = S.hardening;
                     const R yield = S.yield_stretch * rec.rest + h * pl.y;
@@ -1286,7 +1298,7 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
                 }
             }
             R t, c, s;
-            sampleBond<R, Direct>(L, a, b, rec, edge, t, c, s);
+            sampleBond<R, Direct>(L, a, b, rec, edge, len, t, c, s);
             Q4<R> pv = L.prev[j];
             const R pt = maxR(R(0), maxR(pv.x, t));
             const R pc = maxR(R(0), maxR(pv.y, c));
@@ -1314,7 +1326,7 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
                 const R cc = g.w;
                 R energy = R(0);
                 if (!(cc <= R(0))) {
-                    const R ext = length(bondVector<R, Direct>(L, a, b, edge)) - rec.rest - pext;
+                    const R ext = len - rec.rest - pext;
                     energy = R(0.5) * ext * ext / cc;
                 }
                 L.rec[j].a = rec.a | kDeadBit;
@@ -1324,9 +1336,7 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
                 L.ev_ends[js] = make_uint2(a, b);
                 atomicOr(L.ev_bits + (js >> 5), 1U << (js & 31U));
             }
-            // A bond can raise the run's damage maximum only if it exceeds the
-            // maximum as the substep began (CpuLatticeBackend.cpp:462-465).
-            if (static_cast<double>(dmg) > L.ctl->max_damage + 1.0e-6) {
+            if (static_cast<double>(dmg) > damage_floor) {
                 L.ev_damage[js] = dmg;
                 atomicOr(L.dmg_bits + (js >> 5), 1U << (js & 31U));
             }
@@ -1337,13 +1347,19 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
             if (Plastic && S.yield_stretch > R(0)) atomicMax(&peak[3], floatBits(plastic_stretch));
         }
     }
+    // Fixed-order sums of the plastic work; a sum of zeros is +0 whichever
+    // way it is formed, so all-zero warps and tiles skip the FP64 adds.
     double warp_work = 0.0;
-    if (Plastic) warp_work = warpSumFixed(plastic_work);
+    if (Plastic && __any_sync(0xffffffffU, plastic_work != 0.0)) {
+        warp_work = warpSumFixed(plastic_work);
+        if ((threadIdx.x & 31) == 0) any_work = 1;
+    }
     if ((threadIdx.x & 31) == 0) tile_work[threadIdx.x / 32] = warp_work;
     __syncthreads();
     if (threadIdx.x == 0) {
         double wsum = 0.0;
-        for (int q = 0; q < kThreads / 32; ++q) wsum += tile_work[q];
+        if (any_work)
+            for (int q = 0; q < kThreads / 32; ++q) wsum += tile_work[q];
         L.tile_plastic[w.begin / kThreads] = wsum;
         if (peak[0]) atomicMax(&L.ctl->max_t, peak[0]);
         if (peak[1]) atomicMax(&L.ctl->max_c, peak[1]);
