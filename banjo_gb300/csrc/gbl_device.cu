@@ -1181,10 +1181,6 @@ private:
         // With many lattices, the small ones sweep in one CTA each (largest first);
         // the level launches and the isolated-node launch cover the others.
         auto leveled = [this](const Res &l) { return !many_ || !sweptWhole(l); };
-        isolated_ = span([&](const Res &l, U &b, U &e) {
-            b = 0;
-            e = leveled(l) ? static_cast<U>(l.isolated.size()) : 0U;
-        }, kThreads);
         {
             std::vector<std::uint32_t> whole;
             if (many_)
@@ -1205,16 +1201,51 @@ private:
             const U count = static_cast<U>(all.size()) - first;
             broken_ = Span{first, count, 0, count, 1};
         }
-        std::size_t deepest = 0;
-        for (auto k : active_)
-            if (leveled(*slots_[k])) deepest = std::max(deepest, slots_[k]->levels.size());
-        levels_.clear();
-        for (std::size_t d = 0; d < deepest; ++d)
-            levels_.push_back(span([&](const Res &l, U &b, U &e) {
-                const bool in = leveled(l) && d < l.levels.size();
-                b = in ? l.levels[d].begin : 0;
-                e = in ? l.levels[d].end : 0;
-            }, kThreads * kSolvePer));
+        // The level-launched lattices in groups whose node arrays fit in L2
+        // together: a group runs its whole sweep (every iteration, every
+        // level) before the next, so its nodes stay resident across levels.
+        groups_.clear();
+        {
+            std::vector<std::vector<U>> members(1);
+            std::size_t bytes = 0;
+            for (auto k : active_) {
+                const Res &l = *slots_[k];
+                if (!leveled(l)) continue;
+                const std::size_t need = static_cast<std::size_t>(l.N) * sizeof(Q4<R>);
+                if (!members.back().empty() && bytes + need > kGroupNodeBytes) {
+                    members.emplace_back();
+                    bytes = 0;
+                }
+                members.back().push_back(k);
+                bytes += need;
+            }
+            for (const auto &ids : members) {
+                if (ids.empty()) continue;
+                auto over = [&](auto &&bounds, U per) {
+                    const U first = static_cast<U>(all.size());
+                    U b0 = 0, e0 = 0;
+                    bool lead = true;
+                    for (auto k : ids) {
+                        U b = 0, e = 0;
+                        bounds(*slots_[k], b, e);
+                        if (lead) { b0 = b; e0 = e; lead = false; }
+                        ranges(k, b, e, per);
+                    }
+                    return Span{first, static_cast<U>(all.size()) - first, b0, e0, per};
+                };
+                Group g;
+                std::size_t deepest = 0;
+                for (auto k : ids) deepest = std::max(deepest, slots_[k]->levels.size());
+                for (std::size_t d = 0; d < deepest; ++d)
+                    g.levels.push_back(over([&](const Res &l, U &b, U &e) {
+                        b = d < l.levels.size() ? l.levels[d].begin : 0;
+                        e = d < l.levels.size() ? l.levels[d].end : 0;
+                    }, kThreads * kSolvePer));
+                g.isolated = over([](const Res &l, U &b, U &e) { b = 0; e = static_cast<U>(l.isolated.size()); },
+                                  kThreads);
+                groups_.push_back(std::move(g));
+            }
+        }
         if (all.size() > work_cap_) {
             if (work_) cudaFree(work_);
             work_cap_ = std::max<std::size_t>(all.size(), 2 * work_cap_);
@@ -1289,21 +1320,26 @@ private:
             check(cudaEventRecord(join_, side_), "event");
         }
         const unsigned I = S.iterations;
-        for (unsigned it = 0; it < I; ++it) {
-            const bool first = it == 0, last = it + 1 == I;
-            for (const Span &lv : levels_) launchSolve<M>(lv, first, last);
-            if (whole && it + 1 == I) check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
+        for (const Group &g : groups_)
+            for (unsigned it = 0; it < I; ++it) {
+                const bool first = it == 0, last = it + 1 == I;
+                for (const Span &lv : g.levels) launchSolve<M>(lv, first, last, g.levels.size() >= 2);
+                mark(5);
+                if (S.plane_count && g.isolated.count)
+                    kSupportIsolated<R, M><<<g.isolated.count, kThreads, 0, st>>>(grid(g.isolated), S);
+                mark(7);
+            }
+        if (whole) {
+            check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
             mark(5);
-            if (S.plane_count && isolated_.count)
-                kSupportIsolated<R, M><<<isolated_.count, kThreads, 0, st>>>(grid(isolated_), S);
-            mark(7);
         }
         if (nodes_.count)
             kVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S, S.damping_fraction <= R(0) ? 1 : 0);
         mark(8);
         if (S.damping_fraction > R(0)) {
-            for (const Span &lv : levels_)
-                if (lv.count) kDamp<R, M, kDirect><<<lv.count, kThreads, 0, st>>>(grid(lv), S.damping_fraction);
+            for (const Group &g : groups_)
+                for (const Span &lv : g.levels)
+                    if (lv.count) kDamp<R, M, kDirect><<<lv.count, kThreads, 0, st>>>(grid(lv), S.damping_fraction);
             if (nodes_.count) kSupportVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
             mark(9);
         }
@@ -1340,8 +1376,8 @@ private:
     // must be complete -- with a single level that writer would be the very
     // kernel it overlaps.
     template <class... P, class... A>
-    void launchOverlapped(void (*kernel)(P...), unsigned blocks, unsigned threads, A &&...args) {
-        if (levels_.size() < 2) {
+    void launchOverlapped(bool overlap, void (*kernel)(P...), unsigned blocks, unsigned threads, A &&...args) {
+        if (!overlap) {
             kernel<<<blocks, threads, 0, stream_>>>(std::forward<A>(args)...);
             return;
         }
@@ -1396,13 +1432,14 @@ private:
         }
     }
 
-    template <bool M> void launchSolve(const Span &lv, bool first, bool last) {
+    template <bool M> void launchSolve(const Span &lv, bool first, bool last, bool overlap) {
         if (!lv.count) return;
         const bool support = S_.plane_count != 0;
         const int key = (first ? 8 : 0) | (last ? 4 : 0) | (plastic_ ? 2 : 0) | (support ? 1 : 0);
 #define GBL_SOLVE(K)                                                                                                \
     case K:                                                                                                         \
-        launchOverlapped(kSolve<R, M, kDirect, ((K) & 8) != 0, ((K) & 4) != 0, ((K) & 2) != 0, ((K) & 1) != 0>,     \
+        launchOverlapped(overlap,                                                                                   \
+                         kSolve<R, M, kDirect, ((K) & 8) != 0, ((K) & 4) != 0, ((K) & 2) != 0, ((K) & 1) != 0>,     \
                          lv.count, kThreads, grid(lv), S_);                                                         \
         break;
         switch (key) {
@@ -1426,8 +1463,16 @@ private:
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
     Work *work_{};
-    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, isolated_{}, broken_{}, whole_{};
-    std::vector<Span> levels_;
+    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{};
+    // Level-launched lattices, in groups swept one after another.
+    struct Group {
+        std::vector<Span> levels;
+        Span isolated{};
+    };
+    std::vector<Group> groups_;
+    // Node bytes a group may hold: its node arrays stay in the 129 MB L2
+    // beside the streamed bond records of a level.
+    static constexpr std::size_t kGroupNodeBytes = std::size_t(48) << 20;
     cudaStream_t own_stream_{}, stream_{}, side_{};
     cudaEvent_t ev0_{}, ev1_{}, fork_{}, join_{};
     cudaGraph_t graph_{};
