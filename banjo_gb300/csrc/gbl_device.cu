@@ -152,6 +152,68 @@ struct Frame {
     gbl_sphere sphere;
 };
 
+// The device arrays a download reads, copied raw (device layout, storage
+// order), and the permutation back to schedule order: a finished lattice's
+// device memory can be freed at once and the conversion to the state layout
+// done later, off the stepping thread.
+template <class R> struct RawState {
+    std::uint32_t N{}, B{};
+    std::unique_ptr<unsigned char[]> bytes;
+    std::size_t capacity{};
+    Q4<R> *u{}, *up{}, *v{};
+    BondRec<R> *rec{};
+    Q4<R> *prev{};
+    Q2<R> *plastic{};
+    std::uint8_t *mode{};
+    std::vector<std::uint32_t> dev2sched;
+
+    static std::size_t need(std::uint32_t n, std::uint32_t b) {
+        return 3 * static_cast<std::size_t>(n) * sizeof(Q4<R>) +
+               static_cast<std::size_t>(b) * (sizeof(BondRec<R>) + sizeof(Q4<R>) + sizeof(Q2<R>) + 1) + 64;
+    }
+    // Carves the buffer (kept if large enough) for n nodes and b bonds.
+    void shape(std::uint32_t n, std::uint32_t b) {
+        N = n;
+        B = b;
+        const std::size_t want = need(n, b);
+        if (capacity < want) {
+            bytes.reset(new unsigned char[want]);
+            capacity = want;
+        }
+        unsigned char *p = bytes.get();
+        auto take = [&](auto *&ptr, std::size_t count) {
+            using T = std::remove_reference_t<decltype(*ptr)>;
+            p = reinterpret_cast<unsigned char *>((reinterpret_cast<std::uintptr_t>(p) + alignof(T) - 1) &
+                                                  ~(static_cast<std::uintptr_t>(alignof(T)) - 1));
+            ptr = reinterpret_cast<T *>(p);
+            p += count * sizeof(T);
+        };
+        take(u, n); take(up, n); take(v, n); take(rec, b); take(prev, b); take(plastic, b); take(mode, b);
+    }
+
+    // download's conversion (WorkingLattice::toState, LatticeWorking.hpp:126-142).
+    void writeState(gbl_state_view &st) const {
+        if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
+        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t i = lo; i < hi; ++i) {
+                st.u[3 * i] = u[i].x; st.u[3 * i + 1] = u[i].y; st.u[3 * i + 2] = u[i].z;
+                st.u_prev[3 * i] = up[i].x; st.u_prev[3 * i + 1] = up[i].y; st.u_prev[3 * i + 2] = up[i].z;
+                st.v[3 * i] = v[i].x; st.v[3 * i + 1] = v[i].y; st.v[3 * i + 2] = v[i].z;
+            }
+        });
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t dd = lo; dd < hi; ++dd) {
+                const std::uint32_t j = dev2sched[dd];
+                st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
+                st.failure_mode[j] = mode[dd];
+                st.damage[j] = prev[dd].w;
+                st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
+                st.plastic_extension[j] = plastic[dd].x; st.plastic_strain[j] = plastic[dd].y;
+            }
+        });
+    }
+};
+
 // One lattice resident on the device.
 template <class R> struct Resident {
     static constexpr bool kDirect = std::is_same<R, double>::value;
@@ -558,31 +620,26 @@ template <class R> struct Resident {
         ext_dirty = true;
     }
 
+    // The device arrays a download needs, raw, into `raw` (its buffer reused
+    // when large enough); the permutation is copied.
+    void copyRaw(RawState<R> &raw) const {
+        raw.shape(N, B);
+        copyParallel(raw.u, dev.u, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
+        copyParallel(raw.up, dev.up, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
+        copyParallel(raw.v, dev.v, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
+        copyParallel(raw.rec, dev.rec, sizeof(BondRec<R>) * B, cudaMemcpyDeviceToHost);
+        copyParallel(raw.prev, dev.prev, sizeof(Q4<R>) * B, cudaMemcpyDeviceToHost);
+        copyParallel(raw.plastic, dev.plastic, sizeof(Q2<R>) * B, cudaMemcpyDeviceToHost);
+        copyParallel(raw.mode, dev.mode, B, cudaMemcpyDeviceToHost);
+        raw.dev2sched = dev2sched;
+    }
+
     // download (WorkingLattice::toState, LatticeWorking.hpp:126-142)
     void download(gbl_state_view &st, gbl_sphere *sphere) {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
-        const auto u = fetch(dev.u, N), up = fetch(dev.up, N), v = fetch(dev.v, N);
-        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t i = lo; i < hi; ++i) {
-                st.u[3 * i] = u[i].x; st.u[3 * i + 1] = u[i].y; st.u[3 * i + 2] = u[i].z;
-                st.u_prev[3 * i] = up[i].x; st.u_prev[3 * i + 1] = up[i].y; st.u_prev[3 * i + 2] = up[i].z;
-                st.v[3 * i] = v[i].x; st.v[3 * i + 1] = v[i].y; st.v[3 * i + 2] = v[i].z;
-            }
-        });
-        const auto rec = fetch(dev.rec, B);
-        const auto prev = fetch(dev.prev, B);
-        const auto pl = fetch(dev.plastic, B);
-        const auto mode = fetch(dev.mode, B);
-        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t dd = lo; dd < hi; ++dd) {
-                const std::uint32_t j = dev2sched[dd];
-                st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
-                st.failure_mode[j] = mode[dd];
-                st.damage[j] = prev[dd].w;
-                st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
-                st.plastic_extension[j] = pl[dd].x; st.plastic_strain[j] = pl[dd].y;
-            }
-        });
+        RawState<R> raw;
+        copyRaw(raw);
+        raw.writeState(st);
         if (sphere) *sphere = fetchSphere();
     }
 
@@ -1588,32 +1645,6 @@ private:
 // frees their memory for the next in line. Each request's result is the one it
 // would get alone: lattices never interact, and each keeps its own control
 // block and ledgers.
-struct ResultBuffers {
-    std::vector<double> u, u_prev, v, damage, prev_t, prev_c, prev_s, plastic_e, plastic_s;
-    std::vector<std::uint8_t> alive, mode;
-    gbl_state_view view(std::uint32_t n, std::uint32_t b) {
-        u.resize(3 * static_cast<std::size_t>(n)); u_prev.resize(u.size()); v.resize(u.size());
-        damage.resize(b); prev_t.resize(b); prev_c.resize(b); prev_s.resize(b); plastic_e.resize(b);
-        plastic_s.resize(b); alive.resize(b); mode.resize(b);
-        gbl_state_view w{};
-        w.node_count = n;
-        w.bond_count = b;
-        w.u = u.data(); w.u_prev = u_prev.data(); w.v = v.data();
-        w.alive = alive.data(); w.failure_mode = mode.data(); w.damage = damage.data();
-        w.prev_tensile = prev_t.data(); w.prev_compressive = prev_c.data(); w.prev_shear = prev_s.data();
-        w.plastic_extension = plastic_e.data(); w.plastic_strain = plastic_s.data();
-        return w;
-    }
-    void copyTo(gbl_state_view &out) const {
-        auto put = [](auto *dst, const auto &src) {
-            if (dst && !src.empty()) std::memcpy(dst, src.data(), sizeof(src[0]) * src.size());
-        };
-        put(out.u, u); put(out.u_prev, u_prev); put(out.v, v); put(out.alive, alive); put(out.failure_mode, mode);
-        put(out.damage, damage); put(out.prev_tensile, prev_t); put(out.prev_compressive, prev_c);
-        put(out.prev_shear, prev_s); put(out.plastic_extension, plastic_e); put(out.plastic_strain, plastic_s);
-    }
-};
-
 class ServerBase {
 public:
     virtual ~ServerBase() = default;
@@ -1668,7 +1699,9 @@ public:
             c.calm_damage_margin = 0.5;
             c.max_steps = substeps;
             const double before = kernelSeconds();
+            const double t0 = clock();
             engine_.run(c);
+            run_seconds_ += clock() - t0;
             device_seconds_ += kernelSeconds() - before;
             substeps_run_ += substeps;
             retireFinished();
@@ -1692,18 +1725,24 @@ public:
     }
 
     void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) override {
-        std::lock_guard<std::mutex> lock(mutex_);
-        Request &q = find(ticket);
-        if (q.phase != GBL_REQUEST_DONE) invalid("the request has not finished");
-        if (st) {
-            if (st->node_count != q.nodes || st->bond_count != q.bonds)
+        RawState<R> raw;
+        {
+            std::lock_guard<std::mutex> lock(mutex_);
+            Request &q = find(ticket);
+            if (q.phase != GBL_REQUEST_DONE) invalid("the request has not finished");
+            if (st && (st->node_count != q.nodes || st->bond_count != q.bonds))
                 invalid("result state does not match the request's lattice");
-            q.result.copyTo(*st);
+            if (sp) *sp = q.sphere;
+            if (status) *status = q.status;
+            raw = std::move(q.raw);
+            requests_.erase(ticket);
+            --done_;
         }
-        if (sp) *sp = q.sphere;
-        if (status) *status = q.status;
-        requests_.erase(ticket);
-        --done_;
+        // The conversion to the state layout runs on the caller's thread,
+        // outside the lock; the buffer then goes back to the pool.
+        if (st) raw.writeState(*st);
+        std::lock_guard<std::mutex> lock(mutex_);
+        if (pool_.size() < kPoolSize) pool_.push_back(std::move(raw));
     }
 
     void cancel(std::uint64_t ticket) override {
@@ -1719,6 +1758,7 @@ public:
         } else {
             if (q.phase == GBL_REQUEST_DONE) --done_;
         }
+        if (q.phase == GBL_REQUEST_DONE && pool_.size() < kPoolSize) pool_.push_back(std::move(q.raw));
         requests_.erase(ticket);
     }
 
@@ -1738,6 +1778,9 @@ private:
         o.substeps_run = substeps_run_;
         o.device_seconds = device_seconds_;
         o.clock_s = clock() - t0_;
+        o.admit_seconds = admit_seconds_;
+        o.retire_seconds = retire_seconds_;
+        o.run_seconds = run_seconds_;
     }
 
     struct Request {
@@ -1749,7 +1792,7 @@ private:
         std::size_t slot{};
         double submitted{-1}, admitted{-1}, finished{-1};
         gbl_run_status status{};
-        ResultBuffers result;
+        RawState<R> raw;
     };
 
     static double clock() {
@@ -1771,6 +1814,11 @@ private:
 
     // Arrival order, while the next request fits what is left of the budget.
     void admit() {
+        const double t0 = clock();
+        admitQueued();
+        admit_seconds_ += clock() - t0;
+    }
+    void admitQueued() {
         while (!queue_.empty()) {
             Request &q = requests_.at(queue_.front());
             if (used_ + q.bytes > budget_) break;
@@ -1787,14 +1835,31 @@ private:
     }
 
     void retireFinished() {
+        const double t0 = clock();
+        retireDone();
+        retire_seconds_ += clock() - t0;
+    }
+    void retireDone() {
         for (std::size_t k = 0; k < engine_.slots(); ++k) {
             if (!engine_.occupied(k)) continue;
             const Ctl &c = engine_.control(k);
             if (!(c.step_limit != 0 && c.total_steps >= c.step_limit) && c.exit_reason == 0) continue;
             Request &q = requests_.at(slot_ticket_[k]);
             Resident<R> &l = engine_.lattice(k);
-            gbl_state_view out = q.result.view(l.N, l.B);
-            engine_.download(k, out, &q.sphere);
+            // The raw device arrays only: the conversion waits for take().
+            if (!pool_.empty()) {
+                std::size_t best = pool_.size();
+                for (std::size_t p = 0; p < pool_.size(); ++p)
+                    if (pool_[p].capacity >= RawState<R>::need(l.N, l.B) &&
+                        (best == pool_.size() || pool_[p].capacity < pool_[best].capacity))
+                        best = p;
+                if (best < pool_.size()) {
+                    q.raw = std::move(pool_[best]);
+                    pool_.erase(pool_.begin() + static_cast<std::ptrdiff_t>(best));
+                }
+            }
+            l.copyRaw(q.raw);
+            q.sphere = l.fetchSphere();
             q.status = l.status;
             q.status.exit_reason = c.exit_reason;
             q.done_steps = c.total_steps;
@@ -1810,11 +1875,14 @@ private:
     Engine<R> engine_;
     std::uint64_t budget_, used_{0}, last_ticket_{0};
     std::uint64_t queued_{0}, running_{0}, done_{0}, substeps_run_{0};
-    double device_seconds_{0};
+    double device_seconds_{0}, admit_seconds_{0}, retire_seconds_{0}, run_seconds_{0};
     double t0_;
     std::map<std::uint64_t, Request> requests_;
     std::deque<std::uint64_t> queue_;
     std::vector<std::uint64_t> slot_ticket_;
+    // Host buffers of taken results, reused by the next retirements.
+    std::vector<RawState<R>> pool_;
+    static constexpr std::size_t kPoolSize = 16;
     std::mutex mutex_;
 };
 

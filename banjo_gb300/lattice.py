@@ -135,7 +135,8 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("queued", C.c_uint64), ("running", C.c_uint64), ("done", C.c_uint64), ("bytes_in_use", C.c_uint64),
                 ("budget_bytes", C.c_uint64), ("substeps_run", C.c_uint64), ("device_seconds", C.c_double),
-                ("clock_s", C.c_double)]
+                ("clock_s", C.c_double), ("admit_seconds", C.c_double), ("retire_seconds", C.c_double),
+                ("run_seconds", C.c_double)]
 
 
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE = 0, 1, 2

@@ -288,11 +288,15 @@ def served_leg(args, lattice) -> dict:
     producer = threading.Thread(target=produce)
     producer.start()
     done, latency, wait, proj = set(), {}, {}, 0.0
-    sizes = {}
+    steps, step_s, poll_s = 0, 0.0, 0.0
     while len(done) < arrivals.size:
+        t0 = time.perf_counter()
         st = server.step(args.served_chunk)
+        step_s += time.perf_counter() - t0
+        steps += 1
         if st.running == 0 and st.queued == 0:
             time.sleep(0.0005)  # nothing admitted yet: wait for the next arrival
+        t0 = time.perf_counter()
         for i, t in enumerate(tickets):
             if t is None or i in done:
                 continue
@@ -305,6 +309,7 @@ def served_leg(args, lattice) -> dict:
                 b = picks[i][1].bond_count
                 proj += ITERATIONS * (b - st.broken_bonds) * horizon
                 done.add(i)
+        poll_s += time.perf_counter() - t0
         if not producer.is_alive() and all(t is not None for t in tickets) and len(done) == arrivals.size:
             break
     producer.join()
@@ -317,6 +322,8 @@ def served_leg(args, lattice) -> dict:
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "p50_admission_wait_s": float(np.percentile(wq, 50)), "p99_admission_wait_s": float(np.percentile(wq, 99)),
             "wall_s": wall, "device_s": stats.device_seconds, "budget_gb": args.served_budget_gb,
+            "steps": steps, "host_step_s": step_s, "host_poll_s": poll_s, "server_admit_s": stats.admit_seconds,
+            "server_retire_s": stats.retire_seconds, "server_run_s": stats.run_seconds,
             "chunk_substeps": args.served_chunk,
             "workload": f"Poisson arrivals at {args.served_rate:g}/s for {args.served_window:g} s; 90% drawn from "
                         f"{len(pool_small)} config-3 trials, 10% 128^3 lattices; {horizon} substeps each (a bounded "

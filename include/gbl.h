@@ -350,6 +350,9 @@ typedef struct gbl_server_stats {
     uint64_t substeps_run;  /* chunks stepped, in substeps */
     double device_seconds;  /* device time of the steps */
     double clock_s;
+    double admit_seconds;   /* host time admitting (device upload of prepared requests) */
+    double retire_seconds;  /* host time retiring (download of finished requests) */
+    double run_seconds;     /* host time of the stepping itself (graph rebuilds and launches included) */
 } gbl_server_stats;
 gbl_result gbl_serve_create(int precision, const gbl_step_settings *settings, uint64_t budget_bytes, gbl_server **out);
 void gbl_serve_destroy(gbl_server *server);
@@ -360,7 +363,9 @@ gbl_result gbl_serve_submit(gbl_server *server, const gbl_schedule_view *schedul
 gbl_result gbl_serve_step(gbl_server *server, uint64_t substeps, gbl_server_stats *stats);
 gbl_result gbl_serve_poll(gbl_server *server, uint64_t ticket, gbl_request_info *info);
 /* The finished request's state (arrays gbl_download writes), sphere and
- * RunStatus; the request is then forgotten. */
+ * RunStatus; the request is then forgotten. A finished request's device
+ * arrays were copied to host memory as it left the device; the conversion to
+ * the state layout runs here, on the calling thread (state may be null). */
 gbl_result gbl_serve_take(gbl_server *server, uint64_t ticket, gbl_state_view *state, gbl_sphere *sphere,
                           gbl_run_status *status);
 gbl_result gbl_serve_cancel(gbl_server *server, uint64_t ticket);
