@@ -574,51 +574,37 @@ __device__ __forceinline__ void contactApply(V3<R> imp, V3<R> r, R inm, R ism, R
     acc.impulse_z += static_cast<double>(imp.z);
 }
 
-// The contact gate: a candidate whose gap exceeds both the contact margin and
-// what its approach along the normal closes in one substep is left alone and
-// changes nothing (LatticePhysics.hpp:1338-1342).
+// A candidate against the current sphere state: 0 outside the contact gate
+// (LatticePhysics.hpp:1338-1342; nothing happens), 1 a graze (past the gate,
+// but no normal impulse and no position correction: it only raises the
+// penetration record), 2 a hit (it changes the node and the sphere). The
+// normal relative velocity and the normal impulse come back for the hit.
 template <class R>
-__device__ __forceinline__ bool contactGate(const Settings<R> &S, const Sphere<R> &sp, V3<R> nv, V3<R> r, V3<R> normal,
-                                            R gap) {
+__device__ __forceinline__ int contactProbe(const Settings<R> &S, const Sphere<R> &sp, V3<R> nv, V3<R> r,
+                                            V3<R> normal, R gap, R eff_n, bool correct, R &vn, R &ni) {
     const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
-    const R vn = dot(rel, normal);
-    return !(gap > maxR(S.c_margin, -vn * S.dt));
-}
-
-// Whether a candidate past the gate changes any state: a positive normal
-// impulse (which moves the node and the sphere), or in pass 2 a position
-// correction; the same expressions as contactChain.
-template <class R>
-__device__ __forceinline__ bool contactChanges(const Settings<R> &S, const Sphere<R> &sp, V3<R> nv, V3<R> r,
-                                               V3<R> normal, R gap, R eff_n, bool correct) {
-    const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
-    const R vn = dot(rel, normal);
+    vn = dot(rel, normal);
+    if (gap > maxR(S.c_margin, -vn * S.dt)) return 0;
     const R restitution = -vn > S.c_threshold ? S.c_restitution : R(0);
     const R desired = gap > S.c_margin ? -gap / S.dt : -restitution * minR(vn, R(0));
-    const R ni = maxR(R(0), (desired - vn) / eff_n);
-    return ni > R(0) || (correct && gap < -S.c_margin);
+    ni = maxR(R(0), (desired - vn) / eff_n);
+    return (ni > R(0) || (correct && gap < -S.c_margin)) ? 2 : 1;
 }
 
-// The contact of one staged candidate, from its relative velocity on
-// (LatticePhysics.hpp:1338-1386). `max_pen` shadows acc.max_penetration in R:
-// the ledger only ever holds a widened R, so the comparison is the reference's.
+// The contact of one staged candidate past the gate, from its normal
+// relative velocity and normal impulse on (LatticePhysics.hpp:1343-1386).
+// `max_pen` shadows acc.max_penetration in R: the ledger only ever holds a
+// widened R, so the comparison is the reference's.
 template <class R>
 __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp, Staged<R> &c, V3<R> r, V3<R> normal,
-                                             R gap, R eff_n, R ism, R iin, bool correct, ContactAcc &acc, R &max_pen) {
-    const R dt = S.dt;
+                                             R gap, R ni, R ism, R iin, bool correct, ContactAcc &acc, R &max_pen) {
     V3<R> nv = xyz(c.v);
-    const V3<R> rel = nv - sp.velocity - cross(sp.angular, r);
-    const R vn = dot(rel, normal);
-    if (gap > maxR(S.c_margin, -vn * dt)) return;
     if (-gap > max_pen) {
         max_pen = -gap;
         acc.max_penetration = static_cast<double>(-gap);
     }
     const R inm = c.inm;
     const R mass = c.v.w;
-    const R restitution = -vn > S.c_threshold ? S.c_restitution : R(0);
-    const R desired = gap > S.c_margin ? -gap / dt : -restitution * minR(vn, R(0));
-    const R ni = maxR(R(0), (desired - vn) / eff_n);
     if (ni > R(0)) {
         contactApply(ni * normal, r, inm, ism, iin, nv, sp, acc);
         const V3<R> after = nv - sp.velocity - cross(sp.angular, r);
@@ -756,7 +742,7 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             bool hit = false, graze = false;
             R pen = R(0);
             V3<R> r{}, normal{};
-            R gap = R(0), eff_n = R(0);
+            R gap = R(0), eff_n = R(0), vn = R(0), ni = R(0);
             if (k < n) {
                 const Staged<R> &c = st[k];
                 if (c.v.w > R(0)) {
@@ -773,11 +759,10 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
                         eff_n = c.inm + ism + iin * dot(rn, rn);
                         gap = distance - cr;
                     }
-                    if (contactGate(S, sp, xyz(c.v), r, normal, gap)) {
-                        hit = contactChanges(S, sp, xyz(c.v), r, normal, gap, eff_n, pass == 2);
-                        graze = !hit;
-                        pen = -gap;
-                    }
+                    const int probe = contactProbe(S, sp, xyz(c.v), r, normal, gap, eff_n, pass == 2, vn, ni);
+                    hit = probe == 2;
+                    graze = probe == 1;
+                    pen = -gap;
                 }
             }
             const unsigned mask = __ballot_sync(0xffffffffU, hit);
@@ -816,8 +801,8 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             const V3<R> hn{__shfl_sync(0xffffffffU, normal.x, src), __shfl_sync(0xffffffffU, normal.y, src),
                            __shfl_sync(0xffffffffU, normal.z, src)};
             const R hgap = __shfl_sync(0xffffffffU, gap, src);
-            const R heff = __shfl_sync(0xffffffffU, eff_n, src);
-            contactChain(S, sp, c, hr, hn, hgap, heff, ism, iin, pass == 2, acc, max_pen);
+            const R hni = __shfl_sync(0xffffffffU, ni, src);
+            contactChain(S, sp, c, hr, hn, hgap, hni, ism, iin, pass == 2, acc, max_pen);
             __syncwarp();
             if (lane == 0) st[j] = c;
             k0 = j + 1;
