@@ -158,41 +158,48 @@ struct Frame {
 // done later, off the stepping thread.
 template <class R> struct RawState {
     std::uint32_t N{}, B{};
-    std::unique_ptr<unsigned char[]> bytes;
-    std::size_t capacity{};
+    std::size_t capacity{}; // bytes held (nodes and bonds the buffers fit)
+    std::uint32_t cap_n{}, cap_b{};
+    std::unique_ptr<Q4<R>[]> u_buf, up_buf, v_buf, prev_buf;
+    std::unique_ptr<BondRec<R>[]> rec_buf;
+    std::unique_ptr<Q2<R>[]> plastic_buf;
+    std::unique_ptr<std::uint8_t[]> mode_buf;
     Q4<R> *u{}, *up{}, *v{};
     BondRec<R> *rec{};
     Q4<R> *prev{};
     Q2<R> *plastic{};
     std::uint8_t *mode{};
-    std::vector<std::uint32_t> dev2sched;
+    std::vector<std::uint32_t> perm; // storage -> schedule order, when kept apart from its lattice
 
     static std::size_t need(std::uint32_t n, std::uint32_t b) {
         return 3 * static_cast<std::size_t>(n) * sizeof(Q4<R>) +
-               static_cast<std::size_t>(b) * (sizeof(BondRec<R>) + sizeof(Q4<R>) + sizeof(Q2<R>) + 1) + 64;
+               static_cast<std::size_t>(b) * (sizeof(BondRec<R>) + sizeof(Q4<R>) + sizeof(Q2<R>) + 1);
     }
-    // Carves the buffer (kept if large enough) for n nodes and b bonds.
+    // Buffers for n nodes and b bonds (kept when large enough), one per
+    // array: separate allocations stay out of one huge mapping's page faults.
     void shape(std::uint32_t n, std::uint32_t b) {
         N = n;
         B = b;
-        const std::size_t want = need(n, b);
-        if (capacity < want) {
-            bytes.reset(new unsigned char[want]);
-            capacity = want;
+        if (n > cap_n || !u_buf) {
+            u_buf.reset(new Q4<R>[n ? n : 1]);
+            up_buf.reset(new Q4<R>[n ? n : 1]);
+            v_buf.reset(new Q4<R>[n ? n : 1]);
+            cap_n = n;
         }
-        unsigned char *p = bytes.get();
-        auto take = [&](auto *&ptr, std::size_t count) {
-            using T = std::remove_reference_t<decltype(*ptr)>;
-            p = reinterpret_cast<unsigned char *>((reinterpret_cast<std::uintptr_t>(p) + alignof(T) - 1) &
-                                                  ~(static_cast<std::uintptr_t>(alignof(T)) - 1));
-            ptr = reinterpret_cast<T *>(p);
-            p += count * sizeof(T);
-        };
-        take(u, n); take(up, n); take(v, n); take(rec, b); take(prev, b); take(plastic, b); take(mode, b);
+        if (b > cap_b || !rec_buf) {
+            rec_buf.reset(new BondRec<R>[b ? b : 1]);
+            prev_buf.reset(new Q4<R>[b ? b : 1]);
+            plastic_buf.reset(new Q2<R>[b ? b : 1]);
+            mode_buf.reset(new std::uint8_t[b ? b : 1]);
+            cap_b = b;
+        }
+        capacity = need(cap_n, cap_b);
+        u = u_buf.get(); up = up_buf.get(); v = v_buf.get();
+        rec = rec_buf.get(); prev = prev_buf.get(); plastic = plastic_buf.get(); mode = mode_buf.get();
     }
 
     // download's conversion (WorkingLattice::toState, LatticeWorking.hpp:126-142).
-    void writeState(gbl_state_view &st) const {
+    void writeState(gbl_state_view &st, const std::vector<std::uint32_t> &dev2sched) const {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
         parallelFor(N, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t i = lo; i < hi; ++i) {
@@ -620,8 +627,8 @@ template <class R> struct Resident {
         ext_dirty = true;
     }
 
-    // The device arrays a download needs, raw, into `raw` (its buffer reused
-    // when large enough); the permutation is copied.
+    // The device arrays a download needs, raw, into `raw` (its buffers reused
+    // when large enough).
     void copyRaw(RawState<R> &raw) const {
         raw.shape(N, B);
         copyParallel(raw.u, dev.u, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
@@ -631,17 +638,17 @@ template <class R> struct Resident {
         copyParallel(raw.prev, dev.prev, sizeof(Q4<R>) * B, cudaMemcpyDeviceToHost);
         copyParallel(raw.plastic, dev.plastic, sizeof(Q2<R>) * B, cudaMemcpyDeviceToHost);
         copyParallel(raw.mode, dev.mode, B, cudaMemcpyDeviceToHost);
-        raw.dev2sched = dev2sched;
     }
 
-    // download (WorkingLattice::toState, LatticeWorking.hpp:126-142)
+    // download (WorkingLattice::toState, LatticeWorking.hpp:126-142); the host
+    // buffers are kept for the lattice's next download.
     void download(gbl_state_view &st, gbl_sphere *sphere) {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
-        RawState<R> raw;
-        copyRaw(raw);
-        raw.writeState(st);
+        copyRaw(download_raw_);
+        download_raw_.writeState(st, dev2sched);
         if (sphere) *sphere = fetchSphere();
     }
+    RawState<R> download_raw_;
 
     gbl_sphere fetchSphere() const {
         Sphere<R> sp{};
@@ -1740,7 +1747,7 @@ public:
         }
         // The conversion to the state layout runs on the caller's thread,
         // outside the lock; the buffer then goes back to the pool.
-        if (st) raw.writeState(*st);
+        if (st) raw.writeState(*st, raw.perm);
         std::lock_guard<std::mutex> lock(mutex_);
         if (pool_.size() < kPoolSize) pool_.push_back(std::move(raw));
     }
@@ -1859,6 +1866,7 @@ private:
                 }
             }
             l.copyRaw(q.raw);
+            q.raw.perm = std::move(l.dev2sched); // the lattice is retired just below
             q.sphere = l.fetchSphere();
             q.status = l.status;
             q.status.exit_reason = c.exit_reason;
