@@ -345,10 +345,11 @@ class State:
                   "prev_tensile": b, "prev_compressive": b, "prev_shear": b, "plastic_extension": b,
                   "plastic_strain": b}
         self.arrays = {}
-        for name, _ in _STATE_ARRAYS:
+        dtypes = {f64p: np.float64, u32p: np.uint32, u8p: np.uint8}
+        for name, ptype in _STATE_ARRAYS:
             cnt = counts[name]
             ptr = getattr(v, name)
-            self.arrays[name] = np.ctypeslib.as_array(ptr, shape=(cnt,)) if cnt else np.zeros(0)
+            self.arrays[name] = np.ctypeslib.as_array(ptr, shape=(cnt,)) if cnt else np.zeros(0, dtype=dtypes[ptype])
 
     def __getattr__(self, name):
         arrays = self.__dict__.get("arrays")
