@@ -479,6 +479,9 @@ def step_settings(packed: np.ndarray) -> StepSettings:
         pl.footprint_count = int(q[17])
         for f in range(4):
             pl.footprints[f] = Footprint(*q[18 + 4 * f: 22 + 4 * f])
+    if len(packed) > scenes.K_NODE_CONTACT:
+        n = packed[scenes.K_NODE_CONTACT:scenes.K_NODE_CONTACT + 9]
+        s.node_contact = NodeContactSettings(int(n[0]), *n[1:8], int(n[8]))
     return s
 
 

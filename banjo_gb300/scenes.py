@@ -26,7 +26,8 @@ import numpy as np
 K_DT, K_GRAVITY, K_ITER, K_DAMP, K_SPHERE, K_DIRECT = 0, 1, 4, 5, 6, 7
 K_YIELD, K_HARDEN, K_PLATE, K_CONTACT, K_PLANE_COUNT, K_PLANES = 8, 9, 10, 11, 18, 19
 PLANE_WIDTH = 34
-SETTINGS_WIDTH = 19 + 2 * PLANE_WIDTH
+K_NODE_CONTACT = 19 + 2 * PLANE_WIDTH  # 9 slots; a record that ends here has node contact off
+SETTINGS_WIDTH = K_NODE_CONTACT + 9
 SPHERE_WIDTH = 12
 
 GOLDEN = np.uint64(0x9E3779B97F4A7C15)
@@ -162,10 +163,31 @@ def plane(point, normal=(0.0, 1.0, 0.0), tangent=(1.0, 0.0, 0.0), bitangent=(0.0
     return p
 
 
+def contact_bucket_mask(node_count: int) -> int:
+    """The hash table size rule of latticeContactBucketMask (LatticePhysics.hpp:239-243):
+    the smallest power of two >= 2 N, at least 64 and at most 2^22, minus one."""
+    size = 64
+    while size < 2 * node_count and size < (1 << 22):
+        size <<= 1
+    return size - 1
+
+
+def node_contact(mode=2, radius=0.005, skin=0.0025, margin=1e-5, restitution=0.0, threshold=0.5,
+                 static_friction=0.5, dynamic_friction=0.4, node_count=0) -> tuple:
+    """NodeContactSettings (LatticePhysics.hpp:188-202) as the packed record's
+    9 slots: mode (0 off, 1 measure, 2 on), contact radius, Verlet skin, margin,
+    restitution and its speed threshold, static and dynamic friction, and the
+    hash mask for `node_count` nodes."""
+    return (mode, radius, skin, margin, restitution, threshold, static_friction, dynamic_friction,
+            contact_bucket_mask(node_count))
+
+
 def settings(dt=DT_SUBSTEP, gravity=(0.0, -9.81, 0.0), iterations=4, damping_fraction=0.0, sphere_enabled=0,
              direct=0, yield_stretch=0.0, hardening=0.0, contact=(0.5, 0.4, 0.0, 0.5, 0.005, 1e-5, 0.01),
-             planes=()) -> np.ndarray:
+             planes=(), node_contact=None) -> np.ndarray:
     s = np.zeros(SETTINGS_WIDTH, dtype=np.float64)
+    if node_contact is not None:
+        s[K_NODE_CONTACT:K_NODE_CONTACT + 9] = node_contact
     s[K_DT] = dt
     s[K_GRAVITY:K_GRAVITY + 3] = gravity
     s[K_ITER] = iterations
@@ -293,6 +315,59 @@ def drop_trial(nx, ny, nz, compliance, break_strain, drop_height, h=0.01, steps=
         "steps": np.array([steps * substeps], dtype=np.uint64),
         "substeps_per_step": np.array([substeps], dtype=np.uint64),
     })
+    return case
+
+
+def two_cells(separation, bonded=False, mode=2, v0=0.0, v1=0.0, mass_ratio=1.0, dead=False, cell=0.01,
+              steps=2000, density=2500.0):
+    """Two cells on the x axis, `separation` apart, closing (or not) at v0 and
+    v1, in the double lane with node-to-node contact: the pair the reference's
+    contact tests step (fast_lattice_tests.cpp:690-896). Contact radius half a
+    cell (two cells touch one cell apart), skin a quarter cell, dt 1e-6 s, one
+    iteration, no gravity. `bonded` joins them by a bond at rest at
+    `separation` whose thresholds are out of reach; `dead` starts that bond
+    failed. Node 1 is `mass_ratio` times heavier."""
+    ref = np.array([-0.5 * separation, 0.0, 0.0, 0.5 * separation, 0.0, 0.0])
+    mass = density * cell ** 3
+    nb = 1 if bonded else 0
+    case = {
+        "node_count": np.array([2], dtype=np.uint32),
+        "bond_count": np.array([nb], dtype=np.uint32),
+        "ref_pos": ref,
+        "pos": ref.copy(),
+        "vel": np.array([v0, 0.0, 0.0, v1, 0.0, 0.0]),
+        "mass": np.array([mass, mass * mass_ratio]),
+        "bond_a": np.zeros(nb, dtype=np.uint32),
+        "bond_b": np.ones(nb, dtype=np.uint32),
+        "rest_length": np.full(nb, float(separation)),
+        "compliance": np.full(nb, 1e-7),
+        "threshold": np.tile([1.0, 2.0, 1.0, 2.0, 1.0, 2.0], nb).astype(np.float64),
+        "node_block_begin": np.array([0, 2], dtype=np.uint32),
+        "origin": np.zeros(3, dtype=np.float64),
+        "sphere": sphere(radius=1.0),
+        "settings": settings(dt=1e-6, gravity=(0.0, 0.0, 0.0), iterations=1, direct=1,
+                             node_contact=node_contact(mode, 0.5 * cell, 0.25 * cell, node_count=2)),
+        "steps": np.array([steps], dtype=np.uint64),
+    }
+    if bonded and dead:
+        case["alive"] = np.zeros(1, dtype=np.uint8)
+    return case
+
+
+def contact_drop(nx=10, ny=6, nz=8, compliance=1e-6, break_strain=1.5e-3, drop_height=0.002, speed=3.0, h=0.01,
+                 steps=30, mode=2, restitution=0.2):
+    """A box thrown onto the ground at `speed` hard enough to break bonds, with
+    node-to-node contact on: every failed bond puts its pair in the contact
+    list, and the cracked faces meet again."""
+    case = drop_trial(nx, ny, nz, compliance=compliance, break_strain=break_strain, drop_height=drop_height, h=h,
+                      steps=steps, substeps=1)
+    n = nx * ny * nz
+    vel = case["vel"].reshape(-1, 3)
+    vel[:, 1] = -speed
+    case["vel"] = vel.reshape(-1)
+    case["settings"] = settings(planes=[plane((0.0, 0.0, 0.0), node_radius=0.5 * h)],
+                                node_contact=node_contact(mode, 0.5 * h, 0.25 * h, restitution=restitution,
+                                                          node_count=n))
     return case
 
 

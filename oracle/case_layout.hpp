@@ -21,7 +21,11 @@ enum SettingsSlot : int {
     kContact = 11,           // 7: static, dynamic, restitution, threshold, node radius, margin, slack
     kPlaneCount = 18,
     kPlanes = 19,            // 2 x kPlaneWidth
-    kSettingsWidth = 19 + 2 * 34,
+    // 9: mode, radius, skin, margin, restitution, restitution speed threshold,
+    // static friction, dynamic friction, bucket mask. A record that ends here
+    // (kNodeContact wide) has node-to-node contact off.
+    kNodeContact = 19 + 2 * 34,
+    kSettingsWidth = kNodeContact + 9,
 };
 
 enum PlaneSlot : int {
@@ -57,6 +61,11 @@ enum StatusU64Slot : int {
     kCandidateOverflow,
     kBallSupportEvents,
     kLaunches,
+    kNodeContacts,           // node-to-node contact (NodeContactAccumulators)
+    kNodePairTests,
+    kNodeRebuilds,
+    kNodePairsListed,
+    kNodePairOverflow,
     kStatusU64Width,
 };
 
@@ -81,6 +90,12 @@ enum StatusF64Slot : int {
     kExternalImpulseZ,
     kExternalSteps,
     kWallSeconds,
+    kNodeDissipated,         // node-to-node contact (NodeContactAccumulators)
+    kNodeMaxOverlap,
+    kNodeMaxCorrection,
+    kNodeMomentumX,
+    kNodeMomentumY,
+    kNodeMomentumZ,
     kStatusF64Width,
 };
 

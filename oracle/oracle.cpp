@@ -265,6 +265,10 @@ template <class R> struct Settings {
     R c_static, c_dynamic, c_restitution, c_threshold, c_node_radius, c_margin, c_slack;
     std::uint32_t plane_count;
     Plane<R> planes[kPlanes];
+    // NodeContactSettings (LatticePhysics.hpp:188-202); 0 off, 1 measure, 2 on.
+    std::uint8_t nc_mode;
+    R nc_radius, nc_skin, nc_margin, nc_restitution, nc_threshold, nc_static, nc_dynamic;
+    std::uint32_t nc_mask;
 };
 template <class R> struct Sphere { V<R> center, velocity, angular; R radius, mass, inertia; };
 
@@ -273,7 +277,9 @@ template <class R> V<R> v3of(const std::vector<double> &s, int at) {
 }
 
 template <class R> Settings<R> unpackSettings(const std::vector<double> &s) {
-    if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth)) throw std::invalid_argument("settings width");
+    if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth) &&
+        s.size() != static_cast<std::size_t>(lsio::kNodeContact))
+        throw std::invalid_argument("settings width");
     Settings<R> o{};
     o.dt = static_cast<R>(s[lsio::kDt]);
     o.gravity = v3of<R>(s, lsio::kGravity);
@@ -305,6 +311,14 @@ template <class R> Settings<R> unpackSettings(const std::vector<double> &s) {
         pl.footprint_count = static_cast<std::uint32_t>(s[b + lsio::kPlaneFootprintCount]);
         for (unsigned f = 0; f < kFootprints; ++f)
             for (int q = 0; q < 4; ++q) pl.fp[f][q] = static_cast<R>(s[b + lsio::kPlaneFootprints + 4 * static_cast<int>(f) + q]);
+    }
+    if (s.size() == static_cast<std::size_t>(lsio::kSettingsWidth)) {
+        const int n = lsio::kNodeContact;
+        o.nc_mode = static_cast<std::uint8_t>(s[n]);
+        o.nc_radius = static_cast<R>(s[n + 1]); o.nc_skin = static_cast<R>(s[n + 2]);
+        o.nc_margin = static_cast<R>(s[n + 3]); o.nc_restitution = static_cast<R>(s[n + 4]);
+        o.nc_threshold = static_cast<R>(s[n + 5]); o.nc_static = static_cast<R>(s[n + 6]);
+        o.nc_dynamic = static_cast<R>(s[n + 7]); o.nc_mask = static_cast<std::uint32_t>(s[n + 8]);
     }
     return o;
 }
@@ -877,6 +891,189 @@ private:
     unsigned pending_{};
 };
 
+// ---------------------------------------------------------------------------
+// Node-to-node contact (LatticePhysics.hpp:1441-1647; the stage order is
+// CpuLatticeBackend.cpp:424-436). Pairs of nodes that no live bond holds and
+// that lie within 2 r + skin are listed per owner (the lower index) through a
+// hashed grid of that cell size; the list is rebuilt before use when a bond
+// failed in the previous substep or any node drifted more than skin / 2 since
+// the last build. The narrow phase is one response per pair, in list order.
+// ---------------------------------------------------------------------------
+constexpr std::uint32_t kPairsPerNode = 24;
+
+struct NodeAcc {
+    std::uint64_t contacts{}, pair_tests{}, rebuilds{}, pairs_listed{}, pair_overflow{};
+    double dissipated{}, max_overlap{}, max_correction{}, momentum[3]{};
+};
+
+// Teschner et al., "Optimized Spatial Hashing for Collision Detection of
+// Deformable Objects" (2003): the three primes, exclusive-or, masked.
+inline std::uint32_t cellBucket(std::int32_t x, std::int32_t y, std::int32_t z, std::uint32_t mask) {
+    return ((static_cast<std::uint32_t>(x) * 73856093U) ^ (static_cast<std::uint32_t>(y) * 19349663U) ^
+            (static_cast<std::uint32_t>(z) * 83492791U)) & mask;
+}
+
+template <class R> struct PairList {
+    std::vector<std::int32_t> cell;        // 3 per node
+    std::vector<R> built_u;                // u at the last build, 3 per node
+    std::vector<std::uint32_t> bucket_at;  // bucket offsets (buckets + 1)
+    std::vector<std::uint32_t> members;    // movable nodes by bucket, ascending within one
+    std::vector<std::uint32_t> fill, other, bond, owners;
+    bool rebuild{true};
+};
+
+template <class R> R contactCutoff(const Settings<R> &S) { return R(2) * S.nc_radius + S.nc_skin; }
+
+// nodeContactStale: any node farther than skin / 2 from where the list was built.
+template <class R> bool pairListStale(const Lattice<R> &L, const Settings<R> &S, const PairList<R> &P) {
+    const R half = R(0.5) * S.nc_skin;
+    const R limit = half * half;
+    for (std::uint32_t i = 0; i < L.N; ++i) {
+        const V<R> d = sub(ld(L.u, i), ld(P.built_u, i));
+        if (dot(d, d) > limit) return true;
+    }
+    return false;
+}
+
+// The four broad-phase steps (cells, counting sort into the buckets, the
+// per-owner gather, the owner list) in one pass each.
+template <class R> void rebuildPairs(const Lattice<R> &L, const Settings<R> &S, PairList<R> &P, NodeAcc &acc) {
+    const std::uint32_t N = L.N;
+    P.cell.resize(3 * static_cast<std::size_t>(N));
+    P.built_u.resize(3 * static_cast<std::size_t>(N));
+    P.fill.assign(N, 0U);
+    P.other.resize(kPairsPerNode * static_cast<std::size_t>(N));
+    P.bond.resize(kPairsPerNode * static_cast<std::size_t>(N));
+    const R cutoff = contactCutoff(S);
+    const R inverse_cell = R(1) / cutoff;
+    for (std::uint32_t i = 0; i < N; ++i) {
+        const V<R> p = position(L, i);
+        P.cell[3 * i] = static_cast<std::int32_t>(std::floor(p.x * inverse_cell));
+        P.cell[3 * i + 1] = static_cast<std::int32_t>(std::floor(p.y * inverse_cell));
+        P.cell[3 * i + 2] = static_cast<std::int32_t>(std::floor(p.z * inverse_cell));
+        st(P.built_u, i, ld(L.u, i));
+    }
+    auto bucketOf = [&](std::uint32_t i) { return cellBucket(P.cell[3 * i], P.cell[3 * i + 1], P.cell[3 * i + 2], S.nc_mask); };
+    const std::uint32_t buckets = S.nc_mask + 1U;
+    P.bucket_at.assign(static_cast<std::size_t>(buckets) + 1, 0U);
+    P.members.resize(N);
+    for (std::uint32_t i = 0; i < N; ++i)
+        if (!(L.mass[i] <= R(0))) ++P.bucket_at[bucketOf(i) + 1U];
+    for (std::uint32_t b = 0; b < buckets; ++b) P.bucket_at[b + 1U] += P.bucket_at[b];
+    std::vector<std::uint32_t> cursor(P.bucket_at.begin(), P.bucket_at.end() - 1);
+    for (std::uint32_t i = 0; i < N; ++i)
+        if (!(L.mass[i] <= R(0))) P.members[cursor[bucketOf(i)]++] = i;
+    const R cutoff_sq = cutoff * cutoff;
+    for (std::uint32_t i = 0; i < N; ++i) {
+        if (L.mass[i] <= R(0)) continue;
+        const V<R> p = position(L, i);
+        const std::int32_t cx = P.cell[3 * i], cy = P.cell[3 * i + 1], cz = P.cell[3 * i + 2];
+        std::uint32_t fill = 0;
+        for (std::int32_t dz = -1; dz <= 1; ++dz)
+            for (std::int32_t dy = -1; dy <= 1; ++dy)
+                for (std::int32_t dx = -1; dx <= 1; ++dx) {
+                    const std::int32_t gx = cx + dx, gy = cy + dy, gz = cz + dz;
+                    const std::uint32_t b = cellBucket(gx, gy, gz, S.nc_mask);
+                    for (std::uint32_t k = P.bucket_at[b]; k < P.bucket_at[b + 1U]; ++k) {
+                        const std::uint32_t j = P.members[k];
+                        if (j <= i || P.cell[3 * j] != gx || P.cell[3 * j + 1] != gy || P.cell[3 * j + 2] != gz) continue;
+                        const V<R> r = sub(position(L, j), p);
+                        if (dot(r, r) > cutoff_sq) continue;
+                        // The pair's bond, if i lists one to j; a live one holds the pair.
+                        std::uint32_t bond = kNoBond;
+                        bool held = false;
+                        for (std::uint32_t s = 0; s < L.D; ++s) {
+                            const std::size_t slot = static_cast<std::size_t>(s) * N + i;
+                            if (L.nbr_bond[slot] == kNoBond) break;
+                            if (L.nbr_other[slot] != j) continue;
+                            bond = L.nbr_bond[slot];
+                            held = L.nbr_alive[slot] != 0;
+                            break;
+                        }
+                        if (held) continue;
+                        if (fill == kPairsPerNode) { ++acc.pair_overflow; continue; }
+                        P.other[kPairsPerNode * static_cast<std::size_t>(i) + fill] = j;
+                        P.bond[kPairsPerNode * static_cast<std::size_t>(i) + fill] = bond;
+                        ++fill;
+                    }
+                }
+        P.fill[i] = fill;
+    }
+    P.owners.clear();
+    for (std::uint32_t i = 0; i < N; ++i)
+        if (P.fill[i]) {
+            P.owners.push_back(i);
+            acc.pairs_listed += P.fill[i];
+        }
+    ++acc.rebuilds;
+    P.rebuild = false;
+}
+
+// nodeContactPair: restitution-limited normal impulse, Coulomb friction and an
+// overlap correction, each equal and opposite on the two nodes.
+template <class R>
+void contactPair(Lattice<R> &L, const Settings<R> &S, std::uint32_t a, std::uint32_t b, std::uint32_t bond, NodeAcc &acc) {
+    if (bond != kNoBond && L.alive[bond]) return;
+    const R ma = L.mass[a], mb = L.mass[b];
+    if (ma <= R(0) || mb <= R(0)) return;
+    ++acc.pair_tests;
+    const V<R> r = sub(position(L, b), position(L, a));
+    const R distance = len(r);
+    const V<R> n = unit(r);
+    const R gap = distance - R(2) * S.nc_radius;
+    if (gap < R(0) && -gap > static_cast<R>(acc.max_overlap)) acc.max_overlap = static_cast<double>(-gap);
+    if (S.nc_mode != 2) return;
+    V<R> va = ld(L.v, a), vb = ld(L.v, b);
+    const R vn = dot(sub(vb, va), n);
+    if (gap > maxR(S.nc_margin, -vn * S.dt)) return;
+    const R ia = R(1) / ma, ib = R(1) / mb;
+    const R pair_inverse = ia + ib;
+    const R restitution = -vn > S.nc_threshold ? S.nc_restitution : R(0);
+    const R desired = gap > S.nc_margin ? -gap / S.dt : -restitution * minR(vn, R(0));
+    const R impulse = maxR(R(0), (desired - vn) / pair_inverse);
+    if (impulse > R(0)) {
+        const V<R> va0 = va, vb0 = vb;
+        const R before = R(0.5) * ma * dot(va, va) + R(0.5) * mb * dot(vb, vb);
+        auto apply = [&](V<R> j) {
+            vb = add(vb, scale(j, ib));
+            va = sub(va, scale(j, ia));
+        };
+        apply(scale(n, impulse));
+        const V<R> rel = sub(vb, va);
+        const V<R> t = sub(rel, scale(n, dot(rel, n)));
+        const R speed = len(t);
+        if (speed > R(1.0e-12)) {
+            const V<R> dir = divide(t, speed);
+            const R stick = speed / pair_inverse;
+            const R friction = stick <= S.nc_static * impulse ? stick : minR(stick, S.nc_dynamic * impulse);
+            apply(scale(dir, -friction));
+        }
+        st(L.v, a, va);
+        st(L.v, b, vb);
+        acc.dissipated += static_cast<double>(before - (R(0.5) * ma * dot(va, va) + R(0.5) * mb * dot(vb, vb)));
+        acc.momentum[0] += static_cast<double>(ma * (va.x - va0.x) + mb * (vb.x - vb0.x));
+        acc.momentum[1] += static_cast<double>(ma * (va.y - va0.y) + mb * (vb.y - vb0.y));
+        acc.momentum[2] += static_cast<double>(ma * (va.z - va0.z) + mb * (vb.z - vb0.z));
+        ++acc.contacts;
+    }
+    if (gap < -S.nc_margin) {
+        const R correction = minR(-gap - S.nc_margin, R(0.2) * S.nc_radius);
+        const V<R> shift = scale(n, correction / pair_inverse);
+        st(L.u, a, sub(ld(L.u, a), scale(shift, ia)));
+        st(L.u, b, add(ld(L.u, b), scale(shift, ib)));
+        if (correction > static_cast<R>(acc.max_correction)) acc.max_correction = static_cast<double>(correction);
+    }
+}
+
+// nodeContactPass: owners ascending, then slots ascending.
+template <class R> void contactPass(Lattice<R> &L, const Settings<R> &S, const PairList<R> &P, NodeAcc &acc) {
+    for (const std::uint32_t a : P.owners)
+        for (std::uint32_t k = 0; k < P.fill[a]; ++k) {
+            const std::size_t slot = kPairsPerNode * static_cast<std::size_t>(a) + k;
+            contactPair(L, S, a, P.other[slot], P.bond[slot], acc);
+        }
+}
+
 struct Status {
     std::uint64_t total_steps{}, first_failure_step{kNever}, last_failure_step{kNever}, last_energy_gain_step{kNever},
         last_damage_gain_step{};
@@ -887,6 +1084,7 @@ struct Status {
     ContactAcc contact{};
     double ext_work{}, ext_impulse[3]{};
     std::uint64_t ext_steps{};
+    NodeAcc node{};
 };
 
 // External forces (ExternalLoads.hpp:28-50 set, 79-148 kick; forces only).
@@ -944,7 +1142,7 @@ template <class R> class Runner {
 public:
     Runner(Lattice<R> &L, const Settings<R> &S, Sphere<R> sp, unsigned threads) : L_(L), S_(S), sp_(sp), pool_(threads) {
         if (S_.plate_half_thickness > R(0)) throw std::invalid_argument("plate bending is not implemented in this checker");
-        if (S_.damping_fraction > R(0) && false) {}
+        if (S_.nc_mode != 0 && !(contactCutoff(S_) > R(0))) throw std::invalid_argument("node contact needs 2 r + skin > 0");
     }
     Status status;
     Loads<R> loads;
@@ -1057,6 +1255,10 @@ private:
             nodes([&](std::size_t i) { if (!L_.candidate[i]) nodeSupportVelocity(L_, S_, i); });
         }
         if (S_.sphere_enabled) spherePass(L_, S_, sp_, 2, status.contact);
+        if (S_.nc_mode != 0) {
+            if (pairs_.rebuild || pairListStale(L_, S_, pairs_)) rebuildPairs(L_, S_, pairs_, status.node);
+            contactPass(L_, S_, pairs_, status.node);
+        }
         return finishStep(direct);
     }
 
@@ -1107,7 +1309,8 @@ private:
             }
         sp_.center = add(sp_.center, scale(sp_.velocity, S_.dt));
         sphereSupport(S_, sp_, status.contact);
-        if (any) dirty_start_ = true;
+        // A failure changes which pairs no live bond holds.
+        if (any) dirty_start_ = pairs_.rebuild = true;
         return any;
     }
 
@@ -1120,6 +1323,7 @@ private:
     Sphere<R> sp_;
     Pool pool_;
     bool dirty_start_{true};
+    PairList<R> pairs_;
 };
 
 template <class R> std::vector<double> widen(const std::vector<R> &v) {
@@ -1192,6 +1396,9 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     u[lsio::kRankDeficientNodes] = st_.rank_deficient_nodes; u[lsio::kImpulseContacts] = st_.contact.impulse_contacts;
     u[lsio::kCandidateOverflow] = st_.contact.candidate_overflow; u[lsio::kBallSupportEvents] = st_.contact.ball_support_events;
     u[lsio::kLaunches] = st_.launches;
+    u[lsio::kNodeContacts] = st_.node.contacts; u[lsio::kNodePairTests] = st_.node.pair_tests;
+    u[lsio::kNodeRebuilds] = st_.node.rebuilds; u[lsio::kNodePairsListed] = st_.node.pairs_listed;
+    u[lsio::kNodePairOverflow] = st_.node.pair_overflow;
     std::vector<double> d(lsio::kStatusF64Width, 0.0);
     d[lsio::kRemovedEnergy] = st_.removed_energy; d[lsio::kMaxDamage] = st_.max_damage; d[lsio::kPlasticWork] = st_.plastic_work;
     d[lsio::kMaxTensile] = st_.max_t; d[lsio::kMaxCompressive] = st_.max_c; d[lsio::kMaxShear] = st_.max_s;
@@ -1202,6 +1409,9 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     d[lsio::kExternalWork] = st_.ext_work; d[lsio::kExternalImpulseX] = st_.ext_impulse[0];
     d[lsio::kExternalImpulseY] = st_.ext_impulse[1]; d[lsio::kExternalImpulseZ] = st_.ext_impulse[2];
     d[lsio::kExternalSteps] = static_cast<double>(st_.ext_steps); d[lsio::kWallSeconds] = wall;
+    d[lsio::kNodeDissipated] = st_.node.dissipated; d[lsio::kNodeMaxOverlap] = st_.node.max_overlap;
+    d[lsio::kNodeMaxCorrection] = st_.node.max_correction; d[lsio::kNodeMomentumX] = st_.node.momentum[0];
+    d[lsio::kNodeMomentumY] = st_.node.momentum[1]; d[lsio::kNodeMomentumZ] = st_.node.momentum[2];
     out.put("status_u64", u);
     out.put("status_f64", d);
     out.putScalar<double>("wall_seconds", wall);

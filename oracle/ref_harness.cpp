@@ -38,7 +38,9 @@ namespace {
 V3<double> v3at(const std::vector<double> &s, int at) { return {s[at], s[at + 1], s[at + 2]}; }
 
 StepSettings<double> unpackSettings(const std::vector<double> &s) {
-    if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth)) throw std::runtime_error("settings width");
+    if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth) &&
+        s.size() != static_cast<std::size_t>(lsio::kNodeContact))
+        throw std::runtime_error("settings width");
     StepSettings<double> out{};
     out.dt = s[lsio::kDt];
     out.gravity = v3at(s, lsio::kGravity);
@@ -60,6 +62,18 @@ StepSettings<double> unpackSettings(const std::vector<double> &s) {
     out.contact.contact_margin = s[c + 5];
     out.contact.prefilter_slack = s[c + 6];
     out.node_contact.mode = kNodeContactOff;
+    if (s.size() == static_cast<std::size_t>(lsio::kSettingsWidth)) {
+        const int n = lsio::kNodeContact;
+        out.node_contact.mode = static_cast<std::uint8_t>(s[n]);
+        out.node_contact.radius = s[n + 1];
+        out.node_contact.skin = s[n + 2];
+        out.node_contact.margin = s[n + 3];
+        out.node_contact.restitution = s[n + 4];
+        out.node_contact.restitution_speed_threshold = s[n + 5];
+        out.node_contact.static_friction = s[n + 6];
+        out.node_contact.dynamic_friction = s[n + 7];
+        out.node_contact.bucket_mask = static_cast<std::uint32_t>(s[n + 8]);
+    }
     out.support.plane_count = static_cast<std::uint32_t>(s[lsio::kPlaneCount]);
     for (unsigned p = 0; p < kMaxSupportPlanes; ++p) {
         const int b = lsio::kPlanes + static_cast<int>(p) * lsio::kPlaneWidth;
@@ -113,6 +127,11 @@ void packStatus(lsio::Case &out, const RunStatus &st) {
     u[lsio::kCandidateOverflow] = st.contact.candidate_overflow;
     u[lsio::kBallSupportEvents] = st.contact.ball_support_events;
     u[lsio::kLaunches] = st.launches;
+    u[lsio::kNodeContacts] = st.node_contact.contacts;
+    u[lsio::kNodePairTests] = st.node_contact.pair_tests;
+    u[lsio::kNodeRebuilds] = st.node_contact.rebuilds;
+    u[lsio::kNodePairsListed] = st.node_contact.pairs_listed;
+    u[lsio::kNodePairOverflow] = st.node_contact.pair_overflow;
     std::vector<double> d(lsio::kStatusF64Width, 0.0);
     d[lsio::kRemovedEnergy] = st.removed_energy_j;
     d[lsio::kMaxDamage] = st.max_damage;
@@ -134,6 +153,12 @@ void packStatus(lsio::Case &out, const RunStatus &st) {
     d[lsio::kExternalImpulseZ] = st.external_load.impulse_n_s.z;
     d[lsio::kExternalSteps] = static_cast<double>(st.external_load.steps);
     d[lsio::kWallSeconds] = st.wall_seconds;
+    d[lsio::kNodeDissipated] = st.node_contact.dissipated_kinetic_energy_j;
+    d[lsio::kNodeMaxOverlap] = st.node_contact.maximum_overlap_m;
+    d[lsio::kNodeMaxCorrection] = st.node_contact.maximum_position_correction_m;
+    d[lsio::kNodeMomentumX] = st.node_contact.momentum_residual_x;
+    d[lsio::kNodeMomentumY] = st.node_contact.momentum_residual_y;
+    d[lsio::kNodeMomentumZ] = st.node_contact.momentum_residual_z;
     out.put("status_u64", u);
     out.put("status_f64", d);
 }

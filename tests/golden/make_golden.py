@@ -53,6 +53,16 @@ def cases() -> dict:
     # ramped end load), small, through its first failure rounds.
     out["bar_small"] = (scenes.notched_bar(24, 8, 8, ramp_steps=800, steps=20), "float")
     out["bar_small_double"] = (scenes.notched_bar(16, 6, 6, ramp_steps=800, steps=6), "double")
+    # Node-to-node contact: the reference's two-cell pairs (an unbonded pair
+    # closing at 4 m/s; a bonded pair held overlapping by its bond; the same
+    # pair with its bond failed; unequal masses closing unevenly), and a box
+    # thrown onto the ground that cracks, with the cracked faces in contact.
+    out["contact_pair_closing"] = (scenes.two_cells(0.02, v0=2.0, v1=-2.0, steps=6000), "double")
+    out["contact_pair_bonded"] = (scenes.two_cells(0.006, bonded=True, steps=2000), "double")
+    out["contact_pair_dead"] = (scenes.two_cells(0.006, bonded=True, dead=True, steps=2000), "double")
+    out["contact_pair_momentum"] = (scenes.two_cells(0.02, v0=4.0, v1=-1.0, mass_ratio=3.0, steps=8000), "double")
+    out["contact_drop"] = (scenes.contact_drop(), "float")
+    out["contact_drop_measure"] = (scenes.contact_drop(mode=1, steps=20), "float")
     return out
 
 

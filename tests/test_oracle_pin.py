@@ -32,9 +32,31 @@ def test_threaded_port_is_bit_identical(port, name):
 
 
 def test_fixtures_contain_fracture():
-    broken = {n: int(load_golden(n)[1]["status_u64"][4]) for n in golden_names()}
+    # The two-cell contact pairs hold at most one bond and are about contact,
+    # not fracture; every other fixture runs through bond failure.
+    broken = {n: int(load_golden(n)[1]["status_u64"][4]) for n in golden_names() if not n.startswith("contact_pair")}
     assert len(broken) >= 5
     assert all(b > 0 for b in broken.values()), broken
+
+
+def test_contact_fixtures_hold_the_reference_rules():
+    """The reference's own assertions on its two-cell contact pairs
+    (fast_lattice_tests.cpp:800-896), on the fixtures its code produced."""
+    u64 = lambda n: load_golden(n)[1]["status_u64"]  # noqa: E731
+    f64 = lambda n: load_golden(n)[1]["status_f64"]  # noqa: E731
+    contacts, rebuilds, listed, dissipated, correction = 13, 15, 16, 20, 22
+    closing = load_golden("contact_pair_closing")[1]
+    assert u64("contact_pair_closing")[contacts] > 0
+    x = closing["u"].reshape(-1, 3)[:, 0] + np.array([-0.01, 0.01])
+    assert x[1] - x[0] > 0.01 - 2 * 1e-5  # apart by at least the touch distance less the margin
+    assert u64("contact_pair_bonded")[rebuilds] > 0
+    assert u64("contact_pair_bonded")[listed] == 0 and u64("contact_pair_bonded")[contacts] == 0
+    assert u64("contact_pair_dead")[listed] > 0 and f64("contact_pair_dead")[correction] > 0.0
+    m = f64("contact_pair_momentum")
+    assert u64("contact_pair_momentum")[contacts] > 0 and m[dissipated] > 0.0
+    assert max(abs(m[23]), abs(m[24]), abs(m[25])) < 1e-14 * 2.5e-3  # below 1e-14 of the pair's momentum
+    drop = u64("contact_drop")
+    assert drop[contacts] > 0 and drop[listed] > 0 and int(drop[4]) > 0
 
 
 def _reference_built():
