@@ -198,6 +198,17 @@ void statusOf(const gbl_run_status &s, RunStatus &o) {
     o.rank_deficient_nodes = s.rank_deficient_nodes;
     o.plastic_work_j = s.plastic_work_j;
     o.max_plastic_stretch = s.max_plastic_stretch;
+    o.node_contact.contacts = s.node_contact.contacts;
+    o.node_contact.pair_tests = s.node_contact.pair_tests;
+    o.node_contact.rebuilds = s.node_contact.rebuilds;
+    o.node_contact.pairs_listed = s.node_contact.pairs_listed;
+    o.node_contact.pair_overflow = s.node_contact.pair_overflow;
+    o.node_contact.dissipated_kinetic_energy_j = s.node_contact.dissipated_kinetic_energy_j;
+    o.node_contact.maximum_overlap_m = s.node_contact.maximum_overlap_m;
+    o.node_contact.maximum_position_correction_m = s.node_contact.maximum_position_correction_m;
+    o.node_contact.momentum_residual_x = s.node_contact.momentum_residual_x;
+    o.node_contact.momentum_residual_y = s.node_contact.momentum_residual_y;
+    o.node_contact.momentum_residual_z = s.node_contact.momentum_residual_z;
 }
 
 class Gb300LatticeBackend final : public LatticeBackend {

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstdlib>
 #include <chrono>
@@ -257,7 +258,56 @@ template <class R> struct Resident {
     explicit Resident(Schedule s) : sched(std::move(s)) {}
     Resident(const Resident &) = delete;
     Resident &operator=(const Resident &) = delete;
+    // Node-to-node contact scratch (allocated when the settings turn it on).
+    void *nc_mem{};
+
+    // The table size rule of latticeContactBucketMask (LatticePhysics.hpp:239-243),
+    // applied to this lattice's own node count.
+    static std::uint32_t contactBuckets(std::uint32_t n) {
+        std::uint32_t size = 64U;
+        while (size < 2U * n && size < (1U << 22)) size <<= 1U;
+        return size;
+    }
+    // The scratch's parts in allocation order, each rounded to 256 bytes.
+    static std::array<std::size_t, 10> contactParts(std::uint32_t n) {
+        const std::size_t N = n, buckets = contactBuckets(n), tiles = (N + kThreads - 1) / kThreads;
+        const std::size_t pairs = kPairsPerNode * N * 4;
+        std::array<std::size_t, 10> parts{N * sizeof(Q4<R>), N * sizeof(int4), buckets * 4, buckets * 4, N * 4, N * 4,
+                                         (tiles + 1) * 4, pairs, pairs, pairs};
+        for (auto &b : parts) b = (b + 255) & ~std::size_t(255);
+        return parts;
+    }
+    static std::size_t contactBytes(std::uint32_t n) {
+        std::size_t total = 0;
+        for (auto b : contactParts(n)) total += b;
+        return total;
+    }
+    void ensureContact() {
+        if (nc_mem) return;
+        const auto parts = contactParts(N);
+        check(cudaMalloc(&nc_mem, contactBytes(N)), "device allocation");
+        char *p = static_cast<char *>(nc_mem);
+        std::size_t k = 0;
+        auto take = [&]() {
+            char *at = p;
+            p += parts[k++];
+            return at;
+        };
+        dev.nc_built = reinterpret_cast<Q4<R> *>(take());
+        dev.nc_cell = reinterpret_cast<int4 *>(take());
+        dev.nc_count = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_start = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_members = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_fill = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_tile = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_pa = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_pb = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_pbond = reinterpret_cast<std::uint32_t *>(take());
+        dev.nc_mask = contactBuckets(N) - 1U;
+    }
+
     ~Resident() {
+        if (nc_mem) cudaFree(nc_mem);
         if (ext_force) cudaFree(ext_force);
         if (ext_req) cudaFree(ext_req);
         if (ext_contrib) cudaFree(ext_contrib);
@@ -713,6 +763,17 @@ template <class R> struct Resident {
             status.external_load.angular_impulse_kg_m2_s[q] = c.ext.ang[q];
         }
         status.external_load.work_j = c.ext.work;
+        status.node_contact.contacts = c.node.contacts;
+        status.node_contact.pair_tests = c.node.pair_tests;
+        status.node_contact.rebuilds = c.node.rebuilds;
+        status.node_contact.pairs_listed = c.node.pairs_listed;
+        status.node_contact.pair_overflow = c.node.pair_overflow;
+        status.node_contact.dissipated_kinetic_energy_j = c.node.dissipated;
+        status.node_contact.maximum_overlap_m = c.node.max_overlap;
+        status.node_contact.maximum_position_correction_m = c.node.max_correction;
+        status.node_contact.momentum_residual_x = c.node.momentum[0];
+        status.node_contact.momentum_residual_y = c.node.momentum[1];
+        status.node_contact.momentum_residual_z = c.node.momentum[2];
         status.exit_reason = c.exit_reason;
         float f;
         std::memcpy(&f, &c.max_t, 4); status.max_tensile_stretch = f;
@@ -832,6 +893,7 @@ public:
                 plastic_ = true;
                 dropGraph();
             }
+            if (S_.nc_mode != 0) slots_[k]->ensureContact();
             initControl(k, step_limit);
             pushDescriptor(k);
             check(cudaStreamSynchronize(stream_), "admit");
@@ -858,6 +920,8 @@ public:
         S_ = convertSettings(set);
         plastic_ = S_.yield_stretch > R(0);
         for (auto k : active_) plastic_ = plastic_ || slots_[k]->plastic_state;
+        if (S_.nc_mode != 0)
+            for (auto k : active_) slots_[k]->ensureContact();
         growControl(slots_.size());
         for (auto k : active_) initControl(k, 0);
         for (auto k : active_) pushDescriptor(k);
@@ -873,6 +937,13 @@ public:
         S_ = convertSettings(set);
         plastic_ = S_.yield_stretch > R(0);
         for (auto k : active_) plastic_ = plastic_ || slots_[k]->plastic_state;
+        if (S_.nc_mode != 0) {
+            for (auto k : active_) {
+                slots_[k]->ensureContact();
+                pushDescriptor(k);
+            }
+            check(cudaStreamSynchronize(stream_), "descriptors");
+        }
         ready_ = true;
         dirty_ = true;
     }
@@ -1058,7 +1129,10 @@ public:
 
     static void validate(const gbl_step_settings &s) {
         if (s.bond_integrator != 0) invalid("this lattice backend implements the XPBD integrator only");
-        if (s.node_contact.mode != 0) invalid("this lattice backend does not implement node-to-node contact");
+        if (s.node_contact.mode != 0 &&
+            !(2.0 * s.node_contact.radius + s.node_contact.skin > 0.0 &&
+              std::isfinite(2.0 * s.node_contact.radius + s.node_contact.skin)))
+            invalid("node-to-node contact needs a finite positive cutoff (2 radius + skin)");
         if (s.plate_half_thickness > 0.0) invalid("this lattice backend does not implement plate bending");
         if (s.audit_energy) invalid("this lattice backend does not implement the energy audit");
         if ((s.direct_arithmetic != 0) != kDirect)
@@ -1088,6 +1162,11 @@ private:
         o.c_restitution = R(s.contact.restitution); o.c_threshold = R(s.contact.restitution_speed_threshold);
         o.c_node_radius = R(s.contact.node_contact_radius); o.c_margin = R(s.contact.contact_margin);
         o.c_slack = R(s.contact.prefilter_slack);
+        o.nc_mode = s.node_contact.mode;
+        o.nc_radius = R(s.node_contact.radius); o.nc_skin = R(s.node_contact.skin);
+        o.nc_margin = R(s.node_contact.margin); o.nc_restitution = R(s.node_contact.restitution);
+        o.nc_threshold = R(s.node_contact.restitution_speed_threshold);
+        o.nc_static = R(s.node_contact.static_friction); o.nc_dynamic = R(s.node_contact.dynamic_friction);
         o.plane_count = s.plane_count;
         for (unsigned p = 0; p < kPlanes; ++p) {
             const gbl_support_plane &in = s.planes[p];
@@ -1146,6 +1225,7 @@ private:
         Ctl c{};
         c.first_failure_step = c.last_failure_step = c.last_energy_gain_step = ~0ULL;
         c.full_restart = 1;
+        c.nc_rebuild = 1; // the pair list is built before its first use
         c.energy_flat_fraction = 1.0e-3;
         c.calm_damage_margin = 0.5;
         c.step_limit = step_limit;
@@ -1242,6 +1322,7 @@ private:
         blocks_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.dev.tiles_b / kScanBlock + 1; }, 1);
         each_ = span([](const Res &, U &b, U &e) { b = 0; e = 1; }, 1);
         slabs_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.sched.block_count; }, 1);
+        buckets_ = span([](const Res &l, U &b, U &e) { b = 0; e = l.nc_mem ? l.dev.nc_mask + 1U : 0U; }, kThreads);
         // With many lattices, the small ones sweep in one CTA each (largest first);
         // the level launches and the isolated-node launch cover the others.
         auto leveled = [this](const Res &l) { return !many_ || !sweptWhole(l); };
@@ -1409,18 +1490,22 @@ private:
         }
         // With a sphere, the strain and end sample outside the contact halo
         // run on a second stream beside the second contact pass; the halo's
-        // follow it.
-        const bool split = S.sphere_enabled != 0;
+        // follow it. Node-to-node contact moves nodes anywhere after that
+        // pass, so with it on the end phase waits for it whole.
+        const bool contact = S.nc_mode != 0;
+        const bool split = S.sphere_enabled != 0 && !contact;
         if (split) {
             check(cudaEventRecord(fork_, st), "event");
             check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
             endPhase<M>(side_, 1);
             check(cudaEventRecord(join_, side_), "event");
+        }
+        if (S.sphere_enabled)
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 2,
                                                                                                sphere_buffers_);
-        }
         mark(10);
         if (split) check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
+        if (contact) contactPhase<M>(st, mark);
         endPhase<M>(st, split ? 2 : 0, mark);
         if (tiles_.count) kTileCounts<R, M><<<tiles_.count, kThreads, 0, st>>>(grid(tiles_));
         kBlockScan<R, M><<<blocks_.count, kScanBlock, 0, st>>>(grid(blocks_), plastic_ ? 1 : 0);
@@ -1469,6 +1554,24 @@ private:
         case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
         default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
         }
+    }
+
+    // Node-to-node contact: the drift test, the pair-list rebuild (every
+    // kernel of it returns at once when no rebuild is due), the narrow phase.
+    template <bool M, class Mark> void contactPhase(cudaStream_t st, Mark &&mark) {
+        const Settings<R> &S = S_;
+        if (nodes_.count) kContactStale<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
+        if (buckets_.count) kContactClear<R, M><<<buckets_.count, kThreads, 0, st>>>(grid(buckets_));
+        if (nodes_.count) kContactCells<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
+        if (buckets_.count) kContactBuckets<R, M><<<buckets_.count, kThreads, 0, st>>>(grid(buckets_));
+        if (nodes_.count) kContactScatter<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_));
+        if (buckets_.count) kContactSort<R, M><<<buckets_.count, kThreads, 0, st>>>(grid(buckets_));
+        if (nodes_.count) kContactGather<R, M, false><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
+        kContactTiles<R, M><<<each_.count, kContactScanThreads, 0, st>>>(grid(each_));
+        if (nodes_.count) kContactGather<R, M, true><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
+        mark(14);
+        kContactNarrow<R, M><<<each_.count, 32, 0, st>>>(grid(each_), S);
+        mark(15);
     }
 
     // The start-of-substep restart: strain of the dirty (or all) nodes, then
@@ -1527,7 +1630,7 @@ private:
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
     Work *work_{};
-    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{};
+    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{}, buckets_{};
     // Level-launched lattices, in groups swept one after another.
     struct Group {
         std::vector<Span> levels;
@@ -1666,7 +1769,8 @@ public:
 
 template <class R> class Server final : public ServerBase {
 public:
-    Server(const gbl_step_settings &settings, std::uint64_t budget) : budget_(budget), t0_(clock()) {
+    Server(const gbl_step_settings &settings, std::uint64_t budget)
+        : budget_(budget), contact_(settings.node_contact.mode != 0), t0_(clock()) {
         engine_.configure(settings);
     }
 
@@ -1676,7 +1780,8 @@ public:
         if (sv.node_count != st.node_count || sv.bond_count != st.bond_count)
             invalid("lattice schedule does not match the lattice");
         const std::uint64_t bytes =
-            Resident<R>::footprint(st.node_count, st.bond_count, st.max_degree, sv.block_count);
+            Resident<R>::footprint(st.node_count, st.bond_count, st.max_degree, sv.block_count) +
+            (contact_ ? Resident<R>::contactBytes(st.node_count) : 0);
         if (bytes > budget_) invalid("request exceeds the device memory budget on its own");
         Request q;
         q.submitted = clock() - t0_;
@@ -1882,6 +1987,7 @@ private:
 
     Engine<R> engine_;
     std::uint64_t budget_, used_{0}, last_ticket_{0};
+    bool contact_; // node-to-node contact on: every request also holds its pair-list scratch
     std::uint64_t queued_{0}, running_{0}, done_{0}, substeps_run_{0};
     double device_seconds_{0}, admit_seconds_{0}, retire_seconds_{0}, run_seconds_{0};
     double t0_;

@@ -76,6 +76,12 @@ struct LoadLedger {
     double elapsed, req_imp[3], imp[3], req_ang[3], ang[3], work;
 };
 
+// NodeContactAccumulators (LatticePhysics.hpp:204-221).
+struct NodeAcc {
+    unsigned long long contacts, pair_tests, rebuilds, pairs_listed, pair_overflow;
+    double dissipated, max_overlap, max_correction, momentum[3];
+};
+
 // One device control block per lattice: the RunStatus accumulators, the
 // RunControl exit rules, and the substep's transient counters.
 struct Ctl {
@@ -96,6 +102,12 @@ struct Ctl {
     unsigned event_count, ext_count; // broken bonds this substep; loaded nodes (set between runs)
     unsigned dmg_count, energy_gain;  // damage-record candidates; any broken bond passed the gain test
     double plastic_substep, removed_substep;
+    // Node-to-node contact: its accumulators; whether the pair list is rebuilt
+    // this substep (set at upload, after a failure round, or by the drift
+    // test; cleared by the narrow phase), the list's length, and the bucket
+    // fill of the build in progress.
+    NodeAcc node;
+    unsigned nc_rebuild, nc_pairs, nc_members;
 };
 
 constexpr unsigned kErrExternalOverflow = 1;
@@ -142,6 +154,17 @@ template <class R> struct Dev {
     double *ext_req;      // requested force, 3 per node
     double *ext_contrib;  // 13 per node: impulse 3, angular 3, work, requested 3, requested angular 3
     std::uint32_t *ext_nodes;
+    // Node-to-node contact scratch, allocated when the settings turn contact
+    // on: positions at the last build, each node's grid cell (w: its bucket),
+    // the hashed grid (per bucket: count, then scatter cursor; first member;
+    // members ascending within a bucket), pairs per owner and per 256-node
+    // tile (then the tile's first pair), and the pair list in narrow-phase
+    // order (owner, partner, bond or kNoBond).
+    Q4<R> *nc_built;
+    int4 *nc_cell;
+    std::uint32_t *nc_count, *nc_start, *nc_members, *nc_fill, *nc_tile;
+    std::uint32_t *nc_pa, *nc_pb, *nc_pbond;
+    std::uint32_t nc_mask;
     double origin[3];
     Sphere<R> *sphere;
     Ctl *ctl;
@@ -1674,6 +1697,7 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
     }
     const unsigned broken = c.event_count;
     if (broken) {
+        c.nc_rebuild = 1; // a failure changes which pairs no live bond holds
         if (c.broken_bonds == 0) c.ffb_count = broken;
         c.removed_energy += c.removed_substep;
         if (c.energy_gain) c.last_energy_gain_step = step;
@@ -1701,6 +1725,358 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
         c.stop = 1;
         atomicSub(L.running, 1U);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Node-to-node contact (LatticePhysics.hpp:1441-1647; stage order
+// CpuLatticeBackend.cpp:424-436), after the second sphere pass and before the
+// end sample. The pair list holds, for every movable owner node, the movable
+// nodes of higher index within 2 r + skin that no live bond holds, in the
+// order of the 27 grid cells around the owner (z, then y, then x, from -1)
+// and ascending within a cell, at most kPairsPerNode per owner. It is rebuilt
+// when a bond failed in the previous substep or a node drifted more than
+// skin / 2 since the last build. The grid is hashed into buckets whose
+// members are kept ascending; every bucket scan keeps only the nodes of the
+// cell it visits, so which cells share a bucket never changes the list, and
+// each lattice sizes its own table. The narrow phase is the reference's
+// serial chain in list order, run by one warp.
+// ---------------------------------------------------------------------------
+constexpr std::uint32_t kPairsPerNode = 24;
+constexpr unsigned kContactScanThreads = 1024;
+
+// Teschner et al., "Optimized Spatial Hashing for Collision Detection of
+// Deformable Objects" (2003): three primes, exclusive-or, masked.
+__device__ __forceinline__ std::uint32_t cellBucket(int x, int y, int z, std::uint32_t mask) {
+    return ((static_cast<std::uint32_t>(x) * 73856093U) ^ (static_cast<std::uint32_t>(y) * 19349663U) ^
+            (static_cast<std::uint32_t>(z) * 83492791U)) & mask;
+}
+
+template <class R> __device__ __forceinline__ R contactCutoff(const Settings<R> &S) {
+    return R(2) * S.nc_radius + S.nc_skin;
+}
+
+// The drift test (nodeContactStale): any node farther than skin / 2 from where
+// the list was built asks for a rebuild.
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactStale(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop || *static_cast<volatile unsigned *>(&c.nc_rebuild)) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i >= w.end) return;
+    const R half = R(0.5) * S.nc_skin;
+    const R limit = half * half;
+    const V3<R> d = xyz(L.u[i]) - xyz(L.nc_built[i]);
+    if (dot(d, d) > limit) c.nc_rebuild = 1U;
+}
+
+// Rebuild, step 0 (bucket items): clear the bucket counts.
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactClear(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop || !c.nc_rebuild) return;
+    const std::uint32_t b = w.begin + threadIdx.x;
+    if (b < w.end) L.nc_count[b] = 0U;
+    if (w.begin == 0 && threadIdx.x == 0) c.nc_members = 0U;
+}
+
+// Rebuild, step 1 (nodeContactStoreCell, node items): the node's cell at the
+// positions of this substep, the positions kept for the drift test, and the
+// bucket counts of the movable nodes.
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactCells(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop || !L.ctl->nc_rebuild) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i >= w.end) return;
+    const R inverse_cell = R(1) / contactCutoff(S);
+    const V3<R> p = pos(L, i);
+    const int x = static_cast<int>(floor(p.x * inverse_cell));
+    const int y = static_cast<int>(floor(p.y * inverse_cell));
+    const int z = static_cast<int>(floor(p.z * inverse_cell));
+    const std::uint32_t b = cellBucket(x, y, z, L.nc_mask);
+    L.nc_cell[i] = make_int4(x, y, z, static_cast<int>(b));
+    L.nc_built[i] = L.u[i];
+    if (!(L.v[i].w <= R(0))) atomicAdd(&L.nc_count[b], 1U);
+}
+
+// Rebuild, step 2 (bucket items): each bucket's first member slot. Buckets of
+// one CTA are contiguous; the CTAs' runs are placed in any order, which only
+// moves whole buckets. The count becomes the scatter cursor.
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactBuckets(const Grid<R> launch) {
+    __shared__ unsigned buf[kThreads];
+    __shared__ unsigned base;
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop || !c.nc_rebuild) return;
+    const std::uint32_t b = w.begin + threadIdx.x;
+    const unsigned n = b < w.end ? L.nc_count[b] : 0U;
+    unsigned total = 0;
+    const unsigned ex = blockExclusiveScanU(n, buf, total);
+    if (threadIdx.x == 0) base = atomicAdd(&c.nc_members, total);
+    __syncthreads();
+    if (b < w.end) {
+        L.nc_start[b] = base + ex;
+        L.nc_count[b] = 0U;
+    }
+}
+
+// Rebuild, step 3 (node items): the movable nodes into their buckets.
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactScatter(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop || !L.ctl->nc_rebuild) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    if (i >= w.end || L.v[i].w <= R(0)) return;
+    const std::uint32_t b = static_cast<std::uint32_t>(L.nc_cell[i].w);
+    L.nc_members[L.nc_start[b] + atomicAdd(&L.nc_count[b], 1U)] = i;
+}
+
+// Rebuild, step 4 (bucket items): each bucket's members ascending (buckets
+// hold half a node on average; an insertion sort in place).
+template <class R, bool Many>
+__global__ void __launch_bounds__(kThreads) kContactSort(const Grid<R> launch) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    if (L.ctl->stop || !L.ctl->nc_rebuild) return;
+    const std::uint32_t b = w.begin + threadIdx.x;
+    if (b >= w.end) return;
+    const std::uint32_t n = L.nc_count[b];
+    std::uint32_t *m = L.nc_members + L.nc_start[b];
+    for (std::uint32_t k = 1; k < n; ++k) {
+        const std::uint32_t v = m[k];
+        std::uint32_t j = k;
+        for (; j > 0 && m[j - 1] > v; --j) m[j] = m[j - 1];
+        m[j] = v;
+    }
+}
+
+// Rebuild, step 5 (nodeContactGather, node items; tile = the item's 256
+// nodes). Count pass: each owner's pairs and the tile's total, and the pairs
+// that did not fit. Write pass: the pairs at the owner's place in the list.
+template <class R, bool Many, bool Write>
+__global__ void __launch_bounds__(kThreads) kContactGather(const Grid<R> launch, Settings<R> S) {
+    __shared__ unsigned buf[kThreads];
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop || !c.nc_rebuild) return;
+    const std::uint32_t i = w.begin + threadIdx.x;
+    const bool in = i < w.end;
+    const std::uint32_t tile = w.begin / kThreads;
+    std::uint32_t at = 0;
+    if (Write) {
+        unsigned total = 0;
+        at = L.nc_tile[tile] + blockExclusiveScanU(in ? L.nc_fill[i] : 0U, buf, total);
+    }
+    std::uint32_t fill = 0, overflow = 0;
+    if (in && !(L.v[i].w <= R(0))) {
+        const std::size_t N = L.N;
+        const R cutoff = contactCutoff(S);
+        const R cutoff_sq = cutoff * cutoff;
+        const V3<R> p = pos(L, i);
+        const int4 home = L.nc_cell[i];
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int gx = home.x + dx, gy = home.y + dy, gz = home.z + dz;
+                    const std::uint32_t b = cellBucket(gx, gy, gz, L.nc_mask);
+                    const std::uint32_t first = L.nc_start[b], n = L.nc_count[b];
+                    for (std::uint32_t k = 0; k < n; ++k) {
+                        const std::uint32_t j = L.nc_members[first + k];
+                        if (j <= i) continue;
+                        const int4 cj = L.nc_cell[j];
+                        if (cj.x != gx || cj.y != gy || cj.z != gz) continue;
+                        const V3<R> r = pos(L, j) - p;
+                        if (dot(r, r) > cutoff_sq) continue;
+                        // The pair's bond, if the owner lists one to j; a live one holds the pair.
+                        std::uint32_t bond = kNoBond;
+                        bool held = false;
+                        for (std::uint32_t s = 0; s < L.D; ++s) {
+                            const std::size_t slot = s * N + i;
+                            const std::uint32_t bs = L.nbr_bond[slot];
+                            if (bs == kNoBond) break;
+                            if (L.nbr_other[slot] != j) continue;
+                            bond = bs;
+                            held = L.nbr[slot].w != R(0);
+                            break;
+                        }
+                        if (held) continue;
+                        if (fill == kPairsPerNode) {
+                            ++overflow;
+                            continue;
+                        }
+                        if (Write) {
+                            L.nc_pa[at + fill] = i;
+                            L.nc_pb[at + fill] = j;
+                            L.nc_pbond[at + fill] = bond;
+                        }
+                        ++fill;
+                    }
+                }
+    }
+    if (!Write) {
+        if (in) L.nc_fill[i] = fill;
+        unsigned total = 0;
+        blockExclusiveScanU(fill, buf, total);
+        if (threadIdx.x == 0) L.nc_tile[tile] = total;
+        if (overflow) atomicAdd(&c.node.pair_overflow, static_cast<unsigned long long>(overflow));
+    }
+}
+
+// Rebuild, step 6 (one CTA per lattice): the tiles' first pairs in node order,
+// and the list's length (nodeContactActiveList).
+template <class R, bool Many>
+__global__ void __launch_bounds__(kContactScanThreads) kContactTiles(const Grid<R> launch) {
+    __shared__ unsigned buf[kContactScanThreads];
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop || !c.nc_rebuild) return;
+    const std::uint32_t tiles = (L.N + kThreads - 1) / kThreads;
+    unsigned carry = 0;
+    for (std::uint32_t t0 = 0; t0 < tiles; t0 += kContactScanThreads) {
+        const std::uint32_t t = t0 + threadIdx.x;
+        unsigned total = 0;
+        const unsigned ex = blockExclusiveScanU(t < tiles ? L.nc_tile[t] : 0U, buf, total);
+        if (t < tiles) L.nc_tile[t] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        c.nc_pairs = carry;
+        c.node.pairs_listed += carry;
+    }
+}
+
+// The narrow phase (nodeContactPass and nodeContactPair), one warp per lattice.
+// The lanes evaluate the next 32 pairs of the list against the current state
+// at once; the first pair whose response changes a velocity or a position is
+// applied by its lane, and the window restarts after it. Pairs before it
+// changed nothing, so they saw exactly the state the serial order shows them:
+// their tests and overlaps are counted as they are.
+template <class R, bool Many>
+__global__ void __launch_bounds__(32) kContactNarrow(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    const unsigned lane = threadIdx.x;
+    constexpr unsigned kAll = 0xffffffffU;
+    if (lane == 0 && c.nc_rebuild) {
+        ++c.node.rebuilds;
+        c.nc_rebuild = 0U;
+    }
+    __syncwarp();
+    const std::uint32_t count = c.nc_pairs;
+    NodeAcc acc = c.node;
+    const bool respond = S.nc_mode == 2U;
+    for (std::uint32_t at = 0; at < count;) {
+        const std::uint32_t q = at + lane;
+        bool tested = false, acts = false, impulse_on = false;
+        std::uint32_t a = 0, b = 0;
+        R gap = R(0), ma = R(0), mb = R(0), impulse = R(0), pair_inverse = R(0), ia = R(0), ib = R(0);
+        V3<R> n{}, va{}, vb{};
+        if (q < count) {
+            a = L.nc_pa[q];
+            b = L.nc_pb[q];
+            const std::uint32_t bond = L.nc_pbond[q];
+            const Q4<R> qa = L.v[a], qb = L.v[b];
+            ma = qa.w;
+            mb = qb.w;
+            const bool held = bond != kNoBond && !(L.rec[bond].a & kDeadBit);
+            if (!held && !(ma <= R(0) || mb <= R(0))) {
+                tested = true;
+                const V3<R> r = pos(L, b) - pos(L, a);
+                const R distance = length(r);
+                n = normalized(r);
+                gap = distance - R(2) * S.nc_radius;
+                if (respond) {
+                    va = xyz(qa);
+                    vb = xyz(qb);
+                    const R vn = dot(vb - va, n);
+                    if (!(gap > maxR(S.nc_margin, -vn * S.dt))) {
+                        ia = R(1) / ma;
+                        ib = R(1) / mb;
+                        pair_inverse = ia + ib;
+                        const R restitution = -vn > S.nc_threshold ? S.nc_restitution : R(0);
+                        const R desired = gap > S.nc_margin ? -gap / S.dt : -restitution * minR(vn, R(0));
+                        impulse = maxR(R(0), (desired - vn) / pair_inverse);
+                        impulse_on = impulse > R(0);
+                        acts = impulse_on || gap < -S.nc_margin;
+                    }
+                }
+            }
+        }
+        const unsigned acting = __ballot_sync(kAll, acts);
+        const unsigned first = acting ? static_cast<unsigned>(__ffs(acting)) - 1U : 32U;
+        const bool counted = tested && lane <= first;
+        acc.pair_tests += static_cast<unsigned long long>(__popc(__ballot_sync(kAll, counted)));
+        // The deepest overlap among the counted pairs (a running maximum of
+        // the same values, so the order of the lanes does not matter).
+        R deepest = counted && gap < R(0) ? -gap : R(0);
+        for (int o = 16; o > 0; o >>= 1) deepest = maxR(deepest, __shfl_xor_sync(kAll, deepest, o));
+        if (deepest > static_cast<R>(acc.max_overlap)) acc.max_overlap = static_cast<double>(deepest);
+        if (first == 32U) {
+            at += 32;
+            continue;
+        }
+        double dissipated = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+        R correction = R(0);
+        if (lane == first) {
+            if (impulse_on) {
+                const V3<R> va0 = va, vb0 = vb;
+                const R before = R(0.5) * ma * dot(va, va) + R(0.5) * mb * dot(vb, vb);
+                const V3<R> j = impulse * n;
+                vb = vb + ib * j;
+                va = va - ia * j;
+                const V3<R> rel = vb - va;
+                const V3<R> t = rel - dot(rel, n) * n;
+                const R speed = length(t);
+                if (speed > R(1.0e-12)) {
+                    const V3<R> dir = t / speed;
+                    const R stick = speed / pair_inverse;
+                    const R friction = stick <= S.nc_static * impulse ? stick : minR(stick, S.nc_dynamic * impulse);
+                    const V3<R> f = -friction * dir;
+                    vb = vb + ib * f;
+                    va = va - ia * f;
+                }
+                L.v[a] = Q4<R>{va.x, va.y, va.z, ma};
+                L.v[b] = Q4<R>{vb.x, vb.y, vb.z, mb};
+                dissipated = static_cast<double>(before - (R(0.5) * ma * dot(va, va) + R(0.5) * mb * dot(vb, vb)));
+                mx = static_cast<double>(ma * (va.x - va0.x) + mb * (vb.x - vb0.x));
+                my = static_cast<double>(ma * (va.y - va0.y) + mb * (vb.y - vb0.y));
+                mz = static_cast<double>(ma * (va.z - va0.z) + mb * (vb.z - vb0.z));
+            }
+            if (gap < -S.nc_margin) {
+                correction = minR(-gap - S.nc_margin, R(0.2) * S.nc_radius);
+                const V3<R> shift = (correction / pair_inverse) * n;
+                const Q4<R> ua = L.u[a], ub = L.u[b];
+                const V3<R> na = xyz(ua) - ia * shift, nb = xyz(ub) + ib * shift;
+                L.u[a] = Q4<R>{na.x, na.y, na.z, ua.w};
+                L.u[b] = Q4<R>{nb.x, nb.y, nb.z, ub.w};
+            }
+        }
+        // The applied pair's sums, folded in list order on every lane.
+        if (__shfl_sync(kAll, impulse_on, first)) {
+            acc.dissipated += __shfl_sync(kAll, dissipated, first);
+            acc.momentum[0] += __shfl_sync(kAll, mx, first);
+            acc.momentum[1] += __shfl_sync(kAll, my, first);
+            acc.momentum[2] += __shfl_sync(kAll, mz, first);
+            ++acc.contacts;
+        }
+        correction = __shfl_sync(kAll, correction, first);
+        if (correction > static_cast<R>(acc.max_correction)) acc.max_correction = static_cast<double>(correction);
+        __syncwarp(); // the applied pair's writes, before the next window reads
+        at += first + 1U;
+    }
+    if (lane == 0) c.node = acc;
 }
 
 } // namespace gbl

@@ -81,6 +81,10 @@ template <class R> struct Settings {
     R c_static, c_dynamic, c_restitution, c_threshold, c_node_radius, c_margin, c_slack;
     std::uint32_t plane_count;
     Plane<R> planes[kPlanes];
+    // NodeContactSettings (LatticePhysics.hpp:188-202): 0 off, 2 on, any
+    // other value measures (broad and narrow phase, no response).
+    std::uint32_t nc_mode;
+    R nc_radius, nc_skin, nc_margin, nc_restitution, nc_threshold, nc_static, nc_dynamic;
 };
 
 template <class R> struct Sphere { V3<R> center, velocity, angular; R radius, mass, inertia; };

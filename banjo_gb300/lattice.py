@@ -142,6 +142,12 @@ class ServerStats(C.Structure):
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE = 0, 1, 2
 
 
+class NodeContactAccumulators(C.Structure):
+    _fields_ = [(n, C.c_ulonglong) for n in ("contacts", "pair_tests", "rebuilds", "pairs_listed", "pair_overflow")] + \
+        [(n, C.c_double) for n in ("dissipated_kinetic_energy_j", "maximum_overlap_m", "maximum_position_correction_m",
+                                   "momentum_residual_x", "momentum_residual_y", "momentum_residual_z")]
+
+
 class RunStatus(C.Structure):
     _fields_ = [("total_steps", C.c_uint64), ("first_failure_step", C.c_uint64), ("last_failure_step", C.c_uint64),
                 ("failure_rounds", C.c_uint32), ("broken_bonds", C.c_uint32), ("removed_energy_j", C.c_double),
@@ -152,7 +158,7 @@ class RunStatus(C.Structure):
                 ("phase_seconds", C.c_double * 16), ("max_tensile_stretch", C.c_float),
                 ("max_compressive_strain", C.c_float), ("max_shear_strain", C.c_float),
                 ("rank_deficient_nodes", C.c_uint32), ("plastic_work_j", C.c_double),
-                ("max_plastic_stretch", C.c_float)]
+                ("max_plastic_stretch", C.c_float), ("node_contact", NodeContactAccumulators)]
 
 
 PHASE_NAMES = ["capture", "start_sample_nodes", "start_sample_bonds", "kick_classify", "contact_pass_1",
@@ -231,7 +237,7 @@ def library() -> C.CDLL:
                       ("gbl_step_settings", StepSettings), ("gbl_sphere", Sphere),
                       ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
                       ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats),
-                      ("gbl_box_spec", BoxSpec)]:
+                      ("gbl_box_spec", BoxSpec), ("gbl_node_contact_accumulators", NodeContactAccumulators)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -748,18 +754,21 @@ def footprint(node_count: int, bond_count: int, max_degree: int, block_count: in
 
 def status_arrays(st: RunStatus) -> dict:
     """RunStatus packed as the case files pack it (oracle/case_layout.hpp)."""
-    u = np.zeros(13, dtype=np.uint64)
+    nc = st.node_contact
+    u = np.zeros(18, dtype=np.uint64)
     u[:] = [st.total_steps, st.first_failure_step, st.last_failure_step, st.failure_rounds, st.broken_bonds,
             st.last_energy_gain_step, st.last_damage_gain_step, st.exit_reason, st.rank_deficient_nodes,
-            st.contact.impulse_contacts, st.contact.candidate_overflow, st.contact.ball_support_events, st.launches]
-    d = np.zeros(20, dtype=np.float64)
+            st.contact.impulse_contacts, st.contact.candidate_overflow, st.contact.ball_support_events, st.launches,
+            nc.contacts, nc.pair_tests, nc.rebuilds, nc.pairs_listed, nc.pair_overflow]
+    d = np.zeros(26, dtype=np.float64)
     d[:] = [st.removed_energy_j, st.max_damage, st.plastic_work_j, st.max_tensile_stretch,
             st.max_compressive_strain, st.max_shear_strain, st.max_plastic_stretch,
             st.contact.impulse_to_material_x, st.contact.impulse_to_material_y, st.contact.impulse_to_material_z,
             st.contact.dissipated_kinetic_energy_j, st.contact.maximum_penetration_m,
             st.contact.maximum_position_correction_m, st.contact.maximum_center_shift_m, st.external_load.work_j,
             st.external_load.impulse_n_s[0], st.external_load.impulse_n_s[1], st.external_load.impulse_n_s[2],
-            float(st.external_load.steps), st.wall_seconds]
+            float(st.external_load.steps), st.wall_seconds, nc.dissipated_kinetic_energy_j, nc.maximum_overlap_m,
+            nc.maximum_position_correction_m, nc.momentum_residual_x, nc.momentum_residual_y, nc.momentum_residual_z]
     return {"status_u64": u, "status_f64": d}
 
 

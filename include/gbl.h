@@ -129,7 +129,7 @@ typedef struct gbl_contact_settings {
 } gbl_contact_settings;
 
 typedef struct gbl_node_contact_settings {
-    uint8_t mode; /* 0 off; node-to-node contact modes 1 and 2 are refused */
+    uint8_t mode; /* 0 off, 1 measure (pairs tested, overlap recorded, no response), 2 on */
     double radius, skin, margin, restitution, restitution_speed_threshold, static_friction, dynamic_friction;
     uint32_t bucket_mask;
 } gbl_node_contact_settings;
@@ -196,6 +196,15 @@ typedef struct gbl_load_ledger {
     double work_j;
 } gbl_load_ledger;
 
+/* NodeContactAccumulators (LatticePhysics.hpp:204-221). */
+typedef struct gbl_node_contact_accumulators {
+    unsigned long long contacts, pair_tests, rebuilds, pairs_listed, pair_overflow;
+    double dissipated_kinetic_energy_j;
+    double maximum_overlap_m;
+    double maximum_position_correction_m;
+    double momentum_residual_x, momentum_residual_y, momentum_residual_z;
+} gbl_node_contact_accumulators;
+
 typedef struct gbl_run_status {
     uint64_t total_steps;
     uint64_t first_failure_step;
@@ -218,6 +227,7 @@ typedef struct gbl_run_status {
     uint32_t rank_deficient_nodes;
     double plastic_work_j;
     float max_plastic_stretch;
+    gbl_node_contact_accumulators node_contact;
 } gbl_run_status;
 
 typedef struct gbl_backend gbl_backend;
