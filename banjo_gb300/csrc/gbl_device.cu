@@ -1112,6 +1112,110 @@ public:
         }
     }
 
+    // The batch autotuner: times the projection sweep of the lattices present
+    // under candidate launch shapes and keeps the fastest. The sweep writes
+    // positions (saved here and restored after), multipliers (rewritten by
+    // the first iteration of every sweep) and support contact flags (cleared
+    // by every kick), so the lattices' state is unchanged.
+    gbl_tuning tune() {
+        requireReady();
+        if (active_.empty()) invalid("the batch holds no lattice");
+        dropGraph();
+        std::size_t total = 0;
+        for (auto k : active_) total += sizeof(Q4<R>) * slots_[k]->N;
+        void *saved = nullptr;
+        check(cudaMallocAsync(&saved, total ? total : 256, stream_), "device allocation");
+        auto positions = [&](bool save) {
+            std::size_t off = 0;
+            for (auto k : active_) {
+                const std::size_t n = sizeof(Q4<R>) * slots_[k]->N;
+                char *keep = static_cast<char *>(saved) + off;
+                void *u = slots_[k]->dev.u;
+                if (n) check(cudaMemcpyAsync(save ? keep : u, save ? u : keep, n, cudaMemcpyDeviceToDevice, stream_), "copy");
+                off += n;
+            }
+        };
+        positions(true);
+        cudaEvent_t t0 = nullptr, t1 = nullptr;
+        check(cudaEventCreate(&t0), "event");
+        check(cudaEventCreate(&t1), "event");
+        auto timeShape = [&](const Shape &sh) {
+            shape_ = sh;
+            buildWork();
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t e = nullptr;
+            check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
+            if (many_) enqueueSweep<true>([](unsigned) {});
+            else enqueueSweep<false>([](unsigned) {});
+            check(cudaStreamEndCapture(stream_, &g), "graph capture");
+            check(cudaGraphInstantiate(&e, g, 0), "graph instantiate");
+            check(cudaGraphLaunch(e, stream_), "graph launch");
+            float best = 0.0F;
+            for (int rep = 0; rep < 3; ++rep) {
+                check(cudaEventRecord(t0, stream_), "event");
+                check(cudaGraphLaunch(e, stream_), "graph launch");
+                check(cudaEventRecord(t1, stream_), "event");
+                check(cudaEventSynchronize(t1), "tune");
+                float ms = 0.0F;
+                check(cudaEventElapsedTime(&ms, t0, t1), "event");
+                best = rep == 0 ? ms : std::min(best, ms);
+            }
+            cudaGraphExecDestroy(e);
+            cudaGraphDestroy(g);
+            return static_cast<double>(best);
+        };
+        const Shape fallback{};
+        gbl_tuning out{};
+        Shape best = fallback;
+        double best_ms = timeShape(fallback);
+        out.default_ms = best_ms;
+        out.candidates = 1;
+        if (many_) {
+            // The one-CTA sweep's CTA size and reach together, then the group size.
+            for (unsigned threads : {256U, 512U, 1024U})
+                for (std::uint32_t reach : {1U << 16, 1U << 17, 1U << 18, 1U << 19}) {
+                    Shape sh = best;
+                    sh.sweep_threads = threads;
+                    sh.whole_max_bonds = reach;
+                    if (sh.sweep_threads == fallback.sweep_threads && sh.whole_max_bonds == fallback.whole_max_bonds)
+                        continue;
+                    const double ms = timeShape(sh);
+                    ++out.candidates;
+                    if (ms < best_ms) { best_ms = ms; best = sh; }
+                }
+            const Shape base = best;
+            for (std::size_t mb : {16U, 32U, 96U, 192U}) {
+                Shape sh = base;
+                sh.group_bytes = mb << 20;
+                const double ms = timeShape(sh);
+                ++out.candidates;
+                if (ms < best_ms) { best_ms = ms; best = sh; }
+            }
+        }
+        positions(false);
+        check(cudaFreeAsync(saved, stream_), "device free");
+        check(cudaStreamSynchronize(stream_), "tune");
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        shape_ = best;
+        dirty_ = true;
+        out.sweep_threads = best.sweep_threads;
+        out.whole_max_bonds = best.whole_max_bonds;
+        out.group_bytes = best.group_bytes;
+        out.sweep_ms = best_ms;
+        return out;
+    }
+
+    void setShape(const gbl_tuning &t) {
+        if (t.sweep_threads && t.sweep_threads != 256 && t.sweep_threads != 512 && t.sweep_threads != 1024)
+            invalid("the one-CTA sweep takes 256, 512 or 1024 threads");
+        if (t.whole_max_bonds > (1U << 24)) invalid("the one-CTA sweep takes lattices of at most 2^24 bonds");
+        if (t.sweep_threads) shape_.sweep_threads = t.sweep_threads;
+        if (t.whole_max_bonds) shape_.whole_max_bonds = t.whole_max_bonds;
+        if (t.group_bytes) shape_.group_bytes = t.group_bytes;
+        dirty_ = true;
+    }
+
     std::uint64_t kernelsPerSubstep() {
         requireReady();
         if (active_.empty()) return 0;
@@ -1290,8 +1394,8 @@ private:
 
     // A lattice of a batch swept by one CTA (kSweepLattice): small enough to
     // keep its nodes in L2 across its levels, with levels that fit the table.
-    static bool sweptWhole(const Resident<R> &l) {
-        return l.B > 0 && l.B <= kMaxFusedBonds && l.dev.level_count == l.levels.size();
+    bool sweptWhole(const Resident<R> &l) const {
+        return l.B > 0 && l.B <= shape_.whole_max_bonds && l.dev.level_count == l.levels.size();
     }
 
     // Work lists of every phase, one item per CTA, lattices in slot order.
@@ -1357,7 +1461,7 @@ private:
                 const Res &l = *slots_[k];
                 if (!leveled(l)) continue;
                 const std::size_t need = static_cast<std::size_t>(l.N) * sizeof(Q4<R>);
-                if (!members.back().empty() && bytes + need > kGroupNodeBytes) {
+                if (!members.back().empty() && bytes + need > shape_.group_bytes) {
                     members.emplace_back();
                     bytes = 0;
                 }
@@ -1455,29 +1559,7 @@ private:
             check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
         }
         mark(4);
-        // The small lattices of a batch sweep whole, one CTA each, on the
-        // second stream beside the level launches of the others.
-        const bool whole = M && whole_.count;
-        if (whole) {
-            check(cudaEventRecord(fork_, st), "event");
-            check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
-            launchSweepWhole(whole_, side_);
-            check(cudaEventRecord(join_, side_), "event");
-        }
-        const unsigned I = S.iterations;
-        for (const Group &g : groups_)
-            for (unsigned it = 0; it < I; ++it) {
-                const bool first = it == 0, last = it + 1 == I;
-                for (const Span &lv : g.levels) launchSolve<M>(lv, first, last, g.levels.size() >= 2);
-                mark(5);
-                if (S.plane_count && g.isolated.count)
-                    kSupportIsolated<R, M><<<g.isolated.count, kThreads, 0, st>>>(grid(g.isolated), S);
-                mark(7);
-            }
-        if (whole) {
-            check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
-            mark(5);
-        }
+        enqueueSweep<M>(mark);
         if (nodes_.count)
             kVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S, S.damping_fraction <= R(0) ? 1 : 0);
         mark(8);
@@ -1518,6 +1600,34 @@ private:
         check(cudaGetLastError(), "kernel launch");
     }
 
+    // The projection sweep: the small lattices of a batch sweep whole, one
+    // CTA each, on the second stream beside the level launches of the others.
+    template <bool M, class Mark> void enqueueSweep(Mark &&mark) {
+        const Settings<R> &S = S_;
+        cudaStream_t st = stream_;
+        const bool whole = M && whole_.count;
+        if (whole) {
+            check(cudaEventRecord(fork_, st), "event");
+            check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
+            launchSweepWhole(whole_, side_);
+            check(cudaEventRecord(join_, side_), "event");
+        }
+        const unsigned I = S.iterations;
+        for (const Group &g : groups_)
+            for (unsigned it = 0; it < I; ++it) {
+                const bool first = it == 0, last = it + 1 == I;
+                for (const Span &lv : g.levels) launchSolve<M>(lv, first, last, g.levels.size() >= 2);
+                mark(5);
+                if (S.plane_count && g.isolated.count)
+                    kSupportIsolated<R, M><<<g.isolated.count, kThreads, 0, st>>>(grid(g.isolated), S);
+                mark(7);
+            }
+        if (whole) {
+            check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
+            mark(5);
+        }
+    }
+
     // A launch that may start while the previous kernel of the stream still
     // runs (programmatic dependent launch); the kernel waits for it itself.
     // Only between sweep levels of two or more levels per iteration: a level
@@ -1544,15 +1654,21 @@ private:
     }
 
     void launchSweepWhole(const Span &span, cudaStream_t st) {
+        switch (shape_.sweep_threads) {
+        case 256: launchSweepWholeAs<256>(span, st); break;
+        case 1024: launchSweepWholeAs<1024>(span, st); break;
+        default: launchSweepWholeAs<512>(span, st); break;
+        }
+    }
+    template <unsigned T> void launchSweepWholeAs(const Span &span, cudaStream_t st) {
         const bool support = S_.plane_count != 0;
         const int key = (plastic_ ? 2 : 0) | (support ? 1 : 0);
         const Grid<R> g = grid(span);
-        const unsigned smem = 0;
         switch (key) {
-        case 0: kSweepLattice<R, kDirect, false, false><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
-        case 1: kSweepLattice<R, kDirect, false, true><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
-        case 2: kSweepLattice<R, kDirect, true, false><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
-        default: kSweepLattice<R, kDirect, true, true><<<span.count, kSweepThreads, smem, st>>>(g, S_); break;
+        case 0: kSweepLattice<R, kDirect, false, false, T><<<span.count, T, 0, st>>>(g, S_); break;
+        case 1: kSweepLattice<R, kDirect, false, true, T><<<span.count, T, 0, st>>>(g, S_); break;
+        case 2: kSweepLattice<R, kDirect, true, false, T><<<span.count, T, 0, st>>>(g, S_); break;
+        default: kSweepLattice<R, kDirect, true, true, T><<<span.count, T, 0, st>>>(g, S_); break;
         }
     }
 
@@ -1639,7 +1755,16 @@ private:
     std::vector<Group> groups_;
     // Node bytes a group may hold: its node arrays stay in the 129 MB L2
     // beside the streamed bond records of a level.
-    static constexpr std::size_t kGroupNodeBytes = std::size_t(48) << 20;
+    // Launch shapes of a batch's sweep (results do not depend on them): the
+    // one-CTA sweep's CTA size, the largest lattice it takes, and the node
+    // bytes of a level-launched group. Defaults measured on the trial
+    // workload; tune() times candidates on the lattices present.
+    struct Shape {
+        unsigned sweep_threads = kSweepThreads;
+        std::uint32_t whole_max_bonds = kMaxFusedBonds;
+        std::size_t group_bytes = std::size_t(48) << 20;
+    };
+    Shape shape_;
     cudaStream_t own_stream_{}, stream_{}, side_{};
     cudaEvent_t ev0_{}, ev1_{}, fork_{}, join_{};
     cudaGraph_t graph_{};
@@ -1724,6 +1849,8 @@ public:
     virtual void profile(std::uint64_t substeps, double *phase_ms) = 0;
     virtual std::uint64_t kernelsPerSubstep() = 0;
     virtual void setStream(cudaStream_t s) = 0;
+    virtual gbl_tuning tune() = 0;
+    virtual void setShape(const gbl_tuning &t) = 0;
 };
 
 template <class R> class Batch final : public BatchBase {
@@ -1743,6 +1870,8 @@ public:
     void profile(std::uint64_t substeps, double *phase_ms) override { engine_.profile(substeps, phase_ms); }
     std::uint64_t kernelsPerSubstep() override { return engine_.kernelsPerSubstep(); }
     void setStream(cudaStream_t s) override { engine_.setStream(s); }
+    gbl_tuning tune() override { return engine_.tune(); }
+    void setShape(const gbl_tuning &t) override { engine_.setShape(t); }
 
 private:
     Engine<R> engine_;
@@ -2208,6 +2337,21 @@ gbl_result gbl_batch_set_external_forces(gbl_batch *batch, uint32_t index, const
     return gbl::guard([&] {
         if (!batch) gbl::invalid("null batch");
         batch->impl->setExternalForces(index, forces, count, substeps);
+    });
+}
+
+gbl_result gbl_batch_tune(gbl_batch *batch, gbl_tuning *chosen) {
+    return gbl::guard([&] {
+        if (!batch) gbl::invalid("null batch");
+        const gbl_tuning t = batch->impl->tune();
+        if (chosen) *chosen = t;
+    });
+}
+
+gbl_result gbl_batch_set_tuning(gbl_batch *batch, const gbl_tuning *shape) {
+    return gbl::guard([&] {
+        if (!batch || !shape) gbl::invalid("null argument");
+        batch->impl->setShape(*shape);
     });
 }
 

@@ -264,7 +264,7 @@ size_t gbl_struct_size(const char *name) {
 #define GBL_SIZE(T) if (n == #T) return sizeof(T);
     GBL_SIZE(gbl_schedule_view) GBL_SIZE(gbl_state_view) GBL_SIZE(gbl_footprint) GBL_SIZE(gbl_support_plane)
     GBL_SIZE(gbl_contact_settings) GBL_SIZE(gbl_node_contact_settings) GBL_SIZE(gbl_step_settings)
-    GBL_SIZE(gbl_node_contact_accumulators)
+    GBL_SIZE(gbl_node_contact_accumulators) GBL_SIZE(gbl_tuning)
     GBL_SIZE(gbl_sphere) GBL_SIZE(gbl_run_control) GBL_SIZE(gbl_contact_accumulators) GBL_SIZE(gbl_load_ledger)
     GBL_SIZE(gbl_run_status) GBL_SIZE(gbl_matter_view) GBL_SIZE(gbl_request_info) GBL_SIZE(gbl_server_stats)
     GBL_SIZE(gbl_box_spec)

@@ -1037,19 +1037,14 @@ __global__ void __launch_bounds__(kThreads, GBL_SOLVE_MIN_BLOCKS) kSolve(const G
 // L2 (and the SM's L1) across all its levels instead of being streamed from
 // HBM again at every level launch; the arithmetic and the per-node order are
 // those of the level launches.
-#ifndef GBL_SWEEP_THREADS
-#define GBL_SWEEP_THREADS 512
-#endif
-#ifndef GBL_SWEEP_MIN_BLOCKS
-#define GBL_SWEEP_MIN_BLOCKS 2
-#endif
-constexpr unsigned kSweepThreads = GBL_SWEEP_THREADS;
-constexpr unsigned kSweepSlots = kSweepThreads * kSolvePer;
+// The CTA size (256, 512 or 1024 threads) is a launch shape the batch's
+// autotuner picks; two CTAs per SM below 1024 threads.
+constexpr unsigned kSweepThreads = 512; // the default shape
 constexpr std::uint32_t kMaxFusedLevels = 1024;
 // A lattice's one-CTA sweep takes as long as its bonds over one CTA's rate, so
 // only lattices small enough to finish well within the batch's level launches
 // are swept whole (measured: a 48^3 trial alone in one CTA bounded the whole
-// batch's sweep).
+// batch's sweep). The default bound; the autotuner picks its own.
 constexpr std::uint32_t kMaxFusedBonds = 1U << 18;
 
 template <class R, bool Support>
@@ -1064,8 +1059,8 @@ __device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Sett
     }
 }
 
-template <class R, bool Direct, bool Plastic, bool Support>
-__global__ void __launch_bounds__(kSweepThreads, GBL_SWEEP_MIN_BLOCKS) kSweepLattice(const Grid<R> launch, Settings<R> S) {
+template <class R, bool Direct, bool Plastic, bool Support, unsigned T>
+__global__ void __launch_bounds__(T, T >= 1024 ? 1 : 2) kSweepLattice(const Grid<R> launch, Settings<R> S) {
     // The lattice's descriptor, copied once into shared memory: its fields
     // are read throughout the sweep, and shared memory is never written by
     // the sweep's global stores, so the compiler may keep them as it likes.
@@ -1098,7 +1093,7 @@ __global__ void __launch_bounds__(kSweepThreads, GBL_SWEEP_MIN_BLOCKS) kSweepLat
         R lam, pl;
     };
     auto advance = [&](Round &r) {
-        r.base += kSweepThreads;
+        r.base += T;
         if (r.base < L.level_begin[r.lv + 1]) return true;
         if (++r.lv == L.level_count) {
             r.lv = 0;
@@ -1107,7 +1102,7 @@ __global__ void __launch_bounds__(kSweepThreads, GBL_SWEEP_MIN_BLOCKS) kSweepLat
         r.base = L.level_begin[r.lv];
         return true;
     };
-    const bool self_next = L.level_count == 1 && L.level_begin[1] - L.level_begin[0] <= kSweepThreads;
+    const bool self_next = L.level_count == 1 && L.level_begin[1] - L.level_begin[0] <= T;
     auto load = [&](const Round &r, Streamed &x) {
         const std::uint32_t d = r.base + threadIdx.x;
         if (d < L.level_begin[r.lv + 1]) {

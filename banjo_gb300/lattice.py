@@ -126,6 +126,15 @@ class BoxSpec(C.Structure):
                 ("threshold", C.c_double * 6)]
 
 
+class Tuning(C.Structure):
+    """gbl_tuning: a batch's launch shapes (results never depend on them)."""
+    _fields_ = [("sweep_threads", C.c_uint32), ("whole_max_bonds", C.c_uint32), ("group_bytes", C.c_uint64),
+                ("sweep_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RequestInfo(C.Structure):
     _fields_ = [("phase", C.c_int32), ("slot", C.c_uint32), ("substeps", C.c_uint64), ("substeps_done", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("submitted_s", C.c_double), ("admitted_s", C.c_double),
@@ -211,6 +220,8 @@ def library() -> C.CDLL:
         "gbl_batch_download": ([vp, C.c_uint32, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
         "gbl_batch_first_failure_bonds": ([vp, C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
+        "gbl_batch_tune": ([vp, C.POINTER(Tuning)], C.c_int),
+        "gbl_batch_set_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
         "gbl_batch_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_set_stream": ([vp, vp], C.c_int),
         "gbl_build_box": ([C.POINTER(BoxSpec), C.POINTER(vp)], C.c_int),
@@ -237,7 +248,8 @@ def library() -> C.CDLL:
                       ("gbl_step_settings", StepSettings), ("gbl_sphere", Sphere),
                       ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
                       ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats),
-                      ("gbl_box_spec", BoxSpec), ("gbl_node_contact_accumulators", NodeContactAccumulators)]:
+                      ("gbl_box_spec", BoxSpec), ("gbl_node_contact_accumulators", NodeContactAccumulators),
+                      ("gbl_tuning", Tuning)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -695,6 +707,17 @@ class Batch:
         _call(library().gbl_batch_profile_phases, self._h, int(substeps), _ptr(out, C.c_double))
         return {PHASE_NAMES[k]: float(out[k]) for k in range(16)}
 
+    def tune(self) -> dict:
+        """Times the sweep under candidate launch shapes, keeps the fastest
+        (state unchanged); returns the kept shape and the timings."""
+        t = Tuning()
+        _call(library().gbl_batch_tune, self._h, C.byref(t))
+        return t.as_dict()
+
+    def set_tuning(self, sweep_threads: int = 0, whole_max_bonds: int = 0, group_bytes: int = 0) -> None:
+        t = Tuning(sweep_threads, whole_max_bonds, group_bytes, 0.0, 0.0, 0)
+        _call(library().gbl_batch_set_tuning, self._h, C.byref(t))
+
 
 class Server:
     """Continuous batching of lattice requests under a device memory budget
@@ -831,11 +854,12 @@ def _outputs(state: State, sp: Sphere, ffb: np.ndarray, st: RunStatus) -> dict:
     return out
 
 
-def run_batch(cases: list, precision: str = "float", control: RunControl | None = None) -> list:
+def run_batch(cases: list, precision: str = "float", control: RunControl | None = None, tuning=None) -> list:
     """Runs scene cases as one batch (they must share step settings) and
     returns one output dict per case: the state and status keys of run_case.
     Every case runs `control` (default: the longest case's substep count);
-    exit rules stop each case on its own."""
+    exit rules stop each case on its own. `tuning`: "tune" runs the autotuner
+    after settling, a dict sets launch shapes (Batch.set_tuning)."""
     for c in cases[1:]:
         if not np.array_equal(c["settings"], cases[0]["settings"]):
             raise ValueError("the cases of one batch share their step settings")
@@ -850,6 +874,10 @@ def run_batch(cases: list, precision: str = "float", control: RunControl | None 
         batch.add(sched, state, sphere_state(c["sphere"]))
         states.append(state)
     batch.settle(settings)
+    if tuning == "tune":
+        batch.tune()
+    elif tuning:
+        batch.set_tuning(**tuning)
     for k, c in enumerate(cases):
         if c.get("forces") is not None and "force_ramp_steps" not in c:
             batch.set_external_forces(k, c["forces"], int(c["force_substeps"][0]))

@@ -207,6 +207,12 @@ def batched_leg(args, lattice) -> dict:
         sizes = list(ex.map(add, specs))
     build_s = time.perf_counter() - t0
     batch.settle(settings)
+    tuning = None
+    if not args.no_tune:
+        # The autotuner: sweep launch shapes timed on these lattices (state unchanged).
+        t0 = time.perf_counter()
+        tuning = batch.tune()
+        tuning["tune_s"] = time.perf_counter() - t0
     nodes = sum(n for n, _ in sizes)
     bonds = sum(b for _, b in sizes)
     w, k = args.warmup * SUBSTEPS_PER_STEP, args.steps * SUBSTEPS_PER_STEP
@@ -240,7 +246,7 @@ def batched_leg(args, lattice) -> dict:
             "plain": {"value": plain, "unit": "projections/s", "trials": plain_n,
                       "note": "the first trials of the same draw, each alone through the single-lattice backend "
                               "(its own captured substep graph), device time summed"},
-            "speedup_vs_plain": value / plain,
+            "speedup_vs_plain": value / plain, "tuning": tuning,
             "phase_ms_per_substep": {name: v for name, v in phases.items() if v > 0},
             "workload": f"{len(specs)} drop trials, edges 8..48 per axis (seeded), one batch; step = "
                         f"{SUBSTEPS_PER_STEP} substeps, I={ITERATIONS}; device time of {args.steps} steps"}
@@ -598,6 +604,7 @@ def main() -> None:
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--trials", type=int, default=4096, help="batched leg: trials in one batch (0: skip)")
     p.add_argument("--plain-trials", type=int, default=64, help="batched leg: trials timed one at a time")
+    p.add_argument("--no-tune", action="store_true", help="batched leg: keep the default launch shapes")
     p.add_argument("--served-window", type=float, default=0.25, help="served leg: seconds of arrivals (0: skip)")
     p.add_argument("--served-rate", type=float, default=2000.0)
     p.add_argument("--served-substeps", type=int, default=40)

@@ -319,6 +319,23 @@ gbl_result gbl_batch_status(gbl_batch *batch, uint32_t index, gbl_run_status *st
 gbl_result gbl_batch_download(gbl_batch *batch, uint32_t index, gbl_state_view *state, gbl_sphere *sphere);
 gbl_result gbl_batch_first_failure_bonds(gbl_batch *batch, uint32_t index, uint32_t *out, uint64_t capacity,
                                          uint64_t *count);
+/* The batch's launch shapes and the autotuner that picks them. Every shape
+ * runs the same sweep levels in the same order, so results never depend on
+ * it; only speed does. gbl_batch_tune (after gbl_batch_settle) times the
+ * projection sweep of the lattices present under each candidate shape --
+ * positions are saved before and restored after, so the lattices' state is
+ * unchanged -- and keeps the fastest; gbl_batch_set_tuning applies a known
+ * shape without timing (zero fields keep the current value). */
+typedef struct gbl_tuning {
+    uint32_t sweep_threads;   /* CTA size of the one-CTA sweep of a small lattice: 256, 512 or 1024 */
+    uint32_t whole_max_bonds; /* the largest lattice (bonds) swept by one CTA; larger ones are level-launched */
+    uint64_t group_bytes;     /* node bytes of a group of level-launched lattices swept together */
+    double sweep_ms;          /* the kept shape's sweep, per substep (tune only) */
+    double default_ms;        /* the default shape's sweep, per substep (tune only) */
+    uint32_t candidates;      /* shapes timed (tune only) */
+} gbl_tuning;
+gbl_result gbl_batch_tune(gbl_batch *batch, gbl_tuning *chosen);
+gbl_result gbl_batch_set_tuning(gbl_batch *batch, const gbl_tuning *shape);
 /* As gbl_profile_phases, over every lattice of the batch. */
 gbl_result gbl_batch_profile_phases(gbl_batch *batch, uint64_t substeps, double *phase_ms);
 gbl_result gbl_batch_kernels_per_substep(gbl_batch *batch, uint64_t *count);

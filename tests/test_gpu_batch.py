@@ -130,3 +130,39 @@ def test_batch_refuses_mixed_settings(gbl):
     b = scenes.impact_block(nx=8, ny=6, nz=8, blocks=2, radius=0.02, steps=1)
     with pytest.raises(ValueError, match="share"):
         gbl.run_batch([a, b])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["tune", {"sweep_threads": 256, "whole_max_bonds": 1 << 24},
+                                   {"sweep_threads": 1024, "whole_max_bonds": 1}, {"group_bytes": 1 << 16}])
+def test_batch_launch_shapes_leave_results_unchanged(device, shape):
+    """The autotuner's choices (one-CTA sweep size and reach, group size) and
+    its timing runs change nothing: every shape runs the same levels."""
+    cases = _drop_trials()
+    base = device.run_batch(cases)
+    shaped = device.run_batch(cases, tuning=shape)
+    for a, b in zip(base, shaped):
+        assert mismatches(a, b, STATE_KEYS) == []
+        assert status_mismatches(a, b) == []
+
+
+@pytest.mark.gpu
+def test_batch_tuned_mid_run_equals_untuned(device):
+    """Tuning between runs restores every position it moved."""
+    cases = _drop_trials()
+    whole = device.run_batch(cases)
+    batch = device.Batch()
+    states = []
+    for c in cases:
+        sched = device.build_lattice_schedule(int(c["node_count"][0]), c["bond_a"], c["bond_b"], c["node_block_begin"])
+        state = device.build_lattice_state(c, sched)
+        batch.add(sched, state, device.sphere_state(c["sphere"]))
+        states.append(state)
+    batch.settle(device.step_settings(cases[0]["settings"]))
+    batch.run(device.RunControl(max_steps=6))
+    chosen = batch.tune()
+    assert chosen["candidates"] > 1 and chosen["sweep_ms"] > 0.0
+    batch.run(device.RunControl(max_steps=6))
+    for k, state in enumerate(states):
+        batch.download(k, state)
+        assert np.array_equal(state.u, whole[k]["u"]) and np.array_equal(state.alive, whole[k]["alive"])
