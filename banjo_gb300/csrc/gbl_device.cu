@@ -82,19 +82,30 @@ template <class T> void uploadRaw(T *dst, const T *src, std::size_t n, cudaStrea
 template <class T> void zero(T *dst, std::size_t n, cudaStream_t s) {
     if (n) check(cudaMemsetAsync(dst, 0, sizeof(T) * n, s), "memset");
 }
-// A large copy between pageable host memory and the device, split into chunks
-// copied by several host threads at once (each on its own stream): the
-// staging of pageable memory is host-bound, one thread at a time.
-void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind kind) {
-    constexpr std::size_t kChunk = std::size_t(64) << 20;
-    const std::size_t chunks = (bytes + kChunk - 1) / kChunk;
-    if (chunks <= 1) {
-        if (bytes) check(cudaMemcpy(dst, src, bytes, kind), "copy");
+// Copies between pageable host memory and the device, split into pieces of
+// at most 64 MB copied by several host threads at once (each on its own
+// stream): the staging of pageable memory is host-bound, one thread at a time.
+// Returns when every piece has arrived.
+struct Segment {
+    void *dst;
+    const void *src;
+    std::size_t bytes;
+};
+void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
+    constexpr std::size_t kPiece = std::size_t(64) << 20;
+    std::vector<Segment> pieces;
+    for (const Segment &g : segments)
+        for (std::size_t off = 0; off < g.bytes; off += kPiece)
+            pieces.push_back({static_cast<char *>(g.dst) + off, static_cast<const char *>(g.src) + off,
+                              std::min(kPiece, g.bytes - off)});
+    if (pieces.empty()) return;
+    if (pieces.size() == 1) {
+        check(cudaMemcpy(pieces[0].dst, pieces[0].src, pieces[0].bytes, kind), "copy");
         return;
     }
     std::atomic<int> failed{static_cast<int>(cudaSuccess)};
     const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
-    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 16), chunks);
+    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 16), pieces.size());
     std::vector<std::thread> pool;
     auto note = [&](cudaError_t e) {
         int ok = static_cast<int>(cudaSuccess);
@@ -107,10 +118,8 @@ void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind 
             note(made);
             return;
         }
-        for (std::size_t c = t; c < chunks; c += T) {
-            const std::size_t off = c * kChunk, n = std::min(kChunk, bytes - off);
-            note(cudaMemcpyAsync(static_cast<char *>(dst) + off, static_cast<const char *>(src) + off, n, kind, s));
-        }
+        for (std::size_t c = t; c < pieces.size(); c += T)
+            note(cudaMemcpyAsync(pieces[c].dst, pieces[c].src, pieces[c].bytes, kind, s));
         note(cudaStreamSynchronize(s));
         cudaStreamDestroy(s);
     };
@@ -118,6 +127,9 @@ void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind 
     work(0);
     for (auto &th : pool) th.join();
     check(static_cast<cudaError_t>(failed.load()), "copy");
+}
+void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind kind) {
+    copySegments({{dst, src, bytes}}, kind);
 }
 
 // Device array to host, into uninitialised storage (no zero fill).
@@ -170,7 +182,6 @@ template <class R> struct RawState {
     Q4<R> *prev{};
     Q2<R> *plastic{};
     std::uint8_t *mode{};
-    std::vector<std::uint32_t> perm; // storage -> schedule order, when kept apart from its lattice
 
     static std::size_t need(std::uint32_t n, std::uint32_t b) {
         return 3 * static_cast<std::size_t>(n) * sizeof(Q4<R>) +
@@ -199,8 +210,9 @@ template <class R> struct RawState {
         rec = rec_buf.get(); prev = prev_buf.get(); plastic = plastic_buf.get(); mode = mode_buf.get();
     }
 
-    // download's conversion (WorkingLattice::toState, LatticeWorking.hpp:126-142).
-    void writeState(gbl_state_view &st, const std::vector<std::uint32_t> &dev2sched) const {
+    // download's conversion (WorkingLattice::toState, LatticeWorking.hpp:126-142),
+    // in sequence: the bond arrays arrive in schedule order.
+    void writeState(gbl_state_view &st) const {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
         parallelFor(N, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t i = lo; i < hi; ++i) {
@@ -210,13 +222,12 @@ template <class R> struct RawState {
             }
         });
         parallelFor(B, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t dd = lo; dd < hi; ++dd) {
-                const std::uint32_t j = dev2sched[dd];
-                st.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
-                st.failure_mode[j] = mode[dd];
-                st.damage[j] = prev[dd].w;
-                st.prev_tensile[j] = prev[dd].x; st.prev_compressive[j] = prev[dd].y; st.prev_shear[j] = prev[dd].z;
-                st.plastic_extension[j] = plastic[dd].x; st.plastic_strain[j] = plastic[dd].y;
+            for (std::size_t j = lo; j < hi; ++j) {
+                st.alive[j] = (rec[j].a & kDeadBit) ? 0 : 1;
+                st.failure_mode[j] = mode[j];
+                st.damage[j] = prev[j].w;
+                st.prev_tensile[j] = prev[j].x; st.prev_compressive[j] = prev[j].y; st.prev_shear[j] = prev[j].z;
+                st.plastic_extension[j] = plastic[j].x; st.plastic_strain[j] = plastic[j].y;
             }
         });
     }
@@ -232,8 +243,8 @@ template <class R> struct Resident {
     Arena arena;
     Dev<R> dev{};
     std::vector<Level> levels;
-    std::vector<std::uint32_t> dev2sched, sched2dev, isolated;
-    std::vector<std::uint8_t> last_a, last_b;
+    std::vector<std::uint32_t> dev2sched, isolated; // storage -> schedule order; nodes without bonds
+    std::vector<std::uint8_t> last_a, last_b; // the last bond of its end a / b in the sweep, by schedule index
     bool plastic_state{};
     std::vector<R> mass, inv_mass;
     Sphere<R> sphere0{};
@@ -260,6 +271,11 @@ template <class R> struct Resident {
     Resident &operator=(const Resident &) = delete;
     // Node-to-node contact scratch (allocated when the settings turn it on).
     void *nc_mem{};
+    // Upload in progress: the caller's state (direct upload), the sweep's
+    // level boundaries, whether any bond has flowed (read back by commit).
+    gbl_state_view view_{};
+    std::vector<std::uint32_t> level_begin_;
+    unsigned flowed_host_{};
 
     // The table size rule of latticeContactBucketMask (LatticePhysics.hpp:239-243),
     // applied to this lattice's own node count.
@@ -439,7 +455,6 @@ template <class R> struct Resident {
             }
         }
         dev2sched.assign(B, 0);
-        sched2dev.assign(B, 0);
         parallelFor(nchunks, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t c = lo; c < hi; ++c) {
                 std::uint32_t *fill = counts.data() + c * D1;
@@ -449,9 +464,6 @@ template <class R> struct Resident {
                 }
             }
         }, 1);
-        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t d = lo; d < hi; ++d) sched2dev[dev2sched[d]] = static_cast<std::uint32_t>(d);
-        });
         levels.clear();
         for (std::uint32_t d = 1; d <= deepest; ++d)
             if (first[d + 1] > first[d]) levels.push_back({first[d], first[d + 1]});
@@ -460,8 +472,7 @@ template <class R> struct Resident {
         parallelFor(N, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t i = lo; i < hi; ++i) {
                 if (last[i] == kNoBond) continue;
-                const std::uint32_t dd = sched2dev[last[i]];
-                (st.bond_a[last[i]] == i ? last_a : last_b)[dd] = 1;
+                (st.bond_a[last[i]] == i ? last_a : last_b)[last[i]] = 1; // by schedule index
             }
         });
         isolated.clear();
@@ -523,7 +534,7 @@ template <class R> struct Resident {
     // LatticeWorking.hpp:53-124): the device layout of the state, written into
     // a host image of the allocation. No CUDA call: lattices can be prepared
     // on several threads at once.
-    void prepare(const gbl_state_view &st, const gbl_sphere &sphere) {
+    void prepare(const gbl_state_view &st, const gbl_sphere &sphere, bool image = true) {
         N = st.node_count;
         B = st.bond_count;
         if (N > kNodeMask) invalid("lattice exceeds 2^30 nodes");
@@ -536,19 +547,52 @@ template <class R> struct Resident {
         d.words_b = (B + 31) / 32;
         d.tiles_b = (B + kThreads - 1) / kThreads;
         filled_ = reserve(arena, d, N, B, D, sched.block_count, isolated.size());
+        mass.resize(N);
+        inv_mass.resize(N);
+        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
+            for (std::size_t i = lo; i < hi; ++i) {
+                mass[i] = R(st.mass[i]);
+                inv_mass[i] = R(st.inv_mass[i]);
+            }
+        });
+        d.isolated_count = static_cast<std::uint32_t>(isolated.size());
+        // Level boundaries for the one-CTA sweep, when the levels fit its table.
+        d.level_count = levels.size() <= kMaxFusedLevels ? static_cast<std::uint32_t>(levels.size()) : 0U;
+        level_begin_.assign(d.level_count + 1, 0U);
+        for (std::uint32_t k = 0; k < d.level_count; ++k) level_begin_[k] = levels[k].begin;
+        level_begin_[d.level_count] = d.level_count ? levels[d.level_count - 1].end : 0U;
+        sphere0.center = {R(sphere.center[0]), R(sphere.center[1]), R(sphere.center[2])};
+        sphere0.velocity = {R(sphere.velocity[0]), R(sphere.velocity[1]), R(sphere.velocity[2])};
+        sphere0.angular = {R(sphere.angular_velocity[0]), R(sphere.angular_velocity[1]), R(sphere.angular_velocity[2])};
+        sphere0.radius = R(sphere.radius);
+        sphere0.mass = R(sphere.mass);
+        sphere0.inertia = R(sphere.inertia);
+        std::memcpy(d.origin, st.origin, sizeof(d.origin));
+        // Loads do not survive an upload (ExternalLoads.hpp:26 reset).
+        ext_count = 0;
+        ext_remaining = 0;
+        status = gbl_run_status{};
+        status.first_failure_step = status.last_failure_step = status.last_energy_gain_step = ~0ULL;
+        first_failure.clear();
+        frames.clear();
+        if (image) writeImage(st);
+        else view_ = st; // commit reads the caller's arrays, which stay valid until it returns
+    }
+
+    // The device layout written into a host image of the allocation (the
+    // served form: a request's state need not outlive its submission).
+    void writeImage(const gbl_state_view &st) {
+        Dev<R> &d = dev;
+        const std::uint32_t D = d.D;
         image_.reset(static_cast<unsigned char *>(std::aligned_alloc(256, filled_ ? filled_ : 256)));
         if (!image_) throw std::bad_alloc();
         arena.bind(image_.get());
-        mass.resize(N);
-        inv_mass.resize(N);
         parallelFor(N, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t i = lo; i < hi; ++i) {
                 d.u[i] = {R(st.u[3 * i]), R(st.u[3 * i + 1]), R(st.u[3 * i + 2]), R(st.inv_mass[i])};
                 d.v[i] = {R(st.v[3 * i]), R(st.v[3 * i + 1]), R(st.v[3 * i + 2]), R(st.mass[i])};
                 d.x0[i] = {R(st.x0[3 * i]), R(st.x0[3 * i + 1]), R(st.x0[3 * i + 2]), R(0)};
                 d.up[i] = {R(st.u_prev[3 * i]), R(st.u_prev[3 * i + 1]), R(st.u_prev[3 * i + 2]), R(0)};
-                mass[i] = R(st.mass[i]);
-                inv_mass[i] = R(st.inv_mass[i]);
             }
         });
         // Every node starts dirty: the first substep restarts in full.
@@ -563,75 +607,197 @@ template <class R> struct Resident {
                 d.nbr[s] = {R(st.nbr_rest[3 * s]), R(st.nbr_rest[3 * s + 1]), R(st.nbr_rest[3 * s + 2]),
                             (present && st.nbr_alive[s]) ? R(st.nbr_weight[s]) : R(0)};
                 d.nbr_other[s] = present ? st.nbr_other[s] : node;
-                d.nbr_bond[s] = present ? sched2dev[st.nbr_bond[s]] : kNoBond;
+                d.nbr_bond[s] = present ? st.nbr_bond[s] : kNoBond; // schedule index; storage index on the device
             }
         });
-        // Bonds, level-major storage (storage index dd holds schedule index j).
+        // Bonds in schedule order, read and written in sequence; commit moves
+        // them to storage (level-major) order on the device.
         std::atomic<bool> plastic_any{false};
         parallelFor(B, [&](std::size_t lo, std::size_t hi) {
             bool any = false;
-            for (std::size_t dd = lo; dd < hi; ++dd) {
-                const std::uint32_t j = dev2sched[dd];
-                d.rec[dd] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit) | (last_a[dd] ? kLastABit : 0U),
-                             st.bond_b[j] | (last_b[dd] ? kLastBBit : 0U), R(st.rest_length_sq_minus[j]),
-                             R(st.rest_length[j])};
-                d.geo[dd] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]),
-                             R(st.compliance[j])};
-                d.prev[dd] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
-                const double *t = st.threshold + 6 * static_cast<std::size_t>(j);
-                d.thr4[dd] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
-                d.thr2[dd] = {R(t[4]), R(t[5])};
-                d.plastic[dd] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
-                any = any || d.plastic[dd].x != R(0);
-                d.slot_a[dd] = st.bond_slot_a[j];
-                d.slot_b[dd] = st.bond_slot_b[j];
-                d.mode[dd] = st.failure_mode[j];
+            for (std::size_t j = lo; j < hi; ++j) {
+                d.rec[j] = {st.bond_a[j] | (st.alive[j] ? 0U : kDeadBit) | (last_a[j] ? kLastABit : 0U),
+                            st.bond_b[j] | (last_b[j] ? kLastBBit : 0U), R(st.rest_length_sq_minus[j]),
+                            R(st.rest_length[j])};
+                d.geo[j] = {R(st.rest_edge[3 * j]), R(st.rest_edge[3 * j + 1]), R(st.rest_edge[3 * j + 2]),
+                            R(st.compliance[j])};
+                d.prev[j] = {R(st.prev_tensile[j]), R(st.prev_compressive[j]), R(st.prev_shear[j]), R(st.damage[j])};
+                const double *t = st.threshold + 6 * j;
+                d.thr4[j] = {R(t[0]), R(t[1]), R(t[2]), R(t[3])};
+                d.thr2[j] = {R(t[4]), R(t[5])};
+                d.plastic[j] = {R(st.plastic_extension[j]), R(st.plastic_strain[j])};
+                any = any || d.plastic[j].x != R(0);
+                d.slot_a[j] = st.bond_slot_a[j];
+                d.slot_b[j] = st.bond_slot_b[j];
+                d.mode[j] = st.failure_mode[j];
             }
             if (any) plastic_any.store(true);
         });
         plastic_state = plastic_any.load();
         std::memcpy(d.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B);
         if (!isolated.empty()) std::memcpy(d.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size());
-        d.isolated_count = static_cast<std::uint32_t>(isolated.size());
         std::memcpy(d.node_block_begin, sched.node_block_begin.data(), sizeof(std::uint32_t) * (sched.block_count + 1));
-        // Level boundaries for the one-CTA sweep, when the levels fit its table.
-        d.level_count = levels.size() <= kMaxFusedLevels ? static_cast<std::uint32_t>(levels.size()) : 0U;
-        for (std::uint32_t k = 0; k < d.level_count; ++k) d.level_begin[k] = levels[k].begin;
-        d.level_begin[d.level_count] = d.level_count ? levels[d.level_count - 1].end : 0U;
-        sphere0.center = {R(sphere.center[0]), R(sphere.center[1]), R(sphere.center[2])};
-        sphere0.velocity = {R(sphere.velocity[0]), R(sphere.velocity[1]), R(sphere.velocity[2])};
-        sphere0.angular = {R(sphere.angular_velocity[0]), R(sphere.angular_velocity[1]), R(sphere.angular_velocity[2])};
-        sphere0.radius = R(sphere.radius);
-        sphere0.mass = R(sphere.mass);
-        sphere0.inertia = R(sphere.inertia);
+        std::memcpy(d.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size());
         *d.sphere = sphere0;
-        std::memcpy(d.origin, st.origin, sizeof(d.origin));
-        // Loads do not survive an upload (ExternalLoads.hpp:26 reset).
-        ext_count = 0;
-        ext_remaining = 0;
-        status = gbl_run_status{};
-        status.first_failure_step = status.last_failure_step = status.last_energy_gain_step = ~0ULL;
-        first_failure.clear();
-        frames.clear();
+    }
+
+    // The per-bond arrays of the device layout, and the same arrays in a
+    // buffer laid out as the allocation's [slot_a, dev2sched) range.
+    BondSet<R> bonds() const {
+        return {dev.slot_a, dev.slot_b, dev.rec, dev.geo, dev.prev, dev.thr4, dev.thr2, dev.plastic, dev.mode};
+    }
+    BondSet<R> bondsAt(char *region) const {
+        const char *lo = reinterpret_cast<const char *>(dev.slot_a);
+        auto at = [&](auto *p) {
+            return reinterpret_cast<decltype(p)>(region + (reinterpret_cast<const char *>(p) - lo));
+        };
+        return {at(dev.slot_a), at(dev.slot_b), at(dev.rec), at(dev.geo), at(dev.prev),
+                at(dev.thr4), at(dev.thr2), at(dev.plastic), at(dev.mode)};
+    }
+    static unsigned reorderGrid(std::size_t n) {
+        return static_cast<unsigned>(std::min<std::size_t>((n + kThreads - 1) / kThreads, 152 * 16));
     }
 
     // upload, device half: one allocation, the prepared image copied in, the
     // rest cleared. The host image is released.
     void commit(cudaStream_t stream) {
-        if (!image_) logic("lattice committed before it was prepared");
+        if (!image_ && !view_.u && N) logic("lattice committed before it was prepared");
         arena.allocate(stream);
+        char *base = static_cast<char *>(arena.base());
+        // The per-bond arrays, [slot_a, dev2sched) of the allocation, arrive in
+        // schedule order in a staging copy and are moved to storage order.
+        const std::size_t lo = static_cast<std::size_t>(reinterpret_cast<char *>(dev.slot_a) - base);
+        const std::size_t hi = static_cast<std::size_t>(reinterpret_cast<char *>(dev.dev2sched) - base);
+        char *staged = nullptr;
+        if (B) check(cudaMallocAsync(&staged, hi - lo, stream), "device allocation");
         check(cudaStreamSynchronize(stream), "device allocation");
-        copyParallel(arena.base(), image_.get(), filled_, cudaMemcpyHostToDevice);
+        if (image_) {
+            const unsigned char *img = image_.get();
+            copySegments({{base, img, lo}, {staged, img + lo, B ? hi - lo : 0}, {base + hi, img + hi, filled_ - hi}},
+                         cudaMemcpyHostToDevice);
+        } else {
+            convertOnDevice(staged, stream);
+        }
+        if (B) {
+            const unsigned grid = reorderGrid(B);
+            std::uint32_t *sched2dev_dev = dev.ev_list; // scratch of the cleared part, cleared below
+            kInvertOrder<<<grid, kThreads, 0, stream>>>(sched2dev_dev, dev.dev2sched, B);
+            const std::size_t P = static_cast<std::size_t>(dev.D) * N;
+            if (P) kSlotsToStorage<<<reorderGrid(P), kThreads, 0, stream>>>(dev.nbr_bond, sched2dev_dev, P);
+            kBondsToStorage<R><<<grid, kThreads, 0, stream>>>(bonds(), bondsAt(staged), dev.dev2sched, B);
+            check(cudaGetLastError(), "kernel launch");
+            check(cudaFreeAsync(staged, stream), "device free");
+        }
         if (arena.bytes() > filled_)
-            check(cudaMemsetAsync(static_cast<char *>(arena.base()) + filled_, 0, arena.bytes() - filled_, stream),
-                  "memset");
+            check(cudaMemsetAsync(base + filled_, 0, arena.bytes() - filled_, stream), "memset");
         dev.ext_force = ext_force; dev.ext_req = ext_req; dev.ext_contrib = ext_contrib; dev.ext_nodes = ext_nodes;
         check(cudaStreamSynchronize(stream), "upload");
+        if (!image_) plastic_state = flowed_host_ != 0;
         image_.reset();
+        view_ = gbl_state_view{};
+    }
+
+    // The direct upload: the caller's arrays, chunk by chunk, copied as they
+    // are into one of two device staging buffers (the next chunk's copy runs
+    // while the previous chunk converts) and converted there, the bonds into
+    // `staged` in schedule order; then the small arrays.
+    void convertOnDevice(char *staged, cudaStream_t stream) {
+        const gbl_state_view &st = view_;
+        constexpr std::size_t kStage = std::size_t(256) << 20;
+        auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
+        char *stage = nullptr;
+        check(cudaMallocAsync(&stage, 2 * kStage + 256, stream), "device allocation");
+        unsigned *flowed = reinterpret_cast<unsigned *>(stage + 2 * kStage);
+        check(cudaMemsetAsync(flowed, 0, sizeof(unsigned), stream), "memset");
+        check(cudaStreamSynchronize(stream), "device allocation");
+        cudaEvent_t used[2] = {nullptr, nullptr};
+        check(cudaEventCreateWithFlags(&used[0], cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&used[1], cudaEventDisableTiming), "event");
+        bool pending[2] = {false, false};
+        int turn = 0;
+        struct Part { const void *src; std::size_t bytes; };
+        // One chunk: its parts staged into the free buffer, then converted.
+        auto chunk = [&](std::initializer_list<Part> parts, auto &&convert) {
+            if (pending[turn]) check(cudaEventSynchronize(used[turn]), "upload");
+            char *buf = stage + static_cast<std::size_t>(turn) * kStage;
+            std::vector<Segment> segments;
+            std::vector<const char *> at;
+            std::size_t off = 0;
+            for (const Part &q : parts) {
+                at.push_back(buf + off);
+                segments.push_back({buf + off, q.src, q.bytes});
+                off += round(q.bytes);
+            }
+            copySegments(segments, cudaMemcpyHostToDevice);
+            convert(at);
+            check(cudaGetLastError(), "kernel launch");
+            check(cudaEventRecord(used[turn], stream), "event");
+            pending[turn] = true;
+            turn ^= 1;
+        };
+        auto f64 = [](const char *p) { return reinterpret_cast<const double *>(p); };
+        auto u32 = [](const char *p) { return reinterpret_cast<const std::uint32_t *>(p); };
+        auto u8 = [](const char *p) { return reinterpret_cast<const std::uint8_t *>(p); };
+        const std::size_t per_node = (kStage - 6 * 256) / (14 * sizeof(double));
+        for (std::size_t i0 = 0; i0 < N; i0 += per_node) {
+            const std::size_t n = std::min<std::size_t>(per_node, N - i0);
+            chunk({{st.u + 3 * i0, 24 * n}, {st.u_prev + 3 * i0, 24 * n}, {st.v + 3 * i0, 24 * n},
+                   {st.x0 + 3 * i0, 24 * n}, {st.mass + i0, 8 * n}, {st.inv_mass + i0, 8 * n}},
+                  [&](const std::vector<const char *> &at) {
+                      const NodesIn in{f64(at[0]), f64(at[1]), f64(at[2]), f64(at[3]), f64(at[4]), f64(at[5])};
+                      kNodesIn<R><<<reorderGrid(n), kThreads, 0, stream>>>(dev.u, dev.v, dev.x0, dev.up, in, i0, n);
+                  });
+        }
+        const std::size_t P = static_cast<std::size_t>(dev.D) * N;
+        const std::size_t per_slot = (kStage - 5 * 256) / 41;
+        for (std::size_t s0 = 0; s0 < P; s0 += per_slot) {
+            const std::size_t n = std::min(per_slot, P - s0);
+            chunk({{st.nbr_rest + 3 * s0, 24 * n}, {st.nbr_weight + s0, 8 * n}, {st.nbr_alive + s0, n},
+                   {st.nbr_other + s0, 4 * n}, {st.nbr_bond + s0, 4 * n}},
+                  [&](const std::vector<const char *> &at) {
+                      const SlotsIn in{f64(at[0]), f64(at[1]), u8(at[2]), u32(at[3]), u32(at[4])};
+                      kSlotsIn<R><<<reorderGrid(n), kThreads, 0, stream>>>(dev.nbr, dev.nbr_other, dev.nbr_bond, in,
+                                                                           s0, n, N);
+                  });
+        }
+        const BondSet<R> out = B ? bondsAt(staged) : BondSet<R>{};
+        const std::size_t per_bond = (kStage - 19 * 256) / 164;
+        for (std::size_t j0 = 0; j0 < B; j0 += per_bond) {
+            const std::size_t n = std::min<std::size_t>(per_bond, B - j0);
+            chunk({{st.bond_a + j0, 4 * n}, {st.bond_b + j0, 4 * n}, {st.bond_slot_a + j0, 4 * n},
+                   {st.bond_slot_b + j0, 4 * n}, {st.alive + j0, n}, {st.failure_mode + j0, n},
+                   {last_a.data() + j0, n}, {last_b.data() + j0, n}, {st.rest_length_sq_minus + j0, 8 * n},
+                   {st.rest_length + j0, 8 * n}, {st.rest_edge + 3 * j0, 24 * n}, {st.compliance + j0, 8 * n},
+                   {st.prev_tensile + j0, 8 * n}, {st.prev_compressive + j0, 8 * n}, {st.prev_shear + j0, 8 * n},
+                   {st.damage + j0, 8 * n}, {st.threshold + 6 * j0, 48 * n}, {st.plastic_extension + j0, 8 * n},
+                   {st.plastic_strain + j0, 8 * n}},
+                  [&](const std::vector<const char *> &at) {
+                      const BondsIn in{u32(at[0]), u32(at[1]), u32(at[2]), u32(at[3]), u8(at[4]), u8(at[5]),
+                                       u8(at[6]), u8(at[7]), f64(at[8]), f64(at[9]), f64(at[10]), f64(at[11]),
+                                       f64(at[12]), f64(at[13]), f64(at[14]), f64(at[15]), f64(at[16]),
+                                       f64(at[17]), f64(at[18])};
+                      kBondsIn<R><<<reorderGrid(n), kThreads, 0, stream>>>(out, in, j0, n, flowed);
+                  });
+        }
+        // The small arrays, and every node dirty: the first substep restarts in full.
+        copySegments({{dev.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B},
+                      {dev.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size()},
+                      {dev.node_block_begin, sched.node_block_begin.data(),
+                       sizeof(std::uint32_t) * (sched.block_count + 1)},
+                      {dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size()},
+                      {dev.sphere, &sphere0, sizeof(sphere0)}},
+                     cudaMemcpyHostToDevice);
+        check(cudaMemsetAsync(dev.dirty, 1, N, stream), "memset");
+        check(cudaMemsetAsync(dev.dirty + N, 0, 4, stream), "memset");
+        check(cudaMemcpyAsync(&flowed_host_, flowed, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
+        check(cudaFreeAsync(stage, stream), "device free");
+        check(cudaStreamSynchronize(stream), "upload");
+        cudaEventDestroy(used[0]);
+        cudaEventDestroy(used[1]);
     }
 
     void upload(const gbl_state_view &st, const gbl_sphere &sphere, cudaStream_t stream) {
-        prepare(st, sphere);
+        prepare(st, sphere, false);
         commit(stream);
     }
 
@@ -679,26 +845,80 @@ template <class R> struct Resident {
 
     // The device arrays a download needs, raw, into `raw` (its buffers reused
     // when large enough).
-    void copyRaw(RawState<R> &raw) const {
+    // The arrays a download reads; the bond arrays are put back in schedule
+    // order on the device first.
+    void copyRaw(RawState<R> &raw, cudaStream_t stream) const {
         raw.shape(N, B);
+        char *ordered = nullptr;
+        BondSet<R> o{};
+        if (B) {
+            const std::size_t b = B;
+            auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
+            const std::size_t rec = round(b * sizeof(BondRec<R>)), prev = round(b * sizeof(Q4<R>)),
+                              plastic = round(b * sizeof(Q2<R>));
+            check(cudaMallocAsync(&ordered, rec + prev + plastic + b, stream), "device allocation");
+            o.rec = reinterpret_cast<BondRec<R> *>(ordered);
+            o.prev = reinterpret_cast<Q4<R> *>(ordered + rec);
+            o.plastic = reinterpret_cast<Q2<R> *>(ordered + rec + prev);
+            o.mode = reinterpret_cast<std::uint8_t *>(ordered + rec + prev + plastic);
+            kBondsToSchedule<R><<<reorderGrid(b), kThreads, 0, stream>>>(o, bonds(), dev.dev2sched, B);
+            check(cudaGetLastError(), "kernel launch");
+        }
+        check(cudaStreamSynchronize(stream), "download");
         copyParallel(raw.u, dev.u, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
         copyParallel(raw.up, dev.up, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
         copyParallel(raw.v, dev.v, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
-        copyParallel(raw.rec, dev.rec, sizeof(BondRec<R>) * B, cudaMemcpyDeviceToHost);
-        copyParallel(raw.prev, dev.prev, sizeof(Q4<R>) * B, cudaMemcpyDeviceToHost);
-        copyParallel(raw.plastic, dev.plastic, sizeof(Q2<R>) * B, cudaMemcpyDeviceToHost);
-        copyParallel(raw.mode, dev.mode, B, cudaMemcpyDeviceToHost);
+        if (B) {
+            copyParallel(raw.rec, o.rec, sizeof(BondRec<R>) * B, cudaMemcpyDeviceToHost);
+            copyParallel(raw.prev, o.prev, sizeof(Q4<R>) * B, cudaMemcpyDeviceToHost);
+            copyParallel(raw.plastic, o.plastic, sizeof(Q2<R>) * B, cudaMemcpyDeviceToHost);
+            copyParallel(raw.mode, o.mode, B, cudaMemcpyDeviceToHost);
+            check(cudaFreeAsync(ordered, stream), "device free");
+        }
     }
 
     // download (WorkingLattice::toState, LatticeWorking.hpp:126-142); the host
     // buffers are kept for the lattice's next download.
-    void download(gbl_state_view &st, gbl_sphere *sphere) {
+    void download(gbl_state_view &st, gbl_sphere *sphere, cudaStream_t stream) {
         if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
-        copyRaw(download_raw_);
-        download_raw_.writeState(st, dev2sched);
+        // The device writes the state's own layout (doubles, schedule order)
+        // into one scratch buffer; each array is then copied straight into
+        // the caller's, which the caller has already touched.
+        const std::size_t n3 = 3 * static_cast<std::size_t>(N) * sizeof(double), b = B;
+        auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
+        const std::size_t parts[11] = {round(n3), round(n3), round(n3), round(b), round(b), round(8 * b), round(8 * b),
+                                       round(8 * b), round(8 * b), round(8 * b), round(8 * b)};
+        std::size_t total = 0;
+        for (std::size_t q : parts) total += q;
+        char *out = nullptr;
+        check(cudaMallocAsync(&out, total ? total : 256, stream), "device allocation");
+        char *at[11];
+        for (std::size_t q = 0, off = 0; q < 11; off += parts[q], ++q) at[q] = out + off;
+        double *u = reinterpret_cast<double *>(at[0]), *up = reinterpret_cast<double *>(at[1]),
+               *v = reinterpret_cast<double *>(at[2]);
+        const BondsOut o{reinterpret_cast<std::uint8_t *>(at[3]), reinterpret_cast<std::uint8_t *>(at[4]),
+                         reinterpret_cast<double *>(at[5]), reinterpret_cast<double *>(at[6]),
+                         reinterpret_cast<double *>(at[7]), reinterpret_cast<double *>(at[8]),
+                         reinterpret_cast<double *>(at[9]), reinterpret_cast<double *>(at[10])};
+        if (N) kNodesOut<R><<<reorderGrid(N), kThreads, 0, stream>>>(u, up, v, dev.u, dev.up, dev.v, N);
+        if (B) kBondsOut<R><<<reorderGrid(B), kThreads, 0, stream>>>(o, bonds(), dev.dev2sched, B);
+        check(cudaGetLastError(), "kernel launch");
+        check(cudaStreamSynchronize(stream), "download");
+        copyParallel(st.u, u, n3, cudaMemcpyDeviceToHost);
+        copyParallel(st.u_prev, up, n3, cudaMemcpyDeviceToHost);
+        copyParallel(st.v, v, n3, cudaMemcpyDeviceToHost);
+        copyParallel(st.alive, o.alive, b, cudaMemcpyDeviceToHost);
+        copyParallel(st.failure_mode, o.mode, b, cudaMemcpyDeviceToHost);
+        copyParallel(st.damage, o.damage, 8 * b, cudaMemcpyDeviceToHost);
+        copyParallel(st.prev_tensile, o.tensile, 8 * b, cudaMemcpyDeviceToHost);
+        copyParallel(st.prev_compressive, o.compressive, 8 * b, cudaMemcpyDeviceToHost);
+        copyParallel(st.prev_shear, o.shear, 8 * b, cudaMemcpyDeviceToHost);
+        copyParallel(st.plastic_extension, o.plastic_extension, 8 * b, cudaMemcpyDeviceToHost);
+        copyParallel(st.plastic_strain, o.plastic_strain, 8 * b, cudaMemcpyDeviceToHost);
+        check(cudaFreeAsync(out, stream), "device free");
+        check(cudaStreamSynchronize(stream), "download");
         if (sphere) *sphere = fetchSphere();
     }
-    RawState<R> download_raw_;
 
     gbl_sphere fetchSphere() const {
         Sphere<R> sp{};
@@ -865,15 +1085,18 @@ public:
     // RunStatus) with `step_limit` substeps to run (0: no limit).
     std::size_t add(const Schedule &sched, const gbl_state_view &st, const gbl_sphere &sphere,
                     std::uint64_t step_limit = 0) {
-        return place(prepare(sched, st, sphere), step_limit);
+        return place(prepare(sched, st, sphere, false), step_limit);
     }
 
     // The host half of add: no CUDA call and no engine state, so any number
-    // of threads may prepare lattices while the engine runs.
+    // of threads may prepare lattices while the engine runs. With `image`
+    // the device layout is written to a host image and the caller's state is
+    // not read again; without, the lattice converts on the device from the
+    // caller's arrays when it is placed.
     static std::unique_ptr<Resident<R>> prepare(const Schedule &sched, const gbl_state_view &st,
-                                                const gbl_sphere &sphere) {
+                                                const gbl_sphere &sphere, bool image = true) {
         auto r = std::make_unique<Resident<R>>(sched);
-        r->prepare(st, sphere);
+        r->prepare(st, sphere, image);
         return r;
     }
 
@@ -1228,7 +1451,7 @@ public:
     void download(std::size_t k, gbl_state_view &st, gbl_sphere *sphere) {
         requireReady();
         check(cudaStreamSynchronize(stream_), "download");
-        lattice(k).download(st, sphere);
+        lattice(k).download(st, sphere, stream_);
     }
 
     static void validate(const gbl_step_settings &s) {
@@ -1981,7 +2204,7 @@ public:
         }
         // The conversion to the state layout runs on the caller's thread,
         // outside the lock; the buffer then goes back to the pool.
-        if (st) raw.writeState(*st, raw.perm);
+        if (st) raw.writeState(*st);
         std::lock_guard<std::mutex> lock(mutex_);
         if (pool_.size() < kPoolSize) pool_.push_back(std::move(raw));
     }
@@ -2099,8 +2322,7 @@ private:
                     pool_.erase(pool_.begin() + static_cast<std::ptrdiff_t>(best));
                 }
             }
-            l.copyRaw(q.raw);
-            q.raw.perm = std::move(l.dev2sched); // the lattice is retired just below
+            l.copyRaw(q.raw, engine_.stream());
             q.sphere = l.fetchSphere();
             q.status = l.status;
             q.status.exit_reason = c.exit_reason;

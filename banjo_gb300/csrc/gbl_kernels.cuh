@@ -1267,10 +1267,18 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
     __syncthreads();
     double plastic_work = 0.0;
     if (j < w.end) {
-        const BondRec<R> rec = L.rec[j];
+        // Every per-bond array is loaded at once, ahead of the liveness test
+        // and of the node gathers that wait on the record: one trip to memory
+        // for all of them rather than one after another (single-use data,
+        // streamed past L2 so the node arrays stay there).
+        const BondRec<R> rec = ldStream(L.rec + j);
+        const Q4<R> g = ldStream(L.geo + j);
+        Q4<R> pv = L.prev[j];
+        const Q4<R> t4 = ldStream(L.thr4 + j);
+        const Q2<R> t2 = L.thr2[j];
+        Q2<R> pl = Plastic ? L.plastic[j] : Q2<R>{R(0), R(0)};
         if (!(rec.a & kDeadBit)) {
             const std::uint32_t a = endA(rec), b = endB(rec);
-            const Q4<R> g = L.geo[j];
             const V3<R> edge{g.x, g.y, g.z};
             float plastic_stretch = 0.0F;
             R pext = R(0);
@@ -1278,7 +1286,6 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
             // sample and the stored energy of a failure alike.
             const R len = length(bondVector<R, Direct>(L, a, b, edge));
             if (Plastic) {
-                Q2<R> pl = L.plastic[j];
                 pext = pl.x;
                 if (S.yield_stretch > R(0)) {
                     const R elastic = len - rec.rest - pl.x;
@@ -1302,15 +1309,12 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
             }
             R t, c, s;
             sampleBond<R, Direct>(L, a, b, rec, edge, len, t, c, s);
-            Q4<R> pv = L.prev[j];
             const R pt = maxR(R(0), maxR(pv.x, t));
             const R pc = maxR(R(0), maxR(pv.y, c));
             const R ps = maxR(R(0), maxR(pv.z, s));
             pv.x = maxR(R(0), t);
             pv.y = maxR(R(0), c);
             pv.z = maxR(R(0), s);
-            const Q4<R> t4 = L.thr4[j];
-            const Q2<R> t2 = L.thr2[j];
             const R dtn = damageProgress(pt, t4.x, t4.y);
             const R dcp = damageProgress(pc, t4.z, t4.w);
             const R dsh = damageProgress(ps, t2.x, t2.y);
@@ -2072,6 +2076,178 @@ __global__ void __launch_bounds__(32) kContactNarrow(const Grid<R> launch, Setti
         at += first + 1U;
     }
     if (lane == 0) c.node = acc;
+}
+
+// ---------------------------------------------------------------------------
+// Bond order between the state (schedule order) and the device (storage,
+// level-major order), moved on the device: upload writes the per-bond arrays
+// in schedule order and download reads them in schedule order, so the host
+// converts element by element in sequence and never gathers.
+// ---------------------------------------------------------------------------
+template <class R> struct BondSet {
+    std::uint32_t *slot_a, *slot_b;
+    BondRec<R> *rec;
+    Q4<R> *geo, *prev, *thr4;
+    Q2<R> *thr2, *plastic;
+    std::uint8_t *mode;
+};
+
+__device__ __forceinline__ std::size_t gridStride() { return static_cast<std::size_t>(gridDim.x) * blockDim.x; }
+__device__ __forceinline__ std::size_t gridFirst() {
+    return static_cast<std::size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+}
+
+// Upload: storage entry dd takes schedule entry dev2sched[dd].
+template <class R>
+__global__ void __launch_bounds__(kThreads) kBondsToStorage(BondSet<R> dst, BondSet<R> src,
+                                                            const std::uint32_t *dev2sched, std::uint32_t B) {
+    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) {
+        const std::uint32_t j = dev2sched[dd];
+        dst.slot_a[dd] = src.slot_a[j];
+        dst.slot_b[dd] = src.slot_b[j];
+        dst.rec[dd] = src.rec[j];
+        dst.geo[dd] = src.geo[j];
+        dst.prev[dd] = src.prev[j];
+        dst.thr4[dd] = src.thr4[j];
+        dst.thr2[dd] = src.thr2[j];
+        dst.plastic[dd] = src.plastic[j];
+        dst.mode[dd] = src.mode[j];
+    }
+}
+
+// The inverse permutation, schedule index -> storage index.
+__global__ void __launch_bounds__(kThreads) kInvertOrder(std::uint32_t *sched2dev, const std::uint32_t *dev2sched,
+                                                         std::uint32_t B) {
+    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) sched2dev[dev2sched[dd]] = static_cast<std::uint32_t>(dd);
+}
+
+// Neighbour slots name their bond by schedule index on upload; the device
+// keeps storage indices.
+__global__ void __launch_bounds__(kThreads) kSlotsToStorage(std::uint32_t *nbr_bond, const std::uint32_t *sched2dev,
+                                                            std::size_t P) {
+    for (std::size_t s = gridFirst(); s < P; s += gridStride()) {
+        const std::uint32_t j = nbr_bond[s];
+        if (j != kNoBond) nbr_bond[s] = sched2dev[j];
+    }
+}
+
+// Download: the arrays the state takes back, in schedule order.
+template <class R>
+__global__ void __launch_bounds__(kThreads) kBondsToSchedule(BondSet<R> dst, BondSet<R> src,
+                                                             const std::uint32_t *dev2sched, std::uint32_t B) {
+    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) {
+        const std::uint32_t j = dev2sched[dd];
+        dst.rec[j] = src.rec[dd];
+        dst.prev[j] = src.prev[dd];
+        dst.plastic[j] = src.plastic[dd];
+        dst.mode[j] = src.mode[dd];
+    }
+}
+
+// Download straight into the state's layout: doubles (exact widenings), bonds
+// in schedule order, so the host copies each array as it is.
+template <class R>
+__global__ void __launch_bounds__(kThreads) kNodesOut(double *u, double *up, double *v, const Q4<R> *du,
+                                                      const Q4<R> *dup, const Q4<R> *dv, std::uint32_t N) {
+    for (std::size_t i = gridFirst(); i < N; i += gridStride()) {
+        const Q4<R> a = du[i], b = dup[i], c = dv[i];
+        u[3 * i] = a.x; u[3 * i + 1] = a.y; u[3 * i + 2] = a.z;
+        up[3 * i] = b.x; up[3 * i + 1] = b.y; up[3 * i + 2] = b.z;
+        v[3 * i] = c.x; v[3 * i + 1] = c.y; v[3 * i + 2] = c.z;
+    }
+}
+
+struct BondsOut {
+    std::uint8_t *alive, *mode;
+    double *damage, *tensile, *compressive, *shear, *plastic_extension, *plastic_strain;
+};
+
+template <class R>
+__global__ void __launch_bounds__(kThreads) kBondsOut(BondsOut o, BondSet<R> src, const std::uint32_t *dev2sched,
+                                                      std::uint32_t B) {
+    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) {
+        const std::uint32_t j = dev2sched[dd];
+        const Q4<R> p = src.prev[dd];
+        const Q2<R> pl = src.plastic[dd];
+        o.alive[j] = (src.rec[dd].a & kDeadBit) ? 0 : 1;
+        o.mode[j] = src.mode[dd];
+        o.damage[j] = p.w;
+        o.tensile[j] = p.x;
+        o.compressive[j] = p.y;
+        o.shear[j] = p.z;
+        o.plastic_extension[j] = pl.x;
+        o.plastic_strain[j] = pl.y;
+    }
+}
+
+// Upload straight from the state's layout: a chunk of the caller's arrays
+// (doubles, schedule order) staged on the device as it is, converted here to
+// the device layout (WorkingLattice::fromState, LatticeWorking.hpp:53-124;
+// each value rounded once, to nearest, as the host cast rounds it).
+struct NodesIn {
+    const double *u, *up, *v, *x0, *mass, *inv_mass;
+};
+template <class R>
+__global__ void __launch_bounds__(kThreads) kNodesIn(Q4<R> *du, Q4<R> *dv, Q4<R> *dx0, Q4<R> *dup, NodesIn in,
+                                                     std::size_t first, std::size_t n) {
+    for (std::size_t k = gridFirst(); k < n; k += gridStride()) {
+        const std::size_t i = first + k;
+        du[i] = Q4<R>{R(in.u[3 * k]), R(in.u[3 * k + 1]), R(in.u[3 * k + 2]), R(in.inv_mass[k])};
+        dv[i] = Q4<R>{R(in.v[3 * k]), R(in.v[3 * k + 1]), R(in.v[3 * k + 2]), R(in.mass[k])};
+        dx0[i] = Q4<R>{R(in.x0[3 * k]), R(in.x0[3 * k + 1]), R(in.x0[3 * k + 2]), R(0)};
+        dup[i] = Q4<R>{R(in.up[3 * k]), R(in.up[3 * k + 1]), R(in.up[3 * k + 2]), R(0)};
+    }
+}
+
+// Neighbour slots: (rest, weight if alive), the other node (itself when
+// padded), the bond by schedule index (kSlotsToStorage maps it).
+struct SlotsIn {
+    const double *rest, *weight;
+    const std::uint8_t *alive;
+    const std::uint32_t *other, *bond;
+};
+template <class R>
+__global__ void __launch_bounds__(kThreads) kSlotsIn(Q4<R> *nbr, std::uint32_t *nbr_other, std::uint32_t *nbr_bond,
+                                                     SlotsIn in, std::size_t first, std::size_t n, std::uint32_t N) {
+    for (std::size_t k = gridFirst(); k < n; k += gridStride()) {
+        const std::size_t s = first + k;
+        const std::uint32_t bond = in.bond[k];
+        const bool present = bond != kNoBond;
+        nbr[s] = Q4<R>{R(in.rest[3 * k]), R(in.rest[3 * k + 1]), R(in.rest[3 * k + 2]),
+                       (present && in.alive[k]) ? R(in.weight[k]) : R(0)};
+        nbr_other[s] = present ? in.other[k] : static_cast<std::uint32_t>(s % N);
+        nbr_bond[s] = bond;
+    }
+}
+
+// Bonds, in schedule order; `plastic` is set when any bond has flowed.
+struct BondsIn {
+    const std::uint32_t *a, *b, *slot_a, *slot_b;
+    const std::uint8_t *alive, *mode, *last_a, *last_b;
+    const double *rsm, *rest, *edge, *compliance, *tensile, *compressive, *shear, *damage, *threshold, *extension,
+        *strain;
+};
+template <class R>
+__global__ void __launch_bounds__(kThreads) kBondsIn(BondSet<R> out, BondsIn in, std::size_t first, std::size_t n,
+                                                     unsigned *plastic) {
+    bool flowed = false;
+    for (std::size_t k = gridFirst(); k < n; k += gridStride()) {
+        const std::size_t j = first + k;
+        out.rec[j] = BondRec<R>{in.a[k] | (in.alive[k] ? 0U : kDeadBit) | (in.last_a[k] ? kLastABit : 0U),
+                                in.b[k] | (in.last_b[k] ? kLastBBit : 0U), R(in.rsm[k]), R(in.rest[k])};
+        out.geo[j] = Q4<R>{R(in.edge[3 * k]), R(in.edge[3 * k + 1]), R(in.edge[3 * k + 2]), R(in.compliance[k])};
+        out.prev[j] = Q4<R>{R(in.tensile[k]), R(in.compressive[k]), R(in.shear[k]), R(in.damage[k])};
+        const double *t = in.threshold + 6 * k;
+        out.thr4[j] = Q4<R>{R(t[0]), R(t[1]), R(t[2]), R(t[3])};
+        out.thr2[j] = Q2<R>{R(t[4]), R(t[5])};
+        const Q2<R> pl{R(in.extension[k]), R(in.strain[k])};
+        out.plastic[j] = pl;
+        flowed = flowed || pl.x != R(0);
+        out.slot_a[j] = in.slot_a[k];
+        out.slot_b[j] = in.slot_b[k];
+        out.mode[j] = in.mode[k];
+    }
+    if (__any_sync(0xffffffffU, flowed) && (threadIdx.x & 31) == 0) atomicOr(plastic, 1U);
 }
 
 } // namespace gbl

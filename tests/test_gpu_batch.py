@@ -159,10 +159,11 @@ def test_batch_tuned_mid_run_equals_untuned(device):
         batch.add(sched, state, device.sphere_state(c["sphere"]))
         states.append(state)
     batch.settle(device.step_settings(cases[0]["settings"]))
-    batch.run(device.RunControl(max_steps=6))
+    total = max(int(c["steps"][0]) for c in cases)
+    batch.run(device.RunControl(max_steps=total // 2))
     chosen = batch.tune()
     assert chosen["candidates"] > 1 and chosen["sweep_ms"] > 0.0
-    batch.run(device.RunControl(max_steps=6))
+    batch.run(device.RunControl(max_steps=total - total // 2))
     for k, state in enumerate(states):
         batch.download(k, state)
         assert np.array_equal(state.u, whole[k]["u"]) and np.array_equal(state.alive, whole[k]["alive"])
