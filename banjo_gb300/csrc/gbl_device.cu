@@ -83,16 +83,17 @@ template <class T> void zero(T *dst, std::size_t n, cudaStream_t s) {
     if (n) check(cudaMemsetAsync(dst, 0, sizeof(T) * n, s), "memset");
 }
 // Copies between pageable host memory and the device, split into pieces of
-// at most 64 MB copied by several host threads at once (each on its own
-// stream): the staging of pageable memory is host-bound, one thread at a time.
-// Returns when every piece has arrived.
+// at most 16 MB copied by several host threads at once (each on its own
+// stream): the staging of pageable memory is host-bound, one thread at a
+// time, and small pieces keep the threads evenly loaded. Returns when every
+// piece has arrived.
 struct Segment {
     void *dst;
     const void *src;
     std::size_t bytes;
 };
 void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
-    constexpr std::size_t kPiece = std::size_t(64) << 20;
+    constexpr std::size_t kPiece = std::size_t(16) << 20;
     std::vector<Segment> pieces;
     for (const Segment &g : segments)
         for (std::size_t off = 0; off < g.bytes; off += kPiece)
@@ -703,8 +704,13 @@ template <class R> struct Resident {
     // `staged` in schedule order; then the small arrays.
     void convertOnDevice(char *staged, cudaStream_t stream) {
         const gbl_state_view &st = view_;
-        constexpr std::size_t kStage = std::size_t(256) << 20;
+        // Each staging buffer holds up to 1 GB of the caller's arrays (less
+        // when the whole lattice needs less).
+        const std::size_t P = static_cast<std::size_t>(dev.D) * N;
+        const std::size_t whole = std::max({N * 14 * sizeof(double), P * 41, static_cast<std::size_t>(B) * 164});
         auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
+        // A multiple of 256 bytes: the second buffer and every part start aligned.
+        const std::size_t kStage = round(std::min(std::size_t(1) << 30, whole + 32 * 256));
         char *stage = nullptr;
         check(cudaMallocAsync(&stage, 2 * kStage + 256, stream), "device allocation");
         unsigned *flowed = reinterpret_cast<unsigned *>(stage + 2 * kStage);
@@ -748,7 +754,6 @@ template <class R> struct Resident {
                       kNodesIn<R><<<reorderGrid(n), kThreads, 0, stream>>>(dev.u, dev.v, dev.x0, dev.up, in, i0, n);
                   });
         }
-        const std::size_t P = static_cast<std::size_t>(dev.D) * N;
         const std::size_t per_slot = (kStage - 5 * 256) / 41;
         for (std::size_t s0 = 0; s0 < P; s0 += per_slot) {
             const std::size_t n = std::min(per_slot, P - s0);
