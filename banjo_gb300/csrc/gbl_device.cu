@@ -133,6 +133,24 @@ void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind 
     copySegments({{dst, src, bytes}}, kind);
 }
 
+// Whether kernels may read the caller's pageable host memory directly: the
+// device says so (coherent pageable access through the host's page tables,
+// as over a Grace CPU's chip-to-chip link), unless GBL_STAGED_UPLOAD=1 asks
+// for the staged copies every device supports.
+bool pageableAccess() {
+    static const bool yes = [] {
+        const char *env = std::getenv("GBL_STAGED_UPLOAD");
+        if (env && env[0] == '1') return false;
+        int dev = 0, access = 0, tables = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return false;
+        if (cudaDeviceGetAttribute(&access, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+        if (cudaDeviceGetAttribute(&tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+            return false;
+        return access == 1 && tables == 1;
+    }();
+    return yes;
+}
+
 // Device array to host, into uninitialised storage (no zero fill).
 template <class T> std::unique_ptr<T[]> fetch(const T *src, std::size_t n) {
     std::unique_ptr<T[]> out(new T[n ? n : 1]);
@@ -698,12 +716,53 @@ template <class R> struct Resident {
         view_ = gbl_state_view{};
     }
 
+    // The direct upload where the device reads pageable host memory: the
+    // conversion kernels read the caller's arrays in place, in sequence.
+    void convertFromHost(char *staged, cudaStream_t stream) {
+        const gbl_state_view &st = view_;
+        unsigned *flowed = nullptr;
+        check(cudaMallocAsync(&flowed, 256, stream), "device allocation");
+        check(cudaMemsetAsync(flowed, 0, sizeof(unsigned), stream), "memset");
+        if (N)
+            kNodesIn<R><<<reorderGrid(N), kThreads, 0, stream>>>(
+                dev.u, dev.v, dev.x0, dev.up, NodesIn{st.u, st.u_prev, st.v, st.x0, st.mass, st.inv_mass}, 0, N);
+        const std::size_t P = static_cast<std::size_t>(dev.D) * N;
+        if (P)
+            kSlotsIn<R><<<reorderGrid(P), kThreads, 0, stream>>>(
+                dev.nbr, dev.nbr_other, dev.nbr_bond,
+                SlotsIn{st.nbr_rest, st.nbr_weight, st.nbr_alive, st.nbr_other, st.nbr_bond}, 0, P, N);
+        if (B) {
+            const BondsIn in{st.bond_a, st.bond_b, st.bond_slot_a, st.bond_slot_b, st.alive, st.failure_mode,
+                             last_a.data(), last_b.data(), st.rest_length_sq_minus, st.rest_length, st.rest_edge,
+                             st.compliance, st.prev_tensile, st.prev_compressive, st.prev_shear, st.damage,
+                             st.threshold, st.plastic_extension, st.plastic_strain};
+            kBondsIn<R><<<reorderGrid(B), kThreads, 0, stream>>>(bondsAt(staged), in, 0, B, flowed);
+        }
+        check(cudaGetLastError(), "kernel launch");
+        copySegments({{dev.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B},
+                      {dev.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size()},
+                      {dev.node_block_begin, sched.node_block_begin.data(),
+                       sizeof(std::uint32_t) * (sched.block_count + 1)},
+                      {dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size()},
+                      {dev.sphere, &sphere0, sizeof(sphere0)}},
+                     cudaMemcpyHostToDevice);
+        check(cudaMemsetAsync(dev.dirty, 1, N, stream), "memset");
+        check(cudaMemsetAsync(dev.dirty + N, 0, 4, stream), "memset");
+        check(cudaMemcpyAsync(&flowed_host_, flowed, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
+        check(cudaFreeAsync(flowed, stream), "device free");
+        check(cudaStreamSynchronize(stream), "upload");
+    }
+
     // The direct upload: the caller's arrays, chunk by chunk, copied as they
     // are into one of two device staging buffers (the next chunk's copy runs
     // while the previous chunk converts) and converted there, the bonds into
     // `staged` in schedule order; then the small arrays.
     void convertOnDevice(char *staged, cudaStream_t stream) {
         const gbl_state_view &st = view_;
+        if (pageableAccess()) {
+            convertFromHost(staged, stream);
+            return;
+        }
         // Each staging buffer holds up to 1 GB of the caller's arrays (less
         // when the whole lattice needs less).
         const std::size_t P = static_cast<std::size_t>(dev.D) * N;
