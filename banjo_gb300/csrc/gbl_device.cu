@@ -82,6 +82,23 @@ template <class T> void uploadRaw(T *dst, const T *src, std::size_t n, cudaStrea
 template <class T> void zero(T *dst, std::size_t n, cudaStream_t s) {
     if (n) check(cudaMemsetAsync(dst, 0, sizeof(T) * n, s), "memset");
 }
+// Helper threads of the library's parallel loops and copies, counted across
+// every caller: a loop or copy borrows at most the cores not already lent,
+// so concurrent callers (the submitting threads of a server, its admission)
+// share the host instead of oversubscribing it. The caller's own thread
+// always works.
+std::atomic<long> g_helpers{0};
+std::size_t borrowHelpers(std::size_t want) {
+    const long cores = static_cast<long>(std::max(1U, std::thread::hardware_concurrency()));
+    long lent = g_helpers.load();
+    for (;;) {
+        const long take = std::min<long>(static_cast<long>(want), std::max(0L, cores - 1 - lent));
+        if (take <= 0) return 0;
+        if (g_helpers.compare_exchange_weak(lent, lent + take)) return static_cast<std::size_t>(take);
+    }
+}
+void returnHelpers(std::size_t n) { g_helpers -= static_cast<long>(n); }
+
 // Copies between pageable host memory and the device, split into pieces of
 // at most 16 MB copied by several host threads at once (each on its own
 // stream): the staging of pageable memory is host-bound, one thread at a
@@ -105,8 +122,7 @@ void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
         return;
     }
     std::atomic<int> failed{static_cast<int>(cudaSuccess)};
-    const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
-    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 16), pieces.size());
+    const std::size_t T = 1 + borrowHelpers(std::min<std::size_t>(15, pieces.size() - 1));
     std::vector<std::thread> pool;
     auto note = [&](cudaError_t e) {
         int ok = static_cast<int>(cudaSuccess);
@@ -127,6 +143,7 @@ void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
     for (std::size_t t = 1; t < T; ++t) pool.emplace_back(work, t);
     work(0);
     for (auto &th : pool) th.join();
+    returnHelpers(T - 1);
     check(static_cast<cudaError_t>(failed.load()), "copy");
 }
 void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind kind) {
@@ -162,8 +179,8 @@ template <class T> std::unique_ptr<T[]> fetch(const T *src, std::size_t n) {
 // loops of upload and download (f(begin, end) on disjoint ranges; f must not
 // throw). Small ranges stay on the calling thread.
 template <class F> void parallelFor(std::size_t n, F &&f, std::size_t grain = std::size_t(1) << 16) {
-    const std::size_t hw = std::max(1U, std::thread::hardware_concurrency());
-    const std::size_t T = std::min<std::size_t>(std::min<std::size_t>(hw, 32), (n + grain - 1) / grain);
+    const std::size_t want = std::min<std::size_t>(32, (n + grain - 1) / grain);
+    const std::size_t T = want <= 1 ? 1 : 1 + borrowHelpers(want - 1);
     if (T <= 1) {
         f(std::size_t(0), n);
         return;
@@ -173,6 +190,7 @@ template <class F> void parallelFor(std::size_t n, F &&f, std::size_t grain = st
     for (std::size_t t = 1; t < T; ++t) pool.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T); });
     f(std::size_t(0), n / T);
     for (auto &th : pool) th.join();
+    returnHelpers(T - 1);
 }
 
 } // namespace
@@ -2175,7 +2193,7 @@ class ServerBase {
 public:
     virtual ~ServerBase() = default;
     virtual std::uint64_t submit(const gbl_schedule_view &s, const gbl_state_view &st, const gbl_sphere &sp,
-                                 std::uint64_t substeps) = 0;
+                                 std::uint64_t substeps, bool borrowed) = 0;
     virtual void step(std::uint64_t substeps, gbl_server_stats *stats) = 0;
     virtual void poll(std::uint64_t ticket, gbl_request_info &info) = 0;
     virtual void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) = 0;
@@ -2191,7 +2209,7 @@ public:
     }
 
     std::uint64_t submit(const gbl_schedule_view &sv, const gbl_state_view &st, const gbl_sphere &sp,
-                         std::uint64_t substeps) override {
+                         std::uint64_t substeps, bool borrowed) override {
         if (substeps == 0) invalid("a served request needs at least one substep");
         if (sv.node_count != st.node_count || sv.bond_count != st.bond_count)
             invalid("lattice schedule does not match the lattice");
@@ -2201,9 +2219,11 @@ public:
         if (bytes > budget_) invalid("request exceeds the device memory budget on its own");
         Request q;
         q.submitted = clock() - t0_;
-        // The device image is prepared here, on the caller's thread, outside
-        // the lock: a step may be running meanwhile.
-        q.prepared = Engine<R>::prepare(Schedule::fromView(sv), st, sp);
+        // Prepared here, on the caller's thread, outside the lock (a step may
+        // be running meanwhile): the device image, or for a borrowed state
+        // only the sweep order -- the device converts the caller's arrays at
+        // admission.
+        q.prepared = Engine<R>::prepare(Schedule::fromView(sv), st, sp, !borrowed);
         q.nodes = st.node_count;
         q.bonds = st.bond_count;
         q.sphere = sp;
@@ -2718,7 +2738,16 @@ gbl_result gbl_serve_submit(gbl_server *server, const gbl_schedule_view *schedul
                             const gbl_sphere *sphere, uint64_t substeps, uint64_t *ticket) {
     return gbl::guard([&] {
         if (!server || !schedule || !state || !sphere || !ticket) gbl::invalid("null argument");
-        *ticket = server->impl->submit(*schedule, *state, *sphere, substeps);
+        *ticket = server->impl->submit(*schedule, *state, *sphere, substeps, false);
+    });
+}
+
+gbl_result gbl_serve_submit_borrowed(gbl_server *server, const gbl_schedule_view *schedule,
+                                     const gbl_state_view *state, const gbl_sphere *sphere, uint64_t substeps,
+                                     uint64_t *ticket) {
+    return gbl::guard([&] {
+        if (!server || !schedule || !state || !sphere || !ticket) gbl::invalid("null argument");
+        *ticket = server->impl->submit(*schedule, *state, *sphere, substeps, true);
     });
 }
 

@@ -231,6 +231,8 @@ def library() -> C.CDLL:
         "gbl_serve_destroy": ([vp], None),
         "gbl_serve_submit": ([vp, C.POINTER(ScheduleView), C.POINTER(StateView), C.POINTER(Sphere), C.c_uint64,
                               C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_serve_submit_borrowed": ([vp, C.POINTER(ScheduleView), C.POINTER(StateView), C.POINTER(Sphere), C.c_uint64,
+                              C.POINTER(C.c_uint64)], C.c_int),
         "gbl_serve_step": ([vp, C.c_uint64, C.POINTER(ServerStats)], C.c_int),
         "gbl_serve_poll": ([vp, C.c_uint64, C.POINTER(RequestInfo)], C.c_int),
         "gbl_serve_take": ([vp, C.c_uint64, C.POINTER(StateView), C.POINTER(Sphere), C.POINTER(RunStatus)], C.c_int),
@@ -735,10 +737,13 @@ class Server:
             library().gbl_serve_destroy(self._h)
             self._h = None
 
-    def submit(self, schedule: Schedule, state: State, sphere: Sphere, substeps: int) -> int:
+    def submit(self, schedule: Schedule, state: State, sphere: Sphere, substeps: int, borrow: bool = False) -> int:
+        """Queues a request. With `borrow`, the state's arrays are read at
+        admission instead of copied now: keep `state` alive and unchanged
+        until the request is running (gbl_serve_submit_borrowed)."""
         t = C.c_uint64()
-        _call(library().gbl_serve_submit, self._h, C.byref(schedule.view), C.byref(state.view), C.byref(sphere),
-              int(substeps), C.byref(t))
+        fn = library().gbl_serve_submit_borrowed if borrow else library().gbl_serve_submit
+        _call(fn, self._h, C.byref(schedule.view), C.byref(state.view), C.byref(sphere), int(substeps), C.byref(t))
         return int(t.value)
 
     def step(self, substeps: int) -> ServerStats:

@@ -275,13 +275,16 @@ def served_leg(args, lattice) -> dict:
     tickets = [None] * arrivals.size
     start = time.perf_counter()
 
-    # Clients submit from a pool of host threads (submission prepares the
-    # request's device image on the submitting thread), each at its arrival.
+    # Clients submit from a pool of host threads, each request at its arrival
+    # (submission prepares the request's sweep order on the submitting
+    # thread; the library's parallel loops share the host's cores).
     clients = ThreadPoolExecutor(max(1, host_threads() - 2))
 
     def submit(i):
         sched, state = picks[i]
-        tickets[i] = server.submit(sched, state, sphere, horizon)
+        # Borrowed: the pool's states outlive the leg, so the device reads
+        # them at admission and no host image is written per request.
+        tickets[i] = server.submit(sched, state, sphere, horizon, borrow=not args.served_copy)
 
     def produce():
         for i, t in enumerate(arrivals):
@@ -330,7 +333,7 @@ def served_leg(args, lattice) -> dict:
             "wall_s": wall, "device_s": stats.device_seconds, "budget_gb": args.served_budget_gb,
             "steps": steps, "host_step_s": step_s, "host_poll_s": poll_s, "server_admit_s": stats.admit_seconds,
             "server_retire_s": stats.retire_seconds, "server_run_s": stats.run_seconds,
-            "chunk_substeps": args.served_chunk,
+            "chunk_substeps": args.served_chunk, "submission": "copied" if args.served_copy else "borrowed",
             "workload": f"Poisson arrivals at {args.served_rate:g}/s for {args.served_window:g} s; 90% drawn from "
                         f"{len(pool_small)} config-3 trials, 10% 128^3 lattices; {horizon} substeps each (a bounded "
                         f"horizon: the full 2400 would hold the GPU for hours at this arrival rate); latency = "
@@ -610,6 +613,8 @@ def main() -> None:
     p.add_argument("--trials", type=int, default=4096, help="batched leg: trials in one batch (0: skip)")
     p.add_argument("--plain-trials", type=int, default=64, help="batched leg: trials timed one at a time")
     p.add_argument("--no-tune", action="store_true", help="batched leg: keep the default launch shapes")
+    p.add_argument("--served-copy", action="store_true",
+                   help="served leg: submit copied states (a host image per request) instead of borrowed ones")
     p.add_argument("--served-window", type=float, default=0.25, help="served leg: seconds of arrivals (0: skip)")
     p.add_argument("--served-rate", type=float, default=2000.0)
     p.add_argument("--served-substeps", type=int, default=40)

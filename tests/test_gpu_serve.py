@@ -44,7 +44,7 @@ def _result(device, state, sphere, status):
     return out
 
 
-def _serve(device, cases, budget, arrivals, chunk=7):
+def _serve(device, cases, budget, arrivals, chunk=7, borrow=False):
     """Submits case k before step arrivals[k]; steps until every request is done."""
     server = device.Server(device.step_settings(cases[0]["settings"]), budget)
     tickets, states, peak = {}, {}, 0
@@ -55,7 +55,7 @@ def _serve(device, cases, budget, arrivals, chunk=7):
                 sched, state = _prepared(device, cases[k])
                 states[k] = state
                 tickets[k] = server.submit(sched, state, device.sphere_state(cases[k]["sphere"]),
-                                           int(cases[k]["steps"][0]))
+                                           int(cases[k]["steps"][0]), borrow=borrow)
         st = server.step(chunk)
         peak = max(peak, st.running)
         assert st.bytes_in_use <= budget
@@ -121,3 +121,20 @@ def test_oversize_request_and_cancel(device):
         assert mismatches(alone, out, STATE_KEYS[:-1]) == []
     st = server.stats()
     assert st.running == 0 and st.queued == 0 and st.bytes_in_use == 0
+
+
+def test_borrowed_requests_equal_each_request_alone(device):
+    """Borrowed states (read by the device at admission, some after waiting
+    for memory) give the results the same requests get alone."""
+    cases = _requests()
+    sizes = []
+    for c in cases:
+        sched, state = _prepared(device, c)
+        sizes.append(device.footprint(state.node_count, state.bond_count, state.view.max_degree, 1))
+    budget = sorted(sizes)[-1] + sorted(sizes)[-2]
+    outs, peak = _serve(device, cases, budget=budget, arrivals=[0, 0, 0, 1, 1, 2], borrow=True)
+    assert 1 <= peak < len(cases)
+    for k, case in enumerate(cases):
+        alone = device.run_case(case)
+        assert mismatches(alone, outs[k], STATE_KEYS[:-1]) == [], k
+        assert status_mismatches(alone, outs[k]) == [], k
