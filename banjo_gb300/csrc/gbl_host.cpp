@@ -8,11 +8,14 @@
 // runs here, once per topology, and must match the reference bit for bit.
 //
 // buildState restates buildLatticeState (src/fastlattice/FastLattice.cpp:47-169).
+// gbl_build_box and gbl_impact_settings are scene-side helpers (the box
+// generator's walk; the impact scene's step settings).
 #include "gbl_internal.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <mutex>
 
 namespace gbl {
@@ -264,7 +267,7 @@ size_t gbl_struct_size(const char *name) {
 #define GBL_SIZE(T) if (n == #T) return sizeof(T);
     GBL_SIZE(gbl_schedule_view) GBL_SIZE(gbl_state_view) GBL_SIZE(gbl_footprint) GBL_SIZE(gbl_support_plane)
     GBL_SIZE(gbl_contact_settings) GBL_SIZE(gbl_node_contact_settings) GBL_SIZE(gbl_step_settings)
-    GBL_SIZE(gbl_node_contact_accumulators) GBL_SIZE(gbl_tuning)
+    GBL_SIZE(gbl_node_contact_accumulators) GBL_SIZE(gbl_tuning) GBL_SIZE(gbl_impact_scene)
     GBL_SIZE(gbl_sphere) GBL_SIZE(gbl_run_control) GBL_SIZE(gbl_contact_accumulators) GBL_SIZE(gbl_load_ledger)
     GBL_SIZE(gbl_run_status) GBL_SIZE(gbl_matter_view) GBL_SIZE(gbl_request_info) GBL_SIZE(gbl_server_stats)
     GBL_SIZE(gbl_box_spec)
@@ -405,6 +408,87 @@ struct gbl_box {
 };
 
 extern "C" {
+
+// buildSettings (TileImpactScene.cpp:259-336) with makePlane and addFootprint
+// (:83-105): a horizontal plane's frame is normal +y, tangent +x, bitangent +z
+// (makeSupportPlane, src/core/Plane.hpp:18-45, for that normal); a footprint
+// with a finite half extent caps the plane's reach.
+gbl_result gbl_impact_settings(const gbl_impact_scene *scene, gbl_step_settings *out) {
+    return gbl::guard([&] {
+        if (!scene || !out) gbl::invalid("null argument");
+        const gbl_impact_scene &r = *scene;
+        if (r.ledge_count > GBL_MAX_FOOTPRINTS) gbl::logic("too many support footprints");
+        gbl_step_settings s{};
+        s.dt = r.dt;
+        for (int k = 0; k < 3; ++k) s.gravity[k] = r.gravity[k];
+        s.constraint_iterations = std::max(1U, r.constraint_iterations);
+        s.damping_fraction = r.bond_damping > 0.0 ? 1.0 - std::exp(-r.bond_damping * r.dt) : 0.0;
+        s.sphere_enabled = r.multi_body ? 0 : 1;
+        s.direct_arithmetic = r.double_precision ? 1 : 0;
+        s.contact.static_friction = r.ball_tile.static_friction;
+        s.contact.dynamic_friction = r.ball_tile.dynamic_friction;
+        s.contact.restitution = r.ball_tile.restitution;
+        s.contact.restitution_speed_threshold = 0.5;
+        s.contact.node_contact_radius = r.node_contact_radius_factor * r.cell_size;
+        s.contact.contact_margin = 1.0e-5;
+        s.contact.prefilter_slack = 0.05 * r.ball_radius;
+        s.audit_energy = r.audit_energy ? 1 : 0;
+        s.plastic_yield_stretch = r.yield_stretch;
+        s.plastic_hardening = r.plastic_hardening_ratio;
+        s.plate_half_thickness = 0.0;
+        s.node_contact.mode = r.node_contact_mode;
+        s.node_contact.radius = r.node_contact_radius_factor * r.cell_size;
+        s.node_contact.skin = r.node_contact_skin_factor * r.cell_size;
+        s.node_contact.margin = 1.0e-5;
+        s.node_contact.restitution = r.tile_tile.restitution;
+        s.node_contact.restitution_speed_threshold = 0.5;
+        s.node_contact.static_friction = r.tile_tile.static_friction;
+        s.node_contact.dynamic_friction = r.tile_tile.dynamic_friction;
+        std::uint32_t size = 64U; // latticeContactBucketMask (LatticePhysics.hpp:239-243)
+        while (size < 2U * r.node_count && size < (1U << 22)) size <<= 1U;
+        s.node_contact.bucket_mask = size - 1U;
+        const double inf = std::numeric_limits<double>::infinity();
+        const double node_radius = 0.5 * r.cell_size; // a cell centre rests half a cell above a surface
+        auto plane = [&](double y) {
+            gbl_support_plane p{};
+            p.point[0] = 0.0 - r.origin[0];
+            p.point[1] = y - r.origin[1];
+            p.point[2] = 0.0 - r.origin[2];
+            p.normal[1] = 1.0;
+            p.tangent[0] = 1.0;
+            p.bitangent[2] = 1.0;
+            p.restitution = r.tile_ground.restitution;
+            p.static_friction = r.tile_ground.static_friction;
+            p.dynamic_friction = r.tile_ground.dynamic_friction;
+            p.node_radius = node_radius;
+            return p;
+        };
+        auto footprint = [](gbl_support_plane &p, double t, double b, double ht, double hb) {
+            if (p.footprint_count >= GBL_MAX_FOOTPRINTS) gbl::logic("too many support footprints");
+            p.footprints[p.footprint_count++] = {t, b, ht, hb};
+            if (std::isfinite(ht) || std::isfinite(hb)) p.reach_capped = 1;
+        };
+        if (!r.bridge) {
+            gbl_support_plane ground = plane(r.ground_y);
+            footprint(ground, 0.0, 0.0, inf, inf);
+            s.plane_count = 1;
+            s.planes[0] = ground;
+        } else {
+            gbl_support_plane ledges = plane(r.support_y);
+            for (std::uint32_t k = 0; k < r.ledge_count; ++k) {
+                const gbl_ledge &l = r.ledges[k];
+                footprint(ledges, l.center[0] - r.origin[0], l.center[2] - r.origin[2], 0.5 * l.dimensions[0],
+                          0.5 * l.dimensions[2]);
+            }
+            gbl_support_plane ground = plane(r.ground_y);
+            footprint(ground, 0.0, 0.0, inf, inf);
+            s.plane_count = 2;
+            s.planes[0] = ledges;
+            s.planes[1] = ground;
+        }
+        *out = s;
+    });
+}
 
 gbl_result gbl_build_box(const gbl_box_spec *spec, gbl_box **out) {
     return gbl::guard([&] {

@@ -135,6 +135,27 @@ class Tuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ContactPair(C.Structure):
+    _fields_ = [("static_friction", C.c_double), ("dynamic_friction", C.c_double), ("restitution", C.c_double)]
+
+
+class Ledge(C.Structure):
+    _fields_ = [("center", C.c_double * 3), ("dimensions", C.c_double * 3)]
+
+
+class ImpactScene(C.Structure):
+    """gbl_impact_scene: what the impact scene's step settings are built from."""
+    _fields_ = [("dt", C.c_double), ("gravity", C.c_double * 3), ("constraint_iterations", C.c_uint32),
+                ("bond_damping", C.c_double), ("multi_body", C.c_uint8), ("double_precision", C.c_uint8),
+                ("audit_energy", C.c_uint8), ("ball_tile", ContactPair), ("tile_tile", ContactPair),
+                ("tile_ground", ContactPair), ("cell_size", C.c_double), ("node_contact_radius_factor", C.c_double),
+                ("node_contact_skin_factor", C.c_double), ("node_contact_mode", C.c_uint8),
+                ("ball_radius", C.c_double), ("yield_stretch", C.c_double), ("plastic_hardening_ratio", C.c_double),
+                ("bridge", C.c_uint8), ("ground_y", C.c_double), ("support_y", C.c_double),
+                ("ledge_count", C.c_uint32), ("ledges", Ledge * 4), ("origin", C.c_double * 3),
+                ("node_count", C.c_uint32)]
+
+
 class RequestInfo(C.Structure):
     _fields_ = [("phase", C.c_int32), ("slot", C.c_uint32), ("substeps", C.c_uint64), ("substeps_done", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("submitted_s", C.c_double), ("admitted_s", C.c_double),
@@ -221,6 +242,7 @@ def library() -> C.CDLL:
         "gbl_batch_first_failure_bonds": ([vp, C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
         "gbl_batch_tune": ([vp, C.POINTER(Tuning)], C.c_int),
+        "gbl_impact_settings": ([C.POINTER(ImpactScene), C.POINTER(StepSettings)], C.c_int),
         "gbl_batch_set_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
         "gbl_batch_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_batch_set_stream": ([vp, vp], C.c_int),
@@ -251,7 +273,7 @@ def library() -> C.CDLL:
                       ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
                       ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats),
                       ("gbl_box_spec", BoxSpec), ("gbl_node_contact_accumulators", NodeContactAccumulators),
-                      ("gbl_tuning", Tuning)]:
+                      ("gbl_tuning", Tuning), ("gbl_impact_scene", ImpactScene)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -503,6 +525,13 @@ def step_settings(packed: np.ndarray) -> StepSettings:
         n = packed[scenes.K_NODE_CONTACT:scenes.K_NODE_CONTACT + 9]
         s.node_contact = NodeContactSettings(int(n[0]), *n[1:8], int(n[8]))
     return s
+
+
+def impact_settings(scene: ImpactScene) -> StepSettings:
+    """The impact scene's StepSettings (buildSettings, TileImpactScene.cpp:259-336)."""
+    out = StepSettings()
+    _call(library().gbl_impact_settings, C.byref(scene), C.byref(out))
+    return out
 
 
 def sphere_state(packed: np.ndarray) -> Sphere:

@@ -500,6 +500,40 @@ gbl_result gbl_box_view_of(const gbl_box *box, gbl_matter_view *matter, const ui
                            uint32_t *block_count);
 void gbl_box_free(gbl_box *box);
 
+/* ---- Scene-side: the impact scene's step settings (buildSettings,
+ * src/fastlattice/TileImpactScene.cpp:259-336) from the request and the
+ * scene's derived quantities, for a caller that has no physics engine to
+ * build the rest of the scene with. The contact pairs are the scene's
+ * combined materials (ball on tile, tile on tile, tile on ground). */
+typedef struct gbl_contact_pair {
+    double static_friction, dynamic_friction, restitution;
+} gbl_contact_pair;
+typedef struct gbl_ledge {
+    double center[3], dimensions[3]; /* world frame, m */
+} gbl_ledge;
+typedef struct gbl_impact_scene {
+    double dt;                       /* substep, s */
+    double gravity[3];
+    uint32_t constraint_iterations;  /* at least one is used */
+    double bond_damping;             /* the compiled material's damping rate, 1/s (0: none) */
+    uint8_t multi_body;              /* every object is lattice: no rigid striker */
+    uint8_t double_precision;
+    uint8_t audit_energy;
+    gbl_contact_pair ball_tile, tile_tile, tile_ground;
+    double cell_size;                /* m */
+    double node_contact_radius_factor, node_contact_skin_factor; /* times the cell size */
+    uint8_t node_contact_mode;       /* 0 off, 1 measure, 2 on */
+    double ball_radius;
+    double yield_stretch, plastic_hardening_ratio; /* the compiled material's */
+    uint8_t bridge;                  /* 0: ground only; 1: a ledge plane over the ground */
+    double ground_y, support_y;      /* world heights of the ground and of the ledge tops */
+    uint32_t ledge_count;            /* at most GBL_MAX_FOOTPRINTS */
+    gbl_ledge ledges[GBL_MAX_FOOTPRINTS];
+    double origin[3];                /* the lattice's origin (LatticeState::origin) */
+    uint32_t node_count;             /* sizes the node-contact hash table */
+} gbl_impact_scene;
+gbl_result gbl_impact_settings(const gbl_impact_scene *scene, gbl_step_settings *out);
+
 #ifdef __cplusplus
 }
 #endif
