@@ -21,10 +21,12 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <new>
 #include <mutex>
 #include <string>
 #include <thread>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace gbl {
@@ -175,6 +177,21 @@ template <class T> std::unique_ptr<T[]> fetch(const T *src, std::size_t n) {
     return out;
 }
 
+// An allocator that leaves trivial elements uninitialised when a vector is
+// sized: the per-bond scratch of an upload (hundreds of MB for a large
+// lattice) is written in full, or filled in parallel, before it is read, and
+// a vector's own zero fill would be one thread's pass over all of it.
+template <class T> struct NoInit : std::allocator<T> {
+    template <class U> struct rebind { using other = NoInit<U>; };
+    NoInit() = default;
+    template <class U> NoInit(const NoInit<U> &) {}
+    template <class U, class... A> void construct(U *p, A &&...a) {
+        if constexpr (sizeof...(A) == 0) ::new (static_cast<void *>(p)) U;
+        else ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+    }
+};
+template <class T> using Scratch = std::vector<T, NoInit<T>>;
+
 // A static split of [0, n) over host threads, for the O(N + B) conversion
 // loops of upload and download (f(begin, end) on disjoint ranges; f must not
 // throw). Small ranges stay on the calling thread.
@@ -280,8 +297,9 @@ template <class R> struct Resident {
     Arena arena;
     Dev<R> dev{};
     std::vector<Level> levels;
-    std::vector<std::uint32_t> dev2sched, isolated; // storage -> schedule order; nodes without bonds
-    std::vector<std::uint8_t> last_a, last_b; // the last bond of its end a / b in the sweep, by schedule index
+    Scratch<std::uint32_t> dev2sched;         // storage -> schedule order
+    std::vector<std::uint32_t> isolated;      // nodes without bonds
+    Scratch<std::uint8_t> last_a, last_b;     // the last bond of its end a / b in the sweep, by schedule index
     bool plastic_state{};
     std::vector<R> mass, inv_mass;
     Sphere<R> sphere0{};
@@ -424,7 +442,11 @@ template <class R> struct Resident {
             }
         }, 1);
         if (bad.load()) invalid("lattice bond joins invalid nodes");
-        std::vector<std::uint32_t> depth(B), reached(N, 0), last(N, kNoBond);
+        Scratch<std::uint32_t> depth(B);
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            std::memset(depth.data() + lo, 0, sizeof(std::uint32_t) * (hi - lo));
+        });
+        std::vector<std::uint32_t> reached(N, 0), last(N, kNoBond);
         auto walk = [&](const Task &task) {
             std::uint32_t deepest = 0;
             for (std::uint32_t k = task.seg_begin; k < task.seg_end; ++k)
@@ -457,7 +479,7 @@ template <class R> struct Resident {
         }
         // Storage order: by depth, stable in the serial order (a parallel
         // counting sort over chunks of the serial walk).
-        std::vector<std::uint32_t> order(B);
+        Scratch<std::uint32_t> order(B);
         {
             std::vector<std::uint32_t> at(segs.size() + 1, 0);
             for (std::size_t k = 0; k < segs.size(); ++k) at[k + 1] = at[k] + (segs[k].end - segs[k].begin);
@@ -491,7 +513,7 @@ template <class R> struct Resident {
                 run += n;
             }
         }
-        dev2sched.assign(B, 0);
+        dev2sched.resize(B); // every entry written by the scatter below
         parallelFor(nchunks, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t c = lo; c < hi; ++c) {
                 std::uint32_t *fill = counts.data() + c * D1;
@@ -504,8 +526,12 @@ template <class R> struct Resident {
         levels.clear();
         for (std::uint32_t d = 1; d <= deepest; ++d)
             if (first[d + 1] > first[d]) levels.push_back({first[d], first[d + 1]});
-        last_a.assign(B, 0);
-        last_b.assign(B, 0);
+        last_a.resize(B);
+        last_b.resize(B);
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            std::memset(last_a.data() + lo, 0, hi - lo);
+            std::memset(last_b.data() + lo, 0, hi - lo);
+        });
         parallelFor(N, [&](std::size_t lo, std::size_t hi) {
             for (std::size_t i = lo; i < hi; ++i) {
                 if (last[i] == kNoBond) continue;
