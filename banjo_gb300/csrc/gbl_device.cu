@@ -102,17 +102,16 @@ std::size_t borrowHelpers(std::size_t want) {
 void returnHelpers(std::size_t n) { g_helpers -= static_cast<long>(n); }
 
 // Copies between pageable host memory and the device, split into pieces of
-// at most 16 MB copied by several host threads at once (each on its own
+// at most 64 MB copied by several host threads at once (each on its own
 // stream): the staging of pageable memory is host-bound, one thread at a
-// time, and small pieces keep the threads evenly loaded. Returns when every
-// piece has arrived.
+// time. Returns when every piece has arrived.
 struct Segment {
     void *dst;
     const void *src;
     std::size_t bytes;
 };
 void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
-    constexpr std::size_t kPiece = std::size_t(16) << 20;
+    constexpr std::size_t kPiece = std::size_t(64) << 20;
     std::vector<Segment> pieces;
     for (const Segment &g : segments)
         for (std::size_t off = 0; off < g.bytes; off += kPiece)
@@ -807,13 +806,13 @@ template <class R> struct Resident {
             convertFromHost(staged, stream);
             return;
         }
-        // Each staging buffer holds up to 1 GB of the caller's arrays (less
+        // Each staging buffer holds up to 256 MB of the caller's arrays (less
         // when the whole lattice needs less).
         const std::size_t P = static_cast<std::size_t>(dev.D) * N;
         const std::size_t whole = std::max({N * 14 * sizeof(double), P * 41, static_cast<std::size_t>(B) * 164});
         auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
         // A multiple of 256 bytes: the second buffer and every part start aligned.
-        const std::size_t kStage = round(std::min(std::size_t(1) << 30, whole + 32 * 256));
+        const std::size_t kStage = round(std::min(std::size_t(256) << 20, whole + 32 * 256));
         char *stage = nullptr;
         check(cudaMallocAsync(&stage, 2 * kStage + 256, stream), "device allocation");
         unsigned *flowed = reinterpret_cast<unsigned *>(stage + 2 * kStage);
