@@ -302,6 +302,38 @@ def impact_block(nx=256, ny=128, nz=128, h=0.01, blocks=32, steps=120, substeps=
     return case
 
 
+def plate_strike(nx=24, nz=24, h=0.01, steps=40, radius=0.03, speed=8.0, median=2e-3, sigma=0.2, seed_strength=7,
+                 yield_fraction=0.0, span=0.5, plate=True, gap=0.001):
+    """A sheet one cell thick (nx x 1 x nz) resting on two ledges at its x
+    ends (finite footprints, `span` of its length clear between them), struck
+    at the centre by a rigid sphere, with plate bending on (half the cell as
+    the half thickness): the fibre strain of the bending sheet is what breaks
+    its bonds. Per-bond tensile break strain lognormal (median, sigma);
+    compression and shear disabled."""
+    case = _box_case(nx, 1, nz, h, (0.0, 0.0, 0.0), 1e-7, [INF] * 6)
+    nb = int(case["bond_count"][0])
+    strength = lognormal(seed_strength, nb, median, sigma)
+    thr = np.full((nb, 6), INF, dtype=np.float64)
+    thr[:, 0] = strength
+    thr[:, 1] = strength
+    case["threshold"] = thr.reshape(-1)
+    length = nx * h
+    ledge = 0.5 * (1.0 - span) * length  # each ledge's width under the sheet
+    centre = 0.5 * length - 0.5 * ledge
+    ledges = plane((0.0, -0.5 * h, 0.0), node_radius=0.5 * h,
+                   footprints=((-centre, 0.0, 0.5 * ledge, INF), (centre, 0.0, 0.5 * ledge, INF)))
+    s = settings(sphere_enabled=1, yield_stretch=yield_fraction * median,
+                 contact=(0.5, 0.4, 0.0, 0.5, 0.5 * h, 1e-5, 0.05 * radius), planes=[ledges])
+    if plate:
+        s[K_PLATE] = 0.5 * h
+    case.update({
+        "settings": s,
+        "sphere": sphere((0.0, 0.5 * h + gap + radius, 0.0), (0.0, -speed, 0.0), radius),
+        "steps": np.array([steps], dtype=np.uint64),
+    })
+    return case
+
+
 def drop_trial(nx, ny, nz, compliance, break_strain, drop_height, h=0.01, steps=240, substeps=10):
     """One batched trial: a box released at rest `drop_height` above the ground."""
     case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), compliance, [break_strain, break_strain, INF, INF, INF, INF])

@@ -404,8 +404,136 @@ template <class R> int pinv3(const R m[9], R out[9], R unmeasured[3]) {
     return rank;
 }
 
-// Nonlocal node strain (LatticePhysics.hpp:791-907; plate bending is off).
-template <class R> void nodeStrain(Lattice<R> &L, std::size_t i, bool direct, std::uint32_t &rank_deficient) {
+// Bending strain of a sheet one cell thick (plateBendingStrain,
+// LatticePhysics.hpp:575-777): the rest neighbourhood (every bond built, alive
+// or not) says whether the node lies in a sheet and which way the sheet
+// faces; a tilt fit and then a curvature fit over the live neighbours; a fit
+// that explains no more than 0.9 of the out-of-plane motion claims no
+// bending; the tension fibre of |K| at half the thickness, capped at the yield
+// stretch, is added to E in the sheet's frame.
+template <class R>
+void plateBending(const Lattice<R> &L, std::size_t i, bool direct, R half_thickness, R yield_stretch, V<R> xi,
+                  R *e) {
+    const std::size_t N = L.N, D = L.D;
+    R rest_cov[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (std::size_t k = 0; k < D; ++k) {
+        const std::size_t slot = k * N + i;
+        if (L.nbr_bond[slot] == kNoBond) continue;
+        const R w = L.nbr_weight[slot];
+        if (w <= R(0)) continue;
+        const R rr[3] = {L.nbr_rest[3 * slot], L.nbr_rest[3 * slot + 1], L.nbr_rest[3 * slot + 2]};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) rest_cov[r * 3 + c] += w * rr[r] * rr[c];
+    }
+    R rest_inv[9], flat[3];
+    if (pinv3(rest_cov, rest_inv, flat) >= 3) return; // a solid neighbourhood, not a sheet
+    const V<R> normal{flat[0], flat[1], flat[2]};
+    if (!(dot(normal, normal) > R(0))) return;
+    const R *inv = &L.rinv[9 * i];
+    auto neighbour = [&](std::size_t k, R &w, V<R> &rest, V<R> &d) {
+        const std::size_t slot = k * N + i;
+        const bool present = L.nbr_bond[slot] != kNoBond;
+        const std::size_t other = present ? L.nbr_other[slot] : i;
+        w = (present && L.nbr_alive[slot]) ? L.nbr_weight[slot] : R(0);
+        rest = present ? V<R>{L.nbr_rest[3 * slot], L.nbr_rest[3 * slot + 1], L.nbr_rest[3 * slot + 2]}
+                       : V<R>{R(0), R(0), R(0)};
+        const V<R> xo = direct ? position(L, other) : ld(L.u, other);
+        d = direct ? sub(sub(xo, xi), rest) : sub(xo, xi);
+    };
+    // The tilt.
+    R rhs[3] = {0, 0, 0};
+    for (std::size_t k = 0; k < D; ++k) {
+        R w;
+        V<R> rest, d;
+        neighbour(k, w, rest, d);
+        const R out = w * dot(d, normal);
+        rhs[0] += out * rest.x;
+        rhs[1] += out * rest.y;
+        rhs[2] += out * rest.z;
+    }
+    R tilt[3];
+    for (int r = 0; r < 3; ++r) {
+        R acc = R(0);
+        for (int k = 0; k < 3; ++k) acc += inv[r * 3 + k] * rhs[k];
+        tilt[r] = acc;
+    }
+    // The in-plane frame, from the axis the normal leans on least.
+    const R ax = normal.x < R(0) ? -normal.x : normal.x;
+    const R ay = normal.y < R(0) ? -normal.y : normal.y;
+    const R az = normal.z < R(0) ? -normal.z : normal.z;
+    const V<R> axis = (ax <= ay && ax <= az) ? V<R>{R(1), R(0), R(0)}
+                    : (ay <= az)             ? V<R>{R(0), R(1), R(0)}
+                                             : V<R>{R(0), R(0), R(1)};
+    V<R> e1 = cross(normal, axis);
+    const R e1len = len(e1);
+    if (!(e1len > R(0))) return;
+    e1 = scale(e1, R(1) / e1len);
+    const V<R> e2 = cross(normal, e1);
+    // The curvature, over what the tilt leaves.
+    R A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    R g[3] = {0, 0, 0};
+    R out2 = R(0);
+    for (std::size_t k = 0; k < D; ++k) {
+        R w;
+        V<R> rest, d;
+        neighbour(k, w, rest, d);
+        const R left = dot(d, normal) - (tilt[0] * rest.x + tilt[1] * rest.y + tilt[2] * rest.z);
+        const R p1 = dot(rest, e1), p2 = dot(rest, e2);
+        const R psi[3] = {R(0.5) * p1 * p1, p1 * p2, R(0.5) * p2 * p2};
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) A[r * 3 + c] += w * psi[r] * psi[c];
+            g[r] += w * psi[r] * left;
+        }
+        out2 += w * left * left;
+    }
+    R ev[3], axes[9];
+    eigen3(A, ev, axes);
+    R biggest = absR(ev[0]);
+    for (int k = 1; k < 3; ++k) biggest = absR(ev[k]) > biggest ? absR(ev[k]) : biggest;
+    const R determined = R(1.0e-3) * biggest;
+    R c[3] = {0, 0, 0};
+    int along = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (!(ev[k] > determined)) continue;
+        ++along;
+        R projected = R(0);
+        for (int r = 0; r < 3; ++r) projected += axes[r * 3 + k] * g[r];
+        const R amount = projected / ev[k];
+        for (int r = 0; r < 3; ++r) c[r] += amount * axes[r * 3 + k];
+    }
+    if (along < 1) return;
+    const R explained = c[0] * g[0] + c[1] * g[1] + c[2] * g[2];
+    if (!(explained > R(0.9) * out2)) return;
+    // |K| through the trace and the eigenvalue split of [[c0, c1], [c1, c2]].
+    const R half_trace = R(0.5) * (c[0] + c[2]);
+    const R det = c[0] * c[2] - c[1] * c[1];
+    R under = half_trace * half_trace - det;
+    if (under < R(0)) under = R(0);
+    const R disc = std::sqrt(under);
+    const R l1 = half_trace + disc, l2 = half_trace - disc;
+    const R a1 = l1 < R(0) ? -l1 : l1, a2 = l2 < R(0) ? -l2 : l2;
+    const R most = yield_stretch > R(0) ? yield_stretch : R(-1);
+    R s1 = half_thickness * a1, s2 = half_thickness * a2;
+    if (most > R(0)) {
+        if (s1 > most) s1 = most;
+        if (s2 > most) s2 = most;
+    }
+    const R alpha = R(0.5) * (s1 + s2), beta = R(0.5) * (s1 - s2);
+    const R ratio = disc > R(0) ? beta / disc : R(0);
+    const R b11 = alpha + ratio * (c[0] - half_trace);
+    const R b12 = ratio * c[1];
+    const R b22 = alpha + ratio * (c[2] - half_trace);
+    const R u1[3] = {e1.x, e1.y, e1.z}, u2[3] = {e2.x, e2.y, e2.z};
+    static const int rows[6] = {0, 1, 2, 0, 0, 1}, cols[6] = {0, 1, 2, 1, 2, 2};
+    for (int q = 0; q < 6; ++q)
+        e[q] += b11 * u1[rows[q]] * u1[cols[q]] + b22 * u2[rows[q]] * u2[cols[q]] +
+                b12 * (u1[rows[q]] * u2[cols[q]] + u2[rows[q]] * u1[cols[q]]);
+}
+
+// Nonlocal node strain (LatticePhysics.hpp:791-907).
+template <class R>
+void nodeStrain(Lattice<R> &L, std::size_t i, bool direct, std::uint32_t &rank_deficient, R plate_half_thickness,
+                R plate_yield) {
     const std::size_t N = L.N, D = L.D;
     if (L.node_dirty[i]) {
         R cov[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -473,6 +601,7 @@ template <class R> void nodeStrain(Lattice<R> &L, std::size_t i, bool direct, st
         const R s = a[0] * un[0] + a[1] * un[1] + a[2] * un[2];
         for (int q = 0; q < 6; ++q)
             e[q] += -un[rows[q]] * a[cols[q]] - a[rows[q]] * un[cols[q]] + s * un[rows[q]] * un[cols[q]];
+        if (plate_half_thickness > R(0)) plateBending(L, i, direct, plate_half_thickness, plate_yield, xi, e);
     }
     for (int q = 0; q < 6; ++q) L.strain[6 * i + q] = e[q];
 }
@@ -1141,7 +1270,6 @@ template <class R> struct Loads {
 template <class R> class Runner {
 public:
     Runner(Lattice<R> &L, const Settings<R> &S, Sphere<R> sp, unsigned threads) : L_(L), S_(S), sp_(sp), pool_(threads) {
-        if (S_.plate_half_thickness > R(0)) throw std::invalid_argument("plate bending is not implemented in this checker");
         if (S_.nc_mode != 0 && !(contactCutoff(S_) > R(0))) throw std::invalid_argument("node contact needs 2 r + skin > 0");
     }
     Status status;
@@ -1197,7 +1325,8 @@ private:
     void strainAll(bool direct) {
         std::vector<std::uint32_t> rd(pool_.size(), 0);
         pool_.run(L_.N, [&](std::size_t b, std::size_t e, unsigned t) {
-            for (std::size_t i = b; i < e; ++i) nodeStrain(L_, i, direct, rd[t]);
+            for (std::size_t i = b; i < e; ++i)
+                nodeStrain(L_, i, direct, rd[t], S_.plate_half_thickness, S_.yield_stretch);
         });
         for (auto x : rd) status.rank_deficient_nodes += x;
     }

@@ -63,6 +63,10 @@ def cases() -> dict:
     out["contact_pair_momentum"] = (scenes.two_cells(0.02, v0=4.0, v1=-1.0, mass_ratio=3.0, steps=8000), "double")
     out["contact_drop"] = (scenes.contact_drop(), "float")
     out["contact_drop_measure"] = (scenes.contact_drop(mode=1, steps=20), "float")
+    # Plate bending: a sheet one cell thick on two ledges, struck at its
+    # centre, breaking by the fibre strain of its bending; float and double.
+    out["plate_strike"] = (scenes.plate_strike(), "float")
+    out["plate_strike_double"] = (scenes.plate_strike(nx=16, nz=16, steps=25), "double")
     return out
 
 
