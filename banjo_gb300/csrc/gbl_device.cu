@@ -666,8 +666,9 @@ template <class R> struct Resident {
             for (std::size_t s = lo; s < hi; ++s) {
                 const bool present = st.nbr_bond[s] != kNoBond;
                 const std::uint32_t node = static_cast<std::uint32_t>(s % N);
+                const R w = R(st.nbr_weight[s]);
                 d.nbr[s] = {R(st.nbr_rest[3 * s]), R(st.nbr_rest[3 * s + 1]), R(st.nbr_rest[3 * s + 2]),
-                            (present && st.nbr_alive[s]) ? R(st.nbr_weight[s]) : R(0)};
+                            present ? (st.nbr_alive[s] ? w : -absR(w)) : R(0)};
                 d.nbr_other[s] = present ? st.nbr_other[s] : node;
                 d.nbr_bond[s] = present ? st.nbr_bond[s] : kNoBond; // schedule index; storage index on the device
             }
@@ -1567,7 +1568,6 @@ public:
             !(2.0 * s.node_contact.radius + s.node_contact.skin > 0.0 &&
               std::isfinite(2.0 * s.node_contact.radius + s.node_contact.skin)))
             invalid("node-to-node contact needs a finite positive cutoff (2 radius + skin)");
-        if (s.plate_half_thickness > 0.0) invalid("this lattice backend does not implement plate bending");
         if (s.audit_energy) invalid("this lattice backend does not implement the energy audit");
         if ((s.direct_arithmetic != 0) != kDirect)
             invalid(kDirect ? "the double backend runs the direct (absolute position) arithmetic"
@@ -1601,6 +1601,7 @@ private:
         o.nc_margin = R(s.node_contact.margin); o.nc_restitution = R(s.node_contact.restitution);
         o.nc_threshold = R(s.node_contact.restitution_speed_threshold);
         o.nc_static = R(s.node_contact.static_friction); o.nc_dynamic = R(s.node_contact.dynamic_friction);
+        o.plate_half_thickness = R(s.plate_half_thickness);
         o.plane_count = s.plane_count;
         for (unsigned p = 0; p < kPlanes; ++p) {
             const gbl_support_plane &in = s.planes[p];
@@ -2024,7 +2025,15 @@ private:
     // the start samples of their bonds.
     template <bool M, class Mark = void (*)(unsigned)>
     void restartPhase(cudaStream_t st, int after_kick, Mark &&mark = [](unsigned) {}) {
-        if (nodes_.count) kRestartStrain<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), after_kick);
+        if (nodes_.count) {
+            const R plate = S_.plate_half_thickness, yield = S_.yield_stretch;
+            if (plate > R(0))
+                kRestartStrain<R, M, kDirect, true><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), after_kick, plate,
+                                                                                       yield);
+            else
+                kRestartStrain<R, M, kDirect, false><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), after_kick,
+                                                                                        plate, yield);
+        }
         mark(1);
         if (bonds_.count)
             kRestartBondsAll<R, M, kDirect><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), after_kick);
@@ -2037,7 +2046,13 @@ private:
     // (0 all, 1 outside the contact halo, 2 inside it).
     template <bool M, class Mark = void (*)(unsigned)>
     void endPhase(cudaStream_t st, int part, Mark &&mark = [](unsigned) {}) {
-        if (nodes_.count) kStrainAll<R, M, kDirect><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), part);
+        if (nodes_.count) {
+            const R plate = S_.plate_half_thickness, yield = S_.yield_stretch;
+            if (plate > R(0))
+                kStrainAll<R, M, kDirect, true><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), part, plate, yield);
+            else
+                kStrainAll<R, M, kDirect, false><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), part, plate, yield);
+        }
         mark(11);
         if (bonds_.count) {
             if (plastic_) kEndSample<R, M, kDirect, true><<<bonds_.count, kThreads, 0, st>>>(grid(bonds_), S_, part);

@@ -4,7 +4,7 @@
 //   nodes  u[i]   = (u.xyz, inv_mass)   v[i] = (v.xyz, mass)   x0[i] = (x0.xyz, 0)
 //          up[i]  = u_prev              strain[2i..2i+1] = (e0..e3 | e4, e5, valid, 0)
 //          rinv   9 x N, unm 3 x N      (component-major, coalesced per node)
-//          nbr[k*N+i] = (rest.xyz, weight if the slot's bond is alive else 0)
+//          nbr[k*N+i] = (rest.xyz, the slot's weight, negated once its bond has failed; 0 when padded)
 //          nbr_other[k*N+i] (i itself for a padded slot), nbr_bond[k*N+i]
 //   bonds  rec[d] = (a | dead | last-of-a, b | last-of-b, rest_length_sq_minus, rest_length)
 //          geo[d] = (rest_edge.xyz, compliance)
@@ -216,15 +216,145 @@ template <class R> __device__ __forceinline__ V3<R> pos(const Dev<R> &L, std::ui
 // ---------------------------------------------------------------------------
 // Nonlocal node strain (LatticePhysics.hpp:791-907, plate bending off).
 // ---------------------------------------------------------------------------
+// A slot's weight while its bond is alive, else 0 (LatticeArrays::nbr_alive
+// gating nbr_weight); the raw weight stays in the slot, sign-flipped, for the
+// rest geometry of plate bending.
+template <class R> __device__ __forceinline__ R liveWeight(R w) { return signbit(w) ? R(0) : w; }
+
+// Bending strain of a sheet one cell thick (plateBendingStrain,
+// LatticePhysics.hpp:575-777): the rest neighbourhood (every bond built, alive
+// or not) says whether the node lies in a sheet and which way it faces; a
+// tilt fit and then a curvature fit over the live neighbours; a fit that
+// explains no more than 0.9 of the out-of-plane motion claims no bending; the
+// tension fibre of |K| at half the thickness, capped at the yield stretch, is
+// added to E in the sheet's frame.
 template <class R, bool Direct>
-__device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
+__device__ __noinline__ void plateBending(const Dev<R> &L, std::uint32_t i, V3<R> xi, R half_thickness,
+                                          R yield_stretch, R *e) {
+    const std::size_t N = L.N;
+    R rest_cov[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (std::uint32_t k = 0; k < L.D; ++k) {
+        const std::size_t slot = k * N + i;
+        if (L.nbr_bond[slot] == kNoBond) continue;
+        const Q4<R> q = L.nbr[slot];
+        const R w = absR(q.w);
+        if (w <= R(0)) continue;
+        const R rr[3] = {q.x, q.y, q.z};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) rest_cov[r * 3 + c] += w * rr[r] * rr[c];
+    }
+    R rest_inv[9], flat[3];
+    if (pseudoInverse3(rest_cov, rest_inv, flat) >= 3) return; // a solid neighbourhood, not a sheet
+    const V3<R> normal{flat[0], flat[1], flat[2]};
+    if (!(dot(normal, normal) > R(0))) return;
+    R inv[9];
+    for (int k = 0; k < 9; ++k) inv[k] = L.rinv[k * N + i];
+    auto neighbour = [&](std::uint32_t k, R &w, V3<R> &rest, V3<R> &d) {
+        const std::size_t slot = k * N + i;
+        const bool present = L.nbr_bond[slot] != kNoBond;
+        const Q4<R> q = L.nbr[slot];
+        const std::uint32_t other = present ? L.nbr_other[slot] : i;
+        w = present ? liveWeight(q.w) : R(0);
+        rest = present ? V3<R>{q.x, q.y, q.z} : V3<R>{R(0), R(0), R(0)};
+        const V3<R> xo = Direct ? pos(L, other) : xyz(L.u[other]);
+        d = Direct ? (xo - xi) - rest : xo - xi;
+    };
+    R rhs[3] = {0, 0, 0};
+    for (std::uint32_t k = 0; k < L.D; ++k) {
+        R w;
+        V3<R> rest, d;
+        neighbour(k, w, rest, d);
+        const R out = w * dot(d, normal);
+        rhs[0] += out * rest.x;
+        rhs[1] += out * rest.y;
+        rhs[2] += out * rest.z;
+    }
+    R tilt[3];
+    for (int r = 0; r < 3; ++r) {
+        R acc = R(0);
+        for (int k = 0; k < 3; ++k) acc += inv[r * 3 + k] * rhs[k];
+        tilt[r] = acc;
+    }
+    const R ax = normal.x < R(0) ? -normal.x : normal.x;
+    const R ay = normal.y < R(0) ? -normal.y : normal.y;
+    const R az = normal.z < R(0) ? -normal.z : normal.z;
+    const V3<R> axis = (ax <= ay && ax <= az) ? V3<R>{R(1), R(0), R(0)}
+                     : (ay <= az)             ? V3<R>{R(0), R(1), R(0)}
+                                              : V3<R>{R(0), R(0), R(1)};
+    V3<R> e1 = cross(normal, axis);
+    const R e1len = length(e1);
+    if (!(e1len > R(0))) return;
+    e1 = (R(1) / e1len) * e1;
+    const V3<R> e2 = cross(normal, e1);
+    R A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    R g[3] = {0, 0, 0};
+    R out2 = R(0);
+    for (std::uint32_t k = 0; k < L.D; ++k) {
+        R w;
+        V3<R> rest, d;
+        neighbour(k, w, rest, d);
+        const R left = dot(d, normal) - (tilt[0] * rest.x + tilt[1] * rest.y + tilt[2] * rest.z);
+        const R p1 = dot(rest, e1), p2 = dot(rest, e2);
+        const R psi[3] = {R(0.5) * p1 * p1, p1 * p2, R(0.5) * p2 * p2};
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) A[r * 3 + c] += w * psi[r] * psi[c];
+            g[r] += w * psi[r] * left;
+        }
+        out2 += w * left * left;
+    }
+    R ev[3], axes[9];
+    jacobi3(A, ev, axes);
+    R biggest = absR(ev[0]);
+    for (int k = 1; k < 3; ++k) biggest = absR(ev[k]) > biggest ? absR(ev[k]) : biggest;
+    const R determined = R(1.0e-3) * biggest;
+    R c[3] = {0, 0, 0};
+    int along = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (!(ev[k] > determined)) continue;
+        ++along;
+        R projected = R(0);
+        for (int r = 0; r < 3; ++r) projected += axes[r * 3 + k] * g[r];
+        const R amount = projected / ev[k];
+        for (int r = 0; r < 3; ++r) c[r] += amount * axes[r * 3 + k];
+    }
+    if (along < 1) return;
+    const R explained = c[0] * g[0] + c[1] * g[1] + c[2] * g[2];
+    if (!(explained > R(0.9) * out2)) return;
+    const R half_trace = R(0.5) * (c[0] + c[2]);
+    const R det = c[0] * c[2] - c[1] * c[1];
+    R under = half_trace * half_trace - det;
+    if (under < R(0)) under = R(0);
+    const R disc = sqrtR(under);
+    const R l1 = half_trace + disc, l2 = half_trace - disc;
+    const R a1 = l1 < R(0) ? -l1 : l1, a2 = l2 < R(0) ? -l2 : l2;
+    const R most = yield_stretch > R(0) ? yield_stretch : R(-1);
+    R s1 = half_thickness * a1, s2 = half_thickness * a2;
+    if (most > R(0)) {
+        if (s1 > most) s1 = most;
+        if (s2 > most) s2 = most;
+    }
+    const R alpha = R(0.5) * (s1 + s2), beta = R(0.5) * (s1 - s2);
+    const R ratio = disc > R(0) ? beta / disc : R(0);
+    const R b11 = alpha + ratio * (c[0] - half_trace);
+    const R b12 = ratio * c[1];
+    const R b22 = alpha + ratio * (c[2] - half_trace);
+    const R u1[3] = {e1.x, e1.y, e1.z}, u2[3] = {e2.x, e2.y, e2.z};
+    const int rows[6] = {0, 1, 2, 0, 0, 1};
+    const int cols[6] = {0, 1, 2, 1, 2, 2};
+    for (int q = 0; q < 6; ++q)
+        e[q] += b11 * u1[rows[q]] * u1[cols[q]] + b22 * u2[rows[q]] * u2[cols[q]] +
+                b12 * (u1[rows[q]] * u2[cols[q]] + u2[rows[q]] * u1[cols[q]]);
+}
+
+template <class R, bool Direct, bool Plate = false>
+__device__ void nodeStrain(const Dev<R> &L, std::uint32_t i, R plate_half_thickness = R(0), R plate_yield = R(0)) {
     const std::size_t N = L.N;
     if (L.dirty[i]) {
         R cov[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         std::uint32_t live = 0;
         for (std::uint32_t k = 0; k < L.D; ++k) {
             const Q4<R> q = L.nbr[k * N + i];
-            const R w = q.w;
+            const R w = liveWeight(q.w);
             if (w <= R(0)) continue; // dead, padded, or a degenerate rest edge
             const R rr[3] = {q.x, q.y, q.z};
             for (int r = 0; r < 3; ++r)
@@ -258,7 +388,7 @@ __device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
         const V3<R> rest{q.x, q.y, q.z};
         const V3<R> xo = Direct ? pos(L, other) : xyz(L.u[other]);
         const V3<R> cur = Direct ? (xo - xi) - rest : xo - xi;
-        const R w = q.w;
+        const R w = liveWeight(q.w);
         const R cc[3] = {cur.x, cur.y, cur.z};
         const R rr[3] = {rest.x, rest.y, rest.z};
         for (int r = 0; r < 3; ++r)
@@ -268,6 +398,10 @@ __device__ void nodeStrain(const Dev<R> &L, std::uint32_t i) {
     for (int k = 0; k < 9; ++k) inv[k] = L.rinv[k * N + i];
     for (int k = 0; k < 3; ++k) un[k] = L.unm[k * N + i];
     strainFromMoments(acc, inv, un, e);
+    // What a coplanar neighbourhood's plane cannot hold: the bending of a
+    // sheet one cell thick (LatticePhysics.hpp:896-905).
+    if (Plate && plate_half_thickness > R(0) && un[0] * un[0] + un[1] * un[1] + un[2] * un[2] > R(0))
+        plateBending<R, Direct>(L, i, xi, plate_half_thickness, plate_yield, e);
     L.strain[2 * i] = Q4<R>{e[0], e[1], e[2], e[3]};
     L.strain[2 * i + 1] = Q4<R>{e[4], e[5], R(1), R(0)};
 }
@@ -277,8 +411,8 @@ template <class R> __device__ __forceinline__ std::uint32_t substepStamp(const D
     return static_cast<std::uint32_t>(L.ctl->total_steps) + 1U;
 }
 
-template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int part) {
+template <class R, bool Many, bool Direct, bool Plate>
+__global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int part, R plate, R yield) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     if (L.ctl->stop) return;
@@ -289,7 +423,7 @@ __global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int
         const bool halo = L.halo_stamp[i] == substepStamp(L);
         if (halo != (part == 2)) return;
     }
-    nodeStrain<R, Direct>(L, i);
+    nodeStrain<R, Direct, Plate>(L, i, plate, yield);
 }
 
 // The start-of-substep restart after an upload (every node) or after a failure
@@ -298,8 +432,8 @@ __global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int
 // src/fastlattice/ParallelCpuLatticeBackend.cpp:1718-1757 relies on the same fact).
 // It reads the substep's starting positions: before the kick from u, or after
 // it (beside the first contact pass) from u_prev, where the kick copied them.
-template <class R, bool Many, bool Direct>
-__global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch, int after_kick) {
+template <class R, bool Many, bool Direct, bool Plate>
+__global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch, int after_kick, R plate, R yield) {
     const Work w = item<Many>(launch);
     Dev<R> L = descriptor<R, Many>(launch, w);
     if (after_kick) L.u = L.up; // the kick kept the substep's starting positions there
@@ -307,8 +441,8 @@ __global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch,
     // Items cover the node index range; a dirty list is never longer.
     const std::uint32_t t = w.begin + threadIdx.x;
     if (t >= w.end) return;
-    if (L.ctl->full_restart) nodeStrain<R, Direct>(L, t);
-    else if (t < L.ctl->dirty_count) nodeStrain<R, Direct>(L, L.dirty_list[t]);
+    if (L.ctl->full_restart) nodeStrain<R, Direct, Plate>(L, t, plate, yield);
+    else if (t < L.ctl->dirty_count) nodeStrain<R, Direct, Plate>(L, L.dirty_list[t], plate, yield);
 }
 
 // ---------------------------------------------------------------------------
@@ -1337,8 +1471,10 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
                     energy = R(0.5) * ext * ext / cc;
                 }
                 L.rec[j].a = rec.a | kDeadBit;
-                L.nbr[L.slot_a[j]].w = R(0);
-                L.nbr[L.slot_b[j]].w = R(0);
+                // Both slots keep their weight, sign-flipped: dead for the
+                // strain, still there for a sheet's rest geometry.
+                L.nbr[L.slot_a[j]].w = -absR(L.nbr[L.slot_a[j]].w);
+                L.nbr[L.slot_b[j]].w = -absR(L.nbr[L.slot_b[j]].w);
                 L.ev_removed[js] = static_cast<double>(energy);
                 L.ev_ends[js] = make_uint2(a, b);
                 atomicOr(L.ev_bits + (js >> 5), 1U << (js & 31U));
@@ -1904,7 +2040,7 @@ __global__ void __launch_bounds__(kThreads) kContactGather(const Grid<R> launch,
                             if (bs == kNoBond) break;
                             if (L.nbr_other[slot] != j) continue;
                             bond = bs;
-                            held = L.nbr[slot].w != R(0);
+                            held = !signbit(L.nbr[slot].w);
                             break;
                         }
                         if (held) continue;
@@ -2213,8 +2349,9 @@ __global__ void __launch_bounds__(kThreads) kSlotsIn(Q4<R> *nbr, std::uint32_t *
         const std::size_t s = first + k;
         const std::uint32_t bond = in.bond[k];
         const bool present = bond != kNoBond;
+        const R w = R(in.weight[k]);
         nbr[s] = Q4<R>{R(in.rest[3 * k]), R(in.rest[3 * k + 1]), R(in.rest[3 * k + 2]),
-                       (present && in.alive[k]) ? R(in.weight[k]) : R(0)};
+                       present ? (in.alive[k] ? w : -absR(w)) : R(0)};
         nbr_other[s] = present ? in.other[k] : static_cast<std::uint32_t>(s % N);
         nbr_bond[s] = bond;
     }

@@ -85,6 +85,7 @@ template <class R> struct Settings {
     // other value measures (broad and narrow phase, no response).
     std::uint32_t nc_mode;
     R nc_radius, nc_skin, nc_margin, nc_restitution, nc_threshold, nc_static, nc_dynamic;
+    R plate_half_thickness; // > 0: the bending strain of sheets one cell thick
 };
 
 template <class R> struct Sphere { V3<R> center, velocity, angular; R radius, mass, inertia; };
