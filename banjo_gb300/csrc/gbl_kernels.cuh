@@ -209,6 +209,24 @@ template <class R, bool Many> __device__ __forceinline__ Dev<R> descriptor(const
     return g.one;
 }
 
+// The descriptor as a reference a long kernel reads its fields through: for
+// many lattices, the CTA's lattice's descriptor copied once into shared
+// memory (its fields are then read from there as needed, not held in
+// registers across the kernel); for one lattice, the launch's own. Every
+// thread of the CTA must call it (it synchronises).
+template <class R> struct SharedDesc {
+    __align__(16) unsigned char bytes[sizeof(Dev<R>)];
+};
+template <class R, bool Many>
+__device__ __forceinline__ const Dev<R> &descriptorIn(const Grid<R> &g, const Work &w, SharedDesc<R> &smem) {
+    if (!Many) return g.one;
+    const unsigned *src = reinterpret_cast<const unsigned *>(g.table + w.lattice);
+    unsigned *dst = reinterpret_cast<unsigned *>(smem.bytes);
+    for (unsigned k = threadIdx.x; k < sizeof(Dev<R>) / sizeof(unsigned); k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+    return *reinterpret_cast<const Dev<R> *>(smem.bytes);
+}
+
 template <class R> __device__ __forceinline__ V3<R> pos(const Dev<R> &L, std::uint32_t i) {
     return xyz(L.x0[i]) + xyz(L.u[i]);
 }
@@ -414,7 +432,8 @@ template <class R> __device__ __forceinline__ std::uint32_t substepStamp(const D
 template <class R, bool Many, bool Direct, bool Plate>
 __global__ void __launch_bounds__(kThreads) kStrainAll(const Grid<R> launch, int part, R plate, R yield) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    __shared__ SharedDesc<R> desc;
+    const Dev<R> &L = descriptorIn<R, Many>(launch, w, desc);
     if (L.ctl->stop) return;
     const std::uint32_t i = w.begin + threadIdx.x;
     if (i >= w.end) return;
@@ -549,7 +568,8 @@ __device__ __forceinline__ bool sphereCandidate(const Settings<R> &S, const Sphe
 template <class R, bool Many>
 __global__ void __launch_bounds__(kThreads) kKick(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    __shared__ SharedDesc<R> desc;
+    const Dev<R> &L = descriptorIn<R, Many>(launch, w, desc);
     if (L.ctl->stop) return;
     const std::uint32_t i = w.begin + threadIdx.x; // items start on multiples of 256: warps cover whole bit words
     bool cand = false;
@@ -1330,7 +1350,8 @@ __global__ void __launch_bounds__(kThreads) kSupportIsolated(const Grid<R> launc
 template <class R, bool Many>
 __global__ void __launch_bounds__(kThreads) kVelocity(const Grid<R> launch, Settings<R> S, int respond) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    __shared__ SharedDesc<R> desc;
+    const Dev<R> &L = descriptorIn<R, Many>(launch, w, desc);
     if (L.ctl->stop) return;
     const std::uint32_t i = w.begin + threadIdx.x;
     if (i >= w.end) return;
@@ -1378,7 +1399,8 @@ __device__ __forceinline__ double warpSumFixed(double x) {
 template <class R, bool Many, bool Direct, bool Plastic>
 __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Settings<R> S, int part) {
     const Work w = item<Many>(launch);
-    const Dev<R> L = descriptor<R, Many>(launch, w);
+    __shared__ SharedDesc<R> desc;
+    const Dev<R> &L = descriptorIn<R, Many>(launch, w, desc);
     __shared__ double tile_work[kThreads / 32];
     __shared__ unsigned peak[4];
     if (L.ctl->stop) return;
