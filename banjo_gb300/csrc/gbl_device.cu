@@ -218,71 +218,27 @@ struct Frame {
     gbl_sphere sphere;
 };
 
-// The device arrays a download reads, copied raw (device layout, storage
-// order), and the permutation back to schedule order: a finished lattice's
-// device memory can be freed at once and the conversion to the state layout
-// done later, off the stepping thread.
-template <class R> struct RawState {
+// The arrays a download writes, in the state's own layout (doubles, bonds in
+// schedule order), in one device buffer: written by the device from a
+// lattice's arrays, then copied array by array into a caller's state. A
+// finished served request's result waits here for its caller, its lattice's
+// own memory already freed.
+struct StateOut {
+    char *base{};
+    std::size_t bytes{};
     std::uint32_t N{}, B{};
-    std::size_t capacity{}; // bytes held (nodes and bonds the buffers fit)
-    std::uint32_t cap_n{}, cap_b{};
-    std::unique_ptr<Q4<R>[]> u_buf, up_buf, v_buf, prev_buf;
-    std::unique_ptr<BondRec<R>[]> rec_buf;
-    std::unique_ptr<Q2<R>[]> plastic_buf;
-    std::unique_ptr<std::uint8_t[]> mode_buf;
-    Q4<R> *u{}, *up{}, *v{};
-    BondRec<R> *rec{};
-    Q4<R> *prev{};
-    Q2<R> *plastic{};
-    std::uint8_t *mode{};
+    double *u{}, *up{}, *v{};
+    BondsOut o{};
 
-    static std::size_t need(std::uint32_t n, std::uint32_t b) {
-        return 3 * static_cast<std::size_t>(n) * sizeof(Q4<R>) +
-               static_cast<std::size_t>(b) * (sizeof(BondRec<R>) + sizeof(Q4<R>) + sizeof(Q2<R>) + 1);
-    }
-    // Buffers for n nodes and b bonds (kept when large enough), one per
-    // array: separate allocations stay out of one huge mapping's page faults.
-    void shape(std::uint32_t n, std::uint32_t b) {
-        N = n;
-        B = b;
-        if (n > cap_n || !u_buf) {
-            u_buf.reset(new Q4<R>[n ? n : 1]);
-            up_buf.reset(new Q4<R>[n ? n : 1]);
-            v_buf.reset(new Q4<R>[n ? n : 1]);
-            cap_n = n;
-        }
-        if (b > cap_b || !rec_buf) {
-            rec_buf.reset(new BondRec<R>[b ? b : 1]);
-            prev_buf.reset(new Q4<R>[b ? b : 1]);
-            plastic_buf.reset(new Q2<R>[b ? b : 1]);
-            mode_buf.reset(new std::uint8_t[b ? b : 1]);
-            cap_b = b;
-        }
-        capacity = need(cap_n, cap_b);
-        u = u_buf.get(); up = up_buf.get(); v = v_buf.get();
-        rec = rec_buf.get(); prev = prev_buf.get(); plastic = plastic_buf.get(); mode = mode_buf.get();
-    }
-
-    // download's conversion (WorkingLattice::toState, LatticeWorking.hpp:126-142),
-    // in sequence: the bond arrays arrive in schedule order.
-    void writeState(gbl_state_view &st) const {
-        if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
-        parallelFor(N, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t i = lo; i < hi; ++i) {
-                st.u[3 * i] = u[i].x; st.u[3 * i + 1] = u[i].y; st.u[3 * i + 2] = u[i].z;
-                st.u_prev[3 * i] = up[i].x; st.u_prev[3 * i + 1] = up[i].y; st.u_prev[3 * i + 2] = up[i].z;
-                st.v[3 * i] = v[i].x; st.v[3 * i + 1] = v[i].y; st.v[3 * i + 2] = v[i].z;
-            }
-        });
-        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
-            for (std::size_t j = lo; j < hi; ++j) {
-                st.alive[j] = (rec[j].a & kDeadBit) ? 0 : 1;
-                st.failure_mode[j] = mode[j];
-                st.damage[j] = prev[j].w;
-                st.prev_tensile[j] = prev[j].x; st.prev_compressive[j] = prev[j].y; st.prev_shear[j] = prev[j].z;
-                st.plastic_extension[j] = plastic[j].x; st.plastic_strain[j] = plastic[j].y;
-            }
-        });
+    void copyTo(const gbl_state_view &st) const {
+        if (st.node_count != N || st.bond_count != B) invalid("result state does not match the lattice");
+        const std::size_t n3 = 3 * static_cast<std::size_t>(N) * sizeof(double), b = B;
+        copySegments({{st.u, u, n3}, {st.u_prev, up, n3}, {st.v, v, n3}, {st.alive, o.alive, b},
+                      {st.failure_mode, o.mode, b}, {st.damage, o.damage, 8 * b}, {st.prev_tensile, o.tensile, 8 * b},
+                      {st.prev_compressive, o.compressive, 8 * b}, {st.prev_shear, o.shear, 8 * b},
+                      {st.plastic_extension, o.plastic_extension, 8 * b},
+                      {st.plastic_strain, o.plastic_strain, 8 * b}},
+                     cudaMemcpyDeviceToHost);
     }
 };
 
@@ -953,77 +909,42 @@ template <class R> struct Resident {
 
     // The device arrays a download needs, raw, into `raw` (its buffers reused
     // when large enough).
-    // The arrays a download reads; the bond arrays are put back in schedule
-    // order on the device first.
-    void copyRaw(RawState<R> &raw, cudaStream_t stream) const {
-        raw.shape(N, B);
-        char *ordered = nullptr;
-        BondSet<R> o{};
-        if (B) {
-            const std::size_t b = B;
-            auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
-            const std::size_t rec = round(b * sizeof(BondRec<R>)), prev = round(b * sizeof(Q4<R>)),
-                              plastic = round(b * sizeof(Q2<R>));
-            check(cudaMallocAsync(&ordered, rec + prev + plastic + b, stream), "device allocation");
-            o.rec = reinterpret_cast<BondRec<R> *>(ordered);
-            o.prev = reinterpret_cast<Q4<R> *>(ordered + rec);
-            o.plastic = reinterpret_cast<Q2<R> *>(ordered + rec + prev);
-            o.mode = reinterpret_cast<std::uint8_t *>(ordered + rec + prev + plastic);
-            kBondsToSchedule<R><<<reorderGrid(b), kThreads, 0, stream>>>(o, bonds(), dev.dev2sched, B);
-            check(cudaGetLastError(), "kernel launch");
-        }
-        check(cudaStreamSynchronize(stream), "download");
-        copyParallel(raw.u, dev.u, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
-        copyParallel(raw.up, dev.up, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
-        copyParallel(raw.v, dev.v, sizeof(Q4<R>) * N, cudaMemcpyDeviceToHost);
-        if (B) {
-            copyParallel(raw.rec, o.rec, sizeof(BondRec<R>) * B, cudaMemcpyDeviceToHost);
-            copyParallel(raw.prev, o.prev, sizeof(Q4<R>) * B, cudaMemcpyDeviceToHost);
-            copyParallel(raw.plastic, o.plastic, sizeof(Q2<R>) * B, cudaMemcpyDeviceToHost);
-            copyParallel(raw.mode, o.mode, B, cudaMemcpyDeviceToHost);
-            check(cudaFreeAsync(ordered, stream), "device free");
-        }
-    }
-
-    // download (WorkingLattice::toState, LatticeWorking.hpp:126-142); the host
-    // buffers are kept for the lattice's next download.
-    void download(gbl_state_view &st, gbl_sphere *sphere, cudaStream_t stream) {
-        if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
-        // The device writes the state's own layout (doubles, schedule order)
-        // into one scratch buffer; each array is then copied straight into
-        // the caller's, which the caller has already touched.
+    // The state's layout of this lattice's arrays, written by the device into
+    // a new buffer on `stream` (the caller synchronises and frees it).
+    StateOut stateOut(cudaStream_t stream) const {
+        StateOut out;
+        out.N = N;
+        out.B = B;
         const std::size_t n3 = 3 * static_cast<std::size_t>(N) * sizeof(double), b = B;
         auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
         const std::size_t parts[11] = {round(n3), round(n3), round(n3), round(b), round(b), round(8 * b), round(8 * b),
                                        round(8 * b), round(8 * b), round(8 * b), round(8 * b)};
-        std::size_t total = 0;
-        for (std::size_t q : parts) total += q;
-        char *out = nullptr;
-        check(cudaMallocAsync(&out, total ? total : 256, stream), "device allocation");
+        for (std::size_t q : parts) out.bytes += q;
+        check(cudaMallocAsync(&out.base, out.bytes ? out.bytes : 256, stream), "device allocation");
         char *at[11];
-        for (std::size_t q = 0, off = 0; q < 11; off += parts[q], ++q) at[q] = out + off;
-        double *u = reinterpret_cast<double *>(at[0]), *up = reinterpret_cast<double *>(at[1]),
-               *v = reinterpret_cast<double *>(at[2]);
-        const BondsOut o{reinterpret_cast<std::uint8_t *>(at[3]), reinterpret_cast<std::uint8_t *>(at[4]),
+        for (std::size_t q = 0, off = 0; q < 11; off += parts[q], ++q) at[q] = out.base + off;
+        out.u = reinterpret_cast<double *>(at[0]);
+        out.up = reinterpret_cast<double *>(at[1]);
+        out.v = reinterpret_cast<double *>(at[2]);
+        out.o = BondsOut{reinterpret_cast<std::uint8_t *>(at[3]), reinterpret_cast<std::uint8_t *>(at[4]),
                          reinterpret_cast<double *>(at[5]), reinterpret_cast<double *>(at[6]),
                          reinterpret_cast<double *>(at[7]), reinterpret_cast<double *>(at[8]),
                          reinterpret_cast<double *>(at[9]), reinterpret_cast<double *>(at[10])};
-        if (N) kNodesOut<R><<<reorderGrid(N), kThreads, 0, stream>>>(u, up, v, dev.u, dev.up, dev.v, N);
-        if (B) kBondsOut<R><<<reorderGrid(B), kThreads, 0, stream>>>(o, bonds(), dev.dev2sched, B);
+        if (N) kNodesOut<R><<<reorderGrid(N), kThreads, 0, stream>>>(out.u, out.up, out.v, dev.u, dev.up, dev.v, N);
+        if (B) kBondsOut<R><<<reorderGrid(B), kThreads, 0, stream>>>(out.o, bonds(), dev.dev2sched, B);
         check(cudaGetLastError(), "kernel launch");
+        return out;
+    }
+
+    // download (WorkingLattice::toState, LatticeWorking.hpp:126-142): the
+    // device writes the state's layout, copied straight into the caller's
+    // arrays (which the caller has already touched).
+    void download(gbl_state_view &st, gbl_sphere *sphere, cudaStream_t stream) {
+        if (st.node_count != N || st.bond_count != B) invalid("download state does not match the lattice");
+        const StateOut out = stateOut(stream);
         check(cudaStreamSynchronize(stream), "download");
-        copyParallel(st.u, u, n3, cudaMemcpyDeviceToHost);
-        copyParallel(st.u_prev, up, n3, cudaMemcpyDeviceToHost);
-        copyParallel(st.v, v, n3, cudaMemcpyDeviceToHost);
-        copyParallel(st.alive, o.alive, b, cudaMemcpyDeviceToHost);
-        copyParallel(st.failure_mode, o.mode, b, cudaMemcpyDeviceToHost);
-        copyParallel(st.damage, o.damage, 8 * b, cudaMemcpyDeviceToHost);
-        copyParallel(st.prev_tensile, o.tensile, 8 * b, cudaMemcpyDeviceToHost);
-        copyParallel(st.prev_compressive, o.compressive, 8 * b, cudaMemcpyDeviceToHost);
-        copyParallel(st.prev_shear, o.shear, 8 * b, cudaMemcpyDeviceToHost);
-        copyParallel(st.plastic_extension, o.plastic_extension, 8 * b, cudaMemcpyDeviceToHost);
-        copyParallel(st.plastic_strain, o.plastic_strain, 8 * b, cudaMemcpyDeviceToHost);
-        check(cudaFreeAsync(out, stream), "device free");
+        out.copyTo(st);
+        check(cudaFreeAsync(out.base, stream), "device free");
         check(cudaStreamSynchronize(stream), "download");
         if (sphere) *sphere = fetchSphere();
     }
@@ -2247,6 +2168,12 @@ public:
         : budget_(budget), contact_(settings.node_contact.mode != 0), t0_(clock()) {
         engine_.configure(settings);
     }
+    ~Server() override {
+        for (auto &kv : requests_)
+            if (kv.second.phase == GBL_REQUEST_DONE && kv.second.out.base)
+                cudaFreeAsync(kv.second.out.base, engine_.stream());
+        cudaStreamSynchronize(engine_.stream());
+    }
 
     std::uint64_t submit(const gbl_schedule_view &sv, const gbl_state_view &st, const gbl_sphere &sp,
                          std::uint64_t substeps, bool borrowed) override {
@@ -2313,7 +2240,7 @@ public:
     }
 
     void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) override {
-        RawState<R> raw;
+        StateOut out;
         {
             std::lock_guard<std::mutex> lock(mutex_);
             Request &q = find(ticket);
@@ -2322,15 +2249,18 @@ public:
                 invalid("result state does not match the request's lattice");
             if (sp) *sp = q.sphere;
             if (status) *status = q.status;
-            raw = std::move(q.raw);
+            out = q.out;
             requests_.erase(ticket);
             --done_;
         }
-        // The conversion to the state layout runs on the caller's thread,
-        // outside the lock; the buffer then goes back to the pool.
-        if (st) raw.writeState(*st);
+        // The copies into the caller's arrays run on the caller's thread,
+        // outside the lock (they use their own streams); the result's device
+        // memory is then freed, stream-ordered, under the lock (a step may be
+        // capturing on the engine's stream).
+        if (st) out.copyTo(*st);
         std::lock_guard<std::mutex> lock(mutex_);
-        if (pool_.size() < kPoolSize) pool_.push_back(std::move(raw));
+        check(cudaFreeAsync(out.base, engine_.stream()), "device free");
+        used_ -= out.bytes;
     }
 
     void cancel(std::uint64_t ticket) override {
@@ -2343,10 +2273,11 @@ public:
             engine_.retire(q.slot);
             used_ -= q.bytes;
             --running_;
-        } else {
-            if (q.phase == GBL_REQUEST_DONE) --done_;
+        } else if (q.phase == GBL_REQUEST_DONE) {
+            --done_;
+            check(cudaFreeAsync(q.out.base, engine_.stream()), "device free");
+            used_ -= q.out.bytes;
         }
-        if (q.phase == GBL_REQUEST_DONE && pool_.size() < kPoolSize) pool_.push_back(std::move(q.raw));
         requests_.erase(ticket);
     }
 
@@ -2380,7 +2311,7 @@ private:
         std::size_t slot{};
         double submitted{-1}, admitted{-1}, finished{-1};
         gbl_run_status status{};
-        RawState<R> raw;
+        StateOut out; // a finished request's result, on the device until taken
     };
 
     static double clock() {
@@ -2434,25 +2365,17 @@ private:
             if (!(c.step_limit != 0 && c.total_steps >= c.step_limit) && c.exit_reason == 0) continue;
             Request &q = requests_.at(slot_ticket_[k]);
             Resident<R> &l = engine_.lattice(k);
-            // The raw device arrays only: the conversion waits for take().
-            if (!pool_.empty()) {
-                std::size_t best = pool_.size();
-                for (std::size_t p = 0; p < pool_.size(); ++p)
-                    if (pool_[p].capacity >= RawState<R>::need(l.N, l.B) &&
-                        (best == pool_.size() || pool_[p].capacity < pool_[best].capacity))
-                        best = p;
-                if (best < pool_.size()) {
-                    q.raw = std::move(pool_[best]);
-                    pool_.erase(pool_.begin() + static_cast<std::ptrdiff_t>(best));
-                }
-            }
-            l.copyRaw(q.raw, engine_.stream());
+            // The result, in the state's layout, stays on the device until
+            // take() copies it out; the lattice's own memory is freed now.
+            q.out = l.stateOut(engine_.stream());
+            check(cudaStreamSynchronize(engine_.stream()), "retire");
             q.sphere = l.fetchSphere();
             q.status = l.status;
             q.status.exit_reason = c.exit_reason;
             q.done_steps = c.total_steps;
-            engine_.retire(k);
+            engine_.retire(k); // synchronises the stream: the result is written
             used_ -= q.bytes;
+            used_ += q.out.bytes;
             q.phase = GBL_REQUEST_DONE;
             q.finished = clock() - t0_;
             --running_;
@@ -2469,9 +2392,6 @@ private:
     std::map<std::uint64_t, Request> requests_;
     std::deque<std::uint64_t> queue_;
     std::vector<std::uint64_t> slot_ticket_;
-    // Host buffers of taken results, reused by the next retirements.
-    std::vector<RawState<R>> pool_;
-    static constexpr std::size_t kPoolSize = 16;
     std::mutex mutex_;
 };
 

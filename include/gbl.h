@@ -354,7 +354,7 @@ gbl_result gbl_batch_set_stream(gbl_batch *batch, void *cuda_stream);
  * gbl_serve_submit prepares the request's device image from the views on the
  * calling thread, outside the server's lock (so submissions from other threads
  * overlap a running gbl_serve_step); the views may be freed when it returns.
- * The result is kept by the server until gbl_serve_take. Times are seconds on
+ * The result is kept on the device until gbl_serve_take. Times are seconds on
  * the server's steady clock since its creation, -1 before the event. */
 typedef struct gbl_server gbl_server;
 enum { GBL_REQUEST_QUEUED = 0, GBL_REQUEST_RUNNING = 1, GBL_REQUEST_DONE = 2 };
@@ -378,7 +378,7 @@ typedef struct gbl_server_stats {
     double device_seconds;  /* device time of the steps */
     double clock_s;
     double admit_seconds;   /* host time admitting (device upload of prepared requests) */
-    double retire_seconds;  /* host time retiring (download of finished requests) */
+    double retire_seconds;  /* host time retiring (finished requests' results written on the device) */
     double run_seconds;     /* host time of the stepping itself (graph rebuilds and launches included) */
 } gbl_server_stats;
 gbl_result gbl_serve_create(int precision, const gbl_step_settings *settings, uint64_t budget_bytes, gbl_server **out);
@@ -399,9 +399,11 @@ gbl_result gbl_serve_submit_borrowed(gbl_server *server, const gbl_schedule_view
 gbl_result gbl_serve_step(gbl_server *server, uint64_t substeps, gbl_server_stats *stats);
 gbl_result gbl_serve_poll(gbl_server *server, uint64_t ticket, gbl_request_info *info);
 /* The finished request's state (arrays gbl_download writes), sphere and
- * RunStatus; the request is then forgotten. A finished request's device
- * arrays were copied to host memory as it left the device; the conversion to
- * the state layout runs here, on the calling thread (state may be null). */
+ * RunStatus; the request is then forgotten. As a request finishes, the device
+ * writes its result in the state's layout into a buffer of its own (charged
+ * against the budget, about 72 bytes per node and 50 per bond, in place of
+ * the lattice's footprint); the copies into `state` run here, on the calling
+ * thread, and free it (state may be null). */
 gbl_result gbl_serve_take(gbl_server *server, uint64_t ticket, gbl_state_view *state, gbl_sphere *sphere,
                           gbl_run_status *status);
 gbl_result gbl_serve_cancel(gbl_server *server, uint64_t ticket);
