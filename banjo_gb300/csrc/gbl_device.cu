@@ -860,11 +860,6 @@ template <class R> struct Resident {
         cudaEventDestroy(used[1]);
     }
 
-    void upload(const gbl_state_view &st, const gbl_sphere &sphere, cudaStream_t stream) {
-        prepare(st, sphere, false);
-        commit(stream);
-    }
-
     // setExternalForces (ExternalLoads.hpp:28-50): validated in full before
     // anything changes, so an invalid replacement leaves the old load intact.
     void setExternalForces(const double *forces, std::uint64_t count, std::uint64_t substeps, cudaStream_t stream) {

@@ -2289,19 +2289,6 @@ __global__ void __launch_bounds__(kThreads) kSlotsToStorage(std::uint32_t *nbr_b
     }
 }
 
-// Download: the arrays the state takes back, in schedule order.
-template <class R>
-__global__ void __launch_bounds__(kThreads) kBondsToSchedule(BondSet<R> dst, BondSet<R> src,
-                                                             const std::uint32_t *dev2sched, std::uint32_t B) {
-    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) {
-        const std::uint32_t j = dev2sched[dd];
-        dst.rec[j] = src.rec[dd];
-        dst.prev[j] = src.prev[dd];
-        dst.plastic[j] = src.plastic[dd];
-        dst.mode[j] = src.mode[dd];
-    }
-}
-
 // Download straight into the state's layout: doubles (exact widenings), bonds
 // in schedule order, so the host copies each array as it is.
 template <class R>
