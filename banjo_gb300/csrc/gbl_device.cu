@@ -169,13 +169,6 @@ bool pageableAccess() {
     return yes;
 }
 
-// Device array to host, into uninitialised storage (no zero fill).
-template <class T> std::unique_ptr<T[]> fetch(const T *src, std::size_t n) {
-    std::unique_ptr<T[]> out(new T[n ? n : 1]);
-    copyParallel(out.get(), src, sizeof(T) * n, cudaMemcpyDeviceToHost);
-    return out;
-}
-
 // An allocator that leaves trivial elements uninitialised when a vector is
 // sized: the per-bond scratch of an upload (hundreds of MB for a large
 // lattice) is written in full, or filled in parallel, before it is read, and
@@ -955,24 +948,28 @@ template <class R> struct Resident {
         return o;
     }
 
-    void captureFrame(std::uint64_t step) {
+    void captureFrame(std::uint64_t step, cudaStream_t stream) {
         Frame f;
         f.step = step;
-        const auto u = fetch(dev.u, N);
         f.u.resize(3 * static_cast<std::size_t>(N));
-        for (std::uint32_t i = 0; i < N; ++i) {
-            f.u[3 * i] = static_cast<float>(u[i].x); f.u[3 * i + 1] = static_cast<float>(u[i].y);
-            f.u[3 * i + 2] = static_cast<float>(u[i].z);
-        }
-        const auto rec = fetch(dev.rec, B);
-        const auto prev = fetch(dev.prev, B);
         f.alive.resize(B);
         f.damage.resize(B);
-        for (std::uint32_t dd = 0; dd < B; ++dd) {
-            const std::uint32_t j = dev2sched[dd];
-            f.alive[j] = (rec[dd].a & kDeadBit) ? 0 : 1;
-            f.damage[j] = static_cast<float>(prev[dd].w);
-        }
+        // Written on the device in the frame's layout, then copied straight in.
+        auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
+        const std::size_t nu = 3 * static_cast<std::size_t>(N) * sizeof(float), b = B;
+        char *buf = nullptr;
+        check(cudaMallocAsync(&buf, round(nu) + round(b) + round(4 * b) + 256, stream), "device allocation");
+        float *u = reinterpret_cast<float *>(buf);
+        std::uint8_t *alive = reinterpret_cast<std::uint8_t *>(buf + round(nu));
+        float *damage = reinterpret_cast<float *>(buf + round(nu) + round(b));
+        if (N || B)
+            kFrameOut<R><<<reorderGrid(std::max<std::size_t>(N, B)), kThreads, 0, stream>>>(u, alive, damage, dev.u,
+                                                                                         bonds(), dev.dev2sched, N, B);
+        check(cudaGetLastError(), "kernel launch");
+        check(cudaStreamSynchronize(stream), "frame");
+        copySegments({{f.u.data(), u, nu}, {f.alive.data(), alive, b}, {f.damage.data(), damage, 4 * b}},
+                     cudaMemcpyDeviceToHost);
+        check(cudaFreeAsync(buf, stream), "device free");
         f.sphere = fetchSphere();
         frames.push_back(std::move(f));
         ++status.frames_captured;
@@ -1260,7 +1257,7 @@ public:
                             if (allStopped()) { halted = true; break; }
                             synced = true;
                         }
-                        l.captureFrame(step);
+                        l.captureFrame(step, stream_);
                     }
                     if (halted) break;
                 }

@@ -2396,4 +2396,23 @@ __global__ void __launch_bounds__(kThreads) kBondsIn(BondSet<R> out, BondsIn in,
     if (__any_sync(0xffffffffU, flowed) && (threadIdx.x & 31) == 0) atomicOr(plastic, 1U);
 }
 
+// A frame (captureFrame, LatticeWorking.hpp:290-303): positions as float,
+// aliveness and damage (as float) by schedule index.
+template <class R>
+__global__ void __launch_bounds__(kThreads) kFrameOut(float *u, std::uint8_t *alive, float *damage, const Q4<R> *du,
+                                                      BondSet<R> src, const std::uint32_t *dev2sched, std::uint32_t N,
+                                                      std::uint32_t B) {
+    for (std::size_t i = gridFirst(); i < N; i += gridStride()) {
+        const Q4<R> a = du[i];
+        u[3 * i] = static_cast<float>(a.x);
+        u[3 * i + 1] = static_cast<float>(a.y);
+        u[3 * i + 2] = static_cast<float>(a.z);
+    }
+    for (std::size_t dd = gridFirst(); dd < B; dd += gridStride()) {
+        const std::uint32_t j = dev2sched[dd];
+        alive[j] = (src.rec[dd].a & kDeadBit) ? 0 : 1;
+        damage[j] = static_cast<float>(src.prev[dd].w);
+    }
+}
+
 } // namespace gbl
