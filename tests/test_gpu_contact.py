@@ -79,3 +79,49 @@ def test_contact_lattices_in_one_batch(device):
         assert mismatches(alone, out, STATE_KEYS) == []
         assert status_mismatches(alone, out) == []
     assert sum(int(o["status_u64"][NODE_CONTACTS]) > 0 for o in together) >= 3
+
+
+def test_contact_requests_served_equal_alone(device):
+    """Node contact in the served form: the pair-list scratch is charged at
+    admission, each result equals its lattice run alone."""
+    cases = [_drop(nx=nx, ny=ny, nz=nz, speed=sp, steps=20) for nx, ny, nz, sp in
+             ((10, 6, 8, 4.0), (14, 7, 9, 6.0), (8, 5, 6, 3.0))]
+    shared = cases[0]["settings"]
+    for c in cases:
+        c["settings"] = shared
+    server = device.Server(device.step_settings(shared), 1 << 33)
+    held, tickets = [], []
+    for c in cases:
+        n = int(c["node_count"][0])
+        sched = device.build_lattice_schedule(n, c["bond_a"], c["bond_b"], c["node_block_begin"])
+        state = device.build_lattice_state(c, sched)
+        held.append(state)
+        tickets.append(server.submit(sched, state, device.sphere_state(c["sphere"]), int(c["steps"][0]),
+                                     borrow=True))
+    while any(server.poll(t).phase != device.REQUEST_DONE for t in tickets):
+        server.step(7)
+    for c, t, state in zip(cases, tickets, held):
+        _, status = server.take(t, state)
+        alone = device.run_case(c)
+        assert np.array_equal(state.u, alone["u"]) and np.array_equal(state.alive, alone["alive"])
+        assert status.node_contact.contacts == int(alone["status_u64"][NODE_CONTACTS])
+    assert server.stats().bytes_in_use == 0
+
+
+def test_plate_and_contact_batch_equal_alone(device):
+    """Plate bending, node contact and the ledge supports together, in one
+    batch of struck sheets of uneven size: each equals itself alone."""
+    from banjo_gb300 import scenes
+
+    cases = [scenes.plate_strike(nx=nx, nz=nz, steps=25, speed=sp) for nx, nz, sp in
+             ((16, 16, 8.0), (24, 12, 10.0), (12, 20, 6.0))]
+    s = cases[0]["settings"].copy()
+    s[scenes.K_NODE_CONTACT:scenes.K_NODE_CONTACT + 9] = scenes.node_contact(2, 0.005, 0.0025, node_count=600)
+    for c in cases:
+        c["settings"] = s
+    together = device.run_batch(cases)
+    for case, out in zip(cases, together):
+        alone = device.run_case(case)
+        assert mismatches(alone, out, STATE_KEYS) == []
+        assert status_mismatches(alone, out) == []
+    assert all(int(o["status_u64"][4]) > 0 for o in together)
