@@ -67,6 +67,17 @@ def cases() -> dict:
     # centre, breaking by the fibre strain of its bending; float and double.
     out["plate_strike"] = (scenes.plate_strike(), "float")
     out["plate_strike_double"] = (scenes.plate_strike(nx=16, nz=16, steps=25), "double")
+    # Caps: a slab with more sphere candidates than a slab's list holds
+    # (1024), and node contact with more pairs per owner than its slots (24).
+    out["candidate_overflow"] = (scenes.impact_block(nx=40, ny=4, nz=40, blocks=1, radius=0.4, speed=6.0, steps=1,
+                                                     substeps=6, seed_point=3, seed_strength=4, gap=0.0005), "float")
+    dense = scenes.contact_drop(nx=8, ny=5, nz=6, speed=2.0, steps=6)
+    settings = dense["settings"].copy()
+    settings[scenes.K_NODE_CONTACT:scenes.K_NODE_CONTACT + 9] = scenes.node_contact(
+        2, 0.012, 0.01, node_count=int(dense["node_count"][0]))
+    dense["settings"] = settings
+    dense["alive"] = np.zeros(int(dense["bond_count"][0]), dtype=np.uint8)
+    out["contact_pair_overflow"] = (dense, "float")
     return out
 
 
