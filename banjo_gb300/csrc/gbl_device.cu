@@ -279,6 +279,9 @@ template <class R> struct Resident {
     gbl_state_view view_{};
     std::vector<std::uint32_t> level_begin_;
     unsigned flowed_host_{};
+    unsigned *flowed_dev_{};         // the in-place conversion's flag, until commitFinish reads it
+    cudaEvent_t committed_{};        // commitBegin's work, until commitFinish waits for it
+    cudaStream_t commit_stream_{};
 
     // The table size rule of latticeContactBucketMask (LatticePhysics.hpp:239-243),
     // applied to this lattice's own node count.
@@ -326,6 +329,11 @@ template <class R> struct Resident {
     }
 
     ~Resident() {
+        if (committed_) {
+            cudaEventSynchronize(committed_);
+            cudaEventDestroy(committed_);
+        }
+        if (flowed_dev_) cudaFree(flowed_dev_);
         if (nc_mem) cudaFree(nc_mem);
         if (ext_force) cudaFree(ext_force);
         if (ext_req) cudaFree(ext_req);
@@ -673,7 +681,16 @@ template <class R> struct Resident {
     // upload, device half: one allocation, the prepared image copied in, the
     // rest cleared. The host image is released.
     void commit(cudaStream_t stream) {
+        commitBegin(stream);
+        commitFinish();
+    }
+
+    // commit's first half: the allocation, the copies and the conversion and
+    // reordering kernels, enqueued on `stream`; the host waits only for the
+    // allocation (and, on the staged and image paths, for its own copies).
+    void commitBegin(cudaStream_t stream) {
         if (!image_ && !view_.u && N) logic("lattice committed before it was prepared");
+        commit_stream_ = stream;
         arena.allocate(stream);
         char *base = static_cast<char *>(arena.base());
         // The per-bond arrays, [slot_a, dev2sched) of the allocation, arrive in
@@ -682,7 +699,9 @@ template <class R> struct Resident {
         const std::size_t hi = static_cast<std::size_t>(reinterpret_cast<char *>(dev.dev2sched) - base);
         char *staged = nullptr;
         if (B) check(cudaMallocAsync(&staged, hi - lo, stream), "device allocation");
-        check(cudaStreamSynchronize(stream), "device allocation");
+        // Host-side copies on other streams need the allocation made; the
+        // in-place path keeps all its work on `stream`.
+        if (image_ || !pageableAccess()) check(cudaStreamSynchronize(stream), "device allocation");
         if (image_) {
             const unsigned char *img = image_.get();
             copySegments({{base, img, lo}, {staged, img + lo, B ? hi - lo : 0}, {base + hi, img + hi, filled_ - hi}},
@@ -703,8 +722,24 @@ template <class R> struct Resident {
         if (arena.bytes() > filled_)
             check(cudaMemsetAsync(base + filled_, 0, arena.bytes() - filled_, stream), "memset");
         dev.ext_force = ext_force; dev.ext_req = ext_req; dev.ext_contrib = ext_contrib; dev.ext_nodes = ext_nodes;
-        check(cudaStreamSynchronize(stream), "upload");
-        if (!image_) plastic_state = flowed_host_ != 0;
+        check(cudaEventCreateWithFlags(&committed_, cudaEventDisableTiming), "event");
+        check(cudaEventRecord(committed_, stream), "event");
+    }
+
+    // commit's second half: waits for the work commitBegin enqueued, then
+    // reads whether any bond has flowed; the caller's state is not read again.
+    void commitFinish() {
+        if (committed_) {
+            check(cudaEventSynchronize(committed_), "upload");
+            cudaEventDestroy(committed_);
+            committed_ = nullptr;
+        }
+        if (flowed_dev_) {
+            check(cudaMemcpy(&flowed_host_, flowed_dev_, sizeof(unsigned), cudaMemcpyDeviceToHost), "copy");
+            check(cudaFreeAsync(flowed_dev_, commit_stream_), "device free");
+            flowed_dev_ = nullptr;
+            plastic_state = flowed_host_ != 0;
+        }
         image_.reset();
         view_ = gbl_state_view{};
     }
@@ -731,19 +766,24 @@ template <class R> struct Resident {
                              st.threshold, st.plastic_extension, st.plastic_strain};
             kBondsIn<R><<<reorderGrid(B), kThreads, 0, stream>>>(bondsAt(staged), in, 0, B, flowed);
         }
+        // The small arrays, read in place too (this lattice keeps them until
+        // commitFinish), and every node dirty: the first substep restarts in full.
+        auto words = [&](void *dst, const void *src, std::size_t bytes) {
+            if (!bytes) return;
+            const std::size_t n = bytes / sizeof(std::uint32_t);
+            kCopyWords<<<reorderGrid(n), kThreads, 0, stream>>>(static_cast<std::uint32_t *>(dst),
+                                                              static_cast<const std::uint32_t *>(src), n);
+        };
+        static_assert(sizeof(Sphere<R>) % sizeof(std::uint32_t) == 0, "sphere record copied as words");
+        words(dev.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B);
+        words(dev.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size());
+        words(dev.node_block_begin, sched.node_block_begin.data(), sizeof(std::uint32_t) * (sched.block_count + 1));
+        words(dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size());
+        words(dev.sphere, &sphere0, sizeof(sphere0));
         check(cudaGetLastError(), "kernel launch");
-        copySegments({{dev.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B},
-                      {dev.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size()},
-                      {dev.node_block_begin, sched.node_block_begin.data(),
-                       sizeof(std::uint32_t) * (sched.block_count + 1)},
-                      {dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size()},
-                      {dev.sphere, &sphere0, sizeof(sphere0)}},
-                     cudaMemcpyHostToDevice);
         check(cudaMemsetAsync(dev.dirty, 1, N, stream), "memset");
         check(cudaMemsetAsync(dev.dirty + N, 0, 4, stream), "memset");
-        check(cudaMemcpyAsync(&flowed_host_, flowed, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
-        check(cudaFreeAsync(flowed, stream), "device free");
-        check(cudaStreamSynchronize(stream), "upload");
+        flowed_dev_ = flowed; // read by commitFinish
     }
 
     // The direct upload: the caller's arrays, chunk by chunk, copied as they
@@ -849,6 +889,7 @@ template <class R> struct Resident {
         check(cudaMemcpyAsync(&flowed_host_, flowed, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
         check(cudaFreeAsync(stage, stream), "device free");
         check(cudaStreamSynchronize(stream), "upload");
+        plastic_state = flowed_host_ != 0;
         cudaEventDestroy(used[0]);
         cudaEventDestroy(used[1]);
     }
@@ -2324,12 +2365,11 @@ private:
     }
 
     // Arrival order, while the next request fits what is left of the budget.
+    // (Converting admitted requests on a second stream beside the running
+    // ones was measured slower: the conversion's reads of host memory slowed
+    // the running kernels by more than they overlapped.)
     void admit() {
         const double t0 = clock();
-        admitQueued();
-        admit_seconds_ += clock() - t0;
-    }
-    void admitQueued() {
         while (!queue_.empty()) {
             Request &q = requests_.at(queue_.front());
             if (used_ + q.bytes > budget_) break;
@@ -2343,6 +2383,7 @@ private:
             --queued_;
             ++running_;
         }
+        admit_seconds_ += clock() - t0;
     }
 
     void retireFinished() {

@@ -2415,4 +2415,10 @@ __global__ void __launch_bounds__(kThreads) kFrameOut(float *u, std::uint8_t *al
     }
 }
 
+// Words copied by the device from any memory it can read (host memory in
+// place, where the device has coherent pageable access).
+__global__ void __launch_bounds__(kThreads) kCopyWords(std::uint32_t *dst, const std::uint32_t *src, std::size_t n) {
+    for (std::size_t k = gridFirst(); k < n; k += gridStride()) dst[k] = src[k];
+}
+
 } // namespace gbl
