@@ -188,6 +188,37 @@ def host_threads() -> int:
     return max(1, min(32, os.cpu_count() or 1))
 
 
+def trial_cpu_baseline(specs, substeps: int = 2) -> dict:
+    """The CPU checker with trial-level parallelism: one serial lane per host
+    thread, each running whole trials of the same draw one after another (the
+    stronger CPU arrangement for many small lattices). Each trial's first
+    (restart) substep is left out of the rate; the rate is every timed
+    projection over the timed seconds shared by the threads."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    from banjo_gb300 import scenes
+
+    threads = host_threads()
+
+    def one(spec):
+        nx, ny, nz, comp, strain, height = spec
+        case = scenes.drop_trial(nx, ny, nz, compliance=comp, break_strain=strain, drop_height=height, steps=1,
+                                 substeps=substeps + 1)
+        out = oracle.run_port(case, threads=1)
+        secs = float(np.sum(out["substep_seconds"][1:]))
+        live = int(case["bond_count"][0]) - int(out["status_u64"][4])
+        return ITERATIONS * live * substeps, secs
+
+    with ThreadPoolExecutor(threads) as ex:
+        results = list(ex.map(one, specs))
+    proj = sum(p for p, _ in results)
+    secs = sum(t for _, t in results)
+    return {"value": proj / (secs / threads), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{len(specs)} trials of the same draw, {substeps} substeps each after the restart, one "
+                      f"serial lane per thread on {threads} threads; {secs:.1f} thread-seconds timed"}
+
+
 def batched_leg(args, lattice) -> dict:
     """Config-3 trials in one batch against the same trials run one lattice at
     a time through the single-lattice backend ("plain")."""
@@ -240,7 +271,9 @@ def batched_leg(args, lattice) -> dict:
         plain_s += st1.kernel_seconds - st0.kernel_seconds
         plain_proj += ITERATIONS * (state.bond_count - st1.broken_bonds) * k
     plain = plain_proj / plain_s
+    cpu = None if args.no_cpu_baseline else trial_cpu_baseline(specs[:args.cpu_trials])
     return {"value": value, "unit": "projections/s", "trials": len(specs), "nodes": nodes, "bonds": bonds,
+            "cpu_baseline": cpu,
             "ms_per_step": device_s / args.steps * 1e3, "gpu_launches_per_substep": launches,
             "host_build_s": build_s, "host_threads": host_threads(),
             "plain": {"value": plain, "unit": "projections/s", "trials": plain_n,
@@ -613,6 +646,8 @@ def main() -> None:
     p.add_argument("--trials", type=int, default=4096, help="batched leg: trials in one batch (0: skip)")
     p.add_argument("--plain-trials", type=int, default=64, help="batched leg: trials timed one at a time")
     p.add_argument("--no-tune", action="store_true", help="batched leg: keep the default launch shapes")
+    p.add_argument("--cpu-trials", type=int, default=96,
+                   help="batched leg: trials in the trial-parallel CPU baseline sample")
     p.add_argument("--served-copy", action="store_true",
                    help="served leg: submit copied states (a host image per request) instead of borrowed ones")
     p.add_argument("--served-window", type=float, default=0.25, help="served leg: seconds of arrivals (0: skip)")
