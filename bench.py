@@ -580,6 +580,8 @@ def run_gb300(args) -> None:
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, os.cpu_count() or 1)
+        # The serial lane as well (one host thread), on one substep after the restart.
+        line["cpu_baseline_serial"] = cpu_baseline(case, 1, substeps=2)
     del backend, e2e_backend, state, e2e_state, case
     if args.trials > 0:
         line["batched"] = batched_leg(args, lattice)
