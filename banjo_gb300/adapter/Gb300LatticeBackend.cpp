@@ -209,6 +209,9 @@ void statusOf(const gbl_run_status &s, RunStatus &o) {
     o.node_contact.momentum_residual_x = s.node_contact.momentum_residual_x;
     o.node_contact.momentum_residual_y = s.node_contact.momentum_residual_y;
     o.node_contact.momentum_residual_z = s.node_contact.momentum_residual_z;
+    o.damping_dissipated_j = s.damping_dissipated_j;
+    o.striker_dissipated_j = s.striker_dissipated_j;
+    o.energy_audited = s.energy_audited != 0;
 }
 
 class Gb300LatticeBackend final : public LatticeBackend {

@@ -1064,6 +1064,8 @@ template <class R> struct Resident {
         std::memcpy(&f, &c.max_plastic, 4); status.max_plastic_stretch = f;
         status.rank_deficient_nodes = c.rank_deficient;
         status.plastic_work_j = c.plastic_work;
+        status.damping_dissipated_j = c.damping_dissipated;
+        status.striker_dissipated_j = c.striker_dissipated;
     }
 };
 
@@ -1517,12 +1519,13 @@ public:
     }
 
     static void validate(const gbl_step_settings &s) {
+        // The Verlet reference integrator is serial-double only: the reference's
+        // parallel lane refuses it the same way (ParallelCpuLatticeBackend.cpp:1380-1381).
         if (s.bond_integrator != 0) invalid("this lattice backend implements the XPBD integrator only");
         if (s.node_contact.mode != 0 &&
             !(2.0 * s.node_contact.radius + s.node_contact.skin > 0.0 &&
               std::isfinite(2.0 * s.node_contact.radius + s.node_contact.skin)))
             invalid("node-to-node contact needs a finite positive cutoff (2 radius + skin)");
-        if (s.audit_energy) invalid("this lattice backend does not implement the energy audit");
         if ((s.direct_arithmetic != 0) != kDirect)
             invalid(kDirect ? "the double backend runs the direct (absolute position) arithmetic"
                             : "the float backend runs the displacement arithmetic");
@@ -1556,6 +1559,7 @@ private:
         o.nc_threshold = R(s.node_contact.restitution_speed_threshold);
         o.nc_static = R(s.node_contact.static_friction); o.nc_dynamic = R(s.node_contact.dynamic_friction);
         o.plate_half_thickness = R(s.plate_half_thickness);
+        o.audit = s.audit_energy ? 1U : 0U;
         o.plane_count = s.plane_count;
         for (unsigned p = 0; p < kPlanes; ++p) {
             const gbl_support_plane &in = s.planes[p];
@@ -1627,6 +1631,7 @@ private:
         l.ext_dirty = false;
         l.status = gbl_run_status{};
         l.status.first_failure_step = l.status.last_failure_step = l.status.last_energy_gain_step = ~0ULL;
+        l.status.energy_audited = S_.audit ? 1 : 0; // CpuLatticeBackend.cpp:114
         l.first_failure.clear();
         l.frames.clear();
         check(cudaMemcpyAsync(ctl_ + k, &ctl_host_[k], sizeof(Ctl), cudaMemcpyHostToDevice, stream_), "copy");
@@ -1780,6 +1785,26 @@ private:
                 groups_.push_back(std::move(g));
             }
         }
+        // The radial damping sweep runs level by level over every lattice, the
+        // ones swept whole included: it has no whole-lattice form.
+        damp_.clear();
+        if (S_.damping_fraction > R(0)) {
+            std::size_t deepest = 0;
+            for (auto k : active_) deepest = std::max(deepest, slots_[k]->levels.size());
+            for (std::size_t d = 0; d < deepest; ++d) {
+                const U first = static_cast<U>(all.size());
+                U b0 = 0, e0 = 0;
+                bool lead = true;
+                for (auto k : active_) {
+                    const Res &l = *slots_[k];
+                    const U b = d < l.levels.size() ? l.levels[d].begin : 0;
+                    const U e = d < l.levels.size() ? l.levels[d].end : 0;
+                    if (lead) { b0 = b; e0 = e; lead = false; }
+                    ranges(k, b, e, kThreads * kSolvePer);
+                }
+                damp_.push_back(Span{first, static_cast<U>(all.size()) - first, b0, e0, kThreads * kSolvePer});
+            }
+        }
         if (all.size() > work_cap_) {
             if (work_) cudaFree(work_);
             work_cap_ = std::max<std::size_t>(all.size(), 2 * work_cap_);
@@ -1839,8 +1864,10 @@ private:
             check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
             restartPhase<M>(side_, 1);
             check(cudaEventRecord(join_, side_), "event");
+            if (S.audit) audit<M>(st, kAuditMark);
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 1,
                                                                                                sphere_buffers_);
+            if (S.audit) audit<M>(st, kAuditStriker);
             check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
         }
         mark(4);
@@ -1849,9 +1876,10 @@ private:
             kVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S, S.damping_fraction <= R(0) ? 1 : 0);
         mark(8);
         if (S.damping_fraction > R(0)) {
-            for (const Group &g : groups_)
-                for (const Span &lv : g.levels)
-                    if (lv.count) kDamp<R, M, kDirect><<<lv.count, kThreads, 0, st>>>(grid(lv), S.damping_fraction);
+            if (S.audit) audit<M>(st, kAuditMark);
+            for (const Span &lv : damp_)
+                if (lv.count) kDamp<R, M, kDirect><<<lv.count, kThreads, 0, st>>>(grid(lv), S.damping_fraction);
+            if (S.audit) audit<M>(st, kAuditDamping);
             if (nodes_.count) kSupportVelocity<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
             mark(9);
         }
@@ -1867,9 +1895,12 @@ private:
             endPhase<M>(side_, 1);
             check(cudaEventRecord(join_, side_), "event");
         }
-        if (S.sphere_enabled)
+        if (S.sphere_enabled) {
+            if (S.audit) audit<M>(st, kAuditMark);
             kSpherePass<R, M><<<each_.count, kSphereThreads, sphere_buffers_ * kSphereSlab, st>>>(grid(each_), S, 2,
                                                                                                sphere_buffers_);
+            if (S.audit) audit<M>(st, kAuditStriker);
+        }
         mark(10);
         if (split) check(cudaStreamWaitEvent(st, join_, 0), "stream wait");
         if (contact) contactPhase<M>(st, mark);
@@ -1883,6 +1914,12 @@ private:
         kLedger<R, M><<<each_.count, 32, 0, st>>>(grid(each_), S);
         mark(13);
         check(cudaGetLastError(), "kernel launch");
+    }
+
+    // The energy audit (CpuLatticeBackend.cpp:388-422): every lattice's
+    // kinetic energy folded in node order, before a phase or after it.
+    template <bool M> void audit(cudaStream_t st, int mode) {
+        kKineticFold<R, M><<<each_.count, kFoldThreads, 0, st>>>(grid(each_), mode);
     }
 
     // The projection sweep: the small lattices of a batch sweep whole, one
@@ -2052,6 +2089,7 @@ private:
         Span isolated{};
     };
     std::vector<Group> groups_;
+    std::vector<Span> damp_; // the damping sweep's levels, every lattice
     // Node bytes a group may hold: its node arrays stay in the 129 MB L2
     // beside the streamed bond records of a level.
     // Launch shapes of a batch's sweep (results do not depend on them): the

@@ -108,6 +108,9 @@ struct Ctl {
     // fill of the build in progress.
     NodeAcc node;
     unsigned nc_rebuild, nc_pairs, nc_members;
+    // The energy audit: the kinetic energy before the phase being measured,
+    // and what the damping sweep and the striker passes took out.
+    double ke_mark, damping_dissipated, striker_dissipated;
 };
 
 constexpr unsigned kErrExternalOverflow = 1;
@@ -1802,6 +1805,49 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(const Grid<R> launch) 
             if (!(atomicOr(word, bit) & bit)) L.dirty_list[atomicAdd(&c.dirty_count, 1U)] = node;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// The energy audit's measure (LatticePhysics.hpp:1676-1682): a lattice's
+// kinetic energy, each node's term formed in backend precision and widened,
+// folded serially in node order as the reference folds it, so the audit
+// ledgers match the reference's bit for bit. The CTA forms the next chunk of
+// terms in shared memory while thread 0 folds the current one; the fold is
+// one chain of dependent FP64 adds (N of them), so the kernel is bound by FP64
+// add latency. kAuditMark keeps the energy before a phase; the other modes
+// charge the drop across the phase to the striker or the damping ledger.
+// ---------------------------------------------------------------------------
+constexpr unsigned kFoldThreads = 1024;
+constexpr int kAuditMark = 0, kAuditStriker = 1, kAuditDamping = 2;
+
+template <class R, bool Many>
+__global__ void __launch_bounds__(kFoldThreads) kKineticFold(const Grid<R> launch, int mode) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    __shared__ double terms[2][kFoldThreads];
+    double total = 0.0;
+    unsigned buf = 0;
+    // Thread 0 reaches the barrier of chunk k+1 only after folding chunk k,
+    // so chunk k+2 never overwrites a buffer still being read.
+    for (std::uint32_t base = 0; base < L.N; base += kFoldThreads, buf ^= 1U) {
+        const std::uint32_t i = base + threadIdx.x;
+        if (i < L.N) {
+            const Q4<R> q = L.v[i]; // w: the node's mass
+            const V3<R> v = xyz(q);
+            terms[buf][threadIdx.x] = static_cast<double>(R(0.5) * q.w * dot(v, v));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const std::uint32_t n = L.N - base < kFoldThreads ? L.N - base : kFoldThreads;
+            for (std::uint32_t k = 0; k < n; ++k) total += terms[buf][k];
+        }
+    }
+    if (threadIdx.x != 0) return;
+    if (mode == kAuditMark) c.ke_mark = total;
+    else if (mode == kAuditStriker) c.striker_dissipated += c.ke_mark - total;
+    else c.damping_dissipated += c.ke_mark - total;
 }
 
 // ---------------------------------------------------------------------------

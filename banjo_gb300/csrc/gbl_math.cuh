@@ -86,6 +86,7 @@ template <class R> struct Settings {
     std::uint32_t nc_mode;
     R nc_radius, nc_skin, nc_margin, nc_restitution, nc_threshold, nc_static, nc_dynamic;
     R plate_half_thickness; // > 0: the bending strain of sheets one cell thick
+    std::uint32_t audit;    // StepSettings::audit_energy
 };
 
 template <class R> struct Sphere { V3<R> center, velocity, angular; R radius, mass, inertia; };

@@ -188,7 +188,9 @@ class RunStatus(C.Structure):
                 ("phase_seconds", C.c_double * 16), ("max_tensile_stretch", C.c_float),
                 ("max_compressive_strain", C.c_float), ("max_shear_strain", C.c_float),
                 ("rank_deficient_nodes", C.c_uint32), ("plastic_work_j", C.c_double),
-                ("max_plastic_stretch", C.c_float), ("node_contact", NodeContactAccumulators)]
+                ("max_plastic_stretch", C.c_float), ("node_contact", NodeContactAccumulators),
+                ("damping_dissipated_j", C.c_double), ("striker_dissipated_j", C.c_double),
+                ("energy_audited", C.c_uint8)]
 
 
 PHASE_NAMES = ["capture", "start_sample_nodes", "start_sample_bonds", "kick_classify", "contact_pass_1",
@@ -505,7 +507,7 @@ def step_settings(packed: np.ndarray) -> StepSettings:
     s.damping_fraction = packed[scenes.K_DAMP]
     s.sphere_enabled = int(packed[scenes.K_SPHERE])
     s.direct_arithmetic = int(packed[scenes.K_DIRECT])
-    s.audit_energy = 0
+    s.audit_energy = int(packed[scenes.K_AUDIT]) if len(packed) > scenes.K_AUDIT else 0
     s.plastic_yield_stretch = packed[scenes.K_YIELD]
     s.plastic_hardening = packed[scenes.K_HARDEN]
     s.plate_half_thickness = packed[scenes.K_PLATE]
@@ -812,12 +814,12 @@ def footprint(node_count: int, bond_count: int, max_degree: int, block_count: in
 def status_arrays(st: RunStatus) -> dict:
     """RunStatus packed as the case files pack it (oracle/case_layout.hpp)."""
     nc = st.node_contact
-    u = np.zeros(18, dtype=np.uint64)
+    u = np.zeros(19, dtype=np.uint64)
     u[:] = [st.total_steps, st.first_failure_step, st.last_failure_step, st.failure_rounds, st.broken_bonds,
             st.last_energy_gain_step, st.last_damage_gain_step, st.exit_reason, st.rank_deficient_nodes,
             st.contact.impulse_contacts, st.contact.candidate_overflow, st.contact.ball_support_events, st.launches,
-            nc.contacts, nc.pair_tests, nc.rebuilds, nc.pairs_listed, nc.pair_overflow]
-    d = np.zeros(26, dtype=np.float64)
+            nc.contacts, nc.pair_tests, nc.rebuilds, nc.pairs_listed, nc.pair_overflow, st.energy_audited]
+    d = np.zeros(28, dtype=np.float64)
     d[:] = [st.removed_energy_j, st.max_damage, st.plastic_work_j, st.max_tensile_stretch,
             st.max_compressive_strain, st.max_shear_strain, st.max_plastic_stretch,
             st.contact.impulse_to_material_x, st.contact.impulse_to_material_y, st.contact.impulse_to_material_z,
@@ -825,7 +827,8 @@ def status_arrays(st: RunStatus) -> dict:
             st.contact.maximum_position_correction_m, st.contact.maximum_center_shift_m, st.external_load.work_j,
             st.external_load.impulse_n_s[0], st.external_load.impulse_n_s[1], st.external_load.impulse_n_s[2],
             float(st.external_load.steps), st.wall_seconds, nc.dissipated_kinetic_energy_j, nc.maximum_overlap_m,
-            nc.maximum_position_correction_m, nc.momentum_residual_x, nc.momentum_residual_y, nc.momentum_residual_z]
+            nc.maximum_position_correction_m, nc.momentum_residual_x, nc.momentum_residual_y, nc.momentum_residual_z,
+            st.damping_dissipated_j, st.striker_dissipated_j]
     return {"status_u64": u, "status_f64": d}
 
 

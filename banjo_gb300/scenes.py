@@ -27,7 +27,8 @@ K_DT, K_GRAVITY, K_ITER, K_DAMP, K_SPHERE, K_DIRECT = 0, 1, 4, 5, 6, 7
 K_YIELD, K_HARDEN, K_PLATE, K_CONTACT, K_PLANE_COUNT, K_PLANES = 8, 9, 10, 11, 18, 19
 PLANE_WIDTH = 34
 K_NODE_CONTACT = 19 + 2 * PLANE_WIDTH  # 9 slots; a record that ends here has node contact off
-SETTINGS_WIDTH = K_NODE_CONTACT + 9
+K_AUDIT = K_NODE_CONTACT + 9  # StepSettings::audit_energy; a record that ends here has it off
+SETTINGS_WIDTH = K_AUDIT + 1
 SPHERE_WIDTH = 12
 
 GOLDEN = np.uint64(0x9E3779B97F4A7C15)
@@ -184,8 +185,9 @@ def node_contact(mode=2, radius=0.005, skin=0.0025, margin=1e-5, restitution=0.0
 
 def settings(dt=DT_SUBSTEP, gravity=(0.0, -9.81, 0.0), iterations=4, damping_fraction=0.0, sphere_enabled=0,
              direct=0, yield_stretch=0.0, hardening=0.0, contact=(0.5, 0.4, 0.0, 0.5, 0.005, 1e-5, 0.01),
-             planes=(), node_contact=None) -> np.ndarray:
+             planes=(), node_contact=None, audit_energy=False) -> np.ndarray:
     s = np.zeros(SETTINGS_WIDTH, dtype=np.float64)
+    s[K_AUDIT] = 1.0 if audit_energy else 0.0
     if node_contact is not None:
         s[K_NODE_CONTACT:K_NODE_CONTACT + 9] = node_contact
     s[K_DT] = dt

@@ -228,6 +228,14 @@ typedef struct gbl_run_status {
     double plastic_work_j;
     float max_plastic_stretch;
     gbl_node_contact_accumulators node_contact;
+    /* StepSettings::audit_energy only: the kinetic energy the damping sweep
+     * and the striker passes took out of the lattice, each a difference of
+     * the lattice's total kinetic energy across the phase, folded in node
+     * order (RunStatus::damping_dissipated_j, striker_dissipated_j,
+     * energy_audited; FastLattice.hpp:209-216). */
+    double damping_dissipated_j;
+    double striker_dissipated_j;
+    uint8_t energy_audited;
 } gbl_run_status;
 
 typedef struct gbl_backend gbl_backend;

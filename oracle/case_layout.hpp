@@ -25,7 +25,9 @@ enum SettingsSlot : int {
     // static friction, dynamic friction, bucket mask. A record that ends here
     // (kNodeContact wide) has node-to-node contact off.
     kNodeContact = 19 + 2 * 34,
-    kSettingsWidth = kNodeContact + 9,
+    // StepSettings::audit_energy. A record that ends before it has the audit off.
+    kAuditEnergy = kNodeContact + 9,
+    kSettingsWidth = kAuditEnergy + 1,
 };
 
 enum PlaneSlot : int {
@@ -66,6 +68,7 @@ enum StatusU64Slot : int {
     kNodeRebuilds,
     kNodePairsListed,
     kNodePairOverflow,
+    kEnergyAudited,          // RunStatus::energy_audited
     kStatusU64Width,
 };
 
@@ -96,6 +99,8 @@ enum StatusF64Slot : int {
     kNodeMomentumX,
     kNodeMomentumY,
     kNodeMomentumZ,
+    kDampingDissipated,      // the energy audit (StepSettings::audit_energy)
+    kStrikerDissipated,
     kStatusF64Width,
 };
 

@@ -269,6 +269,7 @@ template <class R> struct Settings {
     std::uint8_t nc_mode;
     R nc_radius, nc_skin, nc_margin, nc_restitution, nc_threshold, nc_static, nc_dynamic;
     std::uint32_t nc_mask;
+    std::uint8_t audit; // StepSettings::audit_energy
 };
 template <class R> struct Sphere { V<R> center, velocity, angular; R radius, mass, inertia; };
 
@@ -278,6 +279,7 @@ template <class R> V<R> v3of(const std::vector<double> &s, int at) {
 
 template <class R> Settings<R> unpackSettings(const std::vector<double> &s) {
     if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth) &&
+        s.size() != static_cast<std::size_t>(lsio::kAuditEnergy) &&
         s.size() != static_cast<std::size_t>(lsio::kNodeContact))
         throw std::invalid_argument("settings width");
     Settings<R> o{};
@@ -312,7 +314,8 @@ template <class R> Settings<R> unpackSettings(const std::vector<double> &s) {
         for (unsigned f = 0; f < kFootprints; ++f)
             for (int q = 0; q < 4; ++q) pl.fp[f][q] = static_cast<R>(s[b + lsio::kPlaneFootprints + 4 * static_cast<int>(f) + q]);
     }
-    if (s.size() == static_cast<std::size_t>(lsio::kSettingsWidth)) {
+    if (s.size() > static_cast<std::size_t>(lsio::kAuditEnergy)) o.audit = static_cast<std::uint8_t>(s[lsio::kAuditEnergy]);
+    if (s.size() > static_cast<std::size_t>(lsio::kNodeContact)) {
         const int n = lsio::kNodeContact;
         o.nc_mode = static_cast<std::uint8_t>(s[n]);
         o.nc_radius = static_cast<R>(s[n + 1]); o.nc_skin = static_cast<R>(s[n + 2]);
@@ -1214,6 +1217,8 @@ struct Status {
     double ext_work{}, ext_impulse[3]{};
     std::uint64_t ext_steps{};
     NodeAcc node{};
+    double damping_dissipated{}, striker_dissipated{};
+    bool energy_audited{};
 };
 
 // External forces (ExternalLoads.hpp:28-50 set, 79-148 kick; forces only).
@@ -1267,10 +1272,23 @@ template <class R> struct Loads {
     }
 };
 
+// The lattice's kinetic energy, folded serially in node order with each term
+// formed in backend precision and widened (LatticePhysics.hpp:1676-1682): the
+// energy audit's measure.
+template <class R> double kineticEnergy(const Lattice<R> &L) {
+    double total = 0.0;
+    for (std::uint32_t i = 0; i < L.N; ++i) {
+        const V<R> v = ld(L.v, i);
+        total += static_cast<double>(R(0.5) * L.mass[i] * dot(v, v));
+    }
+    return total;
+}
+
 template <class R> class Runner {
 public:
     Runner(Lattice<R> &L, const Settings<R> &S, Sphere<R> sp, unsigned threads) : L_(L), S_(S), sp_(sp), pool_(threads) {
         if (S_.nc_mode != 0 && !(contactCutoff(S_) > R(0))) throw std::invalid_argument("node contact needs 2 r + skin > 0");
+        status.energy_audited = S_.audit != 0; // CpuLatticeBackend.cpp:114
     }
     Status status;
     Loads<R> loads;
@@ -1367,7 +1385,11 @@ private:
             L_.candidate_count[b] = std::min(count, kCandidatesPerBlock);
         }
         sp_ = kicked;
-        if (S_.sphere_enabled) spherePass(L_, S_, sp_, 1, status.contact);
+        if (S_.sphere_enabled) {
+            const double before = S_.audit ? kineticEnergy(L_) : 0.0;
+            spherePass(L_, S_, sp_, 1, status.contact);
+            if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
+        }
         for (std::uint32_t it = 0; it < S_.iterations; ++it) {
             const bool first = it == 0;
             auto solve = [&](std::size_t j) { solveBond(L_, j, S_.dt, direct, first); };
@@ -1380,10 +1402,16 @@ private:
             if (S_.damping_fraction <= R(0) && !L_.candidate[i]) nodeSupportVelocity(L_, S_, i);
         });
         if (S_.damping_fraction > R(0)) {
+            const double before = S_.audit ? kineticEnergy(L_) : 0.0;
             sweepAll([&](std::size_t j) { dampBond(L_, j, S_.damping_fraction, direct); });
+            if (S_.audit) status.damping_dissipated += before - kineticEnergy(L_);
             nodes([&](std::size_t i) { if (!L_.candidate[i]) nodeSupportVelocity(L_, S_, i); });
         }
-        if (S_.sphere_enabled) spherePass(L_, S_, sp_, 2, status.contact);
+        if (S_.sphere_enabled) {
+            const double before = S_.audit ? kineticEnergy(L_) : 0.0;
+            spherePass(L_, S_, sp_, 2, status.contact);
+            if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
+        }
         if (S_.nc_mode != 0) {
             if (pairs_.rebuild || pairListStale(L_, S_, pairs_)) rebuildPairs(L_, S_, pairs_, status.node);
             contactPass(L_, S_, pairs_, status.node);
@@ -1541,6 +1569,8 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     d[lsio::kNodeDissipated] = st_.node.dissipated; d[lsio::kNodeMaxOverlap] = st_.node.max_overlap;
     d[lsio::kNodeMaxCorrection] = st_.node.max_correction; d[lsio::kNodeMomentumX] = st_.node.momentum[0];
     d[lsio::kNodeMomentumY] = st_.node.momentum[1]; d[lsio::kNodeMomentumZ] = st_.node.momentum[2];
+    d[lsio::kDampingDissipated] = st_.damping_dissipated; d[lsio::kStrikerDissipated] = st_.striker_dissipated;
+    u[lsio::kEnergyAudited] = st_.energy_audited ? 1 : 0;
     out.put("status_u64", u);
     out.put("status_f64", d);
     out.putScalar<double>("wall_seconds", wall);

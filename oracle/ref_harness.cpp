@@ -39,6 +39,7 @@ V3<double> v3at(const std::vector<double> &s, int at) { return {s[at], s[at + 1]
 
 StepSettings<double> unpackSettings(const std::vector<double> &s) {
     if (s.size() != static_cast<std::size_t>(lsio::kSettingsWidth) &&
+        s.size() != static_cast<std::size_t>(lsio::kAuditEnergy) &&
         s.size() != static_cast<std::size_t>(lsio::kNodeContact))
         throw std::runtime_error("settings width");
     StepSettings<double> out{};
@@ -49,7 +50,7 @@ StepSettings<double> unpackSettings(const std::vector<double> &s) {
     out.damping_fraction = s[lsio::kDampingFraction];
     out.sphere_enabled = static_cast<std::uint8_t>(s[lsio::kSphereEnabled]);
     out.direct_arithmetic = static_cast<std::uint8_t>(s[lsio::kDirectArithmetic]);
-    out.audit_energy = 0;
+    out.audit_energy = s.size() > static_cast<std::size_t>(lsio::kAuditEnergy) && s[lsio::kAuditEnergy] != 0 ? 1 : 0;
     out.plastic_yield_stretch = s[lsio::kPlasticYield];
     out.plastic_hardening = s[lsio::kPlasticHardening];
     out.plate_half_thickness = s[lsio::kPlateHalfThickness];
@@ -62,7 +63,7 @@ StepSettings<double> unpackSettings(const std::vector<double> &s) {
     out.contact.contact_margin = s[c + 5];
     out.contact.prefilter_slack = s[c + 6];
     out.node_contact.mode = kNodeContactOff;
-    if (s.size() == static_cast<std::size_t>(lsio::kSettingsWidth)) {
+    if (s.size() > static_cast<std::size_t>(lsio::kNodeContact)) {
         const int n = lsio::kNodeContact;
         out.node_contact.mode = static_cast<std::uint8_t>(s[n]);
         out.node_contact.radius = s[n + 1];
@@ -132,6 +133,7 @@ void packStatus(lsio::Case &out, const RunStatus &st) {
     u[lsio::kNodeRebuilds] = st.node_contact.rebuilds;
     u[lsio::kNodePairsListed] = st.node_contact.pairs_listed;
     u[lsio::kNodePairOverflow] = st.node_contact.pair_overflow;
+    u[lsio::kEnergyAudited] = st.energy_audited ? 1 : 0;
     std::vector<double> d(lsio::kStatusF64Width, 0.0);
     d[lsio::kRemovedEnergy] = st.removed_energy_j;
     d[lsio::kMaxDamage] = st.max_damage;
@@ -159,6 +161,8 @@ void packStatus(lsio::Case &out, const RunStatus &st) {
     d[lsio::kNodeMomentumX] = st.node_contact.momentum_residual_x;
     d[lsio::kNodeMomentumY] = st.node_contact.momentum_residual_y;
     d[lsio::kNodeMomentumZ] = st.node_contact.momentum_residual_z;
+    d[lsio::kDampingDissipated] = st.damping_dissipated_j;
+    d[lsio::kStrikerDissipated] = st.striker_dissipated_j;
     out.put("status_u64", u);
     out.put("status_f64", d);
 }

@@ -18,13 +18,14 @@ STATUS_U64 = {"total_steps": 0, "first_failure_step": 1, "last_failure_step": 2,
               "broken_bonds": 4, "last_energy_gain_step": 5, "last_damage_gain_step": 6, "exit_reason": 7,
               "rank_deficient_nodes": 8, "impulse_contacts": 9, "candidate_overflow": 10, "ball_support_events": 11,
               "node_contacts": 13, "node_pair_tests": 14, "node_rebuilds": 15, "node_pairs_listed": 16,
-              "node_pair_overflow": 17}
+              "node_pair_overflow": 17, "energy_audited": 18}
 STATUS_F64 = {"removed_energy_j": 0, "max_damage": 1, "plastic_work_j": 2, "max_tensile": 3, "max_compressive": 4,
               "max_shear": 5, "max_plastic_stretch": 6, "impulse_x": 7, "impulse_y": 8, "impulse_z": 9,
               "contact_dissipated": 10, "max_penetration": 11, "max_correction": 12, "max_center_shift": 13,
               "external_work": 14, "external_impulse_x": 15, "external_impulse_y": 16, "external_impulse_z": 17,
               "external_steps": 18, "node_dissipated": 20, "node_max_overlap": 21, "node_max_correction": 22,
-              "node_momentum_x": 23, "node_momentum_y": 24, "node_momentum_z": 25}
+              "node_momentum_x": 23, "node_momentum_y": 24, "node_momentum_z": 25, "damping_dissipated": 26,
+              "striker_dissipated": 27}
 
 
 def golden_names() -> list[str]:
@@ -72,8 +73,8 @@ LEDGER_RTOL = 1e-12
 
 
 def _slot(status, i):
-    """A status slot; records written before the node-contact slots existed
-    (node contact off) read zero there."""
+    """A status slot; records written before the node-contact or audit slots
+    existed (both off) read zero there."""
     return status[i] if i < len(status) else 0
 
 

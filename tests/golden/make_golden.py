@@ -67,6 +67,16 @@ def cases() -> dict:
     # centre, breaking by the fibre strain of its bending; float and double.
     out["plate_strike"] = (scenes.plate_strike(), "float")
     out["plate_strike_double"] = (scenes.plate_strike(nx=16, nz=16, steps=25), "double")
+    # The energy audit: what the striker passes and the damping sweep take out
+    # of the lattice, measured as kinetic-energy differences (sphere impact,
+    # radial damping and plastic flow on); float and double.
+    for name, precision, steps in (("audit_impact", "float", 12), ("audit_impact_double", "double", 6)):
+        audited = scenes.impact_block(nx=16, ny=10, nz=12, blocks=4, radius=0.03, speed=12.0, steps=steps,
+                                      seed_point=5, seed_strength=21)
+        audited["settings"] = audited["settings"].copy()
+        audited["settings"][scenes.K_DAMP] = 0.05
+        audited["settings"][scenes.K_AUDIT] = 1.0
+        out[name] = (audited, precision)
     # Caps: a slab with more sphere candidates than a slab's list holds
     # (1024), and node contact with more pairs per owner than its slots (24).
     out["candidate_overflow"] = (scenes.impact_block(nx=40, ny=4, nz=40, blocks=1, radius=0.4, speed=6.0, steps=1,

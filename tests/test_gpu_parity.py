@@ -134,18 +134,14 @@ def test_external_force_rules(device):
 
 
 def test_refused_features(device):
-    """What the device lane refuses at upload, as the reference's lanes refuse
-    what they do not run: the energy audit, the Verlet integrator, node
-    contact with no cutoff, and a double backend asked for the float lane's
-    arithmetic."""
+    """What the device lane refuses at upload, as the reference's parallel lane
+    refuses what it does not run: the Verlet integrator (serial double only,
+    ParallelCpuLatticeBackend.cpp:1380-1381), node contact with no cutoff, and
+    a double backend asked for the float lane's arithmetic."""
     from banjo_gb300 import scenes
 
     case = scenes.cantilever(nx=6, ny=3, nz=3, steps=1)
     sched, state, be = _backend(device, case)
-    s = device.step_settings(case["settings"])
-    s.audit_energy = 1
-    with pytest.raises(ValueError, match="audit"):
-        be.upload(state, s, device.sphere_state(case["sphere"]))
     s = device.step_settings(case["settings"])
     s.bond_integrator = 1
     with pytest.raises(ValueError, match="XPBD"):

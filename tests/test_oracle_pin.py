@@ -39,6 +39,21 @@ def test_fixtures_contain_fracture():
     assert all(b > 0 for b in broken.values()), broken
 
 
+def test_audit_fixtures_carry_the_audit():
+    """The reference records the audit only when asked (RunStatus::energy_audited,
+    CpuLatticeBackend.cpp:114): the damping sweep removes energy, the striker
+    passes move it; every other fixture's audit slots are zero."""
+    damping, striker, audited = 26, 27, 18
+    for name in golden_names():
+        ref = load_golden(name)[1]
+        u, d = ref["status_u64"], ref["status_f64"]
+        if name.startswith("audit_"):
+            assert int(u[audited]) == 1 and d[damping] > 0 and d[striker] != 0, name
+        else:
+            assert (len(u) <= audited or int(u[audited]) == 0) and (len(d) <= damping or
+                                                                      (d[damping] == 0 and d[striker] == 0)), name
+
+
 def test_contact_fixtures_hold_the_reference_rules():
     """The reference's own assertions on its two-cell contact pairs
     (fast_lattice_tests.cpp:800-896), on the fixtures its code produced."""
