@@ -253,6 +253,25 @@ public:
         check(gbl_set_external_forces(backend_, flat.empty() ? nullptr : flat.data(), forces_world_n.size(), substeps));
     }
 
+    void setExternalWrenches(const std::vector<ExternalWrench> &wrenches, std::uint64_t substeps) override {
+        std::vector<gbl_external_wrench> in(wrenches.size());
+        for (std::size_t k = 0; k < wrenches.size(); ++k) {
+            const ExternalWrench &w = wrenches[k];
+            gbl_external_wrench &o = in[k];
+            o.source = w.source.c_str();
+            o.nodes = w.nodes.data();
+            o.node_count = w.nodes.size();
+            const Vec3 *from[3] = {&w.point_world_m, &w.force_n, &w.torque_n_m};
+            double *to[3] = {o.point_world_m, o.force_n, o.torque_n_m};
+            for (int q = 0; q < 3; ++q) {
+                to[q][0] = from[q]->x;
+                to[q][1] = from[q]->y;
+                to[q][2] = from[q]->z;
+            }
+        }
+        check(gbl_set_external_wrenches(backend_, in.empty() ? nullptr : in.data(), in.size(), substeps));
+    }
+
     RunStatus run(const RunControl &control) override {
         gbl_run_control c{};
         c.max_steps = control.max_steps;
@@ -270,7 +289,9 @@ public:
         // std::atomic<bool> of one byte, read between launches.
         c.abandon = reinterpret_cast<const volatile std::uint8_t *>(control.abandon);
         gbl_run_status s{};
-        check(gbl_run(backend_, &c, &s));
+        const gbl_result rc = gbl_run(backend_, &c, &s);
+        readSources();
+        check(rc);
         statusOf(s, status_);
         return status_;
     }
@@ -321,6 +342,34 @@ public:
     }
 
 private:
+    // RunStatus::external_sources, read back after every run.
+    void readSources() {
+        std::uint64_t n = 0;
+        check(gbl_external_source_count(backend_, &n));
+        status_.external_sources.resize(n);
+        for (std::uint64_t k = 0; k < n; ++k) {
+            std::size_t length = 0;
+            check(gbl_external_source(backend_, k, nullptr, 0, &length, nullptr));
+            std::string name(length + 1, '\0');
+            gbl_load_ledger g{};
+            check(gbl_external_source(backend_, k, name.data(), name.size(), &length, &g));
+            name.resize(length);
+            ExternalWrenchLedger &o = status_.external_sources[k];
+            o.source = name;
+            o.load.steps = g.steps;
+            o.load.elapsed_s = g.elapsed_s;
+            o.load.requested_impulse_n_s = {g.requested_impulse_n_s[0], g.requested_impulse_n_s[1],
+                                            g.requested_impulse_n_s[2]};
+            o.load.impulse_n_s = {g.impulse_n_s[0], g.impulse_n_s[1], g.impulse_n_s[2]};
+            o.load.requested_angular_impulse_kg_m2_s = {g.requested_angular_impulse_kg_m2_s[0],
+                                                        g.requested_angular_impulse_kg_m2_s[1],
+                                                        g.requested_angular_impulse_kg_m2_s[2]};
+            o.load.angular_impulse_kg_m2_s = {g.angular_impulse_kg_m2_s[0], g.angular_impulse_kg_m2_s[1],
+                                              g.angular_impulse_kg_m2_s[2]};
+            o.load.work_j = g.work_j;
+        }
+    }
+
     gbl_backend *backend_{};
     RunStatus status_{};
     std::uint32_t node_count_{}, bond_count_{};

@@ -23,6 +23,7 @@
 #include <memory>
 #include <new>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <type_traits>
@@ -258,6 +259,14 @@ template <class R> struct Resident {
     std::uint32_t ext_count{};
     std::uint64_t ext_remaining{};
     bool ext_dirty{};
+    // External wrenches (allocated on first use): the set wrenches in name
+    // order, their nodes listed in ext_nodes; every source kicked since
+    // upload keeps a ledger slot, named by source_names.
+    WrenchDev *wrench_dev{};
+    std::uint32_t wrench_count{}, wrench_cap{};
+    SourceSlot *source_dev{};
+    std::size_t source_cap{};
+    std::vector<std::string> source_names;
     // What a caller reads back.
     gbl_run_status status{};
     std::vector<std::uint32_t> first_failure;
@@ -339,6 +348,8 @@ template <class R> struct Resident {
         if (ext_req) cudaFree(ext_req);
         if (ext_contrib) cudaFree(ext_contrib);
         if (ext_nodes) cudaFree(ext_nodes);
+        if (wrench_dev) cudaFree(wrench_dev);
+        if (source_dev) cudaFree(source_dev);
     }
 
     // Levels of the projection sweep. The reference sweeps bonds in one
@@ -590,6 +601,7 @@ template <class R> struct Resident {
         // Loads do not survive an upload (ExternalLoads.hpp:26 reset).
         ext_count = 0;
         ext_remaining = 0;
+        clearSources();
         status = gbl_run_status{};
         status.first_failure_step = status.last_failure_step = status.last_energy_gain_step = ~0ULL;
         first_failure.clear();
@@ -901,6 +913,7 @@ template <class R> struct Resident {
             if (substeps != 0) invalid("empty external load needs zero substeps");
             ext_count = 0;
             ext_remaining = 0;
+            wrench_count = 0;
             ext_dirty = true;
             return;
         }
@@ -920,20 +933,173 @@ template <class R> struct Resident {
             applied[i] = {cx, cy, cz, R(1)};
             nodes.push_back(i);
         }
-        if (!ext_force) {
-            check(cudaMalloc(&ext_force, sizeof(Q4<R>) * N), "device allocation");
-            check(cudaMalloc(&ext_req, sizeof(double) * 3 * N), "device allocation");
-            check(cudaMalloc(&ext_contrib, sizeof(double) * 13 * N), "device allocation");
-            check(cudaMalloc(&ext_nodes, sizeof(std::uint32_t) * N), "device allocation");
-            dev.ext_force = ext_force; dev.ext_req = ext_req; dev.ext_contrib = ext_contrib; dev.ext_nodes = ext_nodes;
-        }
+        ensureLoadBuffers();
         gbl::upload(ext_force, applied, stream);
         uploadRaw(ext_req, forces, 3 * static_cast<std::size_t>(N), stream);
         gbl::upload(ext_nodes, nodes, stream);
         check(cudaStreamSynchronize(stream), "external load");
         ext_count = static_cast<std::uint32_t>(nodes.size());
         ext_remaining = nodes.empty() ? 0 : substeps;
+        wrench_count = 0; // forces replace any wrenches
         ext_dirty = true;
+    }
+
+    // Loads and source ledgers cleared (an upload; a new control block).
+    void clearSources() {
+        wrench_count = 0;
+        source_names.clear();
+        if (source_dev) check(cudaMemset(source_dev, 0, sizeof(SourceSlot) * source_cap), "clear");
+    }
+
+    void ensureLoadBuffers() {
+        if (ext_force) return;
+        check(cudaMalloc(&ext_force, sizeof(Q4<R>) * N), "device allocation");
+        check(cudaMalloc(&ext_req, sizeof(double) * 3 * N), "device allocation");
+        check(cudaMalloc(&ext_contrib, sizeof(double) * 13 * N), "device allocation");
+        check(cudaMalloc(&ext_nodes, sizeof(std::uint32_t) * N), "device allocation");
+        dev.ext_force = ext_force; dev.ext_req = ext_req; dev.ext_contrib = ext_contrib; dev.ext_nodes = ext_nodes;
+    }
+
+    // setExternalWrenches (ExternalLoads.hpp:52-77): validated in full (the
+    // spread from the current geometry included, on the device) before
+    // anything changes, so an invalid replacement leaves the old load intact.
+    void setExternalWrenches(const gbl_external_wrench *ws, std::uint64_t count, std::uint64_t substeps,
+                             cudaStream_t stream) {
+        if (count == 0) {
+            if (substeps != 0) invalid("empty external load needs zero substeps");
+            ext_count = 0;
+            ext_remaining = 0;
+            wrench_count = 0;
+            ext_dirty = true;
+            return;
+        }
+        if (!ws) invalid("external wrench needs its wrenches");
+        if (substeps == 0) invalid("external wrench needs a finite nonzero span");
+        struct Staged {
+            std::string source;
+            std::vector<std::uint32_t> nodes;
+            double point[3], force[3], torque[3];
+        };
+        auto finite3 = [](const double *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
+        std::vector<Staged> staged(count);
+        std::set<std::string> names;
+        std::vector<std::uint8_t> used(N, 0);
+        for (std::uint64_t k = 0; k < count; ++k) {
+            const gbl_external_wrench &in = ws[k];
+            Staged &w = staged[k];
+            if (in.source) w.source = in.source;
+            if (w.source.empty() || !names.insert(w.source).second || in.node_count == 0 || !in.nodes)
+                invalid("external wrench needs distinct named nonempty regions");
+            if (!finite3(in.point_world_m) || !finite3(in.force_n) || !finite3(in.torque_n_m) ||
+                !std::isfinite(std::hypot(in.force_n[0], in.force_n[1], in.force_n[2])) ||
+                !std::isfinite(std::hypot(in.torque_n_m[0], in.torque_n_m[1], in.torque_n_m[2])))
+                invalid("external wrench must be finite");
+            w.nodes.assign(in.nodes, in.nodes + in.node_count);
+            std::sort(w.nodes.begin(), w.nodes.end());
+            for (const std::uint32_t i : w.nodes) {
+                if (i >= N || used[i]) invalid("external wrench nodes repeat, overlap or exceed the lattice");
+                used[i] = 1;
+            }
+            std::memcpy(w.point, in.point_world_m, sizeof(w.point));
+            std::memcpy(w.force, in.force_n, sizeof(w.force));
+            std::memcpy(w.torque, in.torque_n_m, sizeof(w.torque));
+        }
+        std::sort(staged.begin(), staged.end(), [](const Staged &a, const Staged &b) { return a.source < b.source; });
+        staged.erase(std::remove_if(staged.begin(), staged.end(), [](const Staged &w) {
+            return w.force[0] == 0 && w.force[1] == 0 && w.force[2] == 0 && w.torque[0] == 0 && w.torque[1] == 0 &&
+                   w.torque[2] == 0;
+        }), staged.end());
+        std::vector<std::uint32_t> list;
+        std::vector<WrenchDev> descs;
+        std::vector<std::string> names_after = source_names;
+        for (const Staged &w : staged) {
+            for (const std::uint32_t i : w.nodes)
+                if (!(mass[i] > 0) || !(inv_mass[i] > 0) || !std::isfinite(mass[i]) || !std::isfinite(inv_mass[i]))
+                    invalid("external wrench needs finite movable node masses");
+            WrenchDev d{};
+            d.begin = static_cast<std::uint32_t>(list.size());
+            list.insert(list.end(), w.nodes.begin(), w.nodes.end());
+            d.end = static_cast<std::uint32_t>(list.size());
+            const auto at = std::find(names_after.begin(), names_after.end(), w.source);
+            d.slot = static_cast<std::uint32_t>(at - names_after.begin());
+            if (at == names_after.end()) names_after.push_back(w.source);
+            std::memcpy(d.point, w.point, sizeof(d.point));
+            std::memcpy(d.force, w.force, sizeof(d.force));
+            std::memcpy(d.torque, w.torque, sizeof(d.torque));
+            descs.push_back(d);
+        }
+        if (!descs.empty()) {
+            // The spread at the current geometry, checked on the device.
+            WrenchDev *wd = nullptr;
+            std::uint32_t *ld = nullptr;
+            unsigned *verdict = nullptr;
+            check(cudaMalloc(&wd, sizeof(WrenchDev) * descs.size()), "device allocation");
+            check(cudaMalloc(&ld, sizeof(std::uint32_t) * list.size()), "device allocation");
+            check(cudaMalloc(&verdict, sizeof(unsigned)), "device allocation");
+            gbl::upload(wd, descs, stream);
+            gbl::upload(ld, list, stream);
+            check(cudaMemsetAsync(verdict, 0, sizeof(unsigned), stream), "clear");
+            kWrench<R><<<static_cast<unsigned>(descs.size()), kWrenchThreads, 0, stream>>>(dev, wd, ld, verdict, 0);
+            check(cudaGetLastError(), "kernel launch");
+            unsigned bad = 0;
+            check(cudaMemcpyAsync(&bad, verdict, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
+            check(cudaStreamSynchronize(stream), "external wrench");
+            cudaFree(wd);
+            cudaFree(ld);
+            cudaFree(verdict);
+            if (bad)
+                invalid("external wrench cannot be spread over its nodes at the current geometry (torque, "
+                        "resultant or node force not representable)");
+        }
+        ensureLoadBuffers();
+        if (descs.size() > wrench_cap) {
+            if (wrench_dev) cudaFree(wrench_dev);
+            wrench_cap = static_cast<std::uint32_t>(descs.size());
+            check(cudaMalloc(&wrench_dev, sizeof(WrenchDev) * wrench_cap), "device allocation");
+            dev.wrench = wrench_dev;
+        }
+        if (names_after.size() > source_cap) {
+            const std::size_t cap = std::max<std::size_t>(names_after.size(), 2 * source_cap);
+            SourceSlot *grown = nullptr;
+            check(cudaMalloc(&grown, sizeof(SourceSlot) * cap), "device allocation");
+            check(cudaMemsetAsync(grown, 0, sizeof(SourceSlot) * cap, stream), "clear");
+            if (source_dev) {
+                check(cudaMemcpyAsync(grown, source_dev, sizeof(SourceSlot) * source_cap, cudaMemcpyDeviceToDevice,
+                                      stream), "copy");
+                check(cudaStreamSynchronize(stream), "copy");
+                cudaFree(source_dev);
+            }
+            source_dev = grown;
+            source_cap = cap;
+            dev.sources = source_dev;
+        }
+        check(cudaMemsetAsync(ext_force, 0, sizeof(Q4<R>) * N, stream), "clear"); // the kick writes the wrench nodes
+        if (!descs.empty()) {
+            gbl::upload(wrench_dev, descs, stream);
+            gbl::upload(ext_nodes, list, stream);
+        }
+        check(cudaStreamSynchronize(stream), "external wrench");
+        source_names = std::move(names_after);
+        wrench_count = static_cast<std::uint32_t>(descs.size());
+        ext_count = static_cast<std::uint32_t>(list.size());
+        ext_remaining = list.empty() ? 0 : substeps;
+        ext_dirty = true;
+    }
+
+    // RunStatus::external_sources: every source kicked since upload, in the
+    // order of its first kick (ExternalLoads.hpp:131-140).
+    std::vector<std::pair<std::string, LoadLedger>> sources() const {
+        std::vector<std::pair<std::string, LoadLedger>> out;
+        if (source_names.empty()) return out;
+        std::vector<SourceSlot> slots(source_names.size());
+        check(cudaMemcpy(slots.data(), source_dev, sizeof(SourceSlot) * slots.size(), cudaMemcpyDeviceToHost), "copy");
+        std::vector<std::size_t> kicked;
+        for (std::size_t k = 0; k < slots.size(); ++k)
+            if (slots[k].load.steps) kicked.push_back(k);
+        std::sort(kicked.begin(), kicked.end(),
+                  [&](std::size_t a, std::size_t b) { return slots[a].order < slots[b].order; });
+        for (const std::size_t k : kicked) out.emplace_back(source_names[k], slots[k].load);
+        return out;
     }
 
     // The device arrays a download needs, raw, into `raw` (its buffers reused
@@ -1247,6 +1413,22 @@ public:
         }
     }
 
+    // External wrenches, on a lattice stepped alone (the wrench launch is part
+    // of the single-lattice substep).
+    void setExternalWrenches(std::size_t k, const gbl_external_wrench *ws, std::uint64_t count,
+                             std::uint64_t substeps) {
+        requireReady();
+        if (many_) invalid("external wrenches drive a lattice stepped alone");
+        Resident<R> &l = lattice(k);
+        const void *before[3] = {l.ext_force, l.wrench_dev, l.source_dev};
+        l.setExternalWrenches(ws, count, substeps, stream_);
+        if (before[0] != l.ext_force || before[1] != l.wrench_dev || before[2] != l.source_dev) {
+            pushDescriptor(k);
+            check(cudaStreamSynchronize(stream_), "descriptor");
+            dropGraph();
+        }
+    }
+
     // run (CpuLatticeBackend.cpp:255-304) for every lattice with one control;
     // a lattice whose step limit is spent stays stopped.
     void run(const gbl_run_control &control) {
@@ -1269,6 +1451,7 @@ public:
             c.calm_damage_margin = control.calm_damage_margin; c.removable_energy = control.removable_energy_j;
             if (l.ext_dirty) {
                 c.ext_count = l.ext_count;
+                c.wrench_count = l.wrench_count;
                 c.loads_remaining = l.ext_remaining;
                 l.ext_dirty = false;
             }
@@ -1315,7 +1498,7 @@ public:
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0_, ev1_);
         pullControl();
-        bool overflowed = false;
+        bool overflowed = false, wrenched = false;
         for (auto k : active_) {
             Ctl &c = ctl_host_[k];
             Resident<R> &l = *slots_[k];
@@ -1323,6 +1506,10 @@ public:
             if (c.error & kErrExternalOverflow) {
                 c.error = 0;
                 overflowed = true;
+            }
+            if (c.error & kErrWrench) {
+                c.error = 0;
+                wrenched = true;
             }
             l.ext_remaining = c.loads_remaining;
             l.fillStatus(c);
@@ -1339,6 +1526,12 @@ public:
             pushControl();
             check(cudaStreamSynchronize(stream_), "status");
             overflow("external force kick exceeds backend precision");
+        }
+        if (wrenched) {
+            pushControl();
+            check(cudaStreamSynchronize(stream_), "status");
+            invalid("external wrench cannot be spread over its nodes at the current geometry (torque, resultant "
+                    "or node force not representable)");
         }
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
         for (auto k : active_) slots_[k]->status.wall_seconds += wall;
@@ -1363,6 +1556,7 @@ public:
             Resident<R> &l = *slots_[k];
             if (l.ext_dirty) {
                 c.ext_count = l.ext_count;
+                c.wrench_count = l.wrench_count;
                 c.loads_remaining = l.ext_remaining;
                 l.ext_dirty = false;
             }
@@ -1629,6 +1823,7 @@ private:
         l.ext_count = 0;
         l.ext_remaining = 0;
         l.ext_dirty = false;
+        l.clearSources();
         l.status = gbl_run_status{};
         l.status.first_failure_step = l.status.last_failure_step = l.status.last_energy_gain_step = ~0ULL;
         l.status.energy_audited = S_.audit ? 1 : 0; // CpuLatticeBackend.cpp:114
@@ -1853,6 +2048,10 @@ private:
         // without, before the kick.
         const bool side_restart = S.sphere_enabled != 0;
         if (!side_restart) restartPhase<M>(st, 0, mark);
+        if (!M && slots_[one_]->wrench_cap) {
+            const Resident<R> &l = *slots_[one_];
+            kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr, 1);
+        }
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
         if (S.sphere_enabled && slabs_.count) {
             kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
@@ -2115,6 +2314,8 @@ public:
     virtual std::string name() const = 0;
     virtual void upload(const gbl_state_view &, const gbl_step_settings &, const gbl_sphere &) = 0;
     virtual void setExternalForces(const double *forces, std::uint64_t count, std::uint64_t substeps) = 0;
+    virtual void setExternalWrenches(const gbl_external_wrench *ws, std::uint64_t count, std::uint64_t substeps) = 0;
+    virtual std::vector<std::pair<std::string, LoadLedger>> sources() = 0;
     virtual void run(const gbl_run_control &) = 0;
     virtual void download(gbl_state_view &, gbl_sphere *) = 0;
     virtual void profile(std::uint64_t substeps, double *phase_ms) = 0;
@@ -2139,6 +2340,14 @@ public:
     void setExternalForces(const double *forces, std::uint64_t count, std::uint64_t substeps) override {
         if (engine_.size() == 0) invalid("external load needs an uploaded lattice");
         engine_.setExternalForces(0, forces, count, substeps);
+    }
+    void setExternalWrenches(const gbl_external_wrench *ws, std::uint64_t count, std::uint64_t substeps) override {
+        if (engine_.size() == 0) invalid("external wrench needs an uploaded lattice");
+        engine_.setExternalWrenches(0, ws, count, substeps);
+    }
+    std::vector<std::pair<std::string, LoadLedger>> sources() override {
+        if (engine_.size() == 0) return {};
+        return engine_.lattice(0).sources();
     }
     void run(const gbl_run_control &control) override {
         if (engine_.size() == 0) invalid("lattice run needs an uploaded lattice");
@@ -2554,6 +2763,48 @@ gbl_result gbl_set_external_forces(gbl_backend *backend, const double *forces, u
     return gbl::guard([&] {
         if (!backend) gbl::invalid("null backend");
         backend->impl->setExternalForces(forces, count, substeps);
+    });
+}
+
+gbl_result gbl_set_external_wrenches(gbl_backend *backend, const gbl_external_wrench *wrenches, uint64_t count,
+                                     uint64_t substeps) {
+    return gbl::guard([&] {
+        if (!backend) gbl::invalid("null backend");
+        backend->impl->setExternalWrenches(wrenches, count, substeps);
+    });
+}
+
+gbl_result gbl_external_source_count(gbl_backend *backend, uint64_t *count) {
+    return gbl::guard([&] {
+        if (!backend || !count) gbl::invalid("null argument");
+        *count = backend->impl->sources().size();
+    });
+}
+
+gbl_result gbl_external_source(gbl_backend *backend, uint64_t index, char *name, size_t name_capacity,
+                               size_t *name_length, gbl_load_ledger *load) {
+    return gbl::guard([&] {
+        if (!backend) gbl::invalid("null backend");
+        const auto all = backend->impl->sources();
+        if (index >= all.size()) gbl::invalid("no external source at that index");
+        const auto &[source, g] = all[index];
+        if (name_length) *name_length = source.size();
+        if (name && name_capacity) {
+            const std::size_t n = std::min(source.size(), name_capacity - 1);
+            std::memcpy(name, source.data(), n);
+            name[n] = 0;
+        }
+        if (load) {
+            load->steps = g.steps;
+            load->elapsed_s = g.elapsed;
+            for (int q = 0; q < 3; ++q) {
+                load->requested_impulse_n_s[q] = g.req_imp[q];
+                load->impulse_n_s[q] = g.imp[q];
+                load->requested_angular_impulse_kg_m2_s[q] = g.req_ang[q];
+                load->angular_impulse_kg_m2_s[q] = g.ang[q];
+            }
+            load->work_j = g.work;
+        }
     });
 }
 

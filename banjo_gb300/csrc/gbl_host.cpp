@@ -270,7 +270,7 @@ size_t gbl_struct_size(const char *name) {
     GBL_SIZE(gbl_node_contact_accumulators) GBL_SIZE(gbl_tuning) GBL_SIZE(gbl_impact_scene)
     GBL_SIZE(gbl_sphere) GBL_SIZE(gbl_run_control) GBL_SIZE(gbl_contact_accumulators) GBL_SIZE(gbl_load_ledger)
     GBL_SIZE(gbl_run_status) GBL_SIZE(gbl_matter_view) GBL_SIZE(gbl_request_info) GBL_SIZE(gbl_server_stats)
-    GBL_SIZE(gbl_box_spec)
+    GBL_SIZE(gbl_box_spec) GBL_SIZE(gbl_external_wrench)
 #undef GBL_SIZE
     return 0;
 }

@@ -21,6 +21,7 @@
 
 #include "gbl_math.cuh"
 
+#include <cfloat>
 #include <cstdint>
 #include <type_traits>
 
@@ -111,9 +112,26 @@ struct Ctl {
     // The energy audit: the kinetic energy before the phase being measured,
     // and what the damping sweep and the striker passes took out.
     double ke_mark, damping_dissipated, striker_dissipated;
+    // External wrenches: how many are set, and the count of sources kicked
+    // since upload (a new source's place in the status order).
+    unsigned wrench_count, source_seq;
+};
+
+// An external wrench on the device (ExternalWrench, FastLattice.hpp:153-157):
+// its nodes (a range of the load list, sources in name order, nodes ascending),
+// its source ledger slot, and its point, force and torque.
+struct WrenchDev {
+    std::uint32_t begin, end, slot, pad;
+    double point[3], force[3], torque[3];
+};
+// A source's ledger (ExternalWrenchLedger) and its place in the status order.
+struct SourceSlot {
+    LoadLedger load;
+    unsigned long long order;
 };
 
 constexpr unsigned kErrExternalOverflow = 1;
+constexpr unsigned kErrWrench = 2;
 
 template <class R> struct Dev {
     std::uint32_t N, B, D, blocks, words_b, tiles_b;
@@ -157,6 +175,8 @@ template <class R> struct Dev {
     double *ext_req;      // requested force, 3 per node
     double *ext_contrib;  // 13 per node: impulse 3, angular 3, work, requested 3, requested angular 3
     std::uint32_t *ext_nodes;
+    WrenchDev *wrench;    // the set wrenches (their count is in the control block)
+    SourceSlot *sources;  // every source kicked since upload
     // Node-to-node contact scratch, allocated when the settings turn contact
     // on: positions at the last build, each node's grid cell (w: its bucket),
     // the hashed grid (per bucket: count, then scatter cursor; first member;
@@ -630,6 +650,195 @@ __global__ void __launch_bounds__(kThreads) kKick(const Grid<R> launch, Settings
     if (S.sphere_enabled) {
         const unsigned bits = __ballot_sync(0xffffffffU, cand);
         if ((threadIdx.x & 31) == 0 && i / 32 < (L.N + 31) / 32) L.cand_bits[i / 32] = bits;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// External wrenches (ExternalLoads.hpp:171-238): each wrench's force and
+// torque spread over its nodes by mass about their mass centre, from the
+// current positions, before every kick. One CTA per wrench. The region's sums
+// (mass, centre, inertia tensor, the resultant checks) are folded serially in
+// node order as the reference folds them, each sum a chain on its own
+// thread, from chunks the CTA stages in shared memory; the eigen-solve of the
+// tensor is the reference's cyclic Jacobi in double. apply 1 writes the
+// kick's forces (when loads remain); a wrench the current geometry cannot
+// carry then stops the lattice before the kick changes anything, with
+// kErrWrench set (the reference throws there). apply 0 only validates, into
+// *verdict.
+// ---------------------------------------------------------------------------
+constexpr unsigned kWrenchThreads = 256;
+
+__device__ inline double normD(double x, double y, double z) { return norm3d(x, y, z); }
+
+template <class R>
+__global__ void __launch_bounds__(kWrenchThreads)
+kWrench(const Dev<R> L, const WrenchDev *ws, const std::uint32_t *lists, unsigned *verdict, int apply) {
+    Ctl &c = *L.ctl;
+    if (apply && (c.stop || c.loads_remaining == 0 || blockIdx.x >= c.wrench_count)) return;
+    const WrenchDev w = ws[blockIdx.x];
+    const std::uint32_t *list = lists + w.begin;
+    const std::uint32_t n = w.end - w.begin;
+    const unsigned t = threadIdx.x;
+    __shared__ double sm[kWrenchThreads], sr[3][kWrenchThreads], sf[3][kWrenchThreads];
+    __shared__ double mass, center[3], tensor[9], alpha[3], moment[3], sums[8];
+    __shared__ int bad;
+    if (t == 0) bad = 0;
+    const std::uint32_t a0 = list[0];
+    const V3<R> p0 = xyz(L.x0[a0]) + xyz(L.u[a0]);
+    const double anchor[3] = {double(p0.x), double(p0.y), double(p0.z)};
+    __syncthreads();
+    // One pass over the region: stage(k, slot) for the chunk's nodes, then
+    // fold(count) over the staged chunk.
+    auto pass = [&](auto &&stage, auto &&fold) {
+        for (std::uint32_t base = 0; base < n; base += kWrenchThreads) {
+            if (base + t < n) stage(base + t, t);
+            __syncthreads();
+            fold(n - base < kWrenchThreads ? n - base : kWrenchThreads);
+            __syncthreads();
+        }
+    };
+    // Mass and position relative to the anchor; movable, finite nodes only.
+    auto stageNode = [&](std::uint32_t k, unsigned j) {
+        const std::uint32_t i = list[k];
+        const Q4<R> u = L.u[i], v = L.v[i]; // w: inverse mass, mass
+        const V3<R> p = xyz(L.x0[i]) + xyz(u);
+        sm[j] = double(v.w);
+        sr[0][j] = double(p.x) - anchor[0];
+        sr[1][j] = double(p.y) - anchor[1];
+        sr[2][j] = double(p.z) - anchor[2];
+        if (!(v.w > R(0)) || !(u.w > R(0)) || !isfinite(v.w) || !isfinite(u.w) || !isfinite(sr[0][j]) ||
+            !isfinite(sr[1][j]) || !isfinite(sr[2][j]))
+            bad = 1;
+    };
+    double acc = 0.0;
+    pass(stageNode, [&](unsigned m) {
+        if (t == 0)
+            for (unsigned j = 0; j < m; ++j) acc += sm[j];
+    });
+    if (t == 0) {
+        mass = acc;
+        if (!(acc > 0) || !isfinite(acc)) bad = 1;
+    }
+    __syncthreads();
+    acc = 0.0;
+    pass(stageNode, [&](unsigned m) {
+        if (t < 3)
+            for (unsigned j = 0; j < m; ++j) acc = acc + sr[t][j] * (sm[j] / mass);
+    });
+    if (t < 3) center[t] = acc;
+    __syncthreads();
+    acc = 0.0;
+    pass(stageNode, [&](unsigned m) {
+        if (t < 9) {
+            const unsigned a = t / 3, b = t % 3;
+            for (unsigned j = 0; j < m; ++j) {
+                const double r[3] = {sr[0][j] - center[0], sr[1][j] - center[1], sr[2][j] - center[2]};
+                const double share = sm[j] / mass;
+                acc = acc + share * (a == b ? r[(a + 1) % 3] * r[(a + 1) % 3] + r[(a + 2) % 3] * r[(a + 2) % 3]
+                                            : -r[a] * r[b]);
+            }
+        }
+    });
+    if (t < 9) tensor[t] = acc;
+    __syncthreads();
+    if (t == 0) {
+        const double arm[3] = {((w.point[0] - L.origin[0]) - anchor[0]) - center[0],
+                               ((w.point[1] - L.origin[1]) - anchor[1]) - center[1],
+                               ((w.point[2] - L.origin[2]) - anchor[2]) - center[2]};
+        moment[0] = w.torque[0] + (arm[1] * w.force[2] - arm[2] * w.force[1]);
+        moment[1] = w.torque[1] + (arm[2] * w.force[0] - arm[0] * w.force[2]);
+        moment[2] = w.torque[2] + (arm[0] * w.force[1] - arm[1] * w.force[0]);
+        for (int q = 0; q < 3; ++q)
+            if (!isfinite(center[q]) || !isfinite(moment[q])) bad = 1;
+        double scale = 0.0;
+        for (int e = 0; e < 9; ++e) {
+            if (!isfinite(tensor[e])) bad = 1;
+            const double x = fabs(tensor[e]);
+            scale = scale < x ? x : scale;
+        }
+        double al[3] = {0.0, 0.0, 0.0};
+        const double mn = normD(moment[0], moment[1], moment[2]);
+        if (!bad && scale > 0) {
+            double m9[9], eig[3], axes[9];
+            for (int e = 0; e < 9; ++e) m9[e] = tensor[e] / scale;
+            jacobi3(m9, eig, axes);
+            double largest = fabs(eig[0]);
+            largest = largest < fabs(eig[1]) ? fabs(eig[1]) : largest;
+            largest = largest < fabs(eig[2]) ? fabs(eig[2]) : largest;
+            double un[3] = {moment[0], moment[1], moment[2]};
+            for (int axis = 0; axis < 3; ++axis) {
+                if (!(eig[axis] > 1e-10 * largest)) continue;
+                const double dir[3] = {axes[axis], axes[3 + axis], axes[6 + axis]};
+                const double component = dir[0] * moment[0] + dir[1] * moment[1] + dir[2] * moment[2];
+                const double sc = component / mass / scale / eig[axis];
+                for (int q = 0; q < 3; ++q) {
+                    un[q] = un[q] - dir[q] * component;
+                    al[q] = al[q] + dir[q] * sc;
+                }
+            }
+            if (normD(un[0], un[1], un[2]) > 1024 * DBL_EPSILON * mn) bad = 1;
+        } else if (!bad && mn > 0) {
+            bad = 1; // a torque with no sampled lever arm
+        }
+        for (int q = 0; q < 3; ++q) {
+            if (!isfinite(al[q])) bad = 1;
+            alpha[q] = al[q];
+        }
+    }
+    __syncthreads();
+    // Node forces, written for the kick, then the resultant checks.
+    double part = 0.0;
+    pass([&](std::uint32_t k, unsigned j) {
+        stageNode(k, j);
+        const double m = sm[j], share = m / mass;
+        const double r[3] = {sr[0][j] - center[0], sr[1][j] - center[1], sr[2][j] - center[2]};
+        const double cr[3] = {alpha[1] * r[2] - alpha[2] * r[1], alpha[2] * r[0] - alpha[0] * r[2],
+                              alpha[0] * r[1] - alpha[1] * r[0]};
+        double f[3];
+        for (int q = 0; q < 3; ++q) {
+            f[q] = w.force[q] * share + cr[q] * m;
+            sr[q][j] = r[q];
+            sf[q][j] = f[q];
+        }
+        const R fx = R(f[0]), fy = R(f[1]), fz = R(f[2]);
+        if (!isfinite(f[0]) || !isfinite(f[1]) || !isfinite(f[2]) || !isfinite(fx) || !isfinite(fy) || !isfinite(fz))
+            bad = 1;
+        if (apply) {
+            const std::uint32_t i = list[k];
+            L.ext_force[i] = Q4<R>{fx, fy, fz, R(1)};
+            L.ext_req[3 * static_cast<std::size_t>(i)] = f[0];
+            L.ext_req[3 * static_cast<std::size_t>(i) + 1] = f[1];
+            L.ext_req[3 * static_cast<std::size_t>(i) + 2] = f[2];
+        }
+    }, [&](unsigned m) {
+        if (t >= 8) return;
+        for (unsigned j = 0; j < m; ++j) {
+            const double r[3] = {sr[0][j], sr[1][j], sr[2][j]}, f[3] = {sf[0][j], sf[1][j], sf[2][j]};
+            const double mo[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+            if (t < 3) part = part + f[t];
+            else if (t < 6) part = part + mo[t - 3];
+            else if (t == 6) part += normD(f[0], f[1], f[2]);
+            else part += normD(mo[0], mo[1], mo[2]);
+        }
+    });
+    if (t < 8) sums[t] = part;
+    __syncthreads();
+    if (t == 0) {
+        for (int q = 0; q < 8; ++q)
+            if (!isfinite(sums[q])) bad = 1;
+        const double fn = normD(w.force[0], w.force[1], w.force[2]);
+        const double mn = normD(moment[0], moment[1], moment[2]);
+        const double df = normD(sums[0] - w.force[0], sums[1] - w.force[1], sums[2] - w.force[2]);
+        const double dm = normD(sums[3] - moment[0], sums[4] - moment[1], sums[5] - moment[2]);
+        if (df > 1e-10 * (fn < sums[6] ? sums[6] : fn) || dm > 1e-10 * (mn < sums[7] ? sums[7] : mn)) bad = 1;
+        if (bad) {
+            if (!apply) {
+                atomicOr(verdict, 1U);
+            } else if (!(atomicOr(&c.error, kErrWrench) & kErrWrench)) {
+                c.stop = 1;
+                atomicSub(L.running, 1U);
+            }
+        }
     }
 }
 
@@ -1887,6 +2096,29 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
             g.ang[q] = g.ang[q] + ch[3 + q];
         }
         g.work = g.work + ch[6];
+        // Each wrench source's own change, folded over its nodes, into its
+        // ledger; a source kicked for the first time since upload takes the
+        // next place in the status order (ExternalLoads.hpp:126-140).
+        for (unsigned k = 0; k < c.wrench_count; ++k) {
+            const WrenchDev &wr = L.wrench[k];
+            double cs[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (std::uint32_t e = wr.begin; e < wr.end; ++e) {
+                const double *x = L.ext_contrib + 13 * static_cast<std::size_t>(L.ext_nodes[e]);
+                for (int q = 0; q < 13; ++q) cs[q] += x[q];
+            }
+            SourceSlot &slot = L.sources[wr.slot];
+            if (slot.load.steps == 0) slot.order = c.source_seq++;
+            LoadLedger &sg = slot.load;
+            sg.steps += 1;
+            sg.elapsed = sg.elapsed + static_cast<double>(S.dt);
+            for (int q = 0; q < 3; ++q) {
+                sg.req_imp[q] = sg.req_imp[q] + cs[7 + q];
+                sg.req_ang[q] = sg.req_ang[q] + cs[10 + q];
+                sg.imp[q] = sg.imp[q] + cs[q];
+                sg.ang[q] = sg.ang[q] + cs[3 + q];
+            }
+            sg.work = sg.work + cs[6];
+        }
         c.loads_remaining -= 1;
     }
     c.full_restart = 0;

@@ -119,6 +119,31 @@ class LoadLedger(C.Structure):
                 ("angular_impulse_kg_m2_s", C.c_double * 3), ("work_j", C.c_double)]
 
 
+class ExternalWrench(C.Structure):
+    _fields_ = [("source", C.c_char_p), ("nodes", C.POINTER(C.c_uint32)), ("node_count", C.c_uint64),
+                ("point_world_m", C.c_double * 3), ("force_n", C.c_double * 3), ("torque_n_m", C.c_double * 3)]
+
+
+def case_wrenches(case: dict) -> list:
+    """The wrenches a case carries (scenes.wrenches): (source, nodes, point,
+    force, torque) tuples in the caller's order."""
+    names = bytes(case["wrench_names"]).split(b"\0")
+    counts = case["wrench_node_count"]
+    nodes = case["wrench_nodes"]
+    vec = case["wrench_vectors"].reshape(-1, 9)
+    out, at = [], 0
+    for k, n in enumerate(counts):
+        out.append((names[k].decode(), nodes[at:at + int(n)], vec[k, 0:3], vec[k, 3:6], vec[k, 6:9]))
+        at += int(n)
+    return out
+
+
+def ledger_row(g: LoadLedger) -> list:
+    """A load ledger as the case files pack a source's (oracle/case_layout.hpp)."""
+    return ([float(g.steps), g.elapsed_s] + list(g.requested_impulse_n_s) + list(g.impulse_n_s) +
+            list(g.requested_angular_impulse_kg_m2_s) + list(g.angular_impulse_kg_m2_s) + [g.work_j])
+
+
 class BoxSpec(C.Structure):
     _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("horizon", C.c_uint32),
                 ("max_offset_sq", C.c_uint32), ("slabs", C.c_uint32), ("spacing", C.c_double),
@@ -218,6 +243,10 @@ def library() -> C.CDLL:
         "gbl_destroy": ([vp], None), "gbl_name": ([vp, C.c_char_p, C.c_size_t], C.c_int),
         "gbl_upload": ([vp, C.POINTER(StateView), C.POINTER(StepSettings), C.POINTER(Sphere)], C.c_int),
         "gbl_set_external_forces": ([vp, f64p, C.c_uint64, C.c_uint64], C.c_int),
+        "gbl_set_external_wrenches": ([vp, C.POINTER(ExternalWrench), C.c_uint64, C.c_uint64], C.c_int),
+        "gbl_external_source_count": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_external_source": ([vp, C.c_uint64, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t),
+                                 C.POINTER(LoadLedger)], C.c_int),
         "gbl_run": ([vp, C.POINTER(RunControlC), C.POINTER(RunStatus)], C.c_int),
         "gbl_status": ([vp, C.POINTER(RunStatus)], C.c_int),
         "gbl_download": ([vp, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
@@ -275,7 +304,8 @@ def library() -> C.CDLL:
                       ("gbl_run_control", RunControlC), ("gbl_run_status", RunStatus),
                       ("gbl_request_info", RequestInfo), ("gbl_server_stats", ServerStats),
                       ("gbl_box_spec", BoxSpec), ("gbl_node_contact_accumulators", NodeContactAccumulators),
-                      ("gbl_tuning", Tuning), ("gbl_impact_scene", ImpactScene)]:
+                      ("gbl_tuning", Tuning), ("gbl_impact_scene", ImpactScene),
+                      ("gbl_external_wrench", ExternalWrench), ("gbl_load_ledger", LoadLedger)]:
         if lib.gbl_struct_size(name.encode()) != C.sizeof(cls):
             raise RuntimeError(f"binding layout of {name} does not match libgbl.so")
     _lib = lib
@@ -607,6 +637,36 @@ class Backend:
         f = np.ascontiguousarray(forces, dtype=np.float64).reshape(-1)
         _call(library().gbl_set_external_forces, self._h, _ptr(f, C.c_double), f.size // 3, int(substeps))
 
+    def set_external_wrenches(self, wrenches, substeps: int) -> None:
+        """wrenches: (source, nodes, point, force, torque) tuples."""
+        keep = []
+        arr = (ExternalWrench * max(1, len(wrenches)))()
+        for k, (source, nodes, point, force, torque) in enumerate(wrenches):
+            idx = np.ascontiguousarray(nodes, dtype=np.uint32)
+            name = source.encode() if isinstance(source, str) else source
+            keep += [idx, name]
+            arr[k].source = name
+            arr[k].nodes = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+            arr[k].node_count = idx.size
+            arr[k].point_world_m[:] = [float(x) for x in point]
+            arr[k].force_n[:] = [float(x) for x in force]
+            arr[k].torque_n_m[:] = [float(x) for x in torque]
+        _call(library().gbl_set_external_wrenches, self._h, arr if wrenches else None, len(wrenches), int(substeps))
+
+    def external_sources(self) -> list:
+        """RunStatus::external_sources: (source, LoadLedger) in status order."""
+        n = C.c_uint64()
+        _call(library().gbl_external_source_count, self._h, C.byref(n))
+        out = []
+        for k in range(n.value):
+            length = C.c_size_t()
+            _call(library().gbl_external_source, self._h, k, None, 0, C.byref(length), None)
+            buf = C.create_string_buffer(length.value + 1)
+            g = LoadLedger()
+            _call(library().gbl_external_source, self._h, k, buf, len(buf), C.byref(length), C.byref(g))
+            out.append((buf.value.decode(), g))
+        return out
+
     def run(self, control: RunControl) -> RunStatus:
         st = RunStatus()
         ctl = control.c()
@@ -849,6 +909,8 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
     base = case.get("forces")
     if base is not None and not ramp:
         backend.set_external_forces(base, int(case["force_substeps"][0]))
+    if "wrench_names" in case:
+        backend.set_external_wrenches(case_wrenches(case), int(case["wrench_substeps"][0]))
     break_step = np.full(int(case["bond_count"][0]), NO_BOND, dtype=np.uint32)
     alive_before = state.alive.copy()
     chunk = 1 if per_substep else (per_step if ramp else steps)
@@ -876,6 +938,10 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
            "state_max_degree": np.array([state.view.max_degree], np.uint32)}
     out.update(sched.arrays())
     out.update(status_arrays(st))
+    sources = backend.external_sources()
+    if sources:
+        out["source_names"] = np.frombuffer(b"".join(n.encode() + b"\0" for n, _ in sources), dtype=np.uint8).copy()
+        out["source_ledgers"] = np.asarray([ledger_row(g) for _, g in sources], dtype=np.float64).reshape(-1)
     if per_substep:
         out["break_step"] = break_step
     return out

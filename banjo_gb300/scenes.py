@@ -336,6 +336,51 @@ def plate_strike(nx=24, nz=24, h=0.01, steps=40, radius=0.03, speed=8.0, median=
     return case
 
 
+def wrenches(case: dict, regions, substeps: int) -> dict:
+    """Adds external wrenches to a case (LatticeBackend::setExternalWrenches,
+    FastLattice.hpp:153-157, 278-288): `regions` holds (source name, node
+    indices, point, force, torque) per wrench, applied for `substeps`."""
+    names = bytearray()
+    counts, nodes, vectors = [], [], []
+    for source, idx, point, force, torque in regions:
+        names += source.encode() + b"\0"
+        idx = np.asarray(idx, dtype=np.uint32)
+        counts.append(idx.size)
+        nodes.append(idx)
+        vectors.append(np.concatenate([np.asarray(point, float), np.asarray(force, float), np.asarray(torque, float)]))
+    case = dict(case)
+    case["wrench_names"] = np.frombuffer(bytes(names), dtype=np.uint8).copy()
+    case["wrench_node_count"] = np.asarray(counts, dtype=np.uint32)
+    case["wrench_nodes"] = np.concatenate(nodes) if nodes else np.zeros(0, np.uint32)
+    case["wrench_vectors"] = np.concatenate(vectors) if vectors else np.zeros(0)
+    case["wrench_substeps"] = np.array([substeps], dtype=np.uint64)
+    return case
+
+
+def wrenched_bar(nx=16, ny=6, nz=6, h=0.01, steps=40, grip=(0.0, -4.0, 0.0), twist=(0.04, 0.0, 0.0),
+                 hand=(0.0, 0.0, 2.5)):
+    """A bar pinned at its x=0 face, no gravity, driven by two named wrenches:
+    "grip" on the free end face (a force and a twist about the bar's axis,
+    applied at the face's centre) and "hand" (a sideways push on the top row
+    at mid-length, no torque). Compliance 1e-7, tensile step at 2e-3. The
+    caller's node lists are given unsorted, as the reference sorts them."""
+    case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), 1e-7, [2e-3, 2e-3, INF, INF, INF, INF])
+    n = nx * ny * nz
+    i = np.arange(n)
+    x, y = i % nx, (i // nx) % ny
+    pos = case["ref_pos"].reshape(-1, 3)
+    end = np.flatnonzero(x == nx - 1)[::-1]
+    top = np.flatnonzero((y == ny - 1) & (np.abs(x - (nx - 1) / 2.0) < 1.0))
+    case.update({
+        "pinned": (x == 0).astype(np.uint8),
+        "settings": settings(gravity=(0.0, 0.0, 0.0)),
+        "steps": np.array([steps], dtype=np.uint64),
+        "substeps_per_step": np.array([1], dtype=np.uint64),
+    })
+    return wrenches(case, [("hand", top, pos[top].mean(axis=0), hand, (0.0, 0.0, 0.0)),
+                           ("grip", end, pos[end].mean(axis=0), grip, twist)], steps)
+
+
 def drop_trial(nx, ny, nz, compliance, break_strain, drop_height, h=0.01, steps=240, substeps=10):
     """One batched trial: a box released at rest `drop_height` above the ground."""
     case = _box_case(nx, ny, nz, h, (0.0, 0.0, 0.0), compliance, [break_strain, break_strain, INF, INF, INF, INF])

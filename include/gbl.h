@@ -264,6 +264,31 @@ gbl_result gbl_upload(gbl_backend *backend, const gbl_state_view *state, const g
  * node order; count 0 with substeps 0 cancels. */
 gbl_result gbl_set_external_forces(gbl_backend *backend, const double *forces_world_n, uint64_t count,
                                    uint64_t substeps);
+/* ExternalWrench (FastLattice.hpp:153-157): a named node region driven by a
+ * force and a torque about a world point. */
+typedef struct gbl_external_wrench {
+    const char *source;      /* NUL-terminated, nonempty, distinct per call */
+    const uint32_t *nodes;   /* node_count schedule node indices, any order */
+    uint64_t node_count;
+    double point_world_m[3], force_n[3], torque_n_m[3];
+} gbl_external_wrench;
+/* LatticeBackend::setExternalWrenches (FastLattice.hpp:278-288, the CPU rules
+ * of ExternalLoads.hpp:52-77 and 171-238): replaces any external load; each
+ * wrench is spread over its nodes by mass about their mass centre from the
+ * current geometry at every kick, for `substeps` substeps. count 0 with
+ * substeps 0 cancels. An invalid set leaves the previous load in place
+ * (GBL_INVALID_ARGUMENT). A run whose geometry a wrench can no longer carry
+ * stops before that kick with GBL_INVALID_ARGUMENT, as the reference throws. */
+gbl_result gbl_set_external_wrenches(gbl_backend *backend, const gbl_external_wrench *wrenches, uint64_t count,
+                                     uint64_t substeps);
+/* RunStatus::external_sources (FastLattice.hpp:191): the ledger of every
+ * wrench source kicked since upload, in the order of their first kick.
+ * gbl_external_source_count, then gbl_external_source for each index: the
+ * name (its full length in *name_length; at most name_capacity - 1 bytes and
+ * a NUL written) and its ledger. */
+gbl_result gbl_external_source_count(gbl_backend *backend, uint64_t *count);
+gbl_result gbl_external_source(gbl_backend *backend, uint64_t index, char *name, size_t name_capacity,
+                               size_t *name_length, gbl_load_ledger *load);
 /* LatticeBackend::run (FastLattice.hpp:360); the status accumulates across calls. */
 gbl_result gbl_run(gbl_backend *backend, const gbl_run_control *control, gbl_run_status *status_out);
 /* LatticeBackend::status (FastLattice.hpp:364). */

@@ -48,6 +48,15 @@ enum PlaneSlot : int {
 // center 3, velocity 3, angular velocity 3, radius, mass, inertia
 constexpr int kSphereWidth = 12;
 
+// External wrenches (FastLattice.hpp:153-157) in a case: `wrench_names` (each
+// name followed by a zero byte), `wrench_node_count` and the concatenated
+// `wrench_nodes`, `wrench_vectors` (point, force, torque per wrench) and
+// `wrench_substeps`. A run's source ledgers come back as `source_names` and
+// `source_ledgers`: steps, elapsed, requested impulse 3, impulse 3, requested
+// angular impulse 3, angular impulse 3, work per source, in status order.
+constexpr int kWrenchWidth = 9;
+constexpr int kSourceLedgerWidth = 15;
+
 // Status packing shared by every runner that reports a RunStatus.
 enum StatusU64Slot : int {
     kTotalSteps = 0,

@@ -17,6 +17,7 @@
 #include <functional>
 #include <limits>
 #include <mutex>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -1221,13 +1222,156 @@ struct Status {
     bool energy_audited{};
 };
 
-// External forces (ExternalLoads.hpp:28-50 set, 79-148 kick; forces only).
+// Double vector arithmetic of the load phase (core/Math.hpp:17-69).
+struct D3 { double x, y, z; };
+inline D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator*(double s, D3 a) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dotD(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 crossD(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double normD(D3 a) { return std::hypot(a.x, a.y, a.z); }
+inline bool finiteD(D3 a) { return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z); }
+
+// An external wrench (FastLattice.hpp:153-157) and a source's load ledger
+// (FastLattice.hpp:140-161).
+struct Wrench { std::string source; std::vector<std::uint32_t> nodes; D3 point, force, torque; };
+struct LoadLedger { double steps{}, elapsed{}; D3 req_imp{}, imp{}, req_ang{}, ang{}; double work{}; };
+struct SourceLedger { std::string source; LoadLedger load; };
+
+// External forces and wrenches (ExternalLoads.hpp:28-77 set/setWrenches,
+// 79-148 kick, 171-238 wrenchNodes). Forces keep the run ledger's work,
+// impulse and step count; wrench sources keep their own full ledgers.
 template <class R> struct Loads {
-    struct Node { std::uint32_t index; double req[3]; V<R> applied; };
+    static constexpr std::size_t kNoSource = ~std::size_t(0);
+    struct Node { std::uint32_t index; double req[3]; V<R> applied; std::size_t source = kNoSource; };
     std::vector<Node> nodes;
+    std::vector<Wrench> wrenches;
+    std::vector<SourceLedger> sources; // RunStatus::external_sources, in first-kick order
     std::uint64_t remaining{};
     double origin[3]{};
+
+    D3 where(const Lattice<R> &L, std::uint32_t i) const {
+        const V<R> p = add(ld(L.x0, i), ld(L.u, i));
+        return D3{origin[0], origin[1], origin[2]} + D3{double(p.x), double(p.y), double(p.z)};
+    }
+
+    // A wrench's force and torque over its nodes by mass, about their mass
+    // centre at the current positions (ExternalLoads.hpp:171-238).
+    std::vector<Node> wrenchNodes(const std::vector<Wrench> &ws, const Lattice<R> &L) const {
+        std::vector<Node> out;
+        for (std::size_t k = 0; k < ws.size(); ++k) {
+            const Wrench &w = ws[k];
+            double mass = 0;
+            std::vector<D3> points;
+            const V<R> a0 = add(ld(L.x0, w.nodes.front()), ld(L.u, w.nodes.front()));
+            const D3 anchor{double(a0.x), double(a0.y), double(a0.z)};
+            for (const auto node : w.nodes) {
+                if (!(L.mass[node] > 0) || !(L.inv_mass[node] > 0) || !std::isfinite(L.mass[node]) ||
+                    !std::isfinite(L.inv_mass[node]))
+                    throw std::invalid_argument("external wrench needs finite movable node masses");
+                const V<R> p = add(ld(L.x0, node), ld(L.u, node));
+                const D3 relative = D3{double(p.x), double(p.y), double(p.z)} - anchor;
+                if (!finiteD(relative)) throw std::invalid_argument("external wrench node position is not finite");
+                points.push_back(relative);
+                mass += static_cast<double>(L.mass[node]);
+            }
+            if (!(mass > 0) || !std::isfinite(mass)) throw std::invalid_argument("external wrench mass overflow");
+            D3 center{0, 0, 0};
+            for (std::size_t i = 0; i < points.size(); ++i)
+                center = center + (static_cast<double>(L.mass[w.nodes[i]]) / mass) * points[i];
+            double tensor[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (std::size_t i = 0; i < points.size(); ++i) {
+                points[i] = points[i] - center;
+                const double r[3] = {points[i].x, points[i].y, points[i].z};
+                const double share = static_cast<double>(L.mass[w.nodes[i]]) / mass;
+                for (unsigned a = 0; a < 3; ++a)
+                    for (unsigned b = 0; b < 3; ++b)
+                        tensor[3 * a + b] += share * (a == b ? r[(a + 1) % 3] * r[(a + 1) % 3] + r[(a + 2) % 3] * r[(a + 2) % 3]
+                                                             : -r[a] * r[b]);
+            }
+            const D3 moment = w.torque + crossD(((w.point - D3{origin[0], origin[1], origin[2]}) - anchor) - center, w.force);
+            if (!finiteD(center) || !finiteD(moment)) throw std::invalid_argument("external wrench moment overflow");
+            double scale = 0;
+            for (const double e : tensor) {
+                if (!std::isfinite(e)) throw std::invalid_argument("external wrench inertia overflow");
+                scale = std::max(scale, std::abs(e));
+            }
+            D3 alpha{0, 0, 0};
+            if (scale > 0) {
+                for (double &e : tensor) e /= scale;
+                double eig[3], axes[9];
+                eigen3(tensor, eig, axes);
+                const double largest = std::max({std::abs(eig[0]), std::abs(eig[1]), std::abs(eig[2])});
+                D3 unresolved = moment;
+                for (unsigned axis = 0; axis < 3; ++axis) {
+                    if (!(eig[axis] > 1e-10 * largest)) continue;
+                    const D3 dir{axes[axis], axes[3 + axis], axes[6 + axis]};
+                    const double component = dotD(dir, moment);
+                    unresolved = unresolved - component * dir;
+                    alpha = alpha + (component / mass / scale / eig[axis]) * dir;
+                }
+                if (normD(unresolved) > 1024 * std::numeric_limits<double>::epsilon() * normD(moment))
+                    throw std::invalid_argument("external wrench torque is not represented by these nodes");
+            } else if (normD(moment) > 0) {
+                throw std::invalid_argument("external wrench torque needs a sampled lever arm");
+            }
+            if (!finiteD(alpha)) throw std::invalid_argument("external wrench acceleration overflow");
+            D3 force_sum{0, 0, 0}, moment_sum{0, 0, 0};
+            double absolute_force = 0, absolute_moment = 0;
+            for (std::size_t i = 0; i < points.size(); ++i) {
+                const double m = static_cast<double>(L.mass[w.nodes[i]]);
+                const D3 f = (m / mass) * w.force + m * crossD(alpha, points[i]);
+                const V<R> conv{static_cast<R>(f.x), static_cast<R>(f.y), static_cast<R>(f.z)};
+                if (!finiteD(f) || !std::isfinite(conv.x) || !std::isfinite(conv.y) || !std::isfinite(conv.z))
+                    throw std::invalid_argument("external wrench node force exceeds backend precision");
+                out.push_back({w.nodes[i], {f.x, f.y, f.z}, conv, k});
+                force_sum = force_sum + f;
+                moment_sum = moment_sum + crossD(points[i], f);
+                absolute_force += normD(f);
+                absolute_moment += normD(crossD(points[i], f));
+            }
+            if (!finiteD(force_sum) || !finiteD(moment_sum) || !std::isfinite(absolute_force) ||
+                !std::isfinite(absolute_moment) ||
+                normD(force_sum - w.force) > 1e-10 * std::max(normD(w.force), absolute_force) ||
+                normD(moment_sum - moment) > 1e-10 * std::max(normD(moment), absolute_moment))
+                throw std::invalid_argument("external wrench resultant cannot be represented accurately");
+        }
+        return out;
+    }
+
+    void setWrenches(const std::vector<Wrench> &ws, std::uint64_t substeps, const Lattice<R> &L) {
+        if (ws.empty()) {
+            if (substeps != 0) throw std::invalid_argument("empty external load needs zero substeps");
+            nodes.clear(); wrenches.clear(); remaining = 0; return;
+        }
+        if (!substeps) throw std::invalid_argument("external wrench needs a finite nonzero span");
+        std::vector<Wrench> staged = ws;
+        std::set<std::string> names;
+        std::set<std::uint32_t> used;
+        for (Wrench &w : staged) {
+            if (w.source.empty() || !names.insert(w.source).second || w.nodes.empty())
+                throw std::invalid_argument("external wrench needs distinct named nonempty regions");
+            if (!finiteD(w.point) || !finiteD(w.force) || !finiteD(w.torque) || !std::isfinite(normD(w.force)) ||
+                !std::isfinite(normD(w.torque)))
+                throw std::invalid_argument("external wrench must be finite");
+            std::sort(w.nodes.begin(), w.nodes.end());
+            for (const auto node : w.nodes)
+                if (node >= L.N || !used.insert(node).second)
+                    throw std::invalid_argument("external wrench nodes repeat, overlap or exceed the lattice");
+        }
+        std::sort(staged.begin(), staged.end(), [](const Wrench &a, const Wrench &b) { return a.source < b.source; });
+        staged.erase(std::remove_if(staged.begin(), staged.end(), [](const Wrench &w) {
+            return w.force.x == 0 && w.force.y == 0 && w.force.z == 0 && w.torque.x == 0 && w.torque.y == 0 &&
+                   w.torque.z == 0;
+        }), staged.end());
+        auto staged_nodes = wrenchNodes(staged, L);
+        nodes = std::move(staged_nodes);
+        wrenches = std::move(staged);
+        remaining = nodes.empty() ? 0 : substeps;
+    }
+
     void set(const std::vector<double> &f, std::uint64_t substeps, const Lattice<R> &L) {
+        wrenches.clear();
         if (f.empty()) { nodes.clear(); remaining = 0; return; }
         if (f.size() != 3 * static_cast<std::size_t>(L.N) || substeps == 0)
             throw std::invalid_argument("external load needs one force per node and a finite nonzero span");
@@ -1248,7 +1392,11 @@ template <class R> struct Loads {
     }
     void kick(Lattice<R> &L, R dt, Status &st_) {
         if (!remaining) return;
+        if (!wrenches.empty()) nodes = wrenchNodes(wrenches, L); // the current geometry
         double work = 0, imp[3] = {0, 0, 0};
+        const double dtd = static_cast<double>(dt);
+        std::vector<LoadLedger> change(wrenches.size());
+        for (auto &c : change) { c.steps = 1; c.elapsed = dtd; }
         std::vector<V<R>> after(nodes.size());
         for (std::size_t k = 0; k < nodes.size(); ++k) {
             const Node &n = nodes[k];
@@ -1262,7 +1410,33 @@ template <class R> struct Loads {
             double ii[3];
             for (int q = 0; q < 3; ++q) ii[q] = m * (nxt[q] - old[q]);
             for (int q = 0; q < 3; ++q) imp[q] += ii[q];
-            work += ii[0] * (.5 * (old[0] + nxt[0])) + ii[1] * (.5 * (old[1] + nxt[1])) + ii[2] * (.5 * (old[2] + nxt[2]));
+            const double wk = ii[0] * (.5 * (old[0] + nxt[0])) + ii[1] * (.5 * (old[1] + nxt[1])) + ii[2] * (.5 * (old[2] + nxt[2]));
+            work += wk;
+            if (n.source != kNoSource) {
+                LoadLedger &c = change[n.source];
+                const D3 at = where(L, n.index);
+                const D3 rq = dtd * D3{n.req[0], n.req[1], n.req[2]};
+                const D3 im{ii[0], ii[1], ii[2]};
+                c.req_imp = c.req_imp + rq;
+                c.req_ang = c.req_ang + crossD(at, rq);
+                c.imp = c.imp + im;
+                c.ang = c.ang + crossD(at, im);
+                c.work += wk;
+            }
+        }
+        for (std::size_t k = 0; k < wrenches.size(); ++k) {
+            auto found = std::find_if(sources.begin(), sources.end(),
+                                      [&](const SourceLedger &s) { return s.source == wrenches[k].source; });
+            if (found == sources.end()) {
+                sources.push_back({wrenches[k].source, LoadLedger{}});
+                found = sources.end() - 1;
+            }
+            LoadLedger &t = found->load;
+            const LoadLedger &c = change[k];
+            t.steps = t.steps + c.steps; t.elapsed = t.elapsed + c.elapsed;
+            t.req_imp = t.req_imp + c.req_imp; t.imp = t.imp + c.imp;
+            t.req_ang = t.req_ang + c.req_ang; t.ang = t.ang + c.ang;
+            t.work = t.work + c.work;
         }
         for (std::size_t k = 0; k < nodes.size(); ++k) st(L.v, nodes[k].index, after[k]);
         st_.ext_steps += 1;
@@ -1487,6 +1661,29 @@ template <class R> std::vector<double> widen(const std::vector<R> &v) {
     return std::vector<double>(v.begin(), v.end());
 }
 
+// The wrenches of a case file (case_layout.hpp).
+inline std::vector<Wrench> unpackWrenches(const lsio::Case &c) {
+    const auto names = c.get<std::uint8_t>("wrench_names");
+    const auto counts = c.get<std::uint32_t>("wrench_node_count");
+    const auto nodes = c.get<std::uint32_t>("wrench_nodes");
+    const auto vec = c.get<double>("wrench_vectors");
+    std::vector<Wrench> out(counts.size());
+    std::size_t at = 0, node = 0;
+    for (std::size_t k = 0; k < out.size(); ++k) {
+        Wrench &w = out[k];
+        while (at < names.size() && names[at] != 0) w.source.push_back(static_cast<char>(names[at++]));
+        ++at;
+        w.nodes.assign(nodes.begin() + static_cast<std::ptrdiff_t>(node),
+                       nodes.begin() + static_cast<std::ptrdiff_t>(node + counts[k]));
+        node += counts[k];
+        const double *v = vec.data() + lsio::kWrenchWidth * k;
+        w.point = {v[0], v[1], v[2]};
+        w.force = {v[3], v[4], v[5]};
+        w.torque = {v[6], v[7], v[8]};
+    }
+    return out;
+}
+
 template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned threads, bool per_substep) {
     const auto N = c.scalar<std::uint32_t>("node_count");
     const Schedule s = buildSchedule(N, c.get<std::uint32_t>("bond_a"), c.get<std::uint32_t>("bond_b"),
@@ -1508,10 +1705,15 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     const std::uint64_t per_step = c.scalarOr<std::uint64_t>("substeps_per_step", 1);
     const bool ramp = c.has("force_ramp_steps");
     std::vector<double> base;
+    if (c.has("origin")) {
+        const auto o = c.get<double>("origin");
+        for (int q = 0; q < 3; ++q) run.loads.origin[q] = o[q];
+    }
     if (c.has("forces")) {
         base = c.get<double>("forces");
         if (!ramp) run.loads.set(base, c.scalar<std::uint64_t>("force_substeps"), L);
     }
+    if (c.has("wrench_names")) run.loads.setWrenches(unpackWrenches(c), c.scalar<std::uint64_t>("wrench_substeps"), L);
     std::vector<std::uint32_t> break_step(L.B, 0xffffffffU);
     std::vector<std::uint8_t> alive_before = L.alive;
     const std::uint64_t chunk = per_substep ? 1 : (ramp ? per_step : steps);
@@ -1573,6 +1775,21 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     u[lsio::kEnergyAudited] = st_.energy_audited ? 1 : 0;
     out.put("status_u64", u);
     out.put("status_f64", d);
+    if (!run.loads.sources.empty()) {
+        std::vector<std::uint8_t> names;
+        std::vector<double> ledgers;
+        for (const SourceLedger &sl : run.loads.sources) {
+            names.insert(names.end(), sl.source.begin(), sl.source.end());
+            names.push_back(0);
+            const LoadLedger &g = sl.load;
+            const double row[lsio::kSourceLedgerWidth] = {g.steps, g.elapsed, g.req_imp.x, g.req_imp.y, g.req_imp.z,
+                                                    g.imp.x, g.imp.y, g.imp.z, g.req_ang.x, g.req_ang.y, g.req_ang.z,
+                                                    g.ang.x, g.ang.y, g.ang.z, g.work};
+            ledgers.insert(ledgers.end(), row, row + lsio::kSourceLedgerWidth);
+        }
+        out.put("source_names", names);
+        out.put("source_ledgers", ledgers);
+    }
     out.putScalar<double>("wall_seconds", wall);
     out.putScalar<std::uint32_t>("threads", threads);
     out.put("substep_seconds", run.substep_seconds);

@@ -9,7 +9,7 @@
 //   buildLatticeState         src/fastlattice/FastLattice.cpp:47
 //   makeCpuLatticeBackend     src/fastlattice/CpuLatticeBackend.cpp:569
 //   makeParallelCpuLatticeBackend (ParallelCpuLatticeBackend.cpp:2015)
-//   LatticeBackend::upload/setExternalForces/run/download (FastLattice.hpp:255-369)
+//   LatticeBackend::upload/setExternalForces/setExternalWrenches/run/download (FastLattice.hpp:255-369)
 // and writes the schedule, the final state and the RunStatus to an output case.
 //
 // usage: ref_harness <case> <out> [float|double] [serial|parallel] [threads] [--per-substep]
@@ -165,6 +165,47 @@ void packStatus(lsio::Case &out, const RunStatus &st) {
     d[lsio::kStrikerDissipated] = st.striker_dissipated_j;
     out.put("status_u64", u);
     out.put("status_f64", d);
+    if (!st.external_sources.empty()) {
+        std::vector<std::uint8_t> names;
+        std::vector<double> ledgers;
+        for (const ExternalWrenchLedger &sl : st.external_sources) {
+            names.insert(names.end(), sl.source.begin(), sl.source.end());
+            names.push_back(0);
+            const ExternalLoadLedger &g = sl.load;
+            const double row[lsio::kSourceLedgerWidth] = {
+                static_cast<double>(g.steps), g.elapsed_s, g.requested_impulse_n_s.x, g.requested_impulse_n_s.y,
+                g.requested_impulse_n_s.z, g.impulse_n_s.x, g.impulse_n_s.y, g.impulse_n_s.z,
+                g.requested_angular_impulse_kg_m2_s.x, g.requested_angular_impulse_kg_m2_s.y,
+                g.requested_angular_impulse_kg_m2_s.z, g.angular_impulse_kg_m2_s.x, g.angular_impulse_kg_m2_s.y,
+                g.angular_impulse_kg_m2_s.z, g.work_j};
+            ledgers.insert(ledgers.end(), row, row + lsio::kSourceLedgerWidth);
+        }
+        out.put("source_names", names);
+        out.put("source_ledgers", ledgers);
+    }
+}
+
+// The wrenches of a case file (case_layout.hpp).
+std::vector<ExternalWrench> unpackWrenches(const lsio::Case &c) {
+    const auto names = c.get<std::uint8_t>("wrench_names");
+    const auto counts = c.get<std::uint32_t>("wrench_node_count");
+    const auto nodes = c.get<std::uint32_t>("wrench_nodes");
+    const auto vec = c.get<double>("wrench_vectors");
+    std::vector<ExternalWrench> out(counts.size());
+    std::size_t at = 0, node = 0;
+    for (std::size_t k = 0; k < out.size(); ++k) {
+        ExternalWrench &w = out[k];
+        while (at < names.size() && names[at] != 0) w.source.push_back(static_cast<char>(names[at++]));
+        ++at;
+        w.nodes.assign(nodes.begin() + static_cast<std::ptrdiff_t>(node),
+                       nodes.begin() + static_cast<std::ptrdiff_t>(node + counts[k]));
+        node += counts[k];
+        const double *v = vec.data() + lsio::kWrenchWidth * k;
+        w.point_world_m = {v[0], v[1], v[2]};
+        w.force_n = {v[3], v[4], v[5]};
+        w.torque_n_m = {v[6], v[7], v[8]};
+    }
+    return out;
 }
 
 struct Built {
@@ -319,6 +360,7 @@ int main(int argc, char **argv) {
             for (std::uint32_t i = 0; i < state.node_count; ++i) base[i] = Vec3{f[3 * i], f[3 * i + 1], f[3 * i + 2]};
             if (!ramp) backend->setExternalForces(base, c.scalar<std::uint64_t>("force_substeps"));
         }
+        if (c.has("wrench_names")) backend->setExternalWrenches(unpackWrenches(c), c.scalar<std::uint64_t>("wrench_substeps"));
         std::vector<std::uint32_t> break_step(state.bond_count, std::numeric_limits<std::uint32_t>::max());
         std::vector<std::uint8_t> alive_before = state.alive;
         LatticeState scratch = state;

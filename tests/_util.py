@@ -11,7 +11,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # Outputs held bit for bit between runners (status excludes wall time and the
 # launch count, which differ by construction).
 STATE_KEYS = ["u", "u_prev", "v", "alive", "failure_mode", "damage", "plastic_extension", "plastic_strain",
-              "prev_tensile", "prev_compressive", "prev_shear", "sphere_out", "first_failure_bonds"]
+              "prev_tensile", "prev_compressive", "prev_shear", "sphere_out", "first_failure_bonds", "source_names",
+              "source_ledgers"]
 SCHEDULE_KEYS = ["sched_bond_order", "sched_color", "sched_range_begin", "sched_range_end",
                  "sched_bond_block_begin", "sched_color_count", "sched_boundary_bond_count"]
 STATUS_U64 = {"total_steps": 0, "first_failure_step": 1, "last_failure_step": 2, "failure_rounds": 3,

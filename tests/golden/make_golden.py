@@ -77,6 +77,11 @@ def cases() -> dict:
         audited["settings"][scenes.K_DAMP] = 0.05
         audited["settings"][scenes.K_AUDIT] = 1.0
         out[name] = (audited, precision)
+    # External wrenches: a pinned bar twisted and pushed by two named sources,
+    # each spread over its nodes from the current geometry at every kick and
+    # keeping its own ledger; breaking from substep 9.
+    out["wrench_bar"] = (scenes.wrenched_bar(), "float")
+    out["wrench_bar_double"] = (scenes.wrenched_bar(steps=20), "double")
     # Caps: a slab with more sphere candidates than a slab's list holds
     # (1024), and node contact with more pairs per owner than its slots (24).
     out["candidate_overflow"] = (scenes.impact_block(nx=40, ny=4, nz=40, blocks=1, radius=0.4, speed=6.0, steps=1,
