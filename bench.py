@@ -573,6 +573,10 @@ def run_gb300(args) -> None:
                      "peak_kind": peak_kind, "kernel": "kSolve (projection sweep)",
                      "sweep_ms_per_substep": sweep_ms, "whole_substep_gbs": total_gbs,
                      "whole_substep_frac": total_gbs / peak},
+        # The reference scene's own rate, bonds x substeps / time
+        # (TileImpactScene.cpp:867-868), over the same device and e2e windows.
+        "bond_updates_per_s": {"device": world * b * substeps_k / device_s_max,
+                               "e2e": world * b * substeps_k / e2e_s_max},
         "gpu_launches": launches * substeps_k,
         "clocks": clocks,
         "host_seconds": host_s,
