@@ -1029,24 +1029,25 @@ template <class R> struct Resident {
             descs.push_back(d);
         }
         if (!descs.empty()) {
-            // The spread at the current geometry, checked on the device.
-            WrenchDev *wd = nullptr;
-            std::uint32_t *ld = nullptr;
-            unsigned *verdict = nullptr;
-            check(cudaMalloc(&wd, sizeof(WrenchDev) * descs.size()), "device allocation");
-            check(cudaMalloc(&ld, sizeof(std::uint32_t) * list.size()), "device allocation");
-            check(cudaMalloc(&verdict, sizeof(unsigned)), "device allocation");
-            gbl::upload(wd, descs, stream);
-            gbl::upload(ld, list, stream);
-            check(cudaMemsetAsync(verdict, 0, sizeof(unsigned), stream), "clear");
-            kWrench<R><<<static_cast<unsigned>(descs.size()), kWrenchThreads, 0, stream>>>(dev, wd, ld, verdict, 0);
+            // The spread at the current geometry, checked on the device (in
+            // buffers of its own: the load in place stays untouched).
+            struct Temp {
+                void *p = nullptr;
+                ~Temp() { if (p) cudaFree(p); }
+            } wd, ld, verdict;
+            check(cudaMalloc(&wd.p, sizeof(WrenchDev) * descs.size()), "device allocation");
+            check(cudaMalloc(&ld.p, sizeof(std::uint32_t) * list.size()), "device allocation");
+            check(cudaMalloc(&verdict.p, sizeof(unsigned)), "device allocation");
+            gbl::upload(static_cast<WrenchDev *>(wd.p), descs, stream);
+            gbl::upload(static_cast<std::uint32_t *>(ld.p), list, stream);
+            check(cudaMemsetAsync(verdict.p, 0, sizeof(unsigned), stream), "clear");
+            kWrench<R><<<static_cast<unsigned>(descs.size()), kWrenchThreads, 0, stream>>>(
+                dev, static_cast<const WrenchDev *>(wd.p), static_cast<const std::uint32_t *>(ld.p),
+                static_cast<unsigned *>(verdict.p), 0);
             check(cudaGetLastError(), "kernel launch");
             unsigned bad = 0;
-            check(cudaMemcpyAsync(&bad, verdict, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
+            check(cudaMemcpyAsync(&bad, verdict.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");
             check(cudaStreamSynchronize(stream), "external wrench");
-            cudaFree(wd);
-            cudaFree(ld);
-            cudaFree(verdict);
             if (bad)
                 invalid("external wrench cannot be spread over its nodes at the current geometry (torque, "
                         "resultant or node force not representable)");
