@@ -916,11 +916,21 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
     chunk = 1 if per_substep else (per_step if ramp else steps)
     done = 0
     st = None
+    resume_at = int(case["checkpoint_at"][0]) if "checkpoint_at" in case else 0
     while done < steps:
         if ramp and done % per_step == 0:
             scale = float(case["force_ramp_scale"][0]) * (done // per_step) / float(case["force_ramp_steps"][0])
             backend.set_external_forces(scale * base, per_step)
         nsteps = min(chunk, steps - done)
+        if resume_at:
+            if done < resume_at:
+                nsteps = min(nsteps, resume_at - done)
+            elif done == resume_at:
+                # Checkpoint and resume: the state downloaded, uploaded into a
+                # fresh backend, the run carried on (FastLattice.hpp:359-361).
+                sp = backend.download(state)
+                backend = make_gb300_lattice_backend(sched, precision, threads_per_block)
+                backend.upload(state, settings, sp)
         st = backend.run(RunControl(max_steps=nsteps))
         done += nsteps
         if per_substep:

@@ -381,6 +381,19 @@ int main(int argc, char **argv) {
             }
             RunControl control{};
             control.max_steps = std::min(chunk, steps - done);
+            if (c.has("checkpoint_at")) {
+                // Checkpoint and resume: download the state, upload it into
+                // a fresh backend (FastLattice.hpp:359-361), carry on.
+                const std::uint64_t at = c.scalar<std::uint64_t>("checkpoint_at");
+                if (done < at) control.max_steps = std::min(control.max_steps, at - done);
+                if (done == at && at != 0) {
+                    backend->download(state, sphere);
+                    backend = parallel ? makeParallelCpuLatticeBackend(schedule, precision,
+                                                                        threads == 0 ? availableCpuCount() : threads)
+                                       : makeCpuLatticeBackend(schedule, precision);
+                    backend->upload(state, settings, sphere);
+                }
+            }
             status = backend->run(control);
             done += control.max_steps;
             if (per_substep) {

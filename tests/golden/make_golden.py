@@ -82,6 +82,17 @@ def cases() -> dict:
     # keeping its own ledger; breaking from substep 9.
     out["wrench_bar"] = (scenes.wrenched_bar(), "float")
     out["wrench_bar_double"] = (scenes.wrenched_bar(steps=20), "double")
+    # Checkpoint and resume: the run downloaded mid-way (after failures, with
+    # damage, plastic flow and contact under way) and uploaded into a fresh
+    # backend, which starts afresh from the state as the reference's upload
+    # does (the resumed run is not the uninterrupted one).
+    resumed = scenes.impact_block(nx=16, ny=10, nz=12, blocks=4, radius=0.03, speed=12.0, steps=30, seed_point=5,
+                                  seed_strength=21)
+    resumed["checkpoint_at"] = np.array([11], dtype=np.uint64)
+    out["resume_impact"] = (resumed, "float")
+    resumed = scenes.contact_drop()
+    resumed["checkpoint_at"] = np.array([10], dtype=np.uint64)
+    out["resume_contact_drop"] = (resumed, "float")
     # Caps: a slab with more sphere candidates than a slab's list holds
     # (1024), and node contact with more pairs per owner than its slots (24).
     out["candidate_overflow"] = (scenes.impact_block(nx=40, ny=4, nz=40, blocks=1, radius=0.4, speed=6.0, steps=1,
