@@ -57,3 +57,19 @@ def test_trial_parameters_ranges():
     assert s.min() >= 1e-3 and s.max() <= 5e-3
     assert h.min() >= 0.1 and h.max() <= 1.0
     assert abs(np.mean(e) - 28) < 0.6
+
+
+def test_wrench_case_round_trip():
+    """A case's wrenches unpack as they were packed (the layout every runner
+    reads: names with a zero byte after each, counts, nodes, 9 numbers each)."""
+    from banjo_gb300 import lattice, scenes
+
+    case = scenes.wrenched_bar(nx=8, ny=4, nz=4, steps=5)
+    got = lattice.case_wrenches(case)
+    assert [w[0] for w in got] == ["hand", "grip"]
+    assert int(case["wrench_substeps"][0]) == 5
+    grip = got[1]
+    i = np.asarray(grip[1])
+    assert np.all(i % 8 == 7) and list(i) == sorted(i, reverse=True)  # the end face, given unsorted
+    assert np.allclose(grip[3], (0.0, -4.0, 0.0)) and np.allclose(grip[4], (0.04, 0.0, 0.0))
+    assert case["wrench_vectors"].size == 18 and case["wrench_nodes"].size == sum(len(w[1]) for w in got)
