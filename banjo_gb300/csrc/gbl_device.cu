@@ -1414,12 +1414,11 @@ public:
         }
     }
 
-    // External wrenches, on a lattice stepped alone (the wrench launch is part
-    // of the single-lattice substep).
+    // External wrenches on lattice k (its spread is launched for it alone,
+    // before the shared kick).
     void setExternalWrenches(std::size_t k, const gbl_external_wrench *ws, std::uint64_t count,
                              std::uint64_t substeps) {
         requireReady();
-        if (many_) invalid("external wrenches drive a lattice stepped alone");
         Resident<R> &l = lattice(k);
         const void *before[3] = {l.ext_force, l.wrench_dev, l.source_dev};
         l.setExternalWrenches(ws, count, substeps, stream_);
@@ -2049,9 +2048,10 @@ private:
         // without, before the kick.
         const bool side_restart = S.sphere_enabled != 0;
         if (!side_restart) restartPhase<M>(st, 0, mark);
-        if (!M && slots_[one_]->wrench_cap) {
-            const Resident<R> &l = *slots_[one_];
-            kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr, 1);
+        for (auto k : active_) {
+            const Resident<R> &l = *slots_[k];
+            if (l.wrench_cap)
+                kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr, 1);
         }
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
         if (S.sphere_enabled && slabs_.count) {
@@ -2388,6 +2388,9 @@ public:
     virtual std::size_t add(const Schedule &s, const gbl_state_view &st, const gbl_sphere &sp) = 0;
     virtual void settle(const gbl_step_settings &set) = 0;
     virtual void setExternalForces(std::size_t k, const double *f, std::uint64_t n, std::uint64_t substeps) = 0;
+    virtual void setExternalWrenches(std::size_t k, const gbl_external_wrench *ws, std::uint64_t count,
+                                     std::uint64_t substeps) = 0;
+    virtual std::vector<std::pair<std::string, LoadLedger>> sources(std::size_t k) = 0;
     virtual void run(const gbl_run_control &c) = 0;
     virtual void download(std::size_t k, gbl_state_view &st, gbl_sphere *sp) = 0;
     virtual const gbl_run_status &status(std::size_t k) = 0;
@@ -2408,6 +2411,13 @@ public:
     void settle(const gbl_step_settings &set) override { engine_.settle(set); }
     void setExternalForces(std::size_t k, const double *f, std::uint64_t n, std::uint64_t substeps) override {
         engine_.setExternalForces(k, f, n, substeps);
+    }
+    void setExternalWrenches(std::size_t k, const gbl_external_wrench *ws, std::uint64_t count,
+                             std::uint64_t substeps) override {
+        engine_.setExternalWrenches(k, ws, count, substeps);
+    }
+    std::vector<std::pair<std::string, LoadLedger>> sources(std::size_t k) override {
+        return engine_.lattice(k).sources();
     }
     void run(const gbl_run_control &c) override { engine_.run(c); }
     void download(std::size_t k, gbl_state_view &st, gbl_sphere *sp) override { engine_.download(k, st, sp); }
@@ -2782,30 +2792,37 @@ gbl_result gbl_external_source_count(gbl_backend *backend, uint64_t *count) {
     });
 }
 
+namespace gbl {
+// One entry of RunStatus::external_sources, out through the C ABI.
+void sourceOut(const std::vector<std::pair<std::string, LoadLedger>> &all, uint64_t index, char *name,
+               size_t name_capacity, size_t *name_length, gbl_load_ledger *load) {
+    if (index >= all.size()) invalid("no external source at that index");
+    const auto &[source, g] = all[index];
+    if (name_length) *name_length = source.size();
+    if (name && name_capacity) {
+        const std::size_t n = std::min(source.size(), name_capacity - 1);
+        std::memcpy(name, source.data(), n);
+        name[n] = 0;
+    }
+    if (load) {
+        load->steps = g.steps;
+        load->elapsed_s = g.elapsed;
+        for (int q = 0; q < 3; ++q) {
+            load->requested_impulse_n_s[q] = g.req_imp[q];
+            load->impulse_n_s[q] = g.imp[q];
+            load->requested_angular_impulse_kg_m2_s[q] = g.req_ang[q];
+            load->angular_impulse_kg_m2_s[q] = g.ang[q];
+        }
+        load->work_j = g.work;
+    }
+}
+} // namespace gbl
+
 gbl_result gbl_external_source(gbl_backend *backend, uint64_t index, char *name, size_t name_capacity,
                                size_t *name_length, gbl_load_ledger *load) {
     return gbl::guard([&] {
         if (!backend) gbl::invalid("null backend");
-        const auto all = backend->impl->sources();
-        if (index >= all.size()) gbl::invalid("no external source at that index");
-        const auto &[source, g] = all[index];
-        if (name_length) *name_length = source.size();
-        if (name && name_capacity) {
-            const std::size_t n = std::min(source.size(), name_capacity - 1);
-            std::memcpy(name, source.data(), n);
-            name[n] = 0;
-        }
-        if (load) {
-            load->steps = g.steps;
-            load->elapsed_s = g.elapsed;
-            for (int q = 0; q < 3; ++q) {
-                load->requested_impulse_n_s[q] = g.req_imp[q];
-                load->impulse_n_s[q] = g.imp[q];
-                load->requested_angular_impulse_kg_m2_s[q] = g.req_ang[q];
-                load->angular_impulse_kg_m2_s[q] = g.ang[q];
-            }
-            load->work_j = g.work;
-        }
+        gbl::sourceOut(backend->impl->sources(), index, name, name_capacity, name_length, load);
     });
 }
 
@@ -2926,6 +2943,29 @@ gbl_result gbl_batch_set_external_forces(gbl_batch *batch, uint32_t index, const
     return gbl::guard([&] {
         if (!batch) gbl::invalid("null batch");
         batch->impl->setExternalForces(index, forces, count, substeps);
+    });
+}
+
+gbl_result gbl_batch_set_external_wrenches(gbl_batch *batch, uint32_t index, const gbl_external_wrench *wrenches,
+                                           uint64_t count, uint64_t substeps) {
+    return gbl::guard([&] {
+        if (!batch) gbl::invalid("null batch");
+        batch->impl->setExternalWrenches(index, wrenches, count, substeps);
+    });
+}
+
+gbl_result gbl_batch_external_source_count(gbl_batch *batch, uint32_t index, uint64_t *count) {
+    return gbl::guard([&] {
+        if (!batch || !count) gbl::invalid("null argument");
+        *count = batch->impl->sources(index).size();
+    });
+}
+
+gbl_result gbl_batch_external_source(gbl_batch *batch, uint32_t index, uint64_t source, char *name,
+                                     size_t name_capacity, size_t *name_length, gbl_load_ledger *load) {
+    return gbl::guard([&] {
+        if (!batch) gbl::invalid("null batch");
+        gbl::sourceOut(batch->impl->sources(index), source, name, name_capacity, name_length, load);
     });
 }
 

@@ -144,6 +144,42 @@ def ledger_row(g: LoadLedger) -> list:
             list(g.requested_angular_impulse_kg_m2_s) + list(g.angular_impulse_kg_m2_s) + [g.work_j])
 
 
+def _wrench_array(wrenches):
+    """The C array of (source, nodes, point, force, torque) tuples, and the
+    buffers it points into (kept alive by the caller for the call)."""
+    keep = []
+    arr = (ExternalWrench * max(1, len(wrenches)))()
+    for k, (source, nodes, point, force, torque) in enumerate(wrenches):
+        idx = np.ascontiguousarray(nodes, dtype=np.uint32)
+        name = source.encode() if isinstance(source, str) else source
+        keep += [idx, name]
+        arr[k].source = name
+        arr[k].nodes = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+        arr[k].node_count = idx.size
+        arr[k].point_world_m[:] = [float(x) for x in point]
+        arr[k].force_n[:] = [float(x) for x in force]
+        arr[k].torque_n_m[:] = [float(x) for x in torque]
+    return arr, keep
+
+
+def _source(fn, *lead):
+    """One (source, LoadLedger) through a gbl_*external_source entry point."""
+    length = C.c_size_t()
+    _call(fn, *lead, None, 0, C.byref(length), None)
+    buf = C.create_string_buffer(length.value + 1)
+    g = LoadLedger()
+    _call(fn, *lead, buf, len(buf), C.byref(length), C.byref(g))
+    return buf.value.decode(), g
+
+
+def source_arrays(sources: list) -> dict:
+    """Source ledgers packed as the case files pack them (empty: no keys)."""
+    if not sources:
+        return {}
+    return {"source_names": np.frombuffer(b"".join(n.encode() + b"\0" for n, _ in sources), dtype=np.uint8).copy(),
+            "source_ledgers": np.asarray([ledger_row(g) for _, g in sources], dtype=np.float64).reshape(-1)}
+
+
 class BoxSpec(C.Structure):
     _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("horizon", C.c_uint32),
                 ("max_offset_sq", C.c_uint32), ("slabs", C.c_uint32), ("spacing", C.c_double),
@@ -267,6 +303,11 @@ def library() -> C.CDLL:
         "gbl_batch_settle": ([vp, C.POINTER(StepSettings)], C.c_int),
         "gbl_batch_set_external_forces": ([vp, C.c_uint32, f64p, C.c_uint64, C.c_uint64], C.c_int),
         "gbl_batch_run": ([vp, C.POINTER(RunControlC)], C.c_int),
+        "gbl_batch_set_external_wrenches": ([vp, C.c_uint32, C.POINTER(ExternalWrench), C.c_uint64, C.c_uint64],
+                                            C.c_int),
+        "gbl_batch_external_source_count": ([vp, C.c_uint32, C.POINTER(C.c_uint64)], C.c_int),
+        "gbl_batch_external_source": ([vp, C.c_uint32, C.c_uint64, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t),
+                                       C.POINTER(LoadLedger)], C.c_int),
         "gbl_batch_size": ([vp, C.POINTER(C.c_uint32)], C.c_int),
         "gbl_batch_status": ([vp, C.c_uint32, C.POINTER(RunStatus)], C.c_int),
         "gbl_batch_download": ([vp, C.c_uint32, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
@@ -639,33 +680,15 @@ class Backend:
 
     def set_external_wrenches(self, wrenches, substeps: int) -> None:
         """wrenches: (source, nodes, point, force, torque) tuples."""
-        keep = []
-        arr = (ExternalWrench * max(1, len(wrenches)))()
-        for k, (source, nodes, point, force, torque) in enumerate(wrenches):
-            idx = np.ascontiguousarray(nodes, dtype=np.uint32)
-            name = source.encode() if isinstance(source, str) else source
-            keep += [idx, name]
-            arr[k].source = name
-            arr[k].nodes = idx.ctypes.data_as(C.POINTER(C.c_uint32))
-            arr[k].node_count = idx.size
-            arr[k].point_world_m[:] = [float(x) for x in point]
-            arr[k].force_n[:] = [float(x) for x in force]
-            arr[k].torque_n_m[:] = [float(x) for x in torque]
+        arr, keep = _wrench_array(wrenches)
         _call(library().gbl_set_external_wrenches, self._h, arr if wrenches else None, len(wrenches), int(substeps))
+        del keep
 
     def external_sources(self) -> list:
         """RunStatus::external_sources: (source, LoadLedger) in status order."""
         n = C.c_uint64()
         _call(library().gbl_external_source_count, self._h, C.byref(n))
-        out = []
-        for k in range(n.value):
-            length = C.c_size_t()
-            _call(library().gbl_external_source, self._h, k, None, 0, C.byref(length), None)
-            buf = C.create_string_buffer(length.value + 1)
-            g = LoadLedger()
-            _call(library().gbl_external_source, self._h, k, buf, len(buf), C.byref(length), C.byref(g))
-            out.append((buf.value.decode(), g))
-        return out
+        return [_source(library().gbl_external_source, self._h, k) for k in range(n.value)]
 
     def run(self, control: RunControl) -> RunStatus:
         st = RunStatus()
@@ -757,6 +780,17 @@ class Batch:
         n = C.c_uint32()
         _call(library().gbl_batch_size, self._h, C.byref(n))
         return int(n.value)
+
+    def set_external_wrenches(self, index: int, wrenches, substeps: int) -> None:
+        arr, keep = _wrench_array(wrenches)
+        _call(library().gbl_batch_set_external_wrenches, self._h, index, arr if wrenches else None, len(wrenches),
+              int(substeps))
+        del keep
+
+    def external_sources(self, index: int) -> list:
+        n = C.c_uint64()
+        _call(library().gbl_batch_external_source_count, self._h, index, C.byref(n))
+        return [_source(library().gbl_batch_external_source, self._h, index, k) for k in range(n.value)]
 
     def set_external_forces(self, index: int, forces, substeps: int) -> None:
         if forces is None or len(forces) == 0:
@@ -948,10 +982,7 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
            "state_max_degree": np.array([state.view.max_degree], np.uint32)}
     out.update(sched.arrays())
     out.update(status_arrays(st))
-    sources = backend.external_sources()
-    if sources:
-        out["source_names"] = np.frombuffer(b"".join(n.encode() + b"\0" for n, _ in sources), dtype=np.uint8).copy()
-        out["source_ledgers"] = np.asarray([ledger_row(g) for _, g in sources], dtype=np.float64).reshape(-1)
+    out.update(source_arrays(backend.external_sources()))
     if per_substep:
         out["break_step"] = break_step
     return out
@@ -994,10 +1025,14 @@ def run_batch(cases: list, precision: str = "float", control: RunControl | None 
     for k, c in enumerate(cases):
         if c.get("forces") is not None and "force_ramp_steps" not in c:
             batch.set_external_forces(k, c["forces"], int(c["force_substeps"][0]))
+        if "wrench_names" in c:
+            batch.set_external_wrenches(k, case_wrenches(c), int(c["wrench_substeps"][0]))
     steps = max(int(c["steps"][0]) for c in cases)
     batch.run(control if control is not None else RunControl(max_steps=steps))
     outs = []
     for k, state in enumerate(states):
         sp = batch.download(k, state)
-        outs.append(_outputs(state, sp, batch.first_failure_bonds(k), batch.status(k)))
+        out = _outputs(state, sp, batch.first_failure_bonds(k), batch.status(k))
+        out.update(source_arrays(batch.external_sources(k)))
+        outs.append(out)
     return outs

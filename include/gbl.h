@@ -346,6 +346,14 @@ gbl_result gbl_batch_add(gbl_batch *batch, const gbl_schedule_view *schedule, co
 gbl_result gbl_batch_settle(gbl_batch *batch, const gbl_step_settings *settings);
 gbl_result gbl_batch_set_external_forces(gbl_batch *batch, uint32_t index, const double *forces_world_n,
                                          uint64_t count, uint64_t substeps);
+/* External wrenches and their source ledgers on lattice `index` of the batch,
+ * as gbl_set_external_wrenches / gbl_external_source_count /
+ * gbl_external_source on a backend. */
+gbl_result gbl_batch_set_external_wrenches(gbl_batch *batch, uint32_t index, const gbl_external_wrench *wrenches,
+                                           uint64_t count, uint64_t substeps);
+gbl_result gbl_batch_external_source_count(gbl_batch *batch, uint32_t index, uint64_t *count);
+gbl_result gbl_batch_external_source(gbl_batch *batch, uint32_t index, uint64_t source, char *name,
+                                     size_t name_capacity, size_t *name_length, gbl_load_ledger *load);
 gbl_result gbl_batch_run(gbl_batch *batch, const gbl_run_control *control);
 gbl_result gbl_batch_size(const gbl_batch *batch, uint32_t *count);
 gbl_result gbl_batch_status(gbl_batch *batch, uint32_t index, gbl_run_status *status_out);

@@ -158,3 +158,21 @@ def test_forces_replace_wrenches(device):
     st = be.run(device.RunControl(max_steps=5))
     assert st.external_load.steps == 5
     assert [g.steps for _, g in be.external_sources()] == [2]
+
+
+def test_wrenched_lattices_in_a_batch_equal_each_alone(device):
+    """Bars of three sizes, each driven by its own wrenches, stepped by shared
+    launches: each member's state and source ledgers are its run alone."""
+    from banjo_gb300 import scenes
+
+    cases = [scenes.wrenched_bar(steps=24), scenes.wrenched_bar(nx=12, ny=5, nz=7, steps=24, twist=(0.03, 0.0, 0.0)),
+             scenes.wrenched_bar(nx=20, ny=6, nz=5, steps=24, hand=(0.0, 0.0, -3.0))]
+    together = device.run_batch(cases)
+    broke = 0
+    for case, out in zip(cases, together):
+        alone = device.run_case(case)
+        assert "source_ledgers" in out
+        assert mismatches(alone, out, STATE_KEYS) == []
+        assert status_mismatches(alone, out) == []
+        broke += int(out["status_u64"][4]) > 0
+    assert broke >= 1
