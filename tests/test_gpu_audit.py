@@ -9,7 +9,6 @@ reference's own fixtures (audit_impact*, in the fixture parity test), against
 the CPU checker here, alone and in a batch. The audit measures only: the state
 it leaves is the state of the same run without it.
 """
-import numpy as np
 import pytest
 
 from _util import LEDGER_RTOL, STATE_KEYS, mismatches, status_mismatches

@@ -11,7 +11,6 @@ stop-at-first-failure run has already run every other test; it also passes
 alone in a fresh process.
 """
 import ctypes
-import os
 
 import numpy as np
 import pytest
