@@ -1648,6 +1648,36 @@ private:
 public:
     Sphere<R> sphere() const { return sp_; }
 
+    // upload of the state a download wrote (LatticeWorking.hpp:53-124 on the
+    // arrays LatticeWorking.hpp:126-142 writes back): positions, velocities
+    // and bond state are the current ones, the neighbour slots' aliveness is
+    // the state's as first built (download does not write it), every derived
+    // array starts afresh, and so do the status, the loads, the first-failure
+    // record and the pair list (CpuLatticeBackend.cpp:67-118).
+    void reupload(const std::vector<std::uint8_t> &nbr_alive_built) {
+        L_.nbr_alive = nbr_alive_built;
+        std::fill(L_.rinv.begin(), L_.rinv.end(), R(0));
+        std::fill(L_.unmeasured.begin(), L_.unmeasured.end(), R(0));
+        std::fill(L_.strain.begin(), L_.strain.end(), R(0));
+        std::fill(L_.approach.begin(), L_.approach.end(), R(0));
+        std::fill(L_.node_valid.begin(), L_.node_valid.end(), 0);
+        std::fill(L_.node_dirty.begin(), L_.node_dirty.end(), 1);
+        std::fill(L_.engaged.begin(), L_.engaged.end(), 0);
+        std::fill(L_.candidate.begin(), L_.candidate.end(), 0);
+        std::fill(L_.lambda.begin(), L_.lambda.end(), R(0));
+        std::fill(L_.candidate_list.begin(), L_.candidate_list.end(), 0U);
+        std::fill(L_.candidate_count.begin(), L_.candidate_count.end(), 0U);
+        status = Status{};
+        status.energy_audited = S_.audit != 0;
+        loads.nodes.clear();
+        loads.wrenches.clear();
+        loads.sources.clear();
+        loads.remaining = 0;
+        first_failure_bonds.clear();
+        dirty_start_ = true;
+        pairs_ = PairList<R>{};
+    }
+
 private:
     Lattice<R> &L_;
     Settings<R> S_;
@@ -1716,6 +1746,8 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     if (c.has("wrench_names")) run.loads.setWrenches(unpackWrenches(c), c.scalar<std::uint64_t>("wrench_substeps"), L);
     std::vector<std::uint32_t> break_step(L.B, 0xffffffffU);
     std::vector<std::uint8_t> alive_before = L.alive;
+    const std::vector<std::uint8_t> nbr_alive_built = L.nbr_alive;
+    const std::uint64_t resume_at = c.scalarOr<std::uint64_t>("checkpoint_at", 0);
     const std::uint64_t chunk = per_substep ? 1 : (ramp ? per_step : steps);
     const auto t0 = std::chrono::steady_clock::now();
     for (std::uint64_t done = 0; done < steps;) {
@@ -1726,7 +1758,11 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
             for (std::size_t i = 0; i < f.size(); ++i) f[i] = sc * base[i];
             run.loads.set(f, per_step, L);
         }
-        const std::uint64_t n = std::min(chunk, steps - done);
+        std::uint64_t n = std::min(chunk, steps - done);
+        if (resume_at) {
+            if (done < resume_at) n = std::min(n, resume_at - done);
+            else if (done == resume_at) run.reupload(nbr_alive_built); // checkpoint and resume
+        }
         run.run(n);
         done += n;
         if (per_substep) {

@@ -15,12 +15,7 @@ import pytest
 from _util import SCHEDULE_KEYS, STATE_KEYS, golden_names, load_golden, mismatches, status_mismatches
 
 
-# The checker runs a case in one go; the resume_* fixtures re-upload mid-run,
-# which only the backends do (their device runs hold them to the reference).
-UNBROKEN = [n for n in golden_names() if not n.startswith("resume_")]
-
-
-@pytest.mark.parametrize("name", UNBROKEN)
+@pytest.mark.parametrize("name", golden_names())
 def test_port_reproduces_reference_fixture(port, name):
     case, ref, precision = load_golden(name)
     out = port.run_port(case, precision=precision, per_substep=True)
@@ -28,7 +23,7 @@ def test_port_reproduces_reference_fixture(port, name):
     assert status_mismatches(ref, out) == []
 
 
-@pytest.mark.parametrize("name", UNBROKEN)
+@pytest.mark.parametrize("name", golden_names())
 def test_threaded_port_is_bit_identical(port, name):
     case, ref, precision = load_golden(name)
     out = port.run_port(case, precision=precision, threads=4, per_substep=True)
@@ -37,11 +32,13 @@ def test_threaded_port_is_bit_identical(port, name):
 
 
 def test_resume_fixtures_are_not_the_uninterrupted_run(port):
-    """A LatticeState does not carry all of a running backend's state, and
-    the reference's upload starts afresh from it, so a run resumed from a
-    downloaded state is its own run (here its positions differ from the
-    uninterrupted run's): the fixture exercises the re-upload, not a copy of
-    the uninterrupted result."""
+    """The reference's download does not write the neighbour slots'
+    aliveness back into the LatticeState (LatticeWorking.hpp:126-142), so a
+    lattice uploaded from a downloaded state counts its failed bonds' slots in
+    the strain again, and every derived array starts afresh: a resumed run is
+    its own run (here its positions differ from the uninterrupted run's), and
+    the fixture exercises the re-upload, not a copy of the uninterrupted
+    result."""
     case, ref, precision = load_golden("resume_impact")
     case = {k: v for k, v in case.items() if k != "checkpoint_at"}
     whole = port.run_port(case, precision=precision)
