@@ -729,8 +729,28 @@ template <class R> void startSample(Lattice<R> &L, std::size_t j, bool direct) {
     L.prev_t[j] = maxR(R(0), t); L.prev_c[j] = maxR(R(0), c); L.prev_s[j] = maxR(R(0), s);
 }
 
-// XPBD distance constraint with compliance (LatticePhysics.hpp:1132-1168).
-template <class R> void solveBond(Lattice<R> &L, std::size_t j, R dt, bool direct, bool first) {
+// The per-bond constants of the solve, formed once per run as the reference's
+// threaded lane keeps them (ParallelCpuLatticeBackend.cpp:505-530, 717-745):
+// alpha = compliance / dt^2 and the denominator wa + wb + alpha, the same
+// expressions in the same order, so the same numbers.
+template <class R> struct Kept {
+    std::vector<R> alpha, denominator;
+};
+
+template <class R> Kept<R> keepSolveConstants(const Lattice<R> &L, R dt) {
+    Kept<R> k;
+    k.alpha.resize(L.B);
+    k.denominator.resize(L.B);
+    for (std::size_t j = 0; j < L.B; ++j) {
+        const R alpha = L.compliance[j] / (dt * dt);
+        k.alpha[j] = alpha;
+        k.denominator[j] = L.inv_mass[L.bond_a[j]] + L.inv_mass[L.bond_b[j]] + alpha;
+    }
+    return k;
+}
+
+// bondSolve (LatticePhysics.hpp:1133-1168).
+template <class R> void solveBond(Lattice<R> &L, const Kept<R> &k, std::size_t j, bool direct, bool first) {
     if (!L.alive[j]) return;
     const std::uint32_t a = L.bond_a[j], b = L.bond_b[j];
     const V<R> delta = bondVector(L, j, direct);
@@ -749,9 +769,9 @@ template <class R> void solveBond(Lattice<R> &L, std::size_t j, R dt, bool direc
     }
     const V<R> dir = divide(delta, cl);
     const R wa = L.inv_mass[a], wb = L.inv_mass[b];
-    const R alpha = L.compliance[j] / (dt * dt);
+    const R alpha = k.alpha[j];
     const R lambda = first ? R(0) : L.lambda[j];
-    const R dl = (-constraint - alpha * lambda) / (wa + wb + alpha);
+    const R dl = (-constraint - alpha * lambda) / k.denominator[j];
     L.lambda[j] = lambda + dl;
     st(L.u, a, sub(ld(L.u, a), scale(dir, wa * dl)));
     st(L.u, b, add(ld(L.u, b), scale(dir, wb * dl)));
@@ -968,8 +988,23 @@ unsigned exitReason(std::uint64_t completed, std::uint32_t broken, std::uint64_t
 }
 
 // ---------------------------------------------------------------------------
-// A small fork-join pool: contiguous static ranges per thread, so the
-// per-element work is independent of the thread count.
+// The work pool of the threaded lane, dispatched as the reference's threaded
+// backend dispatches (ParallelCpuLatticeBackend.cpp:135-320, grains at
+// :1347-1356): a phase of `count` elements is cut into chunks of a fixed grain
+// per phase, and the caller and the workers claim chunks from one atomic
+// counter until none is left; below two chunks the caller runs the phase
+// alone. Workers spin between phases (phases come every few microseconds
+// inside a substep) and park on a condition variable after a stretch without
+// work. Which thread runs a chunk never changes a value: elements of a phase
+// are independent, and whatever a phase gathers per participant is folded
+// afterwards in element order or by an order-free operation (integer sums,
+// maxima).
+//
+// The claim word holds the job's chunk count in its high half and the next
+// chunk in its low half, so one fetch-and-add both claims a chunk and says
+// whether it belongs to the job in progress: a worker that wakes late can only
+// ever claim a chunk of the current job, whose body the caller published
+// before the claim word and keeps alive until every chunk is counted done.
 // ---------------------------------------------------------------------------
 class Pool {
 public:
@@ -977,52 +1012,119 @@ public:
         for (unsigned t = 1; t < n_; ++t) workers_.emplace_back([this, t] { loop(t); });
     }
     ~Pool() {
-        { std::lock_guard<std::mutex> g(m_); stop_ = true; ++gen_; }
-        cv_.notify_all();
+        stop_.store(true);
+        publish();
         for (auto &w : workers_) w.join();
     }
+    Pool(const Pool &) = delete;
+    Pool &operator=(const Pool &) = delete;
     [[nodiscard]] unsigned size() const { return n_; }
-    // body(begin, end, thread) over [0, count) split in n contiguous ranges.
-    void run(std::size_t count, const std::function<void(std::size_t, std::size_t, unsigned)> &body) {
-        if (n_ == 1 || count < 2048) { body(0, count, 0); return; }
-        {
-            std::lock_guard<std::mutex> g(m_);
-            body_ = &body; count_ = count; pending_ = n_ - 1; ++gen_;
+
+    // body(begin, end, participant) over [0, count) in chunks of `grain`
+    // elements; the caller is participant 0.
+    template <class F> void run(std::size_t count, std::size_t grain, F &&body) {
+        if (count == 0) return;
+        grain = std::max<std::size_t>(1, grain);
+        const std::size_t chunks = (count + grain - 1) / grain;
+        if (n_ == 1 || chunks < 2) {
+            body(std::size_t{0}, count, 0U);
+            return;
         }
-        cv_.notify_all();
-        body(0, count / n_, 0);
-        std::unique_lock<std::mutex> g(m_);
-        done_cv_.wait(g, [this] { return pending_ == 0; });
+        if (chunks > 0xffffffffULL) throw std::overflow_error("work pool: too many chunks");
+        using Body = std::remove_reference_t<F>;
+        fn_ = [](void *arg, std::size_t b, std::size_t e, unsigned t) { (*static_cast<Body *>(arg))(b, e, t); };
+        arg_ = const_cast<void *>(static_cast<const void *>(&body));
+        count_ = count;
+        grain_ = grain;
+        finished_.store(0, std::memory_order_relaxed);
+        claim_.store(static_cast<std::uint64_t>(chunks) << 32, std::memory_order_release);
+        publish();
+        std::uint32_t mine = 0;
+        for (;;) {
+            const std::uint64_t word = claim_.fetch_add(1, std::memory_order_acq_rel);
+            const std::uint32_t c = static_cast<std::uint32_t>(word);
+            if (c >= chunks) break;
+            const std::size_t b = static_cast<std::size_t>(c) * grain;
+            body(b, std::min(count, b + grain), 0U);
+            ++mine;
+        }
+        const std::uint32_t others = static_cast<std::uint32_t>(chunks) - mine;
+        unsigned spins = 0;
+        while (finished_.load(std::memory_order_acquire) != others)
+            if (++spins % kSpinsBeforeYield == 0) std::this_thread::yield();
     }
 
 private:
-    void loop(unsigned t) {
-        std::uint64_t seen = 0;
-        for (;;) {
-            const std::function<void(std::size_t, std::size_t, unsigned)> *body;
-            std::size_t count;
-            {
-                std::unique_lock<std::mutex> g(m_);
-                cv_.wait(g, [&] { return gen_ != seen; });
-                seen = gen_;
-                if (stop_) return;
-                body = body_; count = count_;
-            }
-            (*body)(count * t / n_, count * (t + 1) / n_, t);
-            std::lock_guard<std::mutex> g(m_);
-            if (--pending_ == 0) done_cv_.notify_one();
+    static constexpr unsigned kSpinsBeforeYield = 4096;
+    static constexpr auto kParkAfter = std::chrono::microseconds(500);
+
+    // A new job (or the stop flag) for the workers; parked ones are woken.
+    void publish() {
+        seq_.fetch_add(1, std::memory_order_seq_cst);
+        if (sleepers_.load(std::memory_order_seq_cst) != 0) {
+            { std::lock_guard<std::mutex> g(park_m_); }
+            park_cv_.notify_all();
         }
     }
+
+    void loop(unsigned index) {
+        std::uint64_t seen = seq_.load(std::memory_order_acquire);
+        for (;;) {
+            std::uint64_t now = seq_.load(std::memory_order_acquire);
+            unsigned spins = 0;
+            auto idle_since = std::chrono::steady_clock::now();
+            while (now == seen) {
+                if (++spins % kSpinsBeforeYield == 0) {
+                    std::this_thread::yield();
+                    if (std::chrono::steady_clock::now() - idle_since > kParkAfter) {
+                        sleepers_.fetch_add(1, std::memory_order_seq_cst);
+                        {
+                            std::unique_lock<std::mutex> g(park_m_);
+                            park_cv_.wait(g, [&] { return seq_.load(std::memory_order_seq_cst) != seen; });
+                        }
+                        sleepers_.fetch_sub(1, std::memory_order_seq_cst);
+                        idle_since = std::chrono::steady_clock::now();
+                    }
+                }
+                now = seq_.load(std::memory_order_acquire);
+            }
+            seen = now;
+            if (stop_.load(std::memory_order_acquire)) return;
+            std::uint32_t done = 0;
+            for (;;) {
+                const std::uint64_t word = claim_.fetch_add(1, std::memory_order_acq_rel);
+                const std::uint32_t c = static_cast<std::uint32_t>(word);
+                const std::uint32_t chunks = static_cast<std::uint32_t>(word >> 32);
+                if (c >= chunks) break;
+                const std::size_t b = static_cast<std::size_t>(c) * grain_;
+                fn_(arg_, b, std::min(count_, b + grain_), index);
+                ++done;
+            }
+            if (done) finished_.fetch_add(done, std::memory_order_release);
+        }
+    }
+
     unsigned n_;
     std::vector<std::thread> workers_;
-    std::mutex m_;
-    std::condition_variable cv_, done_cv_;
-    std::uint64_t gen_{0};
-    bool stop_{false};
-    const std::function<void(std::size_t, std::size_t, unsigned)> *body_{};
-    std::size_t count_{};
-    unsigned pending_{};
+    using Fn = void (*)(void *, std::size_t, std::size_t, unsigned);
+    Fn fn_{nullptr};
+    void *arg_{nullptr};
+    std::size_t count_{0}, grain_{1};
+    alignas(64) std::atomic<std::uint64_t> seq_{0};
+    alignas(64) std::atomic<std::uint64_t> claim_{0};
+    alignas(64) std::atomic<std::uint32_t> finished_{0};
+    alignas(64) std::atomic<std::uint32_t> sleepers_{0};
+    std::atomic<bool> stop_{false};
+    std::mutex park_m_;
+    std::condition_variable park_cv_;
 };
+
+// Grains per phase (elements per claimed chunk): about a microsecond of work
+// each, as the reference sizes them (ParallelCpuLatticeBackend.cpp:1347-1356).
+constexpr std::size_t kNodeGrain = 128;   // the cheap per-node phases
+constexpr std::size_t kStrainGrain = 16;  // the nonlocal strain
+constexpr std::size_t kBondGrain = 64;    // the per-bond samples
+constexpr std::size_t kSolveGrain = 48;   // one colour stage of the sweep
 
 // ---------------------------------------------------------------------------
 // Node-to-node contact (LatticePhysics.hpp:1441-1647; the stage order is
@@ -1463,6 +1565,7 @@ public:
     Runner(Lattice<R> &L, const Settings<R> &S, Sphere<R> sp, unsigned threads) : L_(L), S_(S), sp_(sp), pool_(threads) {
         if (S_.nc_mode != 0 && !(contactCutoff(S_) > R(0))) throw std::invalid_argument("node contact needs 2 r + skin > 0");
         status.energy_audited = S_.audit != 0; // CpuLatticeBackend.cpp:114
+        kept_ = keepSolveConstants(L_, S_.dt);
     }
     Status status;
     Loads<R> loads;
@@ -1497,10 +1600,11 @@ public:
 
 private:
     template <class F> void nodes(F &&f) {
-        pool_.run(L_.N, [&](std::size_t b, std::size_t e, unsigned) { for (std::size_t i = b; i < e; ++i) f(i); });
+        pool_.run(L_.N, kNodeGrain, [&](std::size_t b, std::size_t e, unsigned) { for (std::size_t i = b; i < e; ++i) f(i); });
     }
     template <class F> void range(std::uint32_t b0, std::uint32_t e0, F &&f) {
-        pool_.run(e0 - b0, [&](std::size_t b, std::size_t e, unsigned) { for (std::size_t j = b; j < e; ++j) f(b0 + j); });
+        pool_.run(e0 - b0, kSolveGrain,
+                  [&](std::size_t b, std::size_t e, unsigned) { for (std::size_t j = b; j < e; ++j) f(b0 + j); });
     }
     // The sweep order of CpuLatticeBackend.cpp:336-348, 395-407.
     template <class F> void sweepBlock(std::uint32_t block, std::uint32_t boundary, F &&f) {
@@ -1516,21 +1620,53 @@ private:
     }
     void strainAll(bool direct) {
         std::vector<std::uint32_t> rd(pool_.size(), 0);
-        pool_.run(L_.N, [&](std::size_t b, std::size_t e, unsigned t) {
+        pool_.run(L_.N, kStrainGrain, [&](std::size_t b, std::size_t e, unsigned t) {
             for (std::size_t i = b; i < e; ++i)
                 nodeStrain(L_, i, direct, rd[t], S_.plate_half_thickness, S_.yield_stretch);
         });
         for (auto x : rd) status.rank_deficient_nodes += x;
     }
 
+    // The start-of-substep sample after a failure, or after upload
+    // (CpuLatticeBackend.cpp:363-370). The serial lane redoes every node's
+    // strain and every live bond's start sample; only the nodes flagged dirty
+    // (they lost a bond; every node after upload) can come out different --
+    // every other node reads the positions and live neighbours it read at the
+    // end of the previous substep, and a bond's end sample left exactly what
+    // its start sample writes -- so those nodes and the live bonds at them are
+    // redone, as the reference's threaded lane does
+    // (ParallelCpuLatticeBackend.cpp:1718-1757).
+    void restart(bool direct) {
+        dirty_list_.clear();
+        for (std::uint32_t i = 0; i < L_.N; ++i)
+            if (L_.node_dirty[i]) dirty_list_.push_back(i);
+        std::vector<std::uint32_t> rd(pool_.size(), 0);
+        pool_.run(dirty_list_.size(), kStrainGrain, [&](std::size_t b, std::size_t e, unsigned t) {
+            for (std::size_t k = b; k < e; ++k)
+                nodeStrain(L_, dirty_list_[k], direct, rd[t], S_.plate_half_thickness, S_.yield_stretch);
+        });
+        for (auto x : rd) status.rank_deficient_nodes += x;
+        if (bond_mark_.size() != L_.B) bond_mark_.assign(L_.B, 0U);
+        touched_.clear();
+        for (const std::uint32_t i : dirty_list_)
+            for (std::uint32_t k = 0; k < L_.D; ++k) {
+                const std::uint32_t j = L_.nbr_bond[static_cast<std::size_t>(k) * L_.N + i];
+                if (j == kNoBond) break;
+                if (!L_.alive[j] || bond_mark_[j]) continue;
+                bond_mark_[j] = 1;
+                touched_.push_back(j);
+            }
+        for (const std::uint32_t j : touched_) bond_mark_[j] = 0;
+        pool_.run(touched_.size(), kBondGrain, [&](std::size_t b, std::size_t e, unsigned) {
+            for (std::size_t k = b; k < e; ++k) startSample(L_, touched_[k], direct);
+        });
+    }
+
     // CpuLatticeBackend.cpp:357-439.
     bool advance() {
         const bool direct = S_.direct != 0;
         if (dirty_start_) {
-            strainAll(direct);
-            pool_.run(L_.B, [&](std::size_t b, std::size_t e, unsigned) {
-                for (std::size_t j = b; j < e; ++j) if (L_.alive[j]) startSample(L_, j, direct);
-            });
+            restart(direct);
             dirty_start_ = false;
         }
         loads.kick(L_, S_.dt, status);
@@ -1566,7 +1702,7 @@ private:
         }
         for (std::uint32_t it = 0; it < S_.iterations; ++it) {
             const bool first = it == 0;
-            auto solve = [&](std::size_t j) { solveBond(L_, j, S_.dt, direct, first); };
+            auto solve = [&](std::size_t j) { solveBond(L_, kept_, j, direct, first); };
             sweepAll(solve);
             nodes([&](std::size_t i) { nodeSupportProject(L_, S_, i); });
         }
@@ -1593,51 +1729,67 @@ private:
         return finishStep(direct);
     }
 
-    // CpuLatticeBackend.cpp:441-488. The bond loop runs in contiguous ranges;
-    // its ledger is folded afterwards in bond order, which is the serial order.
+    // CpuLatticeBackend.cpp:441-488. The bond loop runs in chunks on the pool;
+    // the events each participant gathers are sorted by bond index and the
+    // ledger folded in that order, which is the serial order (the reference's
+    // threaded lane does the same, ParallelCpuLatticeBackend.cpp:1885-1910).
     bool finishStep(bool direct) {
         strainAll(direct);
         const unsigned T = pool_.size();
         struct Event { std::uint32_t j; double removed, plastic; float damage; bool broke; };
-        std::vector<std::vector<Event>> events(T);
-        std::vector<float> mt(T, 0.0F), mc(T, 0.0F), ms(T, 0.0F), mp(T, 0.0F);
-        std::vector<bool> seen_t(T, false);
+        // One tally per participant, each on its own cache lines; a chunk
+        // folds its peaks locally and merges them once.
+        struct alignas(64) Tally {
+            std::vector<Event> events;
+            float t{0.0F}, c{0.0F}, s{0.0F}, p{0.0F};
+            bool seen{false};
+        };
+        std::vector<Tally> tally(T);
         const double damage_floor = status.max_damage + 1.0e-6;
-        pool_.run(L_.B, [&](std::size_t b, std::size_t e, unsigned t) {
+        pool_.run(L_.B, kBondGrain, [&](std::size_t b, std::size_t e, unsigned t) {
+            Tally &my = tally[t];
+            float lt = 0.0F, lc = 0.0F, ls = 0.0F, lp = 0.0F;
+            bool seen = false;
             for (std::size_t j = b; j < e; ++j) {
                 if (!L_.alive[j]) continue;
                 const Outcome o = endSample(L_, S_, j, direct);
-                if (!seen_t[t]) { mt[t] = o.peak_t; mc[t] = o.peak_c; ms[t] = o.peak_s; mp[t] = o.plastic_stretch; seen_t[t] = true; }
-                mt[t] = std::max(mt[t], o.peak_t); mc[t] = std::max(mc[t], o.peak_c);
-                ms[t] = std::max(ms[t], o.peak_s); mp[t] = std::max(mp[t], o.plastic_stretch);
+                if (!seen) { lt = o.peak_t; lc = o.peak_c; ls = o.peak_s; lp = o.plastic_stretch; seen = true; }
+                lt = std::max(lt, o.peak_t); lc = std::max(lc, o.peak_c);
+                ls = std::max(ls, o.peak_s); lp = std::max(lp, o.plastic_stretch);
                 if (o.broke || o.plastic != 0.0 || o.damage > damage_floor)
-                    events[t].push_back({static_cast<std::uint32_t>(j), o.removed, o.plastic, o.damage, o.broke});
+                    my.events.push_back({static_cast<std::uint32_t>(j), o.removed, o.plastic, o.damage, o.broke});
             }
+            if (!seen) return;
+            if (!my.seen) { my.t = lt; my.c = lc; my.s = ls; my.p = lp; my.seen = true; }
+            my.t = std::max(my.t, lt); my.c = std::max(my.c, lc); my.s = std::max(my.s, ls); my.p = std::max(my.p, lp);
         });
         for (unsigned t = 0; t < T; ++t) {
-            if (!seen_t[t]) continue;
-            status.max_t = std::max(status.max_t, mt[t]); status.max_c = std::max(status.max_c, mc[t]);
-            status.max_s = std::max(status.max_s, ms[t]); status.max_plastic_stretch = std::max(status.max_plastic_stretch, mp[t]);
+            if (!tally[t].seen) continue;
+            status.max_t = std::max(status.max_t, tally[t].t); status.max_c = std::max(status.max_c, tally[t].c);
+            status.max_s = std::max(status.max_s, tally[t].s);
+            status.max_plastic_stretch = std::max(status.max_plastic_stretch, tally[t].p);
         }
+        std::vector<Event> ordered;
+        for (unsigned t = 0; t < T; ++t) ordered.insert(ordered.end(), tally[t].events.begin(), tally[t].events.end());
+        std::sort(ordered.begin(), ordered.end(), [](const Event &x, const Event &y) { return x.j < y.j; });
         bool any = false;
         const bool first_round = status.broken_bonds == 0;
-        for (unsigned t = 0; t < T; ++t)
-            for (const Event &ev : events[t]) {
-                status.plastic_work += ev.plastic;
-                if (ev.damage > status.max_damage + 1.0e-6) {
-                    status.max_damage = ev.damage;
-                    status.last_damage_gain_step = status.total_steps;
-                }
-                if (!ev.broke) continue;
-                any = true;
-                if (first_round) first_failure_bonds.push_back(ev.j);
-                status.removed_energy += ev.removed;
-                if (ev.removed > energy_flat_fraction * std::max(status.removed_energy, 1.0e-12))
-                    status.last_energy_gain_step = status.total_steps;
-                ++status.broken_bonds;
-                L_.node_dirty[L_.bond_a[ev.j]] = 1;
-                L_.node_dirty[L_.bond_b[ev.j]] = 1;
+        for (const Event &ev : ordered) {
+            status.plastic_work += ev.plastic;
+            if (ev.damage > status.max_damage + 1.0e-6) {
+                status.max_damage = ev.damage;
+                status.last_damage_gain_step = status.total_steps;
             }
+            if (!ev.broke) continue;
+            any = true;
+            if (first_round) first_failure_bonds.push_back(ev.j);
+            status.removed_energy += ev.removed;
+            if (ev.removed > energy_flat_fraction * std::max(status.removed_energy, 1.0e-12))
+                status.last_energy_gain_step = status.total_steps;
+            ++status.broken_bonds;
+            L_.node_dirty[L_.bond_a[ev.j]] = 1;
+            L_.node_dirty[L_.bond_b[ev.j]] = 1;
+        }
         sp_.center = add(sp_.center, scale(sp_.velocity, S_.dt));
         sphereSupport(S_, sp_, status.contact);
         // A failure changes which pairs no live bond holds.
@@ -1685,6 +1837,9 @@ private:
     Pool pool_;
     bool dirty_start_{true};
     PairList<R> pairs_;
+    Kept<R> kept_;
+    std::vector<std::uint32_t> dirty_list_, touched_;
+    std::vector<std::uint8_t> bond_mark_;
 };
 
 template <class R> std::vector<double> widen(const std::vector<R> &v) {
