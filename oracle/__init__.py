@@ -31,8 +31,23 @@ def build_port() -> str:
     return PORT_LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
+def reference_root() -> str:
+    """Where the reference's source tree is read from: the BANJO_REFERENCE_ROOT
+    environment variable, else a checkout named `reference` beside this
+    repository."""
+    env = os.environ.get("BANJO_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def reference_present() -> bool:
+    return os.path.isdir(os.path.join(reference_root(), "src", "fastlattice"))
+
+
+def build_reference(ref_root: str | None = None) -> str | None:
     """Builds oracle/_ref from the reference's sources when they are present."""
+    ref_root = ref_root or reference_root()
     if not os.path.isdir(os.path.join(ref_root, "src", "fastlattice")):
         return None
     jobs = str(max(1, min(8, os.cpu_count() or 1)))

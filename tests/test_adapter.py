@@ -16,7 +16,7 @@ import oracle
 
 
 def _reference_present():
-    return os.path.isdir("/root/reference/src/fastlattice")
+    return oracle.reference_present()
 
 
 @pytest.mark.skipif(not _reference_present(), reason="the reference tree is not present here")
