@@ -28,3 +28,17 @@ def test_binding_replaces_the_cuda_stub(gbl):
     assert "PASS" in r.stdout
     if not gbl.available():
         assert "cudaLatticeAvailable=0" in r.stdout and "runtime_error" in r.stdout
+
+
+@pytest.mark.skipif(not _reference_present(), reason="the reference tree is not present here")
+def test_binding_carries_every_field():
+    """The binding over a recording stand-in for the library (no device): every
+    field of LatticeSchedule, LatticeState, StepSettings, SphereState,
+    RunControl and the wrenches arrives in its C field, and every field of the
+    RunStatus, sources, downloaded state, first-failure list and frames the
+    library hands back arrives in its reference field."""
+    oracle.build_reference()
+    subprocess.run(["make", "-s", "-C", oracle.HERE, "adapter-stub"], check=True)
+    r = subprocess.run([os.path.join(oracle.HERE, "_ref", "adapter_stub_driver")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "[PASS]" in r.stdout
