@@ -243,6 +243,7 @@ template <class R> struct Resident {
 
     Schedule sched;
     std::uint32_t N{}, B{};
+    std::uint64_t live_bonds{}; // bonds alive at upload
     Arena arena;
     Dev<R> dev{};
     std::vector<Level> levels;
@@ -585,6 +586,13 @@ template <class R> struct Resident {
                 inv_mass[i] = R(st.inv_mass[i]);
             }
         });
+        std::atomic<std::uint64_t> live{0};
+        parallelFor(B, [&](std::size_t lo, std::size_t hi) {
+            std::uint64_t n = 0;
+            for (std::size_t j = lo; j < hi; ++j) n += st.alive[j] != 0;
+            live += n;
+        });
+        live_bonds = live;
         d.isolated_count = static_cast<std::uint32_t>(isolated.size());
         // Level boundaries for the one-CTA sweep, when the levels fit its table.
         d.level_count = levels.size() <= kMaxFusedLevels ? static_cast<std::uint32_t>(levels.size()) : 0U;
@@ -1233,6 +1241,7 @@ template <class R> struct Resident {
         status.plastic_work_j = c.plastic_work;
         status.damping_dissipated_j = c.damping_dissipated;
         status.striker_dissipated_j = c.striker_dissipated;
+        status.bond_projections = c.projections;
     }
 };
 
@@ -1244,7 +1253,7 @@ template <class R> struct Resident {
 // work lists and the captured substep graph are rebuilt when the set changes.
 template <class R> class Engine {
     static constexpr bool kDirect = std::is_same<R, double>::value;
-    static constexpr unsigned kSphereSlab = kCandidatesPerBlock * sizeof(Staged<R>);
+    static constexpr unsigned kSphereSlab = sphereSlabBytes<R>();
 
 public:
     Engine() {
@@ -1816,6 +1825,7 @@ private:
         c.energy_flat_fraction = 1.0e-3;
         c.calm_damage_margin = 0.5;
         c.step_limit = step_limit;
+        c.live_bonds = slots_[k]->live_bonds;
         ctl_host_[k] = c;
         Resident<R> &l = *slots_[k];
         l.dev.ctl = ctl_ + k;
@@ -2111,7 +2121,7 @@ private:
         if (tiles_.count) kEmitEvents<R, M><<<tiles_.count, kThreads, 0, st>>>(grid(tiles_));
         kLedgerBroken<R, M><<<broken_.count, kThreads, 0, st>>>(grid(broken_));
         mark(12);
-        kLedger<R, M><<<each_.count, 32, 0, st>>>(grid(each_), S);
+        kLedger<R, M><<<each_.count, kLedgerThreads, 0, st>>>(grid(each_), S);
         mark(13);
         check(cudaGetLastError(), "kernel launch");
     }
@@ -3119,6 +3129,30 @@ gbl_result gbl_serve_footprint(int precision, uint32_t node_count, uint32_t bond
         else if (precision == GBL_PRECISION_FLOAT)
             *bytes = gbl::Resident<float>::footprint(node_count, bond_count, max_degree, block_count);
         else gbl::invalid("unknown precision");
+    });
+}
+
+gbl_result gbl_bounds_report(uint64_t report[4], int *checked) {
+    return gbl::guard([&] {
+        if (!report || !checked) gbl::invalid("null argument");
+#ifdef GBL_BOUNDS_CHECK
+        *checked = 1;
+        unsigned long long v[4] = {};
+        gbl::check(cudaMemcpyFromSymbol(v, gbl::g_bounds_violation, sizeof(v)), "bounds record");
+        for (int k = 0; k < 4; ++k) report[k] = v[k];
+#else
+        *checked = 0;
+        for (int k = 0; k < 4; ++k) report[k] = 0;
+#endif
+    });
+}
+
+gbl_result gbl_bounds_clear(void) {
+    return gbl::guard([&] {
+#ifdef GBL_BOUNDS_CHECK
+        const unsigned long long zero[4] = {};
+        gbl::check(cudaMemcpyToSymbol(gbl::g_bounds_violation, zero, sizeof(zero)), "bounds record");
+#endif
     });
 }
 

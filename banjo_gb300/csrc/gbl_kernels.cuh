@@ -34,6 +34,40 @@ template <> struct alignas(8) BondRec<double> { std::uint32_t a, b; double rsm, 
 template <class R> __device__ __forceinline__ std::uint32_t endA(const BondRec<R> &r) { return r.a & kNodeMask; }
 template <class R> __device__ __forceinline__ std::uint32_t endB(const BondRec<R> &r) { return r.b & kNodeMask; }
 
+// ---------------------------------------------------------------------------
+// The bounds-checked build (GBL_BOUNDS_CHECK defined: libgbl_checked.so). Every
+// index the kernels read out of device data -- bond ends, neighbour slots,
+// candidate, dirty, event, load, halo and isolated-node lists -- is checked
+// against the length of the array it indexes before it is used. A violation is
+// counted in g_bounds_violation, with the first one's site, index and length,
+// and the access is skipped; nothing traps, so the context stays usable and
+// the host reads the record (gbl_bounds_report). In the normal build the check
+// is the constant true.
+// ---------------------------------------------------------------------------
+enum BoundsSite : unsigned {
+    kSiteSolve = 1, kSiteStrain, kSiteDirty, kSiteDirtyBond, kSiteEndSample, kSiteCandidate, kSiteEvent,
+    kSiteEventEnd, kSiteLoad, kSiteIsolated, kSiteHalo, kSiteDamp
+};
+#ifdef GBL_BOUNDS_CHECK
+__device__ unsigned long long g_bounds_violation[4]; // count, then the first's site, index, length
+__device__ __noinline__ bool boundsViolated(std::uint64_t i, std::uint64_t n, unsigned site) {
+    if (atomicAdd(&g_bounds_violation[0], 1ULL) == 0) {
+        g_bounds_violation[1] = site;
+        g_bounds_violation[2] = i;
+        g_bounds_violation[3] = n;
+    }
+    return false;
+}
+__device__ __forceinline__ bool inBounds(std::uint64_t i, std::uint64_t n, unsigned site) {
+    return i < n || boundsViolated(i, n, site);
+}
+#else
+__device__ __forceinline__ constexpr bool inBounds(std::uint64_t, std::uint64_t, unsigned) { return true; }
+#endif
+template <class R> __device__ __forceinline__ bool endsInBounds(const BondRec<R> &r, std::uint32_t n, unsigned site) {
+    return inBounds(endA(r), n, site) && inBounds(endB(r), n, site);
+}
+
 // Streaming loads for data read once per pass (bond records), so that they do
 // not evict the node arrays the gathers keep re-reading from L2.
 __device__ __forceinline__ BondRec<float> ldStream(const BondRec<float> *p) {
@@ -115,6 +149,10 @@ struct Ctl {
     // External wrenches: how many are set, and the count of sources kicked
     // since upload (a new source's place in the status order).
     unsigned wrench_count, source_seq;
+    // Bond projections the sweeps ran: per substep, the bonds alive when its
+    // sweep starts (alive at upload less those broken since) times the
+    // solver iterations.
+    unsigned long long projections, live_bonds;
 };
 
 // An external wrench on the device (ExternalWrench, FastLattice.hpp:153-157):
@@ -294,7 +332,8 @@ __device__ __noinline__ void plateBending(const Dev<R> &L, std::uint32_t i, V3<R
         const std::size_t slot = k * N + i;
         const bool present = L.nbr_bond[slot] != kNoBond;
         const Q4<R> q = L.nbr[slot];
-        const std::uint32_t other = present ? L.nbr_other[slot] : i;
+        std::uint32_t other = present ? L.nbr_other[slot] : i;
+        if (!inBounds(other, N, kSiteStrain)) other = i;
         w = present ? liveWeight(q.w) : R(0);
         rest = present ? V3<R>{q.x, q.y, q.z} : V3<R>{R(0), R(0), R(0)};
         const V3<R> xo = Direct ? pos(L, other) : xyz(L.u[other]);
@@ -426,6 +465,7 @@ __device__ void nodeStrain(const Dev<R> &L, std::uint32_t i, R plate_half_thickn
         const std::size_t slot = k * N + i;
         const Q4<R> q = L.nbr[slot];
         const std::uint32_t other = L.nbr_other[slot];
+        if (!inBounds(other, N, kSiteStrain)) continue;
         const V3<R> rest{q.x, q.y, q.z};
         const V3<R> xo = Direct ? pos(L, other) : xyz(L.u[other]);
         const V3<R> cur = Direct ? (xo - xi) - rest : xo - xi;
@@ -484,7 +524,10 @@ __global__ void __launch_bounds__(kThreads) kRestartStrain(const Grid<R> launch,
     const std::uint32_t t = w.begin + threadIdx.x;
     if (t >= w.end) return;
     if (L.ctl->full_restart) nodeStrain<R, Direct, Plate>(L, t, plate, yield);
-    else if (t < L.ctl->dirty_count) nodeStrain<R, Direct, Plate>(L, L.dirty_list[t], plate, yield);
+    else if (t < L.ctl->dirty_count) {
+        const std::uint32_t node = L.dirty_list[t];
+        if (inBounds(node, L.N, kSiteDirty)) nodeStrain<R, Direct, Plate>(L, node, plate, yield);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -567,9 +610,10 @@ __global__ void __launch_bounds__(kThreads) kRestartBondsDirty(const Grid<R> lau
     const std::uint32_t t = w.begin + threadIdx.x;
     if (t >= w.end || t >= L.ctl->dirty_count) return;
     const std::uint32_t node = L.dirty_list[t];
+    if (!inBounds(node, L.N, kSiteDirty)) return;
     for (std::uint32_t k = 0; k < L.D; ++k) {
         const std::uint32_t d = L.nbr_bond[static_cast<std::size_t>(k) * L.N + node];
-        if (d != kNoBond) startSample<R, Direct>(L, d);
+        if (d != kNoBond && inBounds(d, L.B, kSiteDirtyBond)) startSample<R, Direct>(L, d);
     }
 }
 
@@ -897,7 +941,10 @@ __global__ void __launch_bounds__(1024) kCandidates(const Grid<R> launch) {
     if (threadIdx.x == 0) {
         const std::uint32_t total = carry;
         L.cand_count[blk] = total < kCandidatesPerBlock ? total : kCandidatesPerBlock;
-        if (total > kCandidatesPerBlock) L.ctl->contact.candidate_overflow += total - kCandidatesPerBlock;
+        // Slabs of one lattice finish in any order: the count is shared.
+        if (total > kCandidatesPerBlock)
+            atomicAdd(&L.ctl->contact.candidate_overflow,
+                      static_cast<unsigned long long>(total - kCandidatesPerBlock));
     }
 }
 
@@ -914,14 +961,16 @@ __global__ void __launch_bounds__(1024) kMarkHalo(const Grid<R> launch) {
     const std::uint32_t *list = L.cand_list + w.begin * kCandidatesPerBlock;
     for (std::uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
         const std::uint32_t c = list[k];
+        if (!inBounds(c, L.N, kSiteHalo)) continue;
         L.halo_stamp[c] = stamp;
         for (std::uint32_t q = 0; q < L.D; ++q) {
             const std::size_t slot = static_cast<std::size_t>(q) * L.N + c;
             const std::uint32_t o = L.nbr_other[slot];
+            if (!inBounds(o, L.N, kSiteHalo)) continue;
             L.halo_stamp[o] = stamp;
             for (std::uint32_t r = 0; r < L.D; ++r) {
                 const std::uint32_t bd = L.nbr_bond[static_cast<std::size_t>(r) * L.N + o];
-                if (bd != kNoBond) L.late_tile_stamp[bd / kThreads] = stamp;
+                if (bd != kNoBond && inBounds(bd, L.B, kSiteHalo)) L.late_tile_stamp[bd / kThreads] = stamp;
             }
         }
     }
@@ -951,16 +1000,28 @@ template <class R> struct Staged {
     Q4<R> u, v;    // u (w: inv_mass), v (w: mass)
 };
 
+// What one hit adds to the contact ledger's FP64 sums, in backend precision:
+// the chain writes it to a log in shared memory and goes on, and the fold
+// lanes widen and add it in log order (LatticePhysics.hpp:1354-1381), so the
+// FP64 adds stay off the serial chain.
+template <class R> struct ContactLog {
+    R normal_imp[3], friction_imp[3];
+    R lost;            // the node's kinetic energy before minus after
+    unsigned friction; // friction_imp applies
+};
+
+// Bytes of shared memory per staging buffer of the contact pass: a slab's
+// staged candidates and the log of its hits.
+template <class R> constexpr unsigned sphereSlabBytes() {
+    return kCandidatesPerBlock * static_cast<unsigned>(sizeof(Staged<R>) + sizeof(ContactLog<R>));
+}
+
 template <class R>
-__device__ __forceinline__ void contactApply(V3<R> imp, V3<R> r, R inm, R ism, R iin, V3<R> &nv, Sphere<R> &sp,
-                                             ContactAcc &acc) {
+__device__ __forceinline__ void contactApply(V3<R> imp, V3<R> r, R inm, R ism, R iin, V3<R> &nv, Sphere<R> &sp) {
     nv = nv + inm * imp;
     sp.velocity = sp.velocity - ism * imp;
     const V3<R> ti = -cross(r, imp);
     sp.angular = sp.angular + iin * ti;
-    acc.impulse_x += static_cast<double>(imp.x);
-    acc.impulse_y += static_cast<double>(imp.y);
-    acc.impulse_z += static_cast<double>(imp.z);
 }
 
 // A candidate against the current sphere state: 0 outside the contact gate
@@ -982,11 +1043,13 @@ __device__ __forceinline__ int contactProbe(const Settings<R> &S, const Sphere<R
 
 // The contact of one staged candidate past the gate, from its normal
 // relative velocity and normal impulse on (LatticePhysics.hpp:1343-1386).
-// `max_pen` shadows acc.max_penetration in R: the ledger only ever holds a
-// widened R, so the comparison is the reference's.
+// `max_pen` and `max_corr` shadow acc.max_penetration and acc.max_correction
+// in R: the ledger only ever holds a widened R, so the comparisons are the
+// reference's. A hit's ledger sums go to `log`; it returns whether it hit.
 template <class R>
-__device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp, Staged<R> &c, V3<R> r, V3<R> normal,
-                                             R gap, R ni, R ism, R iin, bool correct, ContactAcc &acc, R &max_pen) {
+__device__ __forceinline__ bool contactChain(const Settings<R> &S, Sphere<R> &sp, Staged<R> &c, V3<R> r, V3<R> normal,
+                                             R gap, R ni, R ism, R iin, bool correct, ContactAcc &acc, R &max_pen,
+                                             R &max_corr, ContactLog<R> &log) {
     V3<R> nv = xyz(c.v);
     if (-gap > max_pen) {
         max_pen = -gap;
@@ -994,8 +1057,14 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
     }
     const R inm = c.inm;
     const R mass = c.v.w;
-    if (ni > R(0)) {
-        contactApply(ni * normal, r, inm, ism, iin, nv, sp, acc);
+    const bool hit = ni > R(0);
+    if (hit) {
+        const V3<R> imp = ni * normal;
+        contactApply(imp, r, inm, ism, iin, nv, sp);
+        log.normal_imp[0] = imp.x;
+        log.normal_imp[1] = imp.y;
+        log.normal_imp[2] = imp.z;
+        log.friction = 0;
         const V3<R> after = nv - sp.velocity - cross(sp.angular, r);
         const V3<R> tangent = after - dot(after, normal) * normal;
         const R ts = length(tangent);
@@ -1004,10 +1073,15 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
             const V3<R> rd = cross(r, d);
             const R stick = ts / (inm + ism + iin * dot(rd, rd));
             const R fi = stick <= S.c_static * ni ? stick : minR(stick, S.c_dynamic * ni);
-            contactApply(-fi * d, r, inm, ism, iin, nv, sp, acc);
+            const V3<R> fimp = -fi * d;
+            contactApply(fimp, r, inm, ism, iin, nv, sp);
+            log.friction_imp[0] = fimp.x;
+            log.friction_imp[1] = fimp.y;
+            log.friction_imp[2] = fimp.z;
+            log.friction = 1;
         }
         c.v = Q4<R>{nv.x, nv.y, nv.z, mass};
-        acc.dissipated += static_cast<double>(c.before - R(0.5) * mass * dot(nv, nv));
+        log.lost = c.before - R(0.5) * mass * dot(nv, nv);
         ++acc.impulse_contacts;
     }
     if (correct && gap < -S.c_margin) {
@@ -1018,17 +1092,21 @@ __device__ __forceinline__ void contactChain(const Settings<R> &S, Sphere<R> &sp
         const V3<R> un = xyz(c.u) + ns;
         c.u = Q4<R>{un.x, un.y, un.z, c.u.w};
         sp.center = sp.center + ss;
-        if (corr > R(acc.max_correction)) acc.max_correction = static_cast<double>(corr);
+        if (corr > max_corr) {
+            max_corr = corr;
+            acc.max_correction = static_cast<double>(corr);
+        }
     }
+    return hit;
 }
 
 constexpr unsigned kSphereThreads = 256;
 // Staging buffers of the contact pass: with two, the chain of one slab runs on
-// warp 0 while the other warps write back the slab before it from the other
-// buffer and then stage the slab after it into that buffer (a thread writes
-// back and stages the same buffer slots, so no barrier is needed between);
-// with one (when two do not fit the device's shared memory), one slab at a
-// time.
+// warp 0 while warp 1 folds the ledger log of the slab before it and the other
+// warps write back the slab before it from the other buffer and then stage
+// the slab after it into that buffer (a thread writes back and stages the
+// same buffer slots, so no barrier is needed between); with one (when two do
+// not fit the device's shared memory), one slab at a time.
 
 // The chain runs on warp 0, with every lane holding the same sphere state and
 // ledgers. Only a candidate that passes the contact gate changes anything, so
@@ -1038,6 +1116,10 @@ constexpr unsigned kSphereThreads = 256;
 // state the serial order shows them, so the result is the serial chain's.
 // Slabs are disjoint sets of nodes: staging one slab's candidates, running
 // another's chain and writing back a third's touch different nodes.
+//
+// The ledger's four FP64 sums (impulse x, y, z and dissipated energy) are four
+// independent serial folds; lanes 0-3 of warp 1 run one each over the hit
+// logs, slab after slab, in the order the chain wrote them.
 template <class R, bool Many>
 __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> launch, Settings<R> S, int pass,
                                                               unsigned buffers) {
@@ -1045,22 +1127,32 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
     const Dev<R> L = descriptor<R, Many>(launch, w);
     extern __shared__ __align__(16) unsigned char sphere_smem[];
     Staged<R> *stage_base = reinterpret_cast<Staged<R> *>(sphere_smem);
+    ContactLog<R> *log_base =
+        reinterpret_cast<ContactLog<R> *>(sphere_smem + buffers * kCandidatesPerBlock * sizeof(Staged<R>));
     __shared__ Sphere<R> start;
+    __shared__ unsigned log_count[2];
+    __shared__ double folded[4];
     if (L.ctl->stop) return;
     const unsigned lane = threadIdx.x & 31U;
     const bool chain = threadIdx.x < 32;
+    const bool fold = threadIdx.x >= 32 && threadIdx.x < 36;
     Sphere<R> sp{};
     ContactAcc acc{};
     V3<R> c0{};
-    R e0 = R(0), max_pen = R(0);
+    R e0 = R(0), max_pen = R(0), max_corr = R(0);
+    double sum = 0.0; // the fold lane's ledger sum
     if (chain) {
         sp = *L.sphere;
         if (pass == 1) sp.velocity = sp.velocity + S.dt * S.gravity; // the kicked sphere becomes the state
         acc = L.ctl->contact;
         max_pen = R(acc.max_penetration);
+        max_corr = R(acc.max_correction);
         c0 = sp.center;
         e0 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
         if (threadIdx.x == 0) start = sp;
+    } else if (fold) {
+        const ContactAcc &a = L.ctl->contact;
+        sum = lane == 0 ? a.impulse_x : lane == 1 ? a.impulse_y : lane == 2 ? a.impulse_z : a.dissipated;
     }
     __syncthreads();
     // Constant over the pass: the sphere's mass and inertia never change.
@@ -1075,6 +1167,11 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
         for (std::uint32_t k = threadIdx.x - t0; k < n; k += nt) {
             const std::uint32_t i = list[k];
             Staged<R> c;
+            if (!inBounds(i, L.N, kSiteCandidate)) {
+                c = Staged<R>{}; // no mass: the chain passes it by
+                st[k] = c;
+                continue;
+            }
             c.u = L.u[i];
             c.v = L.v[i];
             const R mass = c.v.w;
@@ -1102,6 +1199,7 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
         const std::uint32_t *list = L.cand_list + b * kCandidatesPerBlock;
         for (std::uint32_t k = threadIdx.x - t0; k < n; k += nt) {
             const std::uint32_t i = list[k];
+            if (!inBounds(i, L.N, kSiteCandidate)) continue;
             const Q4<R> vq = st[k].v;
             const Q4<R> uq = st[k].u;
             if (pass == 1) {
@@ -1119,9 +1217,21 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             }
         }
     };
-    // The serial chain over a staged slab, on warp 0.
-    auto runChain = [&](std::uint32_t n, Staged<R> *st) {
+    // A slab's hit log into the fold lanes' sums (lane q: sum q).
+    auto foldLog = [&](const ContactLog<R> *lg, unsigned n) {
+        if (lane < 3) {
+            for (unsigned e = 0; e < n; ++e) {
+                sum += static_cast<double>(lg[e].normal_imp[lane]);
+                if (lg[e].friction) sum += static_cast<double>(lg[e].friction_imp[lane]);
+            }
+        } else {
+            for (unsigned e = 0; e < n; ++e) sum += static_cast<double>(lg[e].lost);
+        }
+    };
+    // The serial chain over a staged slab, on warp 0; its hits go to `lg`.
+    auto runChain = [&](std::uint32_t n, Staged<R> *st, ContactLog<R> *lg, unsigned &logged) {
         std::uint32_t k0 = 0;
+        unsigned hits = 0;
         while (k0 < n) {
             const std::uint32_t k = k0 + lane;
             // hit: the contact changes the sphere or the node (an impulse, or
@@ -1191,11 +1301,18 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
                            __shfl_sync(0xffffffffU, normal.z, src)};
             const R hgap = __shfl_sync(0xffffffffU, gap, src);
             const R hni = __shfl_sync(0xffffffffU, ni, src);
-            contactChain(S, sp, c, hr, hn, hgap, hni, ism, iin, pass == 2, acc, max_pen);
+            ContactLog<R> entry;
+            const bool logs = contactChain(S, sp, c, hr, hn, hgap, hni, ism, iin, pass == 2, acc, max_pen, max_corr,
+                                           entry);
             __syncwarp();
-            if (lane == 0) st[j] = c;
+            if (lane == 0) {
+                st[j] = c;
+                if (logs) lg[hits] = entry;
+            }
+            hits += logs ? 1U : 0U;
             k0 = j + 1;
         }
+        if (lane == 0) logged = hits;
     };
     // The next slab with candidates after b (L.blocks: none).
     auto nextSlab = [&](std::uint32_t b) {
@@ -1213,29 +1330,42 @@ __global__ void __launch_bounds__(kSphereThreads) kSpherePass(const Grid<R> laun
             const std::uint32_t nxt = nextSlab(cur + 1);
             const unsigned ob = cb ^ 1U;
             if (chain) {
-                runChain(L.cand_count[cur], stage_base + cb * kCandidatesPerBlock);
+                runChain(L.cand_count[cur], stage_base + cb * kCandidatesPerBlock, log_base + cb * kCandidatesPerBlock,
+                         log_count[cb]);
+            } else if (threadIdx.x < 64) {
+                if (fold && prev < L.blocks) foldLog(log_base + ob * kCandidatesPerBlock, log_count[ob]);
             } else {
                 Staged<R> *other = stage_base + ob * kCandidatesPerBlock;
-                if (prev < L.blocks) writeBack(prev, other, 32, blockDim.x - 32);
-                if (nxt < L.blocks) stageSlab(nxt, other, 32, blockDim.x - 32);
+                if (prev < L.blocks) writeBack(prev, other, 64, blockDim.x - 64);
+                if (nxt < L.blocks) stageSlab(nxt, other, 64, blockDim.x - 64);
             }
             __syncthreads();
             prev = cur;
             cur = nxt;
             cb = ob;
         }
-        if (prev < L.blocks) writeBack(prev, stage_base + (cb ^ 1U) * kCandidatesPerBlock, 0, blockDim.x);
+        if (prev < L.blocks) {
+            if (fold) foldLog(log_base + (cb ^ 1U) * kCandidatesPerBlock, log_count[cb ^ 1U]);
+            writeBack(prev, stage_base + (cb ^ 1U) * kCandidatesPerBlock, 0, blockDim.x);
+        }
     } else {
         for (std::uint32_t b = nextSlab(0); b < L.blocks; b = nextSlab(b + 1)) {
             stageSlab(b, stage_base, 0, blockDim.x);
             __syncthreads();
-            if (chain) runChain(L.cand_count[b], stage_base);
+            if (chain) runChain(L.cand_count[b], stage_base, log_base, log_count[0]);
             __syncthreads();
+            if (fold) foldLog(log_base, log_count[0]);
             writeBack(b, stage_base, 0, blockDim.x);
             __syncthreads();
         }
     }
+    if (fold) folded[lane] = sum;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        acc.impulse_x = folded[0];
+        acc.impulse_y = folded[1];
+        acc.impulse_z = folded[2];
+        acc.dissipated = folded[3];
         const R e1 = R(0.5) * sp.mass * dot(sp.velocity, sp.velocity) + R(0.5) * sp.inertia * dot(sp.angular, sp.angular);
         acc.dissipated += static_cast<double>(e0 - e1);
         const R shift = length(sp.center - c0);
@@ -1381,10 +1511,11 @@ __global__ void __launch_bounds__(kThreads, GBL_SOLVE_MIN_BLOCKS) kSolve(const G
     waitPreviousGrid();
     allowNextGrid();
     if (stop) return;
-    bool live[kSolvePer];
+    bool live[kSolvePer], ok[kSolvePer];
 #pragma unroll
     for (int k = 0; k < kSolvePer; ++k) {
-        live[k] = at[k] < w.end && !(rec[k].a & kDeadBit);
+        ok[k] = at[k] < w.end && endsInBounds(rec[k], L.N, kSiteSolve);
+        live[k] = ok[k] && !(rec[k].a & kDeadBit);
         if (live[k]) {
             qa[k] = ldShared(L.u + endA(rec[k]));
             qb[k] = ldShared(L.u + endB(rec[k]));
@@ -1392,7 +1523,7 @@ __global__ void __launch_bounds__(kThreads, GBL_SOLVE_MIN_BLOCKS) kSolve(const G
     }
 #pragma unroll
     for (int k = 0; k < kSolvePer; ++k)
-        if (at[k] < w.end)
+        if (ok[k])
             finishBond<R, Direct, Plastic, Support>(L, S, at[k], rec[k], live[k], geo[k], lam[k], pl[k], Last, qa[k],
                                                     qb[k]);
 }
@@ -1419,6 +1550,7 @@ __device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Sett
     __syncthreads();
     for (std::uint32_t t = threadIdx.x; t < L.isolated_count; t += blockDim.x) {
         const std::uint32_t i = L.isolated[t];
+        if (!inBounds(i, L.N, kSiteIsolated)) continue;
         const Q4<R> uq = L.u[i];
         V3<R> u = xyz(uq);
         if (supportProject(L, S, i, u)) L.u[i] = Q4<R>{u.x, u.y, u.z, uq.w};
@@ -1487,7 +1619,7 @@ __global__ void __launch_bounds__(T, T >= 1024 ? 1 : 2) kSweepLattice(const Grid
         if (more) load(nxt, next);
         const std::uint32_t end = L.level_begin[cur.lv + 1];
         const std::uint32_t d = cur.base + threadIdx.x;
-        if (d < end) {
+        if (d < end && endsInBounds(now.rec, L.N, kSiteSolve)) {
             if (self_next && cur.it != 0) now.lam = __ldcs(L.lambda + d);
             const bool live = !(now.rec.a & kDeadBit);
             Q4<R> qa{}, qb{};
@@ -1523,7 +1655,7 @@ __global__ void __launch_bounds__(kThreads) kDamp(const Grid<R> launch, R fracti
     // Items are sweep levels' ranges: any length, strided over the CTA.
     for (std::uint32_t d = w.begin + threadIdx.x; d < w.end; d += blockDim.x) {
         const BondRec<R> rec = L.rec[d];
-        if (rec.a & kDeadBit) continue;
+        if ((rec.a & kDeadBit) || !endsInBounds(rec, L.N, kSiteDamp)) continue;
         const std::uint32_t a = endA(rec), b = endB(rec);
         const Q4<R> va = L.v[a], vb = L.v[b];
         const R ma = va.w, mb = vb.w;
@@ -1550,6 +1682,7 @@ __global__ void __launch_bounds__(kThreads) kSupportIsolated(const Grid<R> launc
     const std::uint32_t t = w.begin + threadIdx.x;
     if (t >= w.end) return;
     const std::uint32_t i = L.isolated[t];
+    if (!inBounds(i, L.N, kSiteIsolated)) return;
     const Q4<R> uq = L.u[i];
     V3<R> u = xyz(uq);
     // Written back whenever a projection ran, even by a zero distance, so the
@@ -1645,7 +1778,7 @@ __global__ void __launch_bounds__(kThreads) kEndSample(const Grid<R> launch, Set
         const Q4<R> t4 = ldStream(L.thr4 + j);
         const Q2<R> t2 = L.thr2[j];
         Q2<R> pl = Plastic ? L.plastic[j] : Q2<R>{R(0), R(0)};
-        if (!(rec.a & kDeadBit)) {
+        if (!(rec.a & kDeadBit) && endsInBounds(rec, L.N, kSiteEndSample)) {
             const std::uint32_t a = endA(rec), b = endB(rec);
             const V3<R> edge{g.x, g.y, g.z};
             float plastic_stretch = 0.0F;
@@ -2001,6 +2134,7 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(const Grid<R> launch) 
     // Items: part `begin` of `end` parts of this lattice's event list.
     for (unsigned e = w.begin * blockDim.x + threadIdx.x; e < n; e += w.end * blockDim.x) {
         const std::uint32_t j = L.ev_list[e];
+        if (!inBounds(j, L.B, kSiteEvent)) continue;
         const double running = prior + L.ev_prefix[e];
         const double removed = L.ev_packed[e];
         if (removed > fraction * (running < 1.0e-12 ? 1.0e-12 : running)) atomicOr(&c.energy_gain, 1U);
@@ -2009,9 +2143,13 @@ __global__ void __launch_bounds__(kThreads) kLedgerBroken(const Grid<R> launch) 
         const std::uint32_t ends[2] = {e2.x, e2.y};
         for (int q = 0; q < 2; ++q) {
             const std::uint32_t node = ends[q];
+            if (!inBounds(node, L.N, kSiteEventEnd)) continue;
             unsigned *word = reinterpret_cast<unsigned *>(L.dirty + (node & ~3U));
             const unsigned bit = 1U << (8 * (node & 3U));
-            if (!(atomicOr(word, bit) & bit)) L.dirty_list[atomicAdd(&c.dirty_count, 1U)] = node;
+            if (!(atomicOr(word, bit) & bit)) {
+                const unsigned at = atomicAdd(&c.dirty_count, 1U);
+                if (inBounds(at, L.N, kSiteDirty)) L.dirty_list[at] = node;
+            }
         }
     }
 }
@@ -2060,67 +2198,120 @@ __global__ void __launch_bounds__(kFoldThreads) kKineticFold(const Grid<R> launc
 }
 
 // ---------------------------------------------------------------------------
-// The serial tail of a substep, one thread: the external-load ledger (node
-// order), the substep's FP64 sums into the run totals, the damage-record scan
-// over its (few) candidates in bond order, the sphere drift and support
-// contact, the failure-round bookkeeping and the exit rules
-// (CpuLatticeBackend.cpp:279-298, 441-488).
+// The tail of a substep: the external-load ledger, the substep's FP64 sums
+// into the run totals, the damage-record scan over its (few) candidates in
+// bond order, the sphere drift and support contact, the failure-round
+// bookkeeping and the exit rules (CpuLatticeBackend.cpp:279-298, 441-488).
+//
+// The load ledger is thirteen independent serial folds over the loaded nodes
+// in list order (ExternalLoads.hpp:126-140): impulse, angular impulse, work,
+// requested impulse and requested angular impulse, per component. Lane q of
+// warp 0 runs fold q, so the thirteen chains advance together and each keeps
+// the reference's order; the other warps stage the next chunk of node
+// contributions into shared memory meanwhile. The wrench sources' node runs
+// tile the list in source order, so the same pass folds each source's own
+// change and hands it to its ledger when its run ends. The rest is serial and
+// runs on thread 0.
 // ---------------------------------------------------------------------------
+constexpr unsigned kLedgerThreads = 128;
+constexpr unsigned kLedgerChunk = kLedgerThreads - 32; // entries staged per round
+constexpr int kLedgerFolds = 13;
+
+// Adds a source's folded change (lane q holds component q) to its ledger.
+__device__ __forceinline__ void addLoadComponent(LoadLedger &g, int q, double x) {
+    if (q < 3) g.imp[q] = g.imp[q] + x;
+    else if (q < 6) g.ang[q - 3] = g.ang[q - 3] + x;
+    else if (q == 6) g.work = g.work + x;
+    else if (q < 10) g.req_imp[q - 7] = g.req_imp[q - 7] + x;
+    else g.req_ang[q - 10] = g.req_ang[q - 10] + x;
+}
+
 template <class R, bool Many>
-__global__ void kLedger(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kLedgerThreads) kLedger(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
-    if (threadIdx.x != 0) return;
     Ctl &c = *L.ctl;
-    if (c.stop) return;
-    if (c.error) {
-        c.stop = 1;
-        atomicSub(L.running, 1U);
+    const unsigned stop = c.stop, err = c.error;
+    if (stop) return;
+    if (err) {
+        if (threadIdx.x == 0) {
+            c.stop = 1;
+            atomicSub(L.running, 1U);
+        }
         return;
     }
-    const unsigned long long step = c.total_steps;
+    __shared__ double stage[2][kLedgerChunk * kLedgerFolds];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31U;
     // External loads: this substep's change, folded in node order, then added.
     if (c.ext_count && c.loads_remaining > 0) {
-        double ch[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (std::uint32_t k = 0; k < c.ext_count; ++k) {
-            const double *x = L.ext_contrib + 13 * static_cast<std::size_t>(L.ext_nodes[k]);
-            for (int q = 0; q < 13; ++q) ch[q] += x[q];
-        }
-        LoadLedger &g = c.ext;
-        g.steps += 1;
-        g.elapsed += static_cast<double>(S.dt);
-        for (int q = 0; q < 3; ++q) {
-            g.req_imp[q] = g.req_imp[q] + ch[7 + q];
-            g.req_ang[q] = g.req_ang[q] + ch[10 + q];
-            g.imp[q] = g.imp[q] + ch[q];
-            g.ang[q] = g.ang[q] + ch[3 + q];
-        }
-        g.work = g.work + ch[6];
-        // Each wrench source's own change, folded over its nodes, into its
-        // ledger; a source kicked for the first time since upload takes the
-        // next place in the status order (ExternalLoads.hpp:126-140).
-        for (unsigned k = 0; k < c.wrench_count; ++k) {
-            const WrenchDev &wr = L.wrench[k];
-            double cs[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-            for (std::uint32_t e = wr.begin; e < wr.end; ++e) {
-                const double *x = L.ext_contrib + 13 * static_cast<std::size_t>(L.ext_nodes[e]);
-                for (int q = 0; q < 13; ++q) cs[q] += x[q];
+        const std::uint32_t n = c.ext_count;
+        const unsigned sources = c.wrench_count;
+        const auto fill = [&](std::uint32_t base, unsigned buf) {
+            const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
+            for (unsigned x = threadIdx.x - 32; x < cnt * kLedgerFolds; x += kLedgerThreads - 32) {
+                const unsigned e = x / kLedgerFolds, q = x - e * kLedgerFolds;
+                const std::uint32_t node = L.ext_nodes[base + e];
+                stage[buf][x] = inBounds(node, L.N, kSiteLoad)
+                    ? L.ext_contrib[kLedgerFolds * static_cast<std::size_t>(node) + q] : 0.0;
             }
-            SourceSlot &slot = L.sources[wr.slot];
-            if (slot.load.steps == 0) slot.order = c.source_seq++;
-            LoadLedger &sg = slot.load;
-            sg.steps += 1;
-            sg.elapsed = sg.elapsed + static_cast<double>(S.dt);
-            for (int q = 0; q < 3; ++q) {
-                sg.req_imp[q] = sg.req_imp[q] + cs[7 + q];
-                sg.req_ang[q] = sg.req_ang[q] + cs[10 + q];
-                sg.imp[q] = sg.imp[q] + cs[q];
-                sg.ang[q] = sg.ang[q] + cs[3 + q];
+        };
+        // Flushes every source whose run ends at `at`: lane q adds its
+        // component, lane 0 keeps the step count, the elapsed time and the
+        // source's place in the status order.
+        unsigned k = 0;
+        double run = 0.0;
+        const auto flush = [&](std::uint32_t at) {
+            while (k < sources && L.wrench[k].end == at) {
+                SourceSlot &slot = L.sources[L.wrench[k].slot];
+                if (lane < kLedgerFolds) addLoadComponent(slot.load, static_cast<int>(lane), run);
+                if (lane == 0) {
+                    if (slot.load.steps == 0) slot.order = c.source_seq++;
+                    slot.load.steps += 1;
+                    slot.load.elapsed = slot.load.elapsed + static_cast<double>(S.dt);
+                }
+                run = 0.0;
+                ++k;
             }
-            sg.work = sg.work + cs[6];
+        };
+        if (warp != 0) fill(0, 0);
+        if (warp == 0) flush(0);
+        __syncthreads();
+        double total = 0.0;
+        unsigned buf = 0;
+        for (std::uint32_t base = 0; base < n; base += kLedgerChunk, buf ^= 1U) {
+            if (warp != 0) {
+                if (base + kLedgerChunk < n) fill(base + kLedgerChunk, buf ^ 1U);
+            } else {
+                const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
+                const double *col = stage[buf] + (lane < kLedgerFolds ? lane : 0);
+                if (sources == 0) {
+                    if (lane < kLedgerFolds)
+                        for (std::uint32_t e = 0; e < cnt; ++e) total += col[e * kLedgerFolds];
+                } else {
+                    for (std::uint32_t e = 0; e < cnt; ++e) {
+                        const double x = col[e * kLedgerFolds];
+                        total += x;
+                        run += x;
+                        flush(base + e + 1);
+                    }
+                }
+            }
+            __syncthreads();
         }
-        c.loads_remaining -= 1;
+        if (warp == 0) {
+            flush(n); // only sources with empty runs past the list's end remain
+            LoadLedger &g = c.ext;
+            if (lane < kLedgerFolds) addLoadComponent(g, static_cast<int>(lane), total);
+            if (lane == 0) {
+                g.steps += 1;
+                g.elapsed += static_cast<double>(S.dt);
+                c.loads_remaining -= 1;
+            }
+        }
     }
+    __syncwarp();
+    if (threadIdx.x != 0) return;
+    const unsigned long long step = c.total_steps;
     c.full_restart = 0;
     c.plastic_work += c.plastic_substep;
     for (unsigned e = 0; e < c.dmg_count; ++e) {
@@ -2131,6 +2322,7 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
         }
     }
     const unsigned broken = c.event_count;
+    c.projections += (c.live_bonds - c.broken_bonds) * S.iterations;
     if (broken) {
         c.nc_rebuild = 1; // a failure changes which pairs no live bond holds
         if (c.broken_bonds == 0) c.ffb_count = broken;

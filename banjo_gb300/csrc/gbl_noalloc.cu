@@ -121,11 +121,45 @@ kNoAllocEmit(const std::uint8_t *before, const std::uint8_t *after, std::uint64_
     }
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current: in host code the array's name is only a host-side stand-in.
+// Device address of the scratch array: in host code the array's name is only
+// a host-side stand-in. The address belongs to the context the module was
+// loaded into, so it is kept per device together with that context's unique
+// ID (cuCtxGetId, which a context created after a device reset does not
+// share) and looked up again when the current context is another one.
 std::mutex g_setup_mutex;
 constexpr int kMaxDevices = 64;
-std::uint32_t *g_scratch_address[kMaxDevices] = {};
+struct ScratchAddress {
+    unsigned long long context{};
+    std::uint32_t *address{};
+};
+ScratchAddress g_scratch[kMaxDevices];
+
+// The current context's unique ID, or 0 when none is current or the driver
+// cannot say. The two driver calls are reached through the runtime's entry
+// point table, so the library does not link the driver library itself.
+unsigned long long currentContextId() {
+    using GetCurrent = int (*)(void **);
+    using GetId = int (*)(void *, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) { // under g_setup_mutex
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(a);
+            get_id = reinterpret_cast<GetId>(b);
+        }
+        resolved = true;
+    }
+    if (!get_current || !get_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 std::uint32_t *scratchForCurrentDevice() {
     int device = 0;
@@ -133,14 +167,16 @@ std::uint32_t *scratchForCurrentDevice() {
     if (e != cudaSuccess) runtime(std::string("no current CUDA device: ") + cudaGetErrorString(e));
     if (device < 0 || device >= kMaxDevices) runtime("CUDA device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[device]) {
-        void *ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_tiles);
-        if (e != cudaSuccess || !ptr)
-            runtime(std::string("cannot resolve the static scratch array: ") + cudaGetErrorString(e));
-        g_scratch_address[device] = static_cast<std::uint32_t *>(ptr);
-    }
-    return g_scratch_address[device];
+    ScratchAddress &slot = g_scratch[device];
+    const unsigned long long context = currentContextId();
+    if (slot.address && context != 0 && context == slot.context) return slot.address;
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_tiles); // makes the device's context current if none was
+    if (e != cudaSuccess || !ptr)
+        runtime(std::string("cannot resolve the static scratch array: ") + cudaGetErrorString(e));
+    slot.address = static_cast<std::uint32_t *>(ptr);
+    slot.context = currentContextId();
+    return slot.address;
 }
 
 } // namespace
@@ -156,6 +192,12 @@ extern "C" gbl_result gbl_broken_between_noalloc(const uint8_t *alive_before, co
         if (!broken_count || (bond_count && (!alive_before || !alive_after || !broken)))
             gbl::invalid("gbl_broken_between_noalloc needs device pointers for both snapshots and both outputs");
         cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+        // An error already pending belongs to earlier work: report it without
+        // clearing it, and launch nothing.
+        const cudaError_t pending = cudaPeekAtLastError();
+        if (pending != cudaSuccess)
+            gbl::runtime(std::string("an earlier CUDA error is pending, nothing was listed: ") +
+                         cudaGetErrorString(pending));
         std::uint32_t *tiles = gbl::scratchForCurrentDevice();
         if (bond_count == 0) {
             const cudaError_t e = cudaMemsetAsync(broken_count, 0, sizeof(std::uint32_t), stream);
@@ -167,7 +209,11 @@ extern "C" gbl_result gbl_broken_between_noalloc(const uint8_t *alive_before, co
         gbl::kNoAllocScan<<<1, 1024, 0, stream>>>(tiles, tile_count, broken_count);
         gbl::kNoAllocEmit<<<tile_count, gbl::kNoAllocThreads, 0, stream>>>(alive_before, alive_after, bond_count, tiles,
                                                                             broken);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) gbl::runtime(std::string("broken-bond listing launch: ") + cudaGetErrorString(e));
+        // Nothing was pending before the launches, so an error now is theirs.
+        const cudaError_t e = cudaPeekAtLastError();
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            gbl::runtime(std::string("broken-bond listing launch: ") + cudaGetErrorString(e));
+        }
     });
 }

@@ -23,7 +23,10 @@ import numpy as np
 from . import scenes
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libgbl.so")
+# GBL_LIBRARY=checked loads the bounds-checked build of the same library
+# (every data-driven index checked on the device, violations recorded).
+LIB_PATH = os.path.join(HERE, "_build",
+                        "libgbl_checked.so" if os.environ.get("GBL_LIBRARY") == "checked" else "libgbl.so")
 
 u8p, u32p, f64p, f32p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_float)
 NO_BOND = 0xFFFFFFFF
@@ -251,7 +254,7 @@ class RunStatus(C.Structure):
                 ("rank_deficient_nodes", C.c_uint32), ("plastic_work_j", C.c_double),
                 ("max_plastic_stretch", C.c_float), ("node_contact", NodeContactAccumulators),
                 ("damping_dissipated_j", C.c_double), ("striker_dissipated_j", C.c_double),
-                ("energy_audited", C.c_uint8)]
+                ("energy_audited", C.c_uint8), ("bond_projections", C.c_uint64)]
 
 
 PHASE_NAMES = ["capture", "start_sample_nodes", "start_sample_bonds", "kick_classify", "contact_pass_1",
@@ -291,6 +294,8 @@ def library() -> C.CDLL:
         "gbl_take_frame": ([vp, C.c_uint64, C.POINTER(C.c_uint64), f32p, u8p, f32p, C.POINTER(Sphere)], C.c_int),
         "gbl_clear_frames": ([vp], C.c_int), "gbl_set_stream": ([vp, vp], C.c_int),
         "gbl_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
+        "gbl_bounds_report": ([C.POINTER(C.c_uint64), C.POINTER(C.c_int)], C.c_int),
+        "gbl_bounds_clear": ([], C.c_int),
         "gbl_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_build_schedule": ([C.c_uint32, C.c_uint32, u32p, u32p, u32p, C.c_uint32, C.POINTER(vp)], C.c_int),
         "gbl_schedule_view_of": ([vp, C.POINTER(ScheduleView)], C.c_int), "gbl_schedule_free": ([vp], None),
@@ -386,6 +391,21 @@ def description() -> str:
 
 def multiprocessor_count() -> int:
     return int(library().gbl_multiprocessor_count())
+
+
+def bounds_report() -> dict:
+    """The bounds-checked build's record: whether this library checks, the
+    violations since the last clear, and the first one's site, index and
+    length (all zero in the normal build)."""
+    rep = (C.c_uint64 * 4)()
+    checked = C.c_int()
+    _call(library().gbl_bounds_report, rep, C.byref(checked))
+    return {"checked": bool(checked.value), "violations": int(rep[0]), "site": int(rep[1]), "index": int(rep[2]),
+            "length": int(rep[3])}
+
+
+def bounds_clear() -> None:
+    _call(library().gbl_bounds_clear)
 
 
 class Schedule:
@@ -923,7 +943,7 @@ def status_arrays(st: RunStatus) -> dict:
             float(st.external_load.steps), st.wall_seconds, nc.dissipated_kinetic_energy_j, nc.maximum_overlap_m,
             nc.maximum_position_correction_m, nc.momentum_residual_x, nc.momentum_residual_y, nc.momentum_residual_z,
             st.damping_dissipated_j, st.striker_dissipated_j]
-    return {"status_u64": u, "status_f64": d}
+    return {"status_u64": u, "status_f64": d, "bond_projections": np.array([st.bond_projections], np.uint64)}
 
 
 def run_case(case: dict, precision: str = "float", per_substep: bool = False, threads_per_block: int = 0) -> dict:
@@ -973,22 +993,19 @@ def run_case(case: dict, precision: str = "float", per_substep: bool = False, th
             break_step[newly] = done - 1
             alive_before = state.alive.copy()
     sp = backend.download(state)
-    out = {"u": state.u.copy(), "u_prev": state.u_prev.copy(), "v": state.v.copy(), "alive": state.alive.copy(),
-           "failure_mode": state.failure_mode.copy(), "damage": state.damage.copy(),
-           "plastic_extension": state.plastic_extension.copy(), "plastic_strain": state.plastic_strain.copy(),
-           "prev_tensile": state.prev_tensile.copy(), "prev_compressive": state.prev_compressive.copy(),
-           "prev_shear": state.prev_shear.copy(), "sphere_out": pack_sphere(sp),
-           "first_failure_bonds": backend.first_failure_bonds(), "state_nbr_other": state.nbr_other.copy(),
-           "state_max_degree": np.array([state.view.max_degree], np.uint32)}
+    out = state_outputs(state, sp, backend.first_failure_bonds(), st)
+    out["state_nbr_other"] = state.nbr_other.copy()
+    out["state_max_degree"] = np.array([state.view.max_degree], np.uint32)
     out.update(sched.arrays())
-    out.update(status_arrays(st))
     out.update(source_arrays(backend.external_sources()))
     if per_substep:
         out["break_step"] = break_step
     return out
 
 
-def _outputs(state: State, sp: Sphere, ffb: np.ndarray, st: RunStatus) -> dict:
+def state_outputs(state: State, sp: Sphere, ffb: np.ndarray, st: RunStatus) -> dict:
+    """A downloaded lattice and its status as the output arrays the CPU
+    checkers return (the state and status keys of run_case)."""
     out = {"u": state.u.copy(), "u_prev": state.u_prev.copy(), "v": state.v.copy(), "alive": state.alive.copy(),
            "failure_mode": state.failure_mode.copy(), "damage": state.damage.copy(),
            "plastic_extension": state.plastic_extension.copy(), "plastic_strain": state.plastic_strain.copy(),
@@ -1032,7 +1049,7 @@ def run_batch(cases: list, precision: str = "float", control: RunControl | None 
     outs = []
     for k, state in enumerate(states):
         sp = batch.download(k, state)
-        out = _outputs(state, sp, batch.first_failure_bonds(k), batch.status(k))
+        out = state_outputs(state, sp, batch.first_failure_bonds(k), batch.status(k))
         out.update(source_arrays(batch.external_sources(k)))
         outs.append(out)
     return outs

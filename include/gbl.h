@@ -6,8 +6,8 @@
  * factories). It replaces the removed CUDA backend, whose factory survives as a
  * stub that throws (src/fastlattice/CudaLatticeUnavailable.cpp:11-25). Every
  * struct below mirrors a reference struct field for field, in plain C types, so
- * a C++ adapter converts by member copies and the library needs
- * no reference headers. No torch or CUDA types appear in any signature.
+ * a C++ adapter (banjo_gb300/adapter/Gb300LatticeBackend.cpp) converts by member
+ * copies and the library needs no reference headers. No torch or CUDA types appear in any signature.
  *
  * Errors: every entry point returns a gbl_result. A non-zero value is the C
  * image of the exception the reference throws in the same situation
@@ -236,6 +236,10 @@ typedef struct gbl_run_status {
     double damping_dissipated_j;
     double striker_dissipated_j;
     uint8_t energy_audited;
+    /* Not in the reference's RunStatus: the bond projections the sweeps ran
+     * since upload, per substep the bonds alive when its sweep starts times
+     * the solver iterations -- the throughput measure's numerator. */
+    uint64_t bond_projections;
 } gbl_run_status;
 
 typedef struct gbl_backend gbl_backend;
@@ -467,12 +471,24 @@ gbl_result gbl_serve_footprint(int precision, uint32_t node_count, uint32_t bond
  * the stream reaches that point. At most 134,217,728 bonds (larger counts are
  * refused with GBL_INVALID_ARGUMENT): the scratch is a fixed 64 KiB static
  * device array, held by every GPU that loads the library until the process
- * exits. The first call on a device looks up that array's device address
- * (with the device current); make it before any stream capture. Calls share
- * the array: calls whose work overlaps on the GPU race, so order them on one
- * stream. */
+ * exits. The first call in a context (the device's primary context, again
+ * after a device reset) looks up that array's device address; make it before
+ * any stream capture. A CUDA error already pending on the calling thread is
+ * reported as GBL_RUNTIME_ERROR and left pending, and nothing is launched.
+ * Calls share the array: calls whose work overlaps on the GPU race, so order
+ * them on one stream. */
 gbl_result gbl_broken_between_noalloc(const uint8_t *alive_before, const uint8_t *alive_after, uint64_t bond_count,
                                       uint32_t *broken, uint32_t *broken_count, void *cuda_stream);
+
+/* The bounds-checked build (libgbl_checked.so, compiled with
+ * GBL_BOUNDS_CHECK): every index the kernels read out of device data is
+ * checked against its array's length before use; a violation is counted, the
+ * first one's site, index and length kept, and the access skipped -- nothing
+ * traps. report[0] = violations since the last clear, report[1..3] = the
+ * first one's site, index and length. *checked is 0 in the normal build,
+ * whose report is all zeros. */
+gbl_result gbl_bounds_report(uint64_t report[4], int *checked);
+gbl_result gbl_bounds_clear(void);
 
 /* sizeof of a struct of this header by its name ("gbl_step_settings", ...),
  * 0 for an unknown name: lets a binding check its own layout. */

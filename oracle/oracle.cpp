@@ -1322,6 +1322,10 @@ struct Status {
     NodeAcc node{};
     double damping_dissipated{}, striker_dissipated{};
     bool energy_audited{};
+    // Bond projections the sweeps ran: per substep, the bonds alive when its
+    // sweep starts times the solver iterations. Not a reference counter: the
+    // throughput measure both lanes report alike.
+    std::uint64_t bond_projections{};
 };
 
 // Double vector arithmetic of the load phase (core/Math.hpp:17-69).
@@ -1566,6 +1570,7 @@ public:
         if (S_.nc_mode != 0 && !(contactCutoff(S_) > R(0))) throw std::invalid_argument("node contact needs 2 r + skin > 0");
         status.energy_audited = S_.audit != 0; // CpuLatticeBackend.cpp:114
         kept_ = keepSolveConstants(L_, S_.dt);
+        live_upload_ = countAlive();
     }
     Status status;
     Loads<R> loads;
@@ -1700,6 +1705,7 @@ private:
             spherePass(L_, S_, sp_, 1, status.contact);
             if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
         }
+        status.bond_projections += (live_upload_ - status.broken_bonds) * S_.iterations;
         for (std::uint32_t it = 0; it < S_.iterations; ++it) {
             const bool first = it == 0;
             auto solve = [&](std::size_t j) { solveBond(L_, kept_, j, direct, first); };
@@ -1821,6 +1827,7 @@ public:
         std::fill(L_.candidate_count.begin(), L_.candidate_count.end(), 0U);
         status = Status{};
         status.energy_audited = S_.audit != 0;
+        live_upload_ = countAlive();
         loads.nodes.clear();
         loads.wrenches.clear();
         loads.sources.clear();
@@ -1840,6 +1847,13 @@ private:
     Kept<R> kept_;
     std::vector<std::uint32_t> dirty_list_, touched_;
     std::vector<std::uint8_t> bond_mark_;
+    std::uint64_t live_upload_{}; // bonds alive at upload
+
+    std::uint64_t countAlive() const {
+        std::uint64_t n = 0;
+        for (const std::uint8_t a : L_.alive) n += a != 0;
+        return n;
+    }
 };
 
 template <class R> std::vector<double> widen(const std::vector<R> &v) {
@@ -1983,6 +1997,7 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     }
     out.putScalar<double>("wall_seconds", wall);
     out.putScalar<std::uint32_t>("threads", threads);
+    out.putScalar<std::uint64_t>("bond_projections", st_.bond_projections);
     out.put("substep_seconds", run.substep_seconds);
 }
 

@@ -13,9 +13,11 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_names() -> list[str]:
-    """The lattice-run fixtures (material_*.npz hold material compiles)."""
+    """The lattice-run fixtures (material_*.npz hold material compiles, and
+    cascade_long*.npz the long-horizon record, which keeps digests instead of
+    the case and full outputs)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("material_"))
+                  if not os.path.basename(p).startswith(("material_", "cascade_long")))
 
 
 def load_golden(name: str):

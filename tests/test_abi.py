@@ -33,6 +33,21 @@ def test_every_declared_symbol_is_exported(gbl):
     assert missing == []
 
 
+def test_bounds_checked_build_exports_the_same_symbols(gbl):
+    import ctypes
+
+    from banjo_gb300 import build
+
+    checked = ctypes.CDLL(build.LIB_CHECKED)
+    missing = [n for n in declared_functions() if not hasattr(checked, n)]
+    assert missing == []
+
+
+def test_normal_build_reports_unchecked(gbl):
+    # No CUDA call: the normal build has no record to read.
+    assert gbl.bounds_report() == {"checked": False, "violations": 0, "site": 0, "index": 0, "length": 0}
+
+
 def test_struct_layouts_match_binding(gbl):
     lib = gbl.library()
     import ctypes

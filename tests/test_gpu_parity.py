@@ -34,6 +34,8 @@ def test_gpu_cantilever_full_run_matches_checker(device, port):
     assert int(cpu["status_u64"][4]) > 0
     assert mismatches(cpu, gpu, STATE_KEYS) == []
     assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
+    # The throughput numerator: bonds alive at each sweep times iterations.
+    assert int(gpu["bond_projections"][0]) == int(cpu["bond_projections"][0]) > 0
 
 
 def test_gpu_sliced_impact_matches_checker(device, port):
@@ -45,6 +47,21 @@ def test_gpu_sliced_impact_matches_checker(device, port):
     cpu = port.run_port(case, threads=8, per_substep=True)
     gpu = device.run_case(case, per_substep=True)
     assert int(cpu["status_u64"][4]) > 0 and int(cpu["status_u64"][9]) > 0
+    assert mismatches(cpu, gpu, STATE_KEYS + ["break_step"]) == []
+    assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
+    assert int(gpu["bond_projections"][0]) == int(cpu["bond_projections"][0]) > 0
+
+
+def test_gpu_candidate_overflow_over_several_slabs(device, port):
+    """A sphere large against its slabs: more than 1024 candidates in several
+    slabs of one lattice at once, so every slab's CTA adds to the one overflow
+    counter in the same substep (CpuLatticeBackend.cpp:379-385)."""
+    from banjo_gb300 import scenes
+
+    case = scenes.impact_block(nx=48, ny=24, nz=48, blocks=4, radius=0.25, steps=3)
+    cpu = port.run_port(case, threads=8, per_substep=True)
+    gpu = device.run_case(case, per_substep=True)
+    assert int(cpu["status_u64"][10]) > 10000  # candidate_overflow
     assert mismatches(cpu, gpu, STATE_KEYS + ["break_step"]) == []
     assert status_mismatches(cpu, gpu, ledger_rtol=LEDGER_RTOL) == []
 

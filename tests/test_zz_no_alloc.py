@@ -115,3 +115,32 @@ def test_noalloc_listing_refuses_sizes_beyond_its_scratch(device):
     buf = ctypes.create_string_buffer(256)
     lib.gbl_last_error(buf, 256)
     assert b"134217728" in buf.value
+
+
+@pytest.mark.parametrize("bond_count,seed", [(10_000_019, 3), ((1 << 27) - 5, 4), (1 << 27, 5)])
+def test_noalloc_listing_over_many_tiles(device, bond_count, seed):
+    """Random snapshots of more than 1024 tiles of 8192 bonds: every scan
+    thread adds up several tiles, and the list crosses every tile and warp
+    boundary of the emission. The expected list is numpy's."""
+    lib = device.library()
+    rt = _cudart()
+    rng = np.random.default_rng(seed)
+    before = (rng.random(bond_count) < 0.9).astype(np.uint8)
+    after = before & (rng.random(bond_count) < 0.97).astype(np.uint8)
+    # A few runs of breaks that cross tile boundaries, and a broken last bond.
+    for edge in (8192, 8192 * 1024, 8192 * 1200):
+        if edge + 40 < bond_count:
+            before[edge - 40:edge + 40] = 1
+            after[edge - 40:edge + 40] = 0
+    before[-1], after[-1] = 1, 0
+    expected = np.nonzero((before != 0) & (after == 0))[0].astype(np.uint32)
+    # The output has room for every bond, as the entry point asks.
+    bufs = [DeviceBuffer(rt, bond_count), DeviceBuffer(rt, bond_count), DeviceBuffer(rt, 4 * bond_count),
+            DeviceBuffer(rt, 4)]
+    try:
+        got = _list_broken(lib, rt, before, after, *bufs)
+        assert got.size == expected.size
+        assert np.array_equal(got, expected)
+    finally:
+        for b in bufs:
+            b.free()
