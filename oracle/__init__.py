@@ -116,7 +116,7 @@ OUTPUT_NAMES = ["sched_bond_order", "sched_color", "sched_range_begin", "sched_r
                 "v", "alive", "failure_mode", "damage", "plastic_extension", "plastic_strain", "prev_tensile",
                 "prev_compressive", "prev_shear", "sphere_out", "first_failure_bonds", "break_step", "status_u64",
                 "status_f64", "source_names", "source_ledgers", "wall_seconds", "threads", "substep_seconds",
-                "bond_projections"]
+                "bond_projections", "plastic_increments", "substep_projections"]
 
 
 def run_port(case: dict, precision: str = "float", threads: int = 1, per_substep: bool = False) -> dict:

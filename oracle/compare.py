@@ -85,3 +85,25 @@ def status_mismatches(expected: dict, actual: dict, skip=(), ledger_rtol: float 
         if not (e == a or (np.isnan(e) and np.isnan(a))):
             bad.append(f"{name}: {e!r} != {a!r}")
     return bad
+
+
+def ledger_report(expected: dict, actual: dict) -> dict:
+    """Each FP64 ledger's relative difference beside the most that another
+    summation order of its n non-negative addends can move it, 2 n 2^-53
+    relative (each order's rounding error is at most (n - 1) 2^-53 of the sum
+    of the addends, which for non-negative terms is the sum itself). n is the
+    broken-bond count for the removed energy and the restatement's count of
+    plastic increments for the plastic work; `within` holds when a ledger
+    meets the larger of that bound and LEDGER_RTOL."""
+    n_removed = int(_slot(expected["status_u64"], STATUS_U64["broken_bonds"]))
+    n_plastic = int(np.asarray(expected.get("plastic_increments", [0]))[0])
+    out, ok = {}, True
+    for name, n in (("removed_energy_j", n_removed), ("plastic_work_j", n_plastic)):
+        i = STATUS_F64[name]
+        e, a = float(_slot(expected["status_f64"], i)), float(_slot(actual["status_f64"], i))
+        rel = abs(e - a) / max(abs(e), 1e-300) if e != a else 0.0
+        bound = max(LEDGER_RTOL, 2.0 * n * 2.0 ** -53)
+        out[name] = {"rel_error": rel, "addends": n, "order_bound": bound}
+        ok = ok and rel <= bound
+    out["within"] = ok
+    return out

@@ -1326,6 +1326,10 @@ struct Status {
     // sweep starts times the solver iterations. Not a reference counter: the
     // throughput measure both lanes report alike.
     std::uint64_t bond_projections{};
+    // Non-zero addends folded into plastic_work: with the removed-energy
+    // addends (one per broken bond) it bounds how far another summation
+    // order of these non-negative terms can land, 2 n 2^-53 relative.
+    std::uint64_t plastic_increments{};
 };
 
 // Double vector arithmetic of the load phase (core/Math.hpp:17-69).
@@ -1576,6 +1580,7 @@ public:
     Loads<R> loads;
     std::vector<std::uint32_t> first_failure_bonds;
     std::vector<double> substep_seconds; // wall time of every substep run
+    std::vector<std::uint64_t> substep_projections; // bond projections of every substep run
     double energy_flat_fraction{1.0e-3};
 
     // CpuLatticeBackend.cpp:255-304 for one RunControl with exit rules off.
@@ -1705,7 +1710,9 @@ private:
             spherePass(L_, S_, sp_, 1, status.contact);
             if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
         }
-        status.bond_projections += (live_upload_ - status.broken_bonds) * S_.iterations;
+        const std::uint64_t swept = (live_upload_ - status.broken_bonds) * S_.iterations;
+        status.bond_projections += swept;
+        substep_projections.push_back(swept);
         for (std::uint32_t it = 0; it < S_.iterations; ++it) {
             const bool first = it == 0;
             auto solve = [&](std::size_t j) { solveBond(L_, kept_, j, direct, first); };
@@ -1782,6 +1789,7 @@ private:
         const bool first_round = status.broken_bonds == 0;
         for (const Event &ev : ordered) {
             status.plastic_work += ev.plastic;
+            status.plastic_increments += ev.plastic != 0.0;
             if (ev.damage > status.max_damage + 1.0e-6) {
                 status.max_damage = ev.damage;
                 status.last_damage_gain_step = status.total_steps;
@@ -1998,7 +2006,9 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     out.putScalar<double>("wall_seconds", wall);
     out.putScalar<std::uint32_t>("threads", threads);
     out.putScalar<std::uint64_t>("bond_projections", st_.bond_projections);
+    out.putScalar<std::uint64_t>("plastic_increments", st_.plastic_increments);
     out.put("substep_seconds", run.substep_seconds);
+    out.put("substep_projections", run.substep_projections);
 }
 
 thread_local std::string g_error;
