@@ -1270,8 +1270,11 @@ public:
               "contact pass shared memory");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "stream");
         check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream");
+        check(cudaStreamCreateWithFlags(&loads_, cudaStreamNonBlocking), "stream");
         check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event");
         check(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&load_fork_, cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&load_join_, cudaEventDisableTiming), "event");
         stream_ = own_stream_;
         check(cudaEventCreate(&ev0_), "event");
         check(cudaEventCreate(&ev1_), "event");
@@ -1292,7 +1295,10 @@ public:
         cudaEventDestroy(ev1_);
         cudaEventDestroy(fork_);
         cudaEventDestroy(join_);
+        cudaEventDestroy(load_fork_);
+        cudaEventDestroy(load_join_);
         cudaStreamDestroy(side_);
+        cudaStreamDestroy(loads_);
         cudaStreamDestroy(own_stream_);
     }
 
@@ -2064,6 +2070,11 @@ private:
                 kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr, 1);
         }
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
+        // The load ledger, on its own stream until the serial tail.
+        check(cudaEventRecord(load_fork_, st), "event");
+        check(cudaStreamWaitEvent(loads_, load_fork_, 0), "stream wait");
+        kLoadLedger<R, M><<<each_.count, kLedgerThreads, 0, loads_>>>(grid(each_), S);
+        check(cudaEventRecord(load_join_, loads_), "event");
         if (S.sphere_enabled && slabs_.count) {
             kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
             kMarkHalo<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));
@@ -2121,7 +2132,8 @@ private:
         if (tiles_.count) kEmitEvents<R, M><<<tiles_.count, kThreads, 0, st>>>(grid(tiles_));
         kLedgerBroken<R, M><<<broken_.count, kThreads, 0, st>>>(grid(broken_));
         mark(12);
-        kLedger<R, M><<<each_.count, kLedgerThreads, 0, st>>>(grid(each_), S);
+        check(cudaStreamWaitEvent(st, load_join_, 0), "stream wait");
+        kLedger<R, M><<<each_.count, 32, 0, st>>>(grid(each_), S);
         mark(13);
         check(cudaGetLastError(), "kernel launch");
     }
@@ -2312,8 +2324,8 @@ private:
         std::size_t group_bytes = std::size_t(48) << 20;
     };
     Shape shape_;
-    cudaStream_t own_stream_{}, stream_{}, side_{};
-    cudaEvent_t ev0_{}, ev1_{}, fork_{}, join_{};
+    cudaStream_t own_stream_{}, stream_{}, side_{}, loads_{};
+    cudaEvent_t ev0_{}, ev1_{}, fork_{}, join_{}, load_fork_{}, load_join_{};
     cudaGraph_t graph_{};
     cudaGraphExec_t exec_{};
 };

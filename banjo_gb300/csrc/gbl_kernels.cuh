@@ -2188,6 +2188,7 @@ __global__ void __launch_bounds__(kFoldThreads) kKineticFold(const Grid<R> launc
         __syncthreads();
         if (threadIdx.x == 0) {
             const std::uint32_t n = L.N - base < kFoldThreads ? L.N - base : kFoldThreads;
+#pragma unroll 8
             for (std::uint32_t k = 0; k < n; ++k) total += terms[buf][k];
         }
     }
@@ -2198,20 +2199,21 @@ __global__ void __launch_bounds__(kFoldThreads) kKineticFold(const Grid<R> launc
 }
 
 // ---------------------------------------------------------------------------
-// The tail of a substep: the external-load ledger, the substep's FP64 sums
-// into the run totals, the damage-record scan over its (few) candidates in
-// bond order, the sphere drift and support contact, the failure-round
-// bookkeeping and the exit rules (CpuLatticeBackend.cpp:279-298, 441-488).
+// The external-load ledger of a substep (ExternalLoads.hpp:126-140): thirteen
+// independent serial folds over the loaded nodes in list order -- impulse,
+// angular impulse, work, requested impulse and requested angular impulse, per
+// component -- then added to the run's ledger. Lane q of warp 0 runs fold q,
+// so the thirteen chains advance together and each keeps the reference's
+// order; the other warps stage the next chunk of node contributions into
+// shared memory meanwhile. The wrench sources' node runs tile the list in
+// source order, so the same pass folds each source's own change and hands it
+// to its ledger when its run ends.
 //
-// The load ledger is thirteen independent serial folds over the loaded nodes
-// in list order (ExternalLoads.hpp:126-140): impulse, angular impulse, work,
-// requested impulse and requested angular impulse, per component. Lane q of
-// warp 0 runs fold q, so the thirteen chains advance together and each keeps
-// the reference's order; the other warps stage the next chunk of node
-// contributions into shared memory meanwhile. The wrench sources' node runs
-// tile the list in source order, so the same pass folds each source's own
-// change and hands it to its ledger when its run ends. The rest is serial and
-// runs on thread 0.
+// A fold is a chain of dependent FP64 adds, one per loaded node, so its
+// length sets its time (GB300's FP64 add latency is long). Nothing in the
+// substep reads the ledger before the exit rules at its end, so the kernel
+// runs on a stream of its own from the kick, whose contributions it reads,
+// beside the contact passes, the sweep and the end sample.
 // ---------------------------------------------------------------------------
 constexpr unsigned kLedgerThreads = 128;
 constexpr unsigned kLedgerChunk = kLedgerThreads - 32; // entries staged per round
@@ -2227,19 +2229,13 @@ __device__ __forceinline__ void addLoadComponent(LoadLedger &g, int q, double x)
 }
 
 template <class R, bool Many>
-__global__ void __launch_bounds__(kLedgerThreads) kLedger(const Grid<R> launch, Settings<R> S) {
+__global__ void __launch_bounds__(kLedgerThreads) kLoadLedger(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
     const Dev<R> L = descriptor<R, Many>(launch, w);
     Ctl &c = *L.ctl;
-    const unsigned stop = c.stop, err = c.error;
-    if (stop) return;
-    if (err) {
-        if (threadIdx.x == 0) {
-            c.stop = 1;
-            atomicSub(L.running, 1U);
-        }
-        return;
-    }
+    // A lattice stopped, or whose kick failed this substep, folds nothing
+    // (kLedger stops the latter).
+    if (c.stop || c.error) return;
     __shared__ double stage[2][kLedgerChunk * kLedgerFolds];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31U;
     // External loads: this substep's change, folded in node order, then added.
@@ -2285,7 +2281,10 @@ __global__ void __launch_bounds__(kLedgerThreads) kLedger(const Grid<R> launch, 
                 const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
                 const double *col = stage[buf] + (lane < kLedgerFolds ? lane : 0);
                 if (sources == 0) {
+                    // Unrolled so the shared-memory loads run ahead of the
+                    // dependent adds.
                     if (lane < kLedgerFolds)
+#pragma unroll 8
                         for (std::uint32_t e = 0; e < cnt; ++e) total += col[e * kLedgerFolds];
                 } else {
                     for (std::uint32_t e = 0; e < cnt; ++e) {
@@ -2309,8 +2308,26 @@ __global__ void __launch_bounds__(kLedgerThreads) kLedger(const Grid<R> launch, 
             }
         }
     }
-    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// The serial tail of a substep, one thread: the substep's FP64 sums into the
+// run totals, the damage-record scan over its (few) candidates in bond order,
+// the sphere drift and support contact, the failure-round bookkeeping and the
+// exit rules (CpuLatticeBackend.cpp:279-298, 441-488), after the load ledger.
+// ---------------------------------------------------------------------------
+template <class R, bool Many>
+__global__ void kLedger(const Grid<R> launch, Settings<R> S) {
+    const Work w = item<Many>(launch);
+    const Dev<R> L = descriptor<R, Many>(launch, w);
     if (threadIdx.x != 0) return;
+    Ctl &c = *L.ctl;
+    if (c.stop) return;
+    if (c.error) {
+        c.stop = 1;
+        atomicSub(L.running, 1U);
+        return;
+    }
     const unsigned long long step = c.total_steps;
     c.full_restart = 0;
     c.plastic_work += c.plastic_substep;
