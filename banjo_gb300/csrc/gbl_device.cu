@@ -25,6 +25,7 @@
 #include <mutex>
 #include <set>
 #include <string>
+#include <exception>
 #include <thread>
 #include <type_traits>
 #include <utility>
@@ -1558,6 +1559,56 @@ public:
         requireReady();
         for (unsigned p = 0; p < GBL_PHASE_COUNT; ++p) phase_ms[p] = 0.0;
         if (active_.empty()) return;
+        armUncaptured();
+        std::vector<cudaEvent_t> evs;
+        std::vector<unsigned> ids;
+        auto mark = [&](unsigned phase) {
+            cudaEvent_t e;
+            check(cudaEventCreate(&e), "event");
+            check(cudaEventRecord(e, stream_), "event");
+            evs.push_back(e);
+            ids.push_back(phase);
+        };
+        for (std::uint64_t s = 0; s < substeps; ++s) {
+            mark(0);
+            enqueueSubstep(mark);
+        }
+        check(cudaStreamSynchronize(stream_), "profile");
+        for (std::size_t k = 0; k + 1 < evs.size(); ++k) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, evs[k], evs[k + 1]);
+            phase_ms[ids[k + 1]] += ms;
+        }
+        for (auto e : evs) cudaEventDestroy(e);
+        settleUncaptured(phase_ms);
+    }
+
+    // The phase-diff debug mode: one substep of every lattice, enqueued phase
+    // by phase outside the graph, with lattice `k`'s state downloaded after
+    // each phase whose bit is set in `mask` -- into views[i] for the i-th set
+    // bit, the last occurrence of a phase that repeats (the sweep marks its
+    // phases once per iteration). The state arrays and the sphere are those a
+    // download returns; the run then carries on as a normal substep.
+    void debugSubstep(std::size_t k, std::uint32_t mask, gbl_state_view *views, gbl_sphere *spheres) {
+        requireReady();
+        if (!occupied(k)) invalid("unknown lattice");
+        armUncaptured();
+        auto mark = [&](unsigned phase) {
+            if (phase >= 32 || !((mask >> phase) & 1U)) return;
+            const unsigned i = static_cast<unsigned>(__builtin_popcount(mask & ((1U << phase) - 1U)));
+            check(cudaDeviceSynchronize(), "phase snapshot");
+            lattice(k).download(views[i], spheres ? &spheres[i] : nullptr, stream_);
+        };
+        enqueueSubstep(mark);
+        check(cudaDeviceSynchronize(), "phase snapshot");
+        std::vector<double> none(GBL_PHASE_COUNT, 0.0);
+        settleUncaptured(none.data());
+    }
+
+private:
+    // Before substeps enqueued outside the graph: the control blocks as a run
+    // sets them (exit rules off, spent lattices stopped, loads armed).
+    void armUncaptured() {
         pullControl();
         unsigned running = 0;
         for (auto k : active_) {
@@ -1580,26 +1631,10 @@ public:
         *running_host_ = running;
         check(cudaMemcpyAsync(running_, running_host_, sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "copy");
         prepare();
-        std::vector<cudaEvent_t> evs;
-        std::vector<unsigned> ids;
-        auto mark = [&](unsigned phase) {
-            cudaEvent_t e;
-            check(cudaEventCreate(&e), "event");
-            check(cudaEventRecord(e, stream_), "event");
-            evs.push_back(e);
-            ids.push_back(phase);
-        };
-        for (std::uint64_t s = 0; s < substeps; ++s) {
-            mark(0);
-            enqueueSubstep(mark);
-        }
-        check(cudaStreamSynchronize(stream_), "profile");
-        for (std::size_t k = 0; k + 1 < evs.size(); ++k) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, evs[k], evs[k + 1]);
-            phase_ms[ids[k + 1]] += ms;
-        }
-        for (auto e : evs) cudaEventDestroy(e);
+    }
+
+    // After them: the statuses read back, the phase times added.
+    void settleUncaptured(const double *phase_ms) {
         pullControl();
         for (auto k : active_) {
             slots_[k]->ext_remaining = ctl_host_[k].loads_remaining;
@@ -1607,6 +1642,8 @@ public:
             for (unsigned p = 0; p < GBL_PHASE_COUNT; ++p) slots_[k]->status.phase_seconds[p] += phase_ms[p] * 1e-3;
         }
     }
+
+public:
 
     // The batch autotuner: times the projection sweep of the lattices present
     // under candidate launch shapes and keeps the fastest. The sweep writes
@@ -2341,6 +2378,7 @@ public:
     virtual std::vector<std::pair<std::string, LoadLedger>> sources() = 0;
     virtual void run(const gbl_run_control &) = 0;
     virtual void download(gbl_state_view &, gbl_sphere *) = 0;
+    virtual void debugSubstep(std::uint32_t mask, gbl_state_view *views, gbl_sphere *spheres) = 0;
     virtual void profile(std::uint64_t substeps, double *phase_ms) = 0;
     virtual void setStream(cudaStream_t s) = 0;
     virtual std::uint64_t kernelsPerSubstep() = 0;
@@ -2383,6 +2421,10 @@ public:
     void profile(std::uint64_t substeps, double *phase_ms) override {
         if (engine_.size() == 0) invalid("profiling needs an uploaded lattice");
         engine_.profile(substeps, phase_ms);
+    }
+    void debugSubstep(std::uint32_t mask, gbl_state_view *views, gbl_sphere *spheres) override {
+        if (engine_.size() == 0) invalid("the phase-diff substep needs an uploaded lattice");
+        engine_.debugSubstep(0, mask, views, spheres);
     }
     void setStream(cudaStream_t s) override { engine_.setStream(s); }
     std::uint64_t kernelsPerSubstep() override {
@@ -2463,6 +2505,14 @@ private:
 // frees their memory for the next in line. Each request's result is the one it
 // would get alone: lattices never interact, and each keeps its own control
 // block and ledgers.
+//
+// Two lanes, each an engine with its own streams and substep graph: requests
+// of at least kLargeBonds bonds in one, the rest in the other. A step runs the
+// large lane's chunk on a helper thread while the calling thread keeps
+// stepping the small lane chunk after chunk (retiring and admitting small
+// requests between chunks) until the large chunk is done, so a small request
+// advances at its own lane's pace instead of a large lattice's, and the two
+// lanes' kernels share the GPU.
 class ServerBase {
 public:
     virtual ~ServerBase() = default;
@@ -2473,19 +2523,23 @@ public:
     virtual void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) = 0;
     virtual void cancel(std::uint64_t ticket) = 0;
     virtual void stats(gbl_server_stats &out) = 0;
+    virtual void setLaneThreshold(std::uint32_t bonds) = 0;
 };
 
 template <class R> class Server final : public ServerBase {
 public:
+    static constexpr std::uint32_t kLargeBonds = 1U << 22;
+    static constexpr unsigned kSmall = 0, kLarge = 1;
+
     Server(const gbl_step_settings &settings, std::uint64_t budget)
         : budget_(budget), contact_(settings.node_contact.mode != 0), t0_(clock()) {
-        engine_.configure(settings);
+        for (auto &lane : lanes_) lane.configure(settings);
     }
     ~Server() override {
         for (auto &kv : requests_)
             if (kv.second.phase == GBL_REQUEST_DONE && kv.second.out.base)
-                cudaFreeAsync(kv.second.out.base, engine_.stream());
-        cudaStreamSynchronize(engine_.stream());
+                cudaFreeAsync(kv.second.out.base, lanes_[kv.second.lane].stream());
+        for (auto &lane : lanes_) cudaStreamSynchronize(lane.stream());
     }
 
     std::uint64_t submit(const gbl_schedule_view &sv, const gbl_state_view &st, const gbl_sphere &sp,
@@ -2506,6 +2560,7 @@ public:
         q.prepared = Engine<R>::prepare(Schedule::fromView(sv), st, sp, !borrowed);
         q.nodes = st.node_count;
         q.bonds = st.bond_count;
+        q.lane = st.bond_count >= large_bonds_.load(std::memory_order_relaxed) ? kLarge : kSmall;
         q.sphere = sp;
         q.substeps = substeps;
         q.bytes = bytes;
@@ -2520,20 +2575,50 @@ public:
 
     void step(std::uint64_t substeps, gbl_server_stats *out) override {
         std::lock_guard<std::mutex> lock(mutex_);
-        admit();
-        if (engine_.size() > 0 && substeps > 0) {
+        admit(true);
+        if (substeps > 0 && (lanes_[kSmall].size() > 0 || lanes_[kLarge].size() > 0)) {
             gbl_run_control c{}; // RunControl's defaults (FastLattice.hpp:79-128), exit rules off
             c.energy_flat_fraction = 1.0e-3;
             c.calm_damage_margin = 0.5;
             c.max_steps = substeps;
-            const double before = kernelSeconds();
             const double t0 = clock();
-            engine_.run(c);
+            double large_device = 0.0, small_device = 0.0;
+            if (lanes_[kLarge].size() > 0) {
+                // The large lane's chunk on a helper thread; that thread
+                // touches nothing but its lane until it is joined.
+                std::atomic<bool> large_done{false};
+                std::exception_ptr failure;
+                std::thread large([&] {
+                    try {
+                        const double before = kernelSeconds(kLarge);
+                        lanes_[kLarge].run(c);
+                        large_device = kernelSeconds(kLarge) - before;
+                    } catch (...) {
+                        failure = std::current_exception();
+                    }
+                    large_done.store(true, std::memory_order_release);
+                });
+                try {
+                    bool first = true;
+                    while (lanes_[kSmall].size() > 0 && (first || !large_done.load(std::memory_order_acquire))) {
+                        small_device += runLane(kSmall, c);
+                        admit(false);
+                        first = false;
+                    }
+                } catch (...) {
+                    large.join();
+                    throw;
+                }
+                large.join();
+                if (failure) std::rethrow_exception(failure);
+                substeps_run_ += substeps;
+                retireFinished(kLarge);
+            } else {
+                small_device += runLane(kSmall, c);
+            }
             run_seconds_ += clock() - t0;
-            device_seconds_ += kernelSeconds() - before;
-            substeps_run_ += substeps;
-            retireFinished();
-            admit(); // memory freed this step goes to the next in line now
+            device_seconds_ += std::max(large_device, small_device);
+            admit(true); // memory freed this step goes to the next in line now
         }
         if (out) fillStats(*out);
     }
@@ -2545,7 +2630,8 @@ public:
         info.phase = q.phase;
         info.slot = q.phase == GBL_REQUEST_RUNNING ? static_cast<std::uint32_t>(q.slot) : ~0U;
         info.substeps = q.substeps;
-        info.substeps_done = q.phase == GBL_REQUEST_RUNNING ? engine_.control(q.slot).total_steps : q.done_steps;
+        info.substeps_done =
+            q.phase == GBL_REQUEST_RUNNING ? lanes_[q.lane].control(q.slot).total_steps : q.done_steps;
         info.device_bytes = q.bytes;
         info.submitted_s = q.submitted;
         info.admitted_s = q.admitted;
@@ -2554,6 +2640,7 @@ public:
 
     void take(std::uint64_t ticket, gbl_state_view *st, gbl_sphere *sp, gbl_run_status *status) override {
         StateOut out;
+        unsigned lane = kSmall;
         {
             std::lock_guard<std::mutex> lock(mutex_);
             Request &q = find(ticket);
@@ -2563,16 +2650,17 @@ public:
             if (sp) *sp = q.sphere;
             if (status) *status = q.status;
             out = q.out;
+            lane = q.lane;
             requests_.erase(ticket);
             --done_;
         }
         // The copies into the caller's arrays run on the caller's thread,
         // outside the lock (they use their own streams); the result's device
         // memory is then freed, stream-ordered, under the lock (a step may be
-        // capturing on the engine's stream).
+        // capturing on the lane's stream).
         if (st) out.copyTo(*st);
         std::lock_guard<std::mutex> lock(mutex_);
-        check(cudaFreeAsync(out.base, engine_.stream()), "device free");
+        check(cudaFreeAsync(out.base, lanes_[lane].stream()), "device free");
         used_ -= out.bytes;
     }
 
@@ -2583,12 +2671,12 @@ public:
             queue_.erase(std::find(queue_.begin(), queue_.end(), ticket));
             --queued_;
         } else if (q.phase == GBL_REQUEST_RUNNING) {
-            engine_.retire(q.slot);
+            lanes_[q.lane].retire(q.slot);
             used_ -= q.bytes;
             --running_;
         } else if (q.phase == GBL_REQUEST_DONE) {
             --done_;
-            check(cudaFreeAsync(q.out.base, engine_.stream()), "device free");
+            check(cudaFreeAsync(q.out.base, lanes_[q.lane].stream()), "device free");
             used_ -= q.out.bytes;
         }
         requests_.erase(ticket);
@@ -2598,6 +2686,10 @@ public:
         std::lock_guard<std::mutex> lock(mutex_);
         fillStats(o);
     }
+
+    // Requests submitted from now on with at least `bonds` bonds take the
+    // large lane.
+    void setLaneThreshold(std::uint32_t bonds) override { large_bonds_.store(bonds, std::memory_order_relaxed); }
 
 private:
     void fillStats(gbl_server_stats &o) {
@@ -2618,6 +2710,7 @@ private:
     struct Request {
         std::uint64_t ticket{}, substeps{}, bytes{}, done_steps{};
         std::uint32_t nodes{}, bonds{};
+        unsigned lane{kSmall};
         std::unique_ptr<Resident<R>> prepared;
         gbl_sphere sphere{};
         int phase{GBL_REQUEST_QUEUED};
@@ -2637,28 +2730,43 @@ private:
         return it->second;
     }
 
-    double kernelSeconds() {
+    double kernelSeconds(unsigned lane) {
         double s = 0;
-        for (std::size_t k = 0; k < engine_.slots(); ++k)
-            if (engine_.occupied(k)) s = std::max(s, engine_.lattice(k).status.kernel_seconds);
+        Engine<R> &e = lanes_[lane];
+        for (std::size_t k = 0; k < e.slots(); ++k)
+            if (e.occupied(k)) s = std::max(s, e.lattice(k).status.kernel_seconds);
         return s;
     }
 
+    // One chunk of the small lane, then its finished requests retired.
+    double runLane(unsigned lane, const gbl_run_control &c) {
+        const double before = kernelSeconds(lane);
+        lanes_[lane].run(c);
+        const double device = kernelSeconds(lane) - before;
+        if (lane == kSmall && lanes_[kLarge].size() == 0) substeps_run_ += c.max_steps;
+        retireFinished(lane);
+        return device;
+    }
+
     // Arrival order, while the next request fits what is left of the budget.
+    // With `any_lane` false (the large lane is running on its helper thread)
+    // admission stops at the first large request in line.
     // (Converting admitted requests on a second stream beside the running
     // ones was measured slower: the conversion's reads of host memory slowed
     // the running kernels by more than they overlapped.)
-    void admit() {
+    void admit(bool any_lane) {
         const double t0 = clock();
         while (!queue_.empty()) {
             Request &q = requests_.at(queue_.front());
             if (used_ + q.bytes > budget_) break;
-            q.slot = engine_.place(std::move(q.prepared), q.substeps);
+            if (!any_lane && q.lane != kSmall) break;
+            q.slot = lanes_[q.lane].place(std::move(q.prepared), q.substeps);
             q.phase = GBL_REQUEST_RUNNING;
             q.admitted = clock() - t0_;
             used_ += q.bytes;
-            slot_ticket_.resize(std::max(slot_ticket_.size(), q.slot + 1));
-            slot_ticket_[q.slot] = q.ticket;
+            auto &tickets = slot_ticket_[q.lane];
+            tickets.resize(std::max(tickets.size(), q.slot + 1));
+            tickets[q.slot] = q.ticket;
             queue_.pop_front();
             --queued_;
             ++running_;
@@ -2666,27 +2774,24 @@ private:
         admit_seconds_ += clock() - t0;
     }
 
-    void retireFinished() {
+    void retireFinished(unsigned lane) {
         const double t0 = clock();
-        retireDone();
-        retire_seconds_ += clock() - t0;
-    }
-    void retireDone() {
-        for (std::size_t k = 0; k < engine_.slots(); ++k) {
-            if (!engine_.occupied(k)) continue;
-            const Ctl &c = engine_.control(k);
+        Engine<R> &e = lanes_[lane];
+        for (std::size_t k = 0; k < e.slots(); ++k) {
+            if (!e.occupied(k)) continue;
+            const Ctl &c = e.control(k);
             if (!(c.step_limit != 0 && c.total_steps >= c.step_limit) && c.exit_reason == 0) continue;
-            Request &q = requests_.at(slot_ticket_[k]);
-            Resident<R> &l = engine_.lattice(k);
+            Request &q = requests_.at(slot_ticket_[lane][k]);
+            Resident<R> &l = e.lattice(k);
             // The result, in the state's layout, stays on the device until
             // take() copies it out; the lattice's own memory is freed now.
-            q.out = l.stateOut(engine_.stream());
-            check(cudaStreamSynchronize(engine_.stream()), "retire");
+            q.out = l.stateOut(e.stream());
+            check(cudaStreamSynchronize(e.stream()), "retire");
             q.sphere = l.fetchSphere();
             q.status = l.status;
             q.status.exit_reason = c.exit_reason;
             q.done_steps = c.total_steps;
-            engine_.retire(k); // synchronises the stream: the result is written
+            e.retire(k); // synchronises the stream: the result is written
             used_ -= q.bytes;
             used_ += q.out.bytes;
             q.phase = GBL_REQUEST_DONE;
@@ -2694,9 +2799,11 @@ private:
             --running_;
             ++done_;
         }
+        retire_seconds_ += clock() - t0;
     }
 
-    Engine<R> engine_;
+    Engine<R> lanes_[2];
+    std::atomic<std::uint32_t> large_bonds_{kLargeBonds};
     std::uint64_t budget_, used_{0}, last_ticket_{0};
     bool contact_; // node-to-node contact on: every request also holds its pair-list scratch
     std::uint64_t queued_{0}, running_{0}, done_{0}, substeps_run_{0};
@@ -2704,7 +2811,7 @@ private:
     double t0_;
     std::map<std::uint64_t, Request> requests_;
     std::deque<std::uint64_t> queue_;
-    std::vector<std::uint64_t> slot_ticket_;
+    std::vector<std::uint64_t> slot_ticket_[2];
     std::mutex mutex_;
 };
 
@@ -2930,6 +3037,14 @@ gbl_result gbl_profile_phases(gbl_backend *backend, uint64_t substeps, double *p
     });
 }
 
+gbl_result gbl_debug_substep(gbl_backend *backend, uint32_t phase_mask, gbl_state_view *states, gbl_sphere *spheres) {
+    return gbl::guard([&] {
+        if (!backend || (phase_mask && !states)) gbl::invalid("null argument");
+        if (phase_mask >> GBL_PHASE_COUNT) gbl::invalid("phase mask names no such phase");
+        backend->impl->debugSubstep(phase_mask, states, spheres);
+    });
+}
+
 gbl_result gbl_batch_create(int precision, gbl_batch **out) {
     return gbl::guard([&] {
         if (!out) gbl::invalid("null argument");
@@ -3129,6 +3244,14 @@ gbl_result gbl_serve_stats(gbl_server *server, gbl_server_stats *stats) {
     return gbl::guard([&] {
         if (!server || !stats) gbl::invalid("null argument");
         server->impl->stats(*stats);
+    });
+}
+
+gbl_result gbl_serve_set_lane_threshold(gbl_server *server, uint32_t bonds) {
+    return gbl::guard([&] {
+        if (!server) gbl::invalid("null argument");
+        if (bonds == 0) gbl::invalid("the large lane's threshold must be at least one bond");
+        server->impl->setLaneThreshold(bonds);
     });
 }
 

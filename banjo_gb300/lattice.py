@@ -296,6 +296,8 @@ def library() -> C.CDLL:
         "gbl_profile_phases": ([vp, C.c_uint64, f64p], C.c_int),
         "gbl_bounds_report": ([C.POINTER(C.c_uint64), C.POINTER(C.c_int)], C.c_int),
         "gbl_bounds_clear": ([], C.c_int),
+        "gbl_serve_set_lane_threshold": ([vp, C.c_uint32], C.c_int),
+        "gbl_debug_substep": ([vp, C.c_uint32, C.POINTER(StateView), C.POINTER(Sphere)], C.c_int),
         "gbl_kernels_per_substep": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "gbl_build_schedule": ([C.c_uint32, C.c_uint32, u32p, u32p, u32p, C.c_uint32, C.POINTER(vp)], C.c_int),
         "gbl_schedule_view_of": ([vp, C.POINTER(ScheduleView)], C.c_int), "gbl_schedule_free": ([vp], None),
@@ -762,6 +764,21 @@ class Backend:
         _call(library().gbl_profile_phases, self._h, int(substeps), _ptr(out, C.c_double))
         return {PHASE_NAMES[k]: float(out[k]) for k in range(16)}
 
+    def debug_substep(self, phases, states) -> list:
+        """The phase-diff mode (gbl_debug_substep): one substep, with the
+        lattice's state downloaded into states[i] after phases[i] (ascending
+        phase numbers); returns the spheres at those points."""
+        phases = list(phases)
+        if phases != sorted(set(phases)) or len(states) != len(phases):
+            raise ValueError("phases ascending and distinct, one state each")
+        mask = 0
+        for ph in phases:
+            mask |= 1 << int(ph)
+        views = (StateView * len(states))(*[st.view for st in states])
+        spheres = (Sphere * len(states))()
+        _call(library().gbl_debug_substep, self._h, mask, views, spheres)
+        return list(spheres)
+
 
 def make_gb300_lattice_backend(schedule: Schedule, precision: str = "float", threads_per_block: int = 0) -> Backend:
     """The factory that replaces makeCudaLatticeBackend (FastLattice.hpp:401-402)."""
@@ -916,6 +933,11 @@ class Server:
         st = ServerStats()
         _call(library().gbl_serve_stats, self._h, C.byref(st))
         return st
+
+    def set_lane_threshold(self, bonds: int) -> None:
+        """Requests submitted from now on with at least `bonds` bonds run in
+        the large lane (gbl_serve_set_lane_threshold)."""
+        _call(library().gbl_serve_set_lane_threshold, self._h, int(bonds))
 
 
 def footprint(node_count: int, bond_count: int, max_degree: int, block_count: int, precision: str = "float") -> int:

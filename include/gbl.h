@@ -326,6 +326,21 @@ gbl_result gbl_kernels_per_substep(gbl_backend *backend, uint64_t *count);
  * gbl_run with max_steps = substeps and exit rules off. */
 gbl_result gbl_profile_phases(gbl_backend *backend, uint64_t substeps, double *phase_ms);
 
+/* The phase-diff debug mode: one substep run outside the captured graph,
+ * with the lattice's state downloaded after every phase whose bit is set in
+ * phase_mask (bit p: the phase latticePhaseName(p) names) into states[i] and,
+ * when spheres is not null, spheres[i], for the i-th set bit; a phase the
+ * substep marks more than once (the sweep's, once per iteration) gives its
+ * last. Each view is a caller-owned state of the lattice's counts, as for
+ * gbl_download. The substep then completes like one of gbl_run. The device
+ * fuses or reorders some phases (support projection inside the sweep, the
+ * restart and part of the end sample beside the contact passes), so a
+ * snapshot equals the reference's at the same phase only where both have
+ * finished the same work: after the kick (nodes), the first contact pass,
+ * the sweep with its support projection (phase 7), the velocity update, the
+ * damping, the second contact pass (nodes), the end sample and the ledger. */
+gbl_result gbl_debug_substep(gbl_backend *backend, uint32_t phase_mask, gbl_state_view *states, gbl_sphere *spheres);
+
 /* ---- The batch: many independent lattices advanced together. ----
  * The reference runs a batch of trials as one backend per trial
  * (runTileImpact, src/fastlattice/TileImpactScene.cpp:777; makeBackend
@@ -453,6 +468,12 @@ gbl_result gbl_serve_take(gbl_server *server, uint64_t ticket, gbl_state_view *s
                           gbl_run_status *status);
 gbl_result gbl_serve_cancel(gbl_server *server, uint64_t ticket);
 gbl_result gbl_serve_stats(gbl_server *server, gbl_server_stats *stats);
+/* Requests submitted from now on with at least `bonds` bonds run in the
+ * server's large lane (default 4,194,304): a step advances the large lane one
+ * chunk on a helper thread while the small lane advances chunk after chunk
+ * beside it, so small requests do not wait on a large lattice's substeps.
+ * Results do not depend on the lane. */
+gbl_result gbl_serve_set_lane_threshold(gbl_server *server, uint32_t bonds);
 /* Device bytes a lattice of these counts is charged on admission. */
 gbl_result gbl_serve_footprint(int precision, uint32_t node_count, uint32_t bond_count, uint32_t max_degree,
                                uint32_t block_count, uint64_t *bytes);

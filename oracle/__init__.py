@@ -119,6 +119,12 @@ OUTPUT_NAMES = ["sched_bond_order", "sched_color", "sched_range_begin", "sched_r
                 "bond_projections", "plastic_increments", "substep_projections"]
 
 
+# The arrays the phase-diff mode records after each requested phase (case keys
+# "phase_substep" and "phase_mask"), as "phase<p>__<array>" outputs.
+PHASE_ARRAYS = ["u", "u_prev", "v", "alive", "failure_mode", "damage", "plastic_extension", "plastic_strain",
+                "prev_tensile", "prev_compressive", "prev_shear", "sphere_out"]
+
+
 def run_port(case: dict, precision: str = "float", threads: int = 1, per_substep: bool = False) -> dict:
     """Runs the CPU restatement on a case; returns its outputs."""
     lib = _port()
@@ -134,7 +140,11 @@ def run_port(case: dict, precision: str = "float", threads: int = 1, per_substep
         if rc != 0:
             raise RuntimeError("oracle: " + lib.oracle_last_error().decode())
         out = {}
-        for name in OUTPUT_NAMES:
+        names = list(OUTPUT_NAMES)
+        if "phase_mask" in case:
+            mask = int(np.asarray(case["phase_mask"]).reshape(-1)[0])
+            names += [f"phase{p}__{a}" for p in range(32) if (mask >> p) & 1 for a in PHASE_ARRAYS]
+        for name in names:
             count = lib.oracle_case_count(cout, name.encode())
             if count < 0:
                 continue

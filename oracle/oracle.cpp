@@ -1581,6 +1581,9 @@ public:
     std::vector<std::uint32_t> first_failure_bonds;
     std::vector<double> substep_seconds; // wall time of every substep run
     std::vector<std::uint64_t> substep_projections; // bond projections of every substep run
+    // The phase-diff mode: called at the end of each phase of a substep with
+    // the phase's number (latticePhaseName's, FastLattice.cpp:15-28).
+    std::function<void(unsigned)> phase_hook;
     double energy_flat_fraction{1.0e-3};
 
     // CpuLatticeBackend.cpp:255-304 for one RunControl with exit rules off.
@@ -1705,11 +1708,13 @@ private:
             L_.candidate_count[b] = std::min(count, kCandidatesPerBlock);
         }
         sp_ = kicked;
+        phase(3);
         if (S_.sphere_enabled) {
             const double before = S_.audit ? kineticEnergy(L_) : 0.0;
             spherePass(L_, S_, sp_, 1, status.contact);
             if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
         }
+        phase(4);
         const std::uint64_t swept = (live_upload_ - status.broken_bonds) * S_.iterations;
         status.bond_projections += swept;
         substep_projections.push_back(swept);
@@ -1719,27 +1724,34 @@ private:
             sweepAll(solve);
             nodes([&](std::size_t i) { nodeSupportProject(L_, S_, i); });
         }
+        phase(7);
         nodes([&](std::size_t i) {
             const V<R> vel = divide(sub(ld(L_.u, i), ld(L_.u_prev, i)), S_.dt);
             st(L_.v, i, vel);
             if (S_.damping_fraction <= R(0) && !L_.candidate[i]) nodeSupportVelocity(L_, S_, i);
         });
+        phase(8);
         if (S_.damping_fraction > R(0)) {
             const double before = S_.audit ? kineticEnergy(L_) : 0.0;
             sweepAll([&](std::size_t j) { dampBond(L_, j, S_.damping_fraction, direct); });
             if (S_.audit) status.damping_dissipated += before - kineticEnergy(L_);
             nodes([&](std::size_t i) { if (!L_.candidate[i]) nodeSupportVelocity(L_, S_, i); });
+            phase(9);
         }
         if (S_.sphere_enabled) {
             const double before = S_.audit ? kineticEnergy(L_) : 0.0;
             spherePass(L_, S_, sp_, 2, status.contact);
             if (S_.audit) status.striker_dissipated += before - kineticEnergy(L_);
         }
+        phase(10);
         if (S_.nc_mode != 0) {
             if (pairs_.rebuild || pairListStale(L_, S_, pairs_)) rebuildPairs(L_, S_, pairs_, status.node);
             contactPass(L_, S_, pairs_, status.node);
+            phase(15);
         }
-        return finishStep(direct);
+        const bool failed = finishStep(direct);
+        phase(13);
+        return failed;
     }
 
     // CpuLatticeBackend.cpp:441-488. The bond loop runs in chunks on the pool;
@@ -1748,6 +1760,7 @@ private:
     // threaded lane does the same, ParallelCpuLatticeBackend.cpp:1885-1910).
     bool finishStep(bool direct) {
         strainAll(direct);
+        phase(11);
         const unsigned T = pool_.size();
         struct Event { std::uint32_t j; double removed, plastic; float damage; bool broke; };
         // One tally per participant, each on its own cache lines; a chunk
@@ -1782,6 +1795,7 @@ private:
             status.max_s = std::max(status.max_s, tally[t].s);
             status.max_plastic_stretch = std::max(status.max_plastic_stretch, tally[t].p);
         }
+        phase(12);
         std::vector<Event> ordered;
         for (unsigned t = 0; t < T; ++t) ordered.insert(ordered.end(), tally[t].events.begin(), tally[t].events.end());
         std::sort(ordered.begin(), ordered.end(), [](const Event &x, const Event &y) { return x.j < y.j; });
@@ -1813,6 +1827,9 @@ private:
 
 public:
     Sphere<R> sphere() const { return sp_; }
+    void phase(unsigned p) {
+        if (phase_hook) phase_hook(p);
+    }
 
     // upload of the state a download wrote (LatticeWorking.hpp:53-124 on the
     // arrays LatticeWorking.hpp:126-142 writes back): positions, velocities
@@ -1925,6 +1942,25 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
     std::vector<std::uint8_t> alive_before = L.alive;
     const std::vector<std::uint8_t> nbr_alive_built = L.nbr_alive;
     const std::uint64_t resume_at = c.scalarOr<std::uint64_t>("checkpoint_at", 0);
+    // The phase-diff mode: the state after each phase of `phase_mask` in
+    // substep `phase_substep`, as "phase<p>__<array>" outputs.
+    const bool phases = c.has("phase_substep");
+    const std::uint64_t phase_at = phases ? c.scalar<std::uint64_t>("phase_substep") : 0;
+    const std::uint32_t phase_mask = phases ? c.scalar<std::uint32_t>("phase_mask") : 0;
+    const auto dump = [&](unsigned p) {
+        if (p >= 32 || !((phase_mask >> p) & 1U)) return;
+        const std::string k = "phase" + std::to_string(p) + "__";
+        out.put(k + "u", widen(L.u)); out.put(k + "u_prev", widen(L.u_prev)); out.put(k + "v", widen(L.v));
+        out.put(k + "alive", L.alive); out.put(k + "failure_mode", L.failure_mode);
+        out.put(k + "damage", widen(L.damage)); out.put(k + "plastic_extension", widen(L.plastic_ext));
+        out.put(k + "plastic_strain", widen(L.plastic_strain));
+        out.put(k + "prev_tensile", widen(L.prev_t)); out.put(k + "prev_compressive", widen(L.prev_c));
+        out.put(k + "prev_shear", widen(L.prev_s));
+        const Sphere<R> sp = run.sphere();
+        out.put(k + "sphere_out", std::vector<double>{sp.center.x, sp.center.y, sp.center.z, sp.velocity.x, sp.velocity.y,
+                                                      sp.velocity.z, sp.angular.x, sp.angular.y, sp.angular.z, sp.radius,
+                                                      sp.mass, sp.inertia});
+    };
     const std::uint64_t chunk = per_substep ? 1 : (ramp ? per_step : steps);
     const auto t0 = std::chrono::steady_clock::now();
     for (std::uint64_t done = 0; done < steps;) {
@@ -1940,7 +1976,16 @@ template <class R> void runCase(const lsio::Case &c, lsio::Case &out, unsigned t
             if (done < resume_at) n = std::min(n, resume_at - done);
             else if (done == resume_at) run.reupload(nbr_alive_built); // checkpoint and resume
         }
+        if (phases && done <= phase_at && phase_at < done + n) {
+            if (done < phase_at) {
+                n = phase_at - done;
+            } else {
+                n = 1;
+                run.phase_hook = dump;
+            }
+        }
         run.run(n);
+        run.phase_hook = nullptr;
         done += n;
         if (per_substep) {
             for (std::uint32_t k = 0; k < L.B; ++k)

@@ -47,9 +47,11 @@ def _result(device, state, sphere, status):
     return out
 
 
-def _serve(device, cases, budget, arrivals, chunk=7, borrow=False):
+def _serve(device, cases, budget, arrivals, chunk=7, borrow=False, lane_threshold=None):
     """Submits case k before step arrivals[k]; steps until every request is done."""
     server = device.Server(device.step_settings(cases[0]["settings"]), budget)
+    if lane_threshold is not None:
+        server.set_lane_threshold(lane_threshold)
     tickets, states, peak = {}, {}, 0
     step = 0
     while len(tickets) < len(cases) or any(server.poll(t).phase != device.REQUEST_DONE for t in tickets.values()):
@@ -137,6 +139,24 @@ def test_borrowed_requests_equal_each_request_alone(device):
     budget = sorted(sizes)[-1] + sorted(sizes)[-2]
     outs, peak = _serve(device, cases, budget=budget, arrivals=[0, 0, 0, 1, 1, 2], borrow=True)
     assert 1 <= peak < len(cases)
+    for k, case in enumerate(cases):
+        alone = device.run_case(case)
+        assert mismatches(alone, outs[k], SERVED_KEYS) == [], k
+        assert status_mismatches(alone, outs[k]) == [], k
+
+
+def test_two_lanes_equal_each_request_alone(device):
+    """With the large lane's threshold inside the requests' sizes, the larger
+    requests run on the helper thread's lane while the smaller ones step
+    beside them, several chunks per step: every result is still the one the
+    request gets alone."""
+    cases = _requests()
+    sizes = sorted(int(c["bond_count"][0]) for c in cases)
+    threshold = sizes[len(sizes) // 2]
+    outs, peak = _serve(device, cases, budget=1 << 34, arrivals=[0, 1, 1, 2, 4, 4], chunk=5,
+                        lane_threshold=threshold)
+    assert peak >= 3
+    assert sum(int(c["bond_count"][0]) >= threshold for c in cases) >= 2
     for k, case in enumerate(cases):
         alone = device.run_case(case)
         assert mismatches(alone, outs[k], SERVED_KEYS) == [], k
