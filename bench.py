@@ -56,6 +56,7 @@ projections over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -238,13 +239,23 @@ def impact_parity(args, lattice, case) -> tuple[dict, dict, dict]:
                           f"restart substep left out), {threads} host threads, {timed:.1f} s timed; "
                           "the restatement's threaded lane runs within 1.15x of the reference's threaded lane at "
                           "equal threads (calibration test tests/test_port_speed.py)"}
+    del cpu, gpu
+    gc.collect()
     fp = None
     if args.fp64_steps > 0:
+        # The FP64 run is the device's double lane (direct arithmetic), which
+        # the restatement's double lane and the reference's double fixtures
+        # hold bit for bit (tests/test_gpu_parity.py, test_gpu_edges.py): at
+        # this size the restatement in double would need more host memory
+        # than the benchmark may take.
         f_sub = args.fp64_steps * SUBSTEPS_PER_STEP
-        gpu_f = gpu if f_sub == p_sub else lattice.run_case(prefix(case, f_sub))
-        cpu64 = oracle.run_port(prefix(case, f_sub), precision="double", threads=threads)
-        fp = dict(fp64_error(case, gpu_f, cpu64), steps=args.fp64_steps,
-                  note="device FP32 against the restatement in FP64 (direct arithmetic), same case and substeps")
+        gpu32 = lattice.run_case(prefix(case, f_sub))
+        gpu64 = lattice.run_case(prefix(case, f_sub), precision="double")
+        fp = dict(fp64_error(case, gpu32, gpu64), steps=args.fp64_steps,
+                  note="device FP32 against the device's FP64 lane (direct arithmetic, bit-identical to the "
+                       "restatement's FP64 lane), same case and substeps")
+        del gpu32, gpu64
+        gc.collect()
     return parity, fp, baseline
 
 
@@ -301,6 +312,9 @@ def run_gb300(args) -> None:
     # streamed.
     traffic = args.sweep_traffic_per_bond * b if args.workload.startswith("impact") else None
 
+    d = max(1, state.view.max_degree)
+    del backend, state  # host and device memory for the e2e lattice
+    gc.collect()
     # e2e: through the C ABI from host buffers (upload, K steps, download).
     e2e_state = lattice.build_lattice_state(case, sched)
     e2e_backend = lattice.make_gb300_lattice_backend(sched)
@@ -321,10 +335,10 @@ def run_gb300(args) -> None:
     # vector, weight, alive flag, other node and bond; per bond 19 arrays
     # (ends, slots, flags, rest data, thresholds, damage state) and the
     # storage order -- and download returns u, u_prev, v and 8 bond arrays.
-    d = max(1, state.view.max_degree)
     h2d = n * 14 * 8 + n * d * 41 + b * (164 + 4)
     d2h = n * 3 * 24 + b * (2 + 6 * 8)
-    del e2e_backend, e2e_state
+    del e2e_backend, e2e_state, sched
+    gc.collect()
 
     line = {
         "metric": METRIC,
@@ -364,7 +378,6 @@ def run_gb300(args) -> None:
         "host_seconds": host_s,
         "phase_ms_per_substep": {k: v / args.profile_substeps for k, v in phases.items() if v > 0},
     }
-    del backend, state
     if rank == 0 and args.parity_steps > 0:
         parity, fp, baseline = impact_parity(args, lattice, case)
         line["parity"] = parity
@@ -504,6 +517,36 @@ def trial_cpu_baseline(specs, substeps: int = 2) -> dict:
                       f"serial lane per thread on {threads} threads; {secs:.1f} thread-seconds timed"}
 
 
+class ScratchDownload:
+    """Download targets for lattices of any size up to a bound, sharing one
+    set of host arrays: a view with a lattice's counts whose pointers lead
+    into the shared arrays (download writes positions, velocities and the
+    bond state, nothing else). Keeps a 4096-trial batch's downloads from
+    holding every trial's state in host memory at once."""
+
+    def __init__(self, lattice, max_nodes: int, max_bonds: int):
+        import ctypes as C
+
+        self._C = C
+        self.lattice = lattice
+        self.nodes3 = [np.zeros(3 * max_nodes) for _ in range(3)]
+        self.bytes = [np.zeros(max_bonds, np.uint8) for _ in range(2)]
+        self.doubles = [np.zeros(max_bonds) for _ in range(6)]
+        self.view = lattice.StateView()
+
+    def target(self, nodes: int, bonds: int, degree: int):
+        C = self._C
+        v = self.view
+        v.node_count, v.bond_count, v.max_degree = nodes, bonds, degree
+        f64 = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        u8 = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint8))  # noqa: E731
+        v.u, v.u_prev, v.v = (f64(a) for a in self.nodes3)
+        v.alive, v.failure_mode = (u8(a) for a in self.bytes)
+        (v.damage, v.prev_tensile, v.prev_compressive, v.prev_shear, v.plastic_extension,
+         v.plastic_strain) = (f64(a) for a in self.doubles)
+        return self
+
+
 def batched_leg(args, lattice) -> dict:
     """Config-3 trials in one batch against the same trials run one lattice at
     a time through the single-lattice backend ("plain")."""
@@ -512,29 +555,36 @@ def batched_leg(args, lattice) -> dict:
 
     specs = trial_specs(args.trials)
     settings = trial_settings(lattice)
+    # Parity sample: 8 seeded members, the largest among them.
+    rng = np.random.default_rng(17)
+    largest = int(np.argmax([nx * ny * nz for nx, ny, nz, *_ in specs]))
+    sample = sorted({largest, *[int(x) for x in rng.choice(len(specs), size=7, replace=False)]})[:8]
+    keep = {}
     batch = lattice.Batch()
     t_start = time.perf_counter()
 
-    def make(spec):
-        return build_trial(lattice, spec)
+    def make(i):
+        # Built and added on host threads; only the sample's states are kept.
+        sched, state = build_trial(lattice, specs[i])
+        k = batch.add(sched, state, lattice.Sphere())
+        if i in sample:
+            keep[i] = state
+        return k, state.node_count, state.bond_count, state.view.max_degree
 
     with ThreadPoolExecutor(host_threads()) as ex:
-        built = list(ex.map(make, specs))
-    build_s = time.perf_counter() - t_start
-    t0 = time.perf_counter()
-    index_of = []
-    for sched, state in built:
-        index_of.append(batch.add(sched, state, lattice.Sphere()))
+        added = list(ex.map(make, range(len(specs))))
+    index_of = [a[0] for a in added]
+    counts = [a[1:] for a in added]
     batch.settle(settings)
-    upload_s = time.perf_counter() - t0
+    upload_s = time.perf_counter() - t_start
     tuning = None
     if not args.no_tune:
         # The autotuner: sweep launch shapes timed on these lattices (state unchanged).
         t0 = time.perf_counter()
         tuning = batch.tune()
         tuning["tune_s"] = time.perf_counter() - t0
-    nodes = sum(s.node_count for _, s in built)
-    bonds = sum(s.bond_count for _, s in built)
+    nodes = sum(c[0] for c in counts)
+    bonds = sum(c[1] for c in counts)
     w, k = args.warmup * SUBSTEPS_PER_STEP, args.steps * SUBSTEPS_PER_STEP
     t0 = time.perf_counter()
     batch.run(lattice.RunControl(max_steps=w))
@@ -548,41 +598,45 @@ def batched_leg(args, lattice) -> dict:
     value = proj / device_s
     launches = batch.kernels_per_substep()
 
-    # Parity: a seeded sample of 8 trials, the largest among them, against the
-    # restatement over the same W + K substeps from upload.
-    rng = np.random.default_rng(17)
-    largest = int(np.argmax([s.bond_count for _, s in built]))
-    sample = sorted({largest, *[int(x) for x in rng.choice(len(specs), size=7, replace=False)]})[:8]
-    t0 = time.perf_counter()
+    # Download of every trial (the sample into their own states, the rest
+    # into shared scratch arrays), then the sample against the restatement
+    # run from upload over the same W + K substeps.
+    scratch = ScratchDownload(lattice, max(c[0] for c in counts), max(c[1] for c in counts))
     outs = {}
+    t0 = time.perf_counter()
     for i in range(len(specs)):
-        sp = batch.download(index_of[i], built[i][1])
-        if i in sample:
-            outs[i] = lattice.state_outputs(built[i][1], sp, batch.first_failure_bonds(index_of[i]),
+        if i in keep:
+            sp = batch.download(index_of[i], keep[i])
+            outs[i] = lattice.state_outputs(keep[i], sp, batch.first_failure_bonds(index_of[i]),
                                             batch.status(index_of[i]))
+        else:
+            batch.download(index_of[i], scratch.target(*counts[i]))
     download_s = time.perf_counter() - t0
-    e2e_s = time.perf_counter() - t_start
+    e2e_s = upload_s + run_wall + download_s
     parity, fp = {}, {}
     threads = host_threads()
     for i in sample:
         case = trial_case(specs[i], w + k)
         cpu = oracle.run_port(case, threads=threads)
         rep = parity_report(cpu, outs[i], break_step=False)
-        parity[str(i)] = {"ok": rep["ok"], "bonds": built[i][1].bond_count, "state_mismatches": rep["state_mismatches"],
+        parity[str(i)] = {"ok": rep["ok"], "bonds": counts[i][1], "state_mismatches": rep["state_mismatches"],
                           "status_mismatches": rep["status_mismatches"], "ledgers_within": rep["ledgers"]["within"]}
         if args.fp64_steps > 0:
             cpu64 = oracle.run_port(case, precision="double", threads=threads)
             fp[str(i)] = fp64_error(case, outs[i], cpu64)
-    del outs
+    del outs, keep, scratch
+    gc.collect()
     phases = batch.profile_phases(1)
     sweep_ms = phases["sweep_interior"] + phases["sweep_boundary"]
-    live_now = sum(s.bond_count - a.broken_bonds for (_, s), a in zip(built, after))
-    algo = sum(sweep_bytes(s.node_count, 0) for _, s in built) + ITERATIONS * 40 * live_now
+    live_now = sum(c[1] - a.broken_bonds for c, a in zip(counts, after))
+    algo = sum(sweep_bytes(c[0], 0) for c in counts) + ITERATIONS * 40 * live_now
     peak, peak_kind = peaks()
     del batch
+    gc.collect()
 
     # Plain: the first trials of the same draw, one backend at a time; device
-    # time, and through the API (upload, run, download) on the host clock.
+    # time, and through the API (backend creation, upload, W + K steps,
+    # download) on the host clock.
     plain_n = min(args.plain_trials, len(specs))
     plain_proj, plain_s, plain_wall, plain_api_proj = 0.0, 0.0, 0.0, 0.0
     for spec in specs[:plain_n]:
@@ -606,11 +660,11 @@ def batched_leg(args, lattice) -> dict:
     return {"value": value, "unit": "projections/s", "trials": len(specs), "nodes": nodes, "bonds": bonds,
             "cpu_baseline": cpu,
             "ms_per_step": device_s / args.steps * 1e3, "gpu_launches_per_substep": launches,
-            "host_build_s": build_s, "host_threads": host_threads(),
-            "e2e": {"value": batch_e2e, "unit": "projections/s", "wall_s": e2e_s, "build_s": build_s,
-                    "upload_s": upload_s, "run_s": run_wall, "download_s": download_s,
-                    "note": "host build of every trial, upload, W + K steps, download of every trial; all "
-                            "projections over the wall time"},
+            "host_threads": host_threads(),
+            "e2e": {"value": batch_e2e, "unit": "projections/s", "wall_s": e2e_s,
+                    "build_and_upload_s": upload_s, "run_s": run_wall, "download_s": download_s,
+                    "note": "every trial built by the box builder and added on host threads (upload), W + K "
+                            "steps, every trial downloaded; all projections over that wall time"},
             "plain": {"value": plain, "unit": "projections/s", "trials": plain_n,
                       "e2e": plain_e2e,
                       "note": "the first trials of the same draw, each alone through the single-lattice backend "
@@ -622,7 +676,7 @@ def batched_leg(args, lattice) -> dict:
                          "kernel": "kSweepLattice + kSolve (the batch's projection sweep)",
                          "sweep_ms_per_substep": sweep_ms, "algorithmic_bytes_per_substep_sweep": algo},
             "parity": {"ok": all(v["ok"] for v in parity.values()), "members": parity,
-                       "substeps": w + k, "largest_member_bonds": built[largest][1].bond_count,
+                       "substeps": w + k, "largest_member_bonds": counts[largest][1],
                        "note": "8 seeded members (the largest included) after the timed window against the CPU "
                                "restatement run from upload over the same substeps"},
             "fp64_error": {"members": fp, "max_position_error_over_extent":
