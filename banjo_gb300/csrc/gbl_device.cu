@@ -1269,6 +1269,7 @@ public:
               "contact pass shared memory");
         check(cudaFuncSetAttribute(kSpherePass<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
               "contact pass shared memory");
+        allowStagedSharedMemory();
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "stream");
         check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream");
         check(cudaStreamCreateWithFlags(&loads_, cudaStreamNonBlocking), "stream");
@@ -1514,7 +1515,7 @@ public:
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0_, ev1_);
         pullControl();
-        bool overflowed = false, wrenched = false;
+        bool overflowed = false, wrenched = false, stage_timeout = false;
         for (auto k : active_) {
             Ctl &c = ctl_host_[k];
             Resident<R> &l = *slots_[k];
@@ -1526,6 +1527,10 @@ public:
             if (c.error & kErrWrench) {
                 c.error = 0;
                 wrenched = true;
+            }
+            if (c.error & kErrStageWait) {
+                c.error = 0;
+                stage_timeout = true;
             }
             l.ext_remaining = c.loads_remaining;
             l.fillStatus(c);
@@ -1548,6 +1553,11 @@ public:
             check(cudaStreamSynchronize(stream_), "status");
             invalid("external wrench cannot be spread over its nodes at the current geometry (torque, resultant "
                     "or node force not representable)");
+        }
+        if (stage_timeout) {
+            pushControl();
+            check(cudaStreamSynchronize(stream_), "status");
+            runtime("the staged sweep's bulk copy into shared memory did not complete within its bounded wait");
         }
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
         for (auto k : active_) slots_[k]->status.wall_seconds += wall;
@@ -1724,6 +1734,17 @@ public:
                 ++out.candidates;
                 if (ms < best_ms) { best_ms = ms; best = sh; }
             }
+            // The shared-memory staged sweep for the small whole lattices.
+            if (!kDirect) {
+                const Shape kept = best;
+                for (std::uint32_t nodes : {kStagedMaxNodes / 2, kStagedMaxNodes}) {
+                    Shape sh = kept;
+                    sh.staged_max_nodes = nodes;
+                    const double ms = timeShape(sh);
+                    ++out.candidates;
+                    if (ms < best_ms) { best_ms = ms; best = sh; }
+                }
+            }
         }
         positions(false);
         check(cudaFreeAsync(saved, stream_), "device free");
@@ -1735,6 +1756,7 @@ public:
         out.sweep_threads = best.sweep_threads;
         out.whole_max_bonds = best.whole_max_bonds;
         out.group_bytes = best.group_bytes;
+        out.staged_max_nodes = best.staged_max_nodes;
         out.sweep_ms = best_ms;
         return out;
     }
@@ -1746,6 +1768,11 @@ public:
         if (t.sweep_threads) shape_.sweep_threads = t.sweep_threads;
         if (t.whole_max_bonds) shape_.whole_max_bonds = t.whole_max_bonds;
         if (t.group_bytes) shape_.group_bytes = t.group_bytes;
+        // staged_max_nodes: 0 keeps the current value, ~0 turns staging off.
+        if (t.staged_max_nodes != ~0U && t.staged_max_nodes > kStagedMaxNodes)
+            invalid("the staged sweep holds at most 14,336 nodes in shared memory");
+        if (t.staged_max_nodes == ~0U) shape_.staged_max_nodes = 0;
+        else if (t.staged_max_nodes) shape_.staged_max_nodes = t.staged_max_nodes;
         dirty_ = true;
     }
 
@@ -1969,15 +1996,30 @@ private:
         // the level launches and the isolated-node launch cover the others.
         auto leveled = [this](const Res &l) { return !many_ || !sweptWhole(l); };
         {
-            std::vector<std::uint32_t> whole;
+            // Those whose positions fit the staged sweep's shared memory take
+            // it when the shape asks for it.
+            std::vector<std::uint32_t> whole, staged;
+            staged_nodes_ = 0;
             if (many_)
-                for (auto k : active_)
-                    if (sweptWhole(*slots_[k])) whole.push_back(k);
-            std::stable_sort(whole.begin(), whole.end(),
-                             [this](std::uint32_t x, std::uint32_t y) { return slots_[x]->B > slots_[y]->B; });
-            const U first = static_cast<U>(all.size());
+                for (auto k : active_) {
+                    const Res &l = *slots_[k];
+                    if (!sweptWhole(l)) continue;
+                    if (!kDirect && l.N <= shape_.staged_max_nodes) {
+                        staged.push_back(k);
+                        staged_nodes_ = std::max(staged_nodes_, l.N);
+                    } else {
+                        whole.push_back(k);
+                    }
+                }
+            const auto larger = [this](std::uint32_t x, std::uint32_t y) { return slots_[x]->B > slots_[y]->B; };
+            std::stable_sort(whole.begin(), whole.end(), larger);
+            std::stable_sort(staged.begin(), staged.end(), larger);
+            U first = static_cast<U>(all.size());
             for (auto k : whole) all.push_back({k, 0, 1});
             whole_ = Span{first, static_cast<U>(whole.size()), 0, 1, 1};
+            first = static_cast<U>(all.size());
+            for (auto k : staged) all.push_back({k, 0, 1});
+            staged_ = Span{first, static_cast<U>(staged.size()), 0, 1, 1};
         }
         {
             const U first = static_cast<U>(all.size());
@@ -2186,11 +2228,12 @@ private:
     template <bool M, class Mark> void enqueueSweep(Mark &&mark) {
         const Settings<R> &S = S_;
         cudaStream_t st = stream_;
-        const bool whole = M && whole_.count;
+        const bool whole = M && (whole_.count || staged_.count);
         if (whole) {
             check(cudaEventRecord(fork_, st), "event");
             check(cudaStreamWaitEvent(side_, fork_, 0), "stream wait");
-            launchSweepWhole(whole_, side_);
+            if (whole_.count) launchSweepWhole(whole_, side_);
+            if (staged_.count) launchSweepStaged(staged_, side_);
             check(cudaEventRecord(join_, side_), "event");
         }
         const unsigned I = S.iterations;
@@ -2250,6 +2293,52 @@ private:
         case 1: kSweepLattice<R, kDirect, false, true, T><<<span.count, T, 0, st>>>(g, S_); break;
         case 2: kSweepLattice<R, kDirect, true, false, T><<<span.count, T, 0, st>>>(g, S_); break;
         default: kSweepLattice<R, kDirect, true, true, T><<<span.count, T, 0, st>>>(g, S_); break;
+        }
+    }
+
+    // The whole sweeps of the lattices whose positions fit in shared memory
+    // (float lane): staged in by one bulk copy, swept in the SM, written back.
+    void launchSweepStaged(const Span &span, cudaStream_t st) {
+        if constexpr (!kDirect) {
+            switch (shape_.sweep_threads) {
+            case 256: launchSweepStagedAs<256>(span, st); break;
+            case 1024: launchSweepStagedAs<1024>(span, st); break;
+            default: launchSweepStagedAs<512>(span, st); break;
+            }
+        }
+    }
+    template <unsigned T> void launchSweepStagedAs(const Span &span, cudaStream_t st) {
+        const bool support = S_.plane_count != 0;
+        const int key = (plastic_ ? 2 : 0) | (support ? 1 : 0);
+        const Grid<R> g = grid(span);
+        const std::size_t smem = static_cast<std::size_t>(staged_nodes_) * sizeof(Q4<R>);
+        switch (key) {
+        case 0: kSweepLattice<R, kDirect, false, false, T, true><<<span.count, T, smem, st>>>(g, S_); break;
+        case 1: kSweepLattice<R, kDirect, false, true, T, true><<<span.count, T, smem, st>>>(g, S_); break;
+        case 2: kSweepLattice<R, kDirect, true, false, T, true><<<span.count, T, smem, st>>>(g, S_); break;
+        default: kSweepLattice<R, kDirect, true, true, T, true><<<span.count, T, smem, st>>>(g, S_); break;
+        }
+    }
+    // The shared memory every staged instance may take: set once.
+    void allowStagedSharedMemory() {
+        if constexpr (!kDirect) {
+            const int bytes = static_cast<int>(kStagedMaxNodes * sizeof(Q4<R>));
+            auto allow = [&](auto kernel) {
+                check(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                      "staged sweep shared memory");
+            };
+            allow(kSweepLattice<R, kDirect, false, false, 256, true>);
+            allow(kSweepLattice<R, kDirect, false, true, 256, true>);
+            allow(kSweepLattice<R, kDirect, true, false, 256, true>);
+            allow(kSweepLattice<R, kDirect, true, true, 256, true>);
+            allow(kSweepLattice<R, kDirect, false, false, 512, true>);
+            allow(kSweepLattice<R, kDirect, false, true, 512, true>);
+            allow(kSweepLattice<R, kDirect, true, false, 512, true>);
+            allow(kSweepLattice<R, kDirect, true, true, 512, true>);
+            allow(kSweepLattice<R, kDirect, false, false, 1024, true>);
+            allow(kSweepLattice<R, kDirect, false, true, 1024, true>);
+            allow(kSweepLattice<R, kDirect, true, false, 1024, true>);
+            allow(kSweepLattice<R, kDirect, true, true, 1024, true>);
         }
     }
 
@@ -2341,7 +2430,8 @@ private:
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
     Work *work_{};
-    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{}, buckets_{};
+    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{}, staged_{}, buckets_{};
+    std::uint32_t staged_nodes_{0}; // the staged sweep's shared memory, in nodes
     // Level-launched lattices, in groups swept one after another.
     struct Group {
         std::vector<Span> levels;
@@ -2359,6 +2449,7 @@ private:
         unsigned sweep_threads = kSweepThreads;
         std::uint32_t whole_max_bonds = kMaxFusedBonds;
         std::size_t group_bytes = std::size_t(48) << 20;
+        std::uint32_t staged_max_nodes = 0; // whole sweeps staged in shared memory up to this many nodes
     };
     Shape shape_;
     cudaStream_t own_stream_{}, stream_{}, side_{}, loads_{};

@@ -170,6 +170,7 @@ struct SourceSlot {
 
 constexpr unsigned kErrExternalOverflow = 1;
 constexpr unsigned kErrWrench = 2;
+constexpr unsigned kErrStageWait = 4; // a bounded wait for a bulk copy into shared memory ran out
 
 template <class R> struct Dev {
     std::uint32_t N, B, D, blocks, words_b, tiles_b;
@@ -1557,12 +1558,75 @@ __device__ __forceinline__ void supportIsolatedInCta(const Dev<R> &L, const Sett
     }
 }
 
-template <class R, bool Direct, bool Plastic, bool Support, unsigned T>
+// Shared-memory staging of a small lattice's nodes for its one-CTA sweep: the
+// whole position array (one 16-byte record per node) comes in by one bulk
+// copy (the copy engine, cp.async.bulk, completing on an mbarrier), every
+// gather and write of the sweep then stays in the SM, and the array goes back
+// to global memory once at the end. The waits are bounded: a copy that has
+// not landed after kStageSpins polls marks the lattice's control block with
+// kErrStageWait (the host reports it), waits as long again for the copy to
+// drain, and the CTA leaves.
+constexpr std::uint32_t kStageSpins = 1U << 26;
+// Positions the staged sweep holds: 14,336 x 16 B = 224 KiB of dynamic shared
+// memory, with the descriptor and the barrier inside the 227 KiB a CTA may take.
+constexpr std::uint32_t kStagedMaxNodes = 14336;
+constexpr std::uint32_t kStageChunk = 32768; // bytes per bulk copy
+
+__device__ __forceinline__ std::uint32_t smemAddress(const void *p) {
+    return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool barrierDone(std::uint64_t *bar, std::uint32_t parity) {
+    std::uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smemAddress(bar)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool waitBarrier(std::uint64_t *bar, std::uint32_t parity) {
+    for (std::uint32_t spin = 0; spin < kStageSpins; ++spin)
+        if (barrierDone(bar, parity)) return true;
+    return false;
+}
+
+// The CTA's nodes [0, n) from global `src` into shared `dst` (n x 16 bytes,
+// both 16-byte aligned). Returns false, after the bounded drain, when the
+// copy did not land in time (every thread returns the same).
+template <class R>
+__device__ bool stageNodesIn(Q4<R> *dst, const Q4<R> *src, std::uint32_t n, std::uint64_t *bar, Ctl *ctl) {
+    const std::uint32_t bytes = n * static_cast<std::uint32_t>(sizeof(Q4<R>));
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smemAddress(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddress(bar)), "r"(bytes)
+                     : "memory");
+        for (std::uint32_t off = 0; off < bytes; off += kStageChunk) {
+            const std::uint32_t len = bytes - off < kStageChunk ? bytes - off : kStageChunk;
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                             "r"(smemAddress(reinterpret_cast<unsigned char *>(dst) + off)),
+                         "l"(__cvta_generic_to_global(reinterpret_cast<const unsigned char *>(src) + off)), "r"(len),
+                         "r"(smemAddress(bar))
+                         : "memory");
+        }
+    }
+    __syncthreads(); // the barrier is initialised before anyone waits on it
+    const bool landed = waitBarrier(bar, 0);
+    if (__syncthreads_and(landed ? 1 : 0)) return true;
+    if (threadIdx.x == 0) atomicOr(&ctl->error, kErrStageWait);
+    (void)waitBarrier(bar, 0); // the copy still writes this CTA's shared memory: let it drain
+    __syncthreads();
+    return false;
+}
+
+template <class R, bool Direct, bool Plastic, bool Support, unsigned T, bool Staged = false>
 __global__ void __launch_bounds__(T, T >= 1024 ? 1 : 2) kSweepLattice(const Grid<R> launch, Settings<R> S) {
     // The lattice's descriptor, copied once into shared memory: its fields
     // are read throughout the sweep, and shared memory is never written by
     // the sweep's global stores, so the compiler may keep them as it likes.
     __shared__ __align__(16) unsigned char desc[sizeof(Dev<R>)];
+    __shared__ std::uint64_t stage_bar;
+    extern __shared__ __align__(128) unsigned char sweep_nodes[];
     {
         const Work w = item<true>(launch);
         const unsigned *src = reinterpret_cast<const unsigned *>(launch.table + w.lattice);
@@ -1570,8 +1634,20 @@ __global__ void __launch_bounds__(T, T >= 1024 ? 1 : 2) kSweepLattice(const Grid
         for (unsigned k = threadIdx.x; k < sizeof(Dev<R>) / sizeof(unsigned); k += blockDim.x) dst[k] = src[k];
     }
     __syncthreads();
+    Q4<R> *const global_u = reinterpret_cast<const Dev<R> *>(desc)->u;
+    const std::uint32_t node_count = reinterpret_cast<const Dev<R> *>(desc)->N;
+    if (reinterpret_cast<const Dev<R> *>(desc)->ctl->stop) return;
+    if constexpr (Staged) {
+        // The sweep's node reads and writes go to the staged copy: the
+        // shared-memory descriptor's position pointer is swapped for it
+        // (generic loads and stores reach shared memory through it).
+        Q4<R> *nodes = reinterpret_cast<Q4<R> *>(sweep_nodes);
+        if (!stageNodesIn(nodes, global_u, node_count, &stage_bar, reinterpret_cast<const Dev<R> *>(desc)->ctl))
+            return;
+        if (threadIdx.x == 0) reinterpret_cast<Dev<R> *>(desc)->u = nodes;
+        __syncthreads();
+    }
     const Dev<R> &L = *reinterpret_cast<const Dev<R> *>(desc);
-    if (L.ctl->stop) return;
     const unsigned I = S.iterations;
     // One bond per thread per round; the rounds of the whole sweep in order
     // (iteration, level, base). The next round's streamed data (record,
@@ -1624,14 +1700,24 @@ __global__ void __launch_bounds__(T, T >= 1024 ? 1 : 2) kSweepLattice(const Grid
             const bool live = !(now.rec.a & kDeadBit);
             Q4<R> qa{}, qb{};
             if (live) {
-                qa = ldShared(L.u + endA(now.rec));
-                qb = ldShared(L.u + endB(now.rec));
+                if constexpr (Staged) {
+                    qa = L.u[endA(now.rec)];
+                    qb = L.u[endB(now.rec)];
+                } else {
+                    qa = ldShared(L.u + endA(now.rec));
+                    qb = ldShared(L.u + endB(now.rec));
+                }
             }
             finishBond<R, Direct, Plastic, Support>(L, S, d, now.rec, live, now.geo, now.lam, now.pl,
                                                     cur.it + 1 == I, qa, qb);
         }
         if (!more) {
             supportIsolatedInCta<R, Support>(L, S);
+            if constexpr (Staged) {
+                // The staged positions back to global memory.
+                __syncthreads();
+                for (std::uint32_t i = threadIdx.x; i < node_count; i += blockDim.x) global_u[i] = L.u[i];
+            }
             break;
         }
         if (nxt.lv != cur.lv || nxt.it != cur.it) {

@@ -193,7 +193,8 @@ class BoxSpec(C.Structure):
 class Tuning(C.Structure):
     """gbl_tuning: a batch's launch shapes (results never depend on them)."""
     _fields_ = [("sweep_threads", C.c_uint32), ("whole_max_bonds", C.c_uint32), ("group_bytes", C.c_uint64),
-                ("sweep_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_uint32)]
+                ("sweep_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_uint32),
+                ("staged_max_nodes", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -878,8 +879,11 @@ class Batch:
         _call(library().gbl_batch_tune, self._h, C.byref(t))
         return t.as_dict()
 
-    def set_tuning(self, sweep_threads: int = 0, whole_max_bonds: int = 0, group_bytes: int = 0) -> None:
-        t = Tuning(sweep_threads, whole_max_bonds, group_bytes, 0.0, 0.0, 0)
+    def set_tuning(self, sweep_threads: int = 0, whole_max_bonds: int = 0, group_bytes: int = 0,
+                   staged_max_nodes: int = 0) -> None:
+        """Launch shapes (0 keeps a value; staged_max_nodes 0xFFFFFFFF turns
+        the shared-memory staged sweep off)."""
+        t = Tuning(sweep_threads, whole_max_bonds, group_bytes, 0.0, 0.0, 0, staged_max_nodes)
         _call(library().gbl_batch_set_tuning, self._h, C.byref(t))
 
 

@@ -393,6 +393,9 @@ typedef struct gbl_tuning {
     double sweep_ms;          /* the kept shape's sweep, per substep (tune only) */
     double default_ms;        /* the default shape's sweep, per substep (tune only) */
     uint32_t candidates;      /* shapes timed (tune only) */
+    uint32_t staged_max_nodes; /* one-CTA sweeps of lattices up to this many nodes stage their positions in
+                                  shared memory (float lane; at most 14,336; 0 off in tune's output; in
+                                  set_tuning 0 keeps the current value and 0xFFFFFFFF turns staging off) */
 } gbl_tuning;
 gbl_result gbl_batch_tune(gbl_batch *batch, gbl_tuning *chosen);
 gbl_result gbl_batch_set_tuning(gbl_batch *batch, const gbl_tuning *shape);

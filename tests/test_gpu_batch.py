@@ -61,11 +61,16 @@ def test_batch_sphere_impacts_equal_alone(device):
              scenes.impact_block(nx=16, ny=12, nz=40, blocks=4, radius=0.04, speed=12.0, steps=6, seed_point=7,
                                  seed_strength=4)]
     together = device.run_batch(cases)
-    for case, out in zip(cases, together):
+    # The same lattices swept whole in one CTA each with their positions
+    # staged in shared memory (plastic flow and the ground plane included).
+    staged = device.run_batch(cases, tuning={"whole_max_bonds": 1 << 24, "staged_max_nodes": 14336})
+    for case, out, st in zip(cases, together, staged):
         alone = device.run_case(case)
         assert int(out["status_u64"][9]) > 0  # the sphere touched this lattice
         assert mismatches(alone, out, STATE_KEYS) == []
         assert status_mismatches(alone, out) == []
+        assert mismatches(alone, st, STATE_KEYS) == []
+        assert status_mismatches(alone, st) == []
 
 
 @pytest.mark.gpu
@@ -134,7 +139,8 @@ def test_batch_refuses_mixed_settings(gbl):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", ["tune", {"sweep_threads": 256, "whole_max_bonds": 1 << 24},
-                                   {"sweep_threads": 1024, "whole_max_bonds": 1}, {"group_bytes": 1 << 16}])
+                                   {"sweep_threads": 1024, "whole_max_bonds": 1}, {"group_bytes": 1 << 16},
+                                   {"staged_max_nodes": 14336}, {"sweep_threads": 256, "staged_max_nodes": 300}])
 def test_batch_launch_shapes_leave_results_unchanged(device, shape):
     """The autotuner's choices (one-CTA sweep size and reach, group size) and
     its timing runs change nothing: every shape runs the same levels."""
