@@ -2620,11 +2620,19 @@ public:
 template <class R> class Server final : public ServerBase {
 public:
     static constexpr std::uint32_t kLargeBonds = 1U << 22;
+    static constexpr std::uint32_t kServedWholeBonds = 1U << 14;
     static constexpr unsigned kSmall = 0, kLarge = 1;
 
     Server(const gbl_step_settings &settings, std::uint64_t budget)
         : budget_(budget), contact_(settings.node_contact.mode != 0), t0_(clock()) {
         for (auto &lane : lanes_) lane.configure(settings);
+        // A server holds few lattices at a time: a lattice swept whole by one
+        // CTA takes that CTA's serial time per substep (about 3.5 ms for
+        // 2^18 bonds), where level launches spread it over the GPU. Only
+        // tiny lattices sweep whole here.
+        gbl_tuning shape{};
+        shape.whole_max_bonds = kServedWholeBonds;
+        for (auto &lane : lanes_) lane.setShape(shape);
     }
     ~Server() override {
         for (auto &kv : requests_)
