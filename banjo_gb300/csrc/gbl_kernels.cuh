@@ -2336,13 +2336,21 @@ __global__ void __launch_bounds__(kLedgerThreads) kLoadLedger(const Grid<R> laun
     if (c.ext_count && c.loads_remaining > 0) {
         const std::uint32_t n = c.ext_count;
         const unsigned sources = c.wrench_count;
+        // A staging thread takes whole entries: the node index, then its
+        // thirteen contributions as independent loads, so a chunk costs a
+        // couple of memory round trips rather than one per value.
         const auto fill = [&](std::uint32_t base, unsigned buf) {
             const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
-            for (unsigned x = threadIdx.x - kLedgerFolds * 32; x < cnt * kLedgerFolds; x += kLedgerStagers) {
-                const unsigned e = x / kLedgerFolds, k = x - e * kLedgerFolds;
+#pragma unroll 2
+            for (unsigned e = threadIdx.x - kLedgerFolds * 32; e < cnt; e += kLedgerStagers) {
                 const std::uint32_t node = L.ext_nodes[base + e];
-                stage[buf][x] = inBounds(node, L.N, kSiteLoad)
-                    ? L.ext_contrib[kLedgerFolds * static_cast<std::size_t>(node) + k] : 0.0;
+                const bool ok = inBounds(node, L.N, kSiteLoad);
+                const double *src = L.ext_contrib + kLedgerFolds * static_cast<std::size_t>(ok ? node : 0U);
+                double x[kLedgerFolds];
+#pragma unroll
+                for (int k = 0; k < kLedgerFolds; ++k) x[k] = src[k];
+#pragma unroll
+                for (int k = 0; k < kLedgerFolds; ++k) stage[buf][e * kLedgerFolds + k] = ok ? x[k] : 0.0;
             }
         };
         // Flushes every source whose run ends at `at`: each fold adds its
