@@ -190,3 +190,28 @@ def test_frames_and_phase_profile(device):
     be3.download(state3)
     assert np.array_equal(state3.u, state2.u)
     assert phases["sweep_interior"] > 0 and phases["end_sample_bonds"] > 0
+
+
+def test_frames_match_the_checker_at_their_substeps(device, port):
+    """FrameCapture (FastLattice.hpp:247-253; captured before the substep it
+    is named for, CpuLatticeBackend.cpp:274-278): every frame of a sliced
+    impact -- positions as float, aliveness, damage, the sphere -- equals the
+    CPU checker's state after that many substeps."""
+    from banjo_gb300 import scenes
+
+    case = scenes.impact_block(nx=32, ny=16, nz=24, blocks=4, radius=0.06, steps=3)
+    _, _, be = _backend(device, case)
+    be.run(device.RunControl(max_steps=30, capture_stride=7, max_frames=10))
+    frames = be.take_frames()
+    assert [f["step"] for f in frames] == [0, 7, 14, 21, 28]
+    broke = 0
+    for f in frames:
+        sub = dict(case)
+        sub["steps"] = np.array([f["step"]], dtype=np.uint64)
+        cpu = port.run_port(sub, threads=4)
+        assert np.array_equal(f["u"], cpu["u"].astype(np.float32)), f["step"]
+        assert np.array_equal(f["alive"], cpu["alive"]), f["step"]
+        assert np.array_equal(f["damage"], cpu["damage"].astype(np.float32)), f["step"]
+        assert np.array_equal(f["sphere"], cpu["sphere_out"]), f["step"]
+        broke = int(cpu["status_u64"][4])
+    assert broke > 0
