@@ -159,10 +159,17 @@ def test_refused_features(device):
 
     case = scenes.cantilever(nx=6, ny=3, nz=3, steps=1)
     sched, state, be = _backend(device, case)
+    be.run(device.RunControl(max_steps=3))
+    be.download(state)
+    before = state.u.copy()
     s = device.step_settings(case["settings"])
     s.bond_integrator = 1
     with pytest.raises(ValueError, match="XPBD"):
         be.upload(state, s, device.sphere_state(case["sphere"]))
+    # A refused upload leaves the lattice it had (lattice_verlet_tests.cpp:165-185).
+    assert be.status().total_steps == 3
+    be.download(state)
+    assert np.array_equal(state.u, before)
     s = device.step_settings(case["settings"])
     s.node_contact.mode = 2  # radius and skin left at zero
     with pytest.raises(ValueError, match="cutoff"):
