@@ -2152,7 +2152,7 @@ private:
         // The load ledger, on its own stream until the serial tail.
         check(cudaEventRecord(load_fork_, st), "event");
         check(cudaStreamWaitEvent(loads_, load_fork_, 0), "stream wait");
-        kLoadLedger<R, M><<<each_.count, kLedgerThreads, 0, loads_>>>(grid(each_), S);
+        kLoadLedger<R, M><<<dim3(each_.count, kLedgerFolds), kLedgerThreads, 0, loads_>>>(grid(each_), S);
         check(cudaEventRecord(load_join_, loads_), "event");
         if (S.sphere_enabled && slabs_.count) {
             kCandidates<R, M><<<slabs_.count, 1024, 0, st>>>(grid(slabs_));

@@ -2302,9 +2302,9 @@ __global__ void __launch_bounds__(kFoldThreads) kKineticFold(const Grid<R> launc
 // beside the contact passes, the sweep and the end sample.
 // ---------------------------------------------------------------------------
 constexpr int kLedgerFolds = 13;
-constexpr unsigned kLedgerStagers = 96;                                   // threads staging contributions
-constexpr unsigned kLedgerThreads = kLedgerFolds * 32 + kLedgerStagers;  // 13 fold warps + 3 staging warps
-constexpr unsigned kLedgerChunk = 192;                                    // entries staged per round
+constexpr unsigned kLedgerThreads = 128;                   // one folding lane, three staging warps
+constexpr unsigned kLedgerStagers = kLedgerThreads - 32;
+constexpr unsigned kLedgerChunk = 384;                      // entries staged per round
 
 // Adds a source's folded change (component q) to its ledger.
 __device__ __forceinline__ void addLoadComponent(LoadLedger &g, int q, double x) {
@@ -2315,10 +2315,12 @@ __device__ __forceinline__ void addLoadComponent(LoadLedger &g, int q, double x)
     else g.req_ang[q - 10] = g.req_ang[q - 10] + x;
 }
 
-// Fold q runs on lane 0 of warp q: one active lane per warp, so the thirteen
-// chains' FP64 adds issue from thirteen warps across the SM's schedulers
-// instead of as one thirteen-lane instruction (measured on GB300: 182 us for
-// 1,984 nodes as one warp's lanes).
+// One CTA per (lattice, component): blockIdx.y is the component q. Thread 0
+// folds it; the other warps stage the next chunk of its node contributions.
+// Each fold is one chain of dependent FP64 adds, and GB300 has little FP64
+// issue per SM, so the thirteen chains run on thirteen SMs (measured, 1,984
+// loaded nodes: 246 us with the chains on thirteen warps of one CTA, 182 us
+// on thirteen lanes of one warp).
 template <class R, bool Many>
 __global__ void __launch_bounds__(kLedgerThreads) kLoadLedger(const Grid<R> launch, Settings<R> S) {
     const Work w = item<Many>(launch);
@@ -2327,88 +2329,78 @@ __global__ void __launch_bounds__(kLedgerThreads) kLoadLedger(const Grid<R> laun
     // A lattice stopped, or whose kick failed this substep, folds nothing
     // (kLedger stops the latter).
     if (c.stop || c.error) return;
-    __shared__ double stage[2][kLedgerChunk * kLedgerFolds];
-    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31U;
-    const bool folder = warp < static_cast<unsigned>(kLedgerFolds) && lane == 0;
-    const bool stager = warp >= static_cast<unsigned>(kLedgerFolds);
-    const int q = static_cast<int>(warp);
-    // External loads: this substep's change, folded in node order, then added.
-    if (c.ext_count && c.loads_remaining > 0) {
-        const std::uint32_t n = c.ext_count;
-        const unsigned sources = c.wrench_count;
-        // A staging thread takes whole entries: the node index, then its
-        // thirteen contributions as independent loads, so a chunk costs a
-        // couple of memory round trips rather than one per value.
-        const auto fill = [&](std::uint32_t base, unsigned buf) {
-            const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
-#pragma unroll 2
-            for (unsigned e = threadIdx.x - kLedgerFolds * 32; e < cnt; e += kLedgerStagers) {
-                const std::uint32_t node = L.ext_nodes[base + e];
-                const bool ok = inBounds(node, L.N, kSiteLoad);
-                const double *src = L.ext_contrib + kLedgerFolds * static_cast<std::size_t>(ok ? node : 0U);
-                double x[kLedgerFolds];
-#pragma unroll
-                for (int k = 0; k < kLedgerFolds; ++k) x[k] = src[k];
-#pragma unroll
-                for (int k = 0; k < kLedgerFolds; ++k) stage[buf][e * kLedgerFolds + k] = ok ? x[k] : 0.0;
-            }
-        };
-        // Flushes every source whose run ends at `at`: each fold adds its
-        // component, fold 0 also keeps the step count, the elapsed time and
-        // the source's place in the status order.
-        unsigned k = 0;
-        double run = 0.0;
-        const auto flush = [&](std::uint32_t at) {
-            while (k < sources && L.wrench[k].end == at) {
-                SourceSlot &slot = L.sources[L.wrench[k].slot];
-                addLoadComponent(slot.load, q, run);
-                if (q == 0) {
-                    if (slot.load.steps == 0) slot.order = c.source_seq++;
-                    slot.load.steps += 1;
-                    slot.load.elapsed = slot.load.elapsed + static_cast<double>(S.dt);
-                }
-                run = 0.0;
-                ++k;
-            }
-        };
-        if (stager) fill(0, 0);
-        if (folder) flush(0);
-        __syncthreads();
-        double total = 0.0;
-        unsigned buf = 0;
-        for (std::uint32_t base = 0; base < n; base += kLedgerChunk, buf ^= 1U) {
-            if (stager) {
-                if (base + kLedgerChunk < n) fill(base + kLedgerChunk, buf ^ 1U);
-            } else if (folder) {
-                const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
-                const double *col = stage[buf] + q;
-                if (sources == 0) {
-                    // Unrolled so the shared-memory loads run ahead of the
-                    // dependent adds.
-#pragma unroll 8
-                    for (std::uint32_t e = 0; e < cnt; ++e) total += col[e * kLedgerFolds];
-                } else {
-                    for (std::uint32_t e = 0; e < cnt; ++e) {
-                        const double x = col[e * kLedgerFolds];
-                        total += x;
-                        run += x;
-                        flush(base + e + 1);
-                    }
-                }
-            }
-            __syncthreads();
+    if (!(c.ext_count && c.loads_remaining > 0)) return;
+    __shared__ double stage[2][kLedgerChunk];
+    const int q = static_cast<int>(blockIdx.y);
+    const bool folder = threadIdx.x == 0;
+    const bool stager = threadIdx.x >= 32;
+    const std::uint32_t n = c.ext_count;
+    const unsigned sources = c.wrench_count;
+    const auto fill = [&](std::uint32_t base, unsigned buf) {
+        const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
+#pragma unroll 4
+        for (unsigned e = threadIdx.x - 32; e < cnt; e += kLedgerStagers) {
+            const std::uint32_t node = L.ext_nodes[base + e];
+            stage[buf][e] = inBounds(node, L.N, kSiteLoad)
+                ? L.ext_contrib[kLedgerFolds * static_cast<std::size_t>(node) + q] : 0.0;
         }
-        if (folder) {
-            flush(n); // only sources with empty runs past the list's end remain
-            LoadLedger &g = c.ext;
-            addLoadComponent(g, q, total);
+    };
+    // Flushes every source whose run ends at `at`: the component's change to
+    // the source's ledger; component 0 also keeps the step count, the elapsed
+    // time and the source's place in the status order.
+    unsigned k = 0;
+    double run = 0.0;
+    const auto flush = [&](std::uint32_t at) {
+        while (k < sources && L.wrench[k].end == at) {
+            SourceSlot &slot = L.sources[L.wrench[k].slot];
+            addLoadComponent(slot.load, q, run);
             if (q == 0) {
-                g.steps += 1;
-                g.elapsed += static_cast<double>(S.dt);
-                c.loads_remaining -= 1;
+                if (slot.load.steps == 0) slot.order = c.source_seq++;
+                slot.load.steps += 1;
+                slot.load.elapsed = slot.load.elapsed + static_cast<double>(S.dt);
             }
+            run = 0.0;
+            ++k;
+        }
+    };
+    if (stager) fill(0, 0);
+    if (folder) flush(0);
+    __syncthreads();
+    double total = 0.0;
+    unsigned buf = 0;
+    for (std::uint32_t base = 0; base < n; base += kLedgerChunk, buf ^= 1U) {
+        if (stager) {
+            if (base + kLedgerChunk < n) fill(base + kLedgerChunk, buf ^ 1U);
+        } else if (folder) {
+            const std::uint32_t cnt = n - base < kLedgerChunk ? n - base : kLedgerChunk;
+            const double *col = stage[buf];
+            if (sources == 0) {
+                // Unrolled so the shared-memory loads run ahead of the
+                // dependent adds.
+#pragma unroll 8
+                for (std::uint32_t e = 0; e < cnt; ++e) total += col[e];
+            } else {
+                for (std::uint32_t e = 0; e < cnt; ++e) {
+                    const double x = col[e];
+                    total += x;
+                    run += x;
+                    flush(base + e + 1);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (folder) {
+        flush(n); // only sources with empty runs past the list's end remain
+        LoadLedger &g = c.ext;
+        addLoadComponent(g, q, total);
+        if (q == 0) {
+            g.steps += 1;
+            g.elapsed += static_cast<double>(S.dt);
         }
     }
+    // loads_remaining counts down in kLedger, after every component's CTA
+    // has read it.
 }
 
 // ---------------------------------------------------------------------------
@@ -2430,6 +2422,7 @@ __global__ void kLedger(const Grid<R> launch, Settings<R> S) {
         return;
     }
     const unsigned long long step = c.total_steps;
+    if (c.ext_count && c.loads_remaining > 0) c.loads_remaining -= 1; // the substep's load, folded by kLoadLedger
     c.full_restart = 0;
     c.plastic_work += c.plastic_substep;
     for (unsigned e = 0; e < c.dmg_count; ++e) {
