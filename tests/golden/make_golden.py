@@ -93,6 +93,11 @@ def cases() -> dict:
     resumed = scenes.contact_drop()
     resumed["checkpoint_at"] = np.array([10], dtype=np.uint64)
     out["resume_contact_drop"] = (resumed, "float")
+    # A loaded run resumed: external loads are not part of the state, so the
+    # fresh backend runs on without them (the caller would set them again).
+    resumed = scenes.cantilever(nx=16, ny=6, nz=6, steps=5)
+    resumed["checkpoint_at"] = np.array([27], dtype=np.uint64)
+    out["resume_loaded"] = (resumed, "float")
     # Caps: a slab with more sphere candidates than a slab's list holds
     # (1024), and node contact with more pairs per owner than its slots (24).
     out["candidate_overflow"] = (scenes.impact_block(nx=40, ny=4, nz=40, blocks=1, radius=0.4, speed=6.0, steps=1,
