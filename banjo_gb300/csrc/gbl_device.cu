@@ -1442,7 +1442,7 @@ public:
         if (before[0] != l.ext_force || before[1] != l.wrench_dev || before[2] != l.source_dev) {
             pushDescriptor(k);
             check(cudaStreamSynchronize(stream_), "descriptor");
-            dropGraph();
+            dirty_ = true; // the wrench slots' work items and the graph
         }
     }
 
@@ -2030,6 +2030,13 @@ private:
             const U count = static_cast<U>(all.size()) - first;
             broken_ = Span{first, count, 0, count, 1};
         }
+        {
+            // One item per (lattice, wrench slot): the batch's spreads in one launch.
+            const U first = static_cast<U>(all.size());
+            for (auto k : active_)
+                for (U q = 0; q < slots_[k]->wrench_cap; ++q) all.push_back({k, q, slots_[k]->wrench_cap});
+            wrench_ = Span{first, static_cast<U>(all.size()) - first, 0, 0, 1};
+        }
         // The level-launched lattices in groups whose node arrays fit in L2
         // together: a group runs its whole sweep (every iteration, every
         // level) before the next, so its nodes stay resident across levels.
@@ -2143,10 +2150,15 @@ private:
         // without, before the kick.
         const bool side_restart = S.sphere_enabled != 0;
         if (!side_restart) restartPhase<M>(st, 0, mark);
-        for (auto k : active_) {
-            const Resident<R> &l = *slots_[k];
-            if (l.wrench_cap)
-                kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr, 1);
+        if (M) {
+            if (wrench_.count) kWrenchMany<R><<<wrench_.count, kWrenchThreads, 0, st>>>(grid(wrench_));
+        } else {
+            for (auto k : active_) {
+                const Resident<R> &l = *slots_[k];
+                if (l.wrench_cap)
+                    kWrench<R><<<l.wrench_cap, kWrenchThreads, 0, st>>>(l.dev, l.dev.wrench, l.dev.ext_nodes, nullptr,
+                                                                       1);
+            }
         }
         if (nodes_.count) kKick<R, M><<<nodes_.count, kThreads, 0, st>>>(grid(nodes_), S);
         // The load ledger, on its own stream until the serial tail.
@@ -2430,7 +2442,8 @@ private:
     unsigned *running_{}, *running_host_{};
     Dev<R> *table_{};
     Work *work_{};
-    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{}, staged_{}, buckets_{};
+    Span nodes_{}, bonds_{}, tiles_{}, blocks_{}, each_{}, slabs_{}, broken_{}, whole_{}, staged_{}, buckets_{},
+        wrench_{};
     std::uint32_t staged_nodes_{0}; // the staged sweep's shared memory, in nodes
     // Level-launched lattices, in groups swept one after another.
     struct Group {

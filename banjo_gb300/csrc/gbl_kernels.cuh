@@ -716,11 +716,11 @@ constexpr unsigned kWrenchThreads = 256;
 __device__ inline double normD(double x, double y, double z) { return norm3d(x, y, z); }
 
 template <class R>
-__global__ void __launch_bounds__(kWrenchThreads)
-kWrench(const Dev<R> L, const WrenchDev *ws, const std::uint32_t *lists, unsigned *verdict, int apply) {
+__device__ __forceinline__ void wrenchSpread(const Dev<R> &L, const WrenchDev *ws, const std::uint32_t *lists,
+                                             unsigned *verdict, int apply, unsigned index) {
     Ctl &c = *L.ctl;
-    if (apply && (c.stop || c.loads_remaining == 0 || blockIdx.x >= c.wrench_count)) return;
-    const WrenchDev w = ws[blockIdx.x];
+    if (apply && (c.stop || c.loads_remaining == 0 || index >= c.wrench_count)) return;
+    const WrenchDev w = ws[index];
     const std::uint32_t *list = lists + w.begin;
     const std::uint32_t n = w.end - w.begin;
     const unsigned t = threadIdx.x;
@@ -885,6 +885,21 @@ kWrench(const Dev<R> L, const WrenchDev *ws, const std::uint32_t *lists, unsigne
             }
         }
     }
+}
+
+// One lattice's wrenches: one CTA per wrench.
+template <class R>
+__global__ void __launch_bounds__(kWrenchThreads)
+kWrench(const Dev<R> L, const WrenchDev *ws, const std::uint32_t *lists, unsigned *verdict, int apply) {
+    wrenchSpread(L, ws, lists, verdict, apply, blockIdx.x);
+}
+
+// A batch's wrenches in one launch: one CTA per (lattice, wrench) item.
+template <class R>
+__global__ void __launch_bounds__(kWrenchThreads) kWrenchMany(const Grid<R> launch) {
+    const Work w = launch.list[blockIdx.x];
+    const Dev<R> &L = launch.table[w.lattice];
+    wrenchSpread(L, L.wrench, L.ext_nodes, nullptr, 1, w.begin);
 }
 
 // Ordered candidate lists per slab, capped at 1024 (CpuLatticeBackend.cpp:375-386):
