@@ -967,16 +967,22 @@ def distributed():
     return rank, world, local, None, None
 
 
+def _reduce_device(dist) -> str:
+    # NCCL reduces device tensors; gloo (the CPU tests of this logic) host ones.
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def barrier(dist, torch):
     if dist is not None:
         dist.barrier()
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(x: float, dist, torch) -> float:
     if dist is None:
         return x
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -984,7 +990,7 @@ def max_over_ranks(x: float, dist, torch) -> float:
 def sum_over_ranks(x: float, dist, torch) -> float:
     if dist is None:
         return x
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
