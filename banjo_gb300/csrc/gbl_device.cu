@@ -765,39 +765,58 @@ template <class R> struct Resident {
         view_ = gbl_state_view{};
     }
 
-    // One of the caller's arrays into a device buffer, read in place by a
-    // kernel (coherent pageable access), in the widest units its alignment
-    // allows; the destination is 256-byte aligned.
-    static void copyIn(void *dst, const void *src, std::size_t bytes, cudaStream_t stream) {
-        if (!bytes) return;
-        const std::uintptr_t a = reinterpret_cast<std::uintptr_t>(src) | bytes;
-        if (a % 16 == 0)
-            kCopyIn<uint4><<<reorderGrid(bytes / 16), kThreads, 0, stream>>>(
-                static_cast<uint4 *>(dst), static_cast<const uint4 *>(src), bytes / 16);
-        else if (a % 8 == 0)
-            kCopyIn<uint2><<<reorderGrid(bytes / 8), kThreads, 0, stream>>>(
-                static_cast<uint2 *>(dst), static_cast<const uint2 *>(src), bytes / 8);
-        else if (a % 4 == 0)
-            kCopyIn<std::uint32_t><<<reorderGrid(bytes / 4), kThreads, 0, stream>>>(
-                static_cast<std::uint32_t *>(dst), static_cast<const std::uint32_t *>(src), bytes / 4);
-        else
-            kCopyIn<std::uint8_t><<<reorderGrid(bytes), kThreads, 0, stream>>>(
-                static_cast<std::uint8_t *>(dst), static_cast<const std::uint8_t *>(src), bytes);
+    // The direct upload where the device reads pageable host memory: the
+    // conversion kernels read the caller's arrays in place, in sequence.
+    void convertFromHost(char *staged, cudaStream_t stream) {
+        const gbl_state_view &st = view_;
+        unsigned *flowed = nullptr;
+        check(cudaMallocAsync(&flowed, 256, stream), "device allocation");
+        check(cudaMemsetAsync(flowed, 0, sizeof(unsigned), stream), "memset");
+        if (N)
+            kNodesIn<R><<<reorderGrid(N), kThreads, 0, stream>>>(
+                dev.u, dev.v, dev.x0, dev.up, NodesIn{st.u, st.u_prev, st.v, st.x0, st.mass, st.inv_mass}, 0, N);
+        const std::size_t P = static_cast<std::size_t>(dev.D) * N;
+        if (P)
+            kSlotsIn<R><<<reorderGrid(P), kThreads, 0, stream>>>(
+                dev.nbr, dev.nbr_other, dev.nbr_bond,
+                SlotsIn{st.nbr_rest, st.nbr_weight, st.nbr_alive, st.nbr_other, st.nbr_bond}, 0, P, N);
+        if (B) {
+            const BondsIn in{st.bond_a, st.bond_b, st.bond_slot_a, st.bond_slot_b, st.alive, st.failure_mode,
+                             last_a.data(), last_b.data(), st.rest_length_sq_minus, st.rest_length, st.rest_edge,
+                             st.compliance, st.prev_tensile, st.prev_compressive, st.prev_shear, st.damage,
+                             st.threshold, st.plastic_extension, st.plastic_strain};
+            kBondsIn<R><<<reorderGrid(B), kThreads, 0, stream>>>(bondsAt(staged), in, 0, B, flowed);
+        }
+        // The small arrays, read in place too (this lattice keeps them until
+        // commitFinish), and every node dirty: the first substep restarts in full.
+        auto words = [&](void *dst, const void *src, std::size_t bytes) {
+            if (!bytes) return;
+            const std::size_t n = bytes / sizeof(std::uint32_t);
+            kCopyWords<<<reorderGrid(n), kThreads, 0, stream>>>(static_cast<std::uint32_t *>(dst),
+                                                              static_cast<const std::uint32_t *>(src), n);
+        };
+        static_assert(sizeof(Sphere<R>) % sizeof(std::uint32_t) == 0, "sphere record copied as words");
+        words(dev.dev2sched, dev2sched.data(), sizeof(std::uint32_t) * B);
+        words(dev.isolated, isolated.data(), sizeof(std::uint32_t) * isolated.size());
+        words(dev.node_block_begin, sched.node_block_begin.data(), sizeof(std::uint32_t) * (sched.block_count + 1));
+        words(dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size());
+        words(dev.sphere, &sphere0, sizeof(sphere0));
+        check(cudaGetLastError(), "kernel launch");
+        check(cudaMemsetAsync(dev.dirty, 1, N, stream), "memset");
+        check(cudaMemsetAsync(dev.dirty + N, 0, 4, stream), "memset");
+        flowed_dev_ = flowed; // read by commitFinish
     }
 
     // The direct upload: the caller's arrays, chunk by chunk, copied as they
     // are into one of two device staging buffers (the next chunk's copy runs
     // while the previous chunk converts) and converted there, the bonds into
     // `staged` in schedule order; then the small arrays.
-    //
-    // Where the device reads pageable host memory in place, the copies are
-    // kernels on the stream, one array at a time (a few pages in flight, so
-    // the host page-table walks stay cached; converting straight from the
-    // caller's nineteen bond arrays at once measured 0.18-0.74 s for the
-    // impact lattice), and the stream orders every buffer's reuse.
     void convertOnDevice(char *staged, cudaStream_t stream) {
         const gbl_state_view &st = view_;
-        const bool inplace = pageableAccess();
+        if (pageableAccess()) {
+            convertFromHost(staged, stream);
+            return;
+        }
         // Each staging buffer holds up to 256 MB of the caller's arrays (less
         // when the whole lattice needs less).
         const std::size_t P = static_cast<std::size_t>(dev.D) * N;
@@ -818,18 +837,17 @@ template <class R> struct Resident {
         struct Part { const void *src; std::size_t bytes; };
         // One chunk: its parts staged into the free buffer, then converted.
         auto chunk = [&](std::initializer_list<Part> parts, auto &&convert) {
-            if (pending[turn] && !inplace) check(cudaEventSynchronize(used[turn]), "upload");
+            if (pending[turn]) check(cudaEventSynchronize(used[turn]), "upload");
             char *buf = stage + static_cast<std::size_t>(turn) * kStage;
             std::vector<Segment> segments;
             std::vector<const char *> at;
             std::size_t off = 0;
             for (const Part &q : parts) {
                 at.push_back(buf + off);
-                if (inplace) copyIn(buf + off, q.src, q.bytes, stream);
-                else segments.push_back({buf + off, q.src, q.bytes});
+                segments.push_back({buf + off, q.src, q.bytes});
                 off += round(q.bytes);
             }
-            if (!inplace) copySegments(segments, cudaMemcpyHostToDevice);
+            copySegments(segments, cudaMemcpyHostToDevice);
             convert(at);
             check(cudaGetLastError(), "kernel launch");
             check(cudaEventRecord(used[turn], stream), "event");

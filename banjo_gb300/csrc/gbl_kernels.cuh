@@ -3017,10 +3017,4 @@ __global__ void __launch_bounds__(kThreads) kCopyWords(std::uint32_t *dst, const
     for (std::size_t k = gridFirst(); k < n; k += gridStride()) dst[k] = src[k];
 }
 
-// One array of the caller's, read in place from host memory, into a device
-// staging buffer, in units of T (the widest the source's alignment allows).
-template <class T> __global__ void __launch_bounds__(kThreads) kCopyIn(T *dst, const T *src, std::size_t n) {
-    for (std::size_t k = gridFirst(); k < n; k += gridStride()) dst[k] = src[k];
-}
-
 } // namespace gbl

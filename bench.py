@@ -270,9 +270,10 @@ def run_gb300(args) -> None:
     sched = lattice.build_lattice_schedule(n, case["bond_a"], case["bond_b"], case["node_block_begin"])
     state = lattice.build_lattice_state(case, sched)
     # The caller's state for the e2e run, built up front as a caller's would
-    # be. (Host memory allocated into address ranges the device read from and
-    # that were freed since uploads at a third of the speed on this machine:
-    # 0.43-0.65 s against 0.12-0.19 s for the impact lattice.)
+    # be, before the main lattice's memory is freed and reused. The upload
+    # reads it through the host's page tables; its time varies from process
+    # to process on this machine (0.12-1.3 s for the impact lattice, the first
+    # reads of a process's pages costing the most).
     e2e_state = lattice.build_lattice_state(case, sched)
     settings = lattice.step_settings(case["settings"])
     sphere = lattice.sphere_state(case["sphere"])
