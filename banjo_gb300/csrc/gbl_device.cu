@@ -17,8 +17,10 @@
 #include <cstdlib>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <new>
@@ -103,16 +105,234 @@ std::size_t borrowHelpers(std::size_t want) {
 }
 void returnHelpers(std::size_t n) { g_helpers -= static_cast<long>(n); }
 
-// Copies between pageable host memory and the device, split into pieces of
-// at most 64 MB copied by several host threads at once (each on its own
-// stream): the staging of pageable memory is host-bound, one thread at a
-// time. Returns when every piece has arrived.
 struct Segment {
     void *dst;
     const void *src;
     std::size_t bytes;
 };
-void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind) {
+
+// A crew of host threads that runs one job after another, each job split over
+// the crew (the calling thread included) as job(t, T). The helpers are
+// borrowed once for the crew's life, so a copy of many slices starts its
+// threads once. A job must not throw.
+class Crew {
+public:
+    using Job = std::function<void(std::size_t, std::size_t)>;
+    explicit Crew(std::size_t want) : T_(1 + borrowHelpers(want)) {
+        for (std::size_t t = 1; t < T_; ++t) threads_.emplace_back([this, t] { serve(t); });
+    }
+    Crew(const Crew &) = delete;
+    Crew &operator=(const Crew &) = delete;
+    ~Crew() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            quit_ = true;
+        }
+        go_.notify_all();
+        for (auto &th : threads_) th.join();
+        returnHelpers(T_ - 1);
+    }
+    // job(t, T) on every member; returns when all have finished.
+    void run(const Job &job) {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            job_ = &job;
+            ++round_;
+            left_ = T_ - 1;
+        }
+        go_.notify_all();
+        job(0, T_);
+        std::unique_lock<std::mutex> g(m_);
+        done_.wait(g, [&] { return left_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void serve(std::size_t t) {
+        std::size_t seen = 0;
+        for (;;) {
+            const Job *job = nullptr;
+            {
+                std::unique_lock<std::mutex> g(m_);
+                go_.wait(g, [&] { return quit_ || round_ != seen; });
+                if (quit_) return;
+                seen = round_;
+                job = job_;
+            }
+            (*job)(t, T_);
+            std::lock_guard<std::mutex> g(m_);
+            if (--left_ == 0) done_.notify_one();
+        }
+    }
+    std::size_t T_;
+    std::vector<std::thread> threads_;
+    std::mutex m_;
+    std::condition_variable go_, done_;
+    const Job *job_{};
+    std::size_t round_{}, left_{};
+    bool quit_{};
+};
+
+// How large copies between pageable host memory and the device move
+// (GBL_HOST_COPY): "pinned" (the default) -- host threads copy between the
+// caller's memory and two page-locked staging buffers, whose contents the copy
+// engines move while the threads fill or drain the other one; "driver" -- one
+// cudaMemcpyAsync per 64 MB piece from several threads, the driver staging
+// pageable memory itself.
+bool pinnedCopies() {
+    static const bool yes = [] {
+        const char *env = std::getenv("GBL_HOST_COPY");
+        return !(env && std::strcmp(env, "driver") == 0);
+    }();
+    return yes;
+}
+
+// The page-locked staging buffers of the pinned copies, per device: two
+// slices, allocated at the device's first such copy and kept for the process
+// (pinning memory costs about as much as copying it, so it is done once),
+// under the ID of the context they were allocated in -- a device reset frees
+// them, and the next copy allocates them again. Copies to one device take
+// turns on its buffers.
+constexpr std::size_t kPinnedSlice = std::size_t(64) << 20;
+constexpr std::size_t kPinnedMinBytes = kPinnedSlice;
+constexpr int kPinnedDevices = 64;
+struct PinnedStage {
+    std::mutex m;
+    char *buf{};
+    unsigned long long context{};
+};
+PinnedStage &pinnedStage(int device) {
+    static PinnedStage *stages = new PinnedStage[kPinnedDevices]; // never destroyed: copies may run at teardown
+    if (device < 0 || device >= kPinnedDevices) runtime("CUDA device ordinal out of range");
+    return stages[device];
+}
+
+// One slice of a pinned copy: pieces of segments, each at its offset in a
+// staging buffer.
+struct SlicePiece {
+    char *host;
+    char *device;
+    std::size_t bytes, at;
+};
+
+// The pinned copy of `segments` (host to device or device to host), slice by
+// slice through the two staging buffers on a stream of its own: to the device,
+// the crew fills one buffer while the copy engines empty the other; from the
+// device, the engines fill one while the crew drains the other (the caller's
+// crew, or one of the copy's own). Returns when every byte has arrived.
+void copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew_in) {
+    const bool up = kind == cudaMemcpyHostToDevice;
+    std::vector<std::vector<SlicePiece>> slices(1);
+    std::size_t used = 0, total = 0;
+    for (const Segment &g : segments) {
+        char *host = up ? static_cast<char *>(const_cast<void *>(g.src)) : static_cast<char *>(g.dst);
+        char *device = up ? static_cast<char *>(g.dst) : static_cast<char *>(const_cast<void *>(g.src));
+        for (std::size_t off = 0; off < g.bytes;) {
+            if (used == kPinnedSlice) {
+                slices.emplace_back();
+                used = 0;
+            }
+            const std::size_t n = std::min(g.bytes - off, kPinnedSlice - used);
+            slices.back().push_back({host + off, device + off, n, used});
+            used += n;
+            off += n;
+            total += n;
+        }
+    }
+    if (!total) return;
+    int device = 0;
+    check(cudaGetDevice(&device), "device");
+    check(cudaSetDevice(device), "device"); // its context current on this thread, so its ID can be read
+    PinnedStage &stage = pinnedStage(device);
+    std::lock_guard<std::mutex> lock(stage.m);
+    const unsigned long long context = currentContextId();
+    if (!stage.buf || (context != 0 && context != stage.context)) {
+        // Buffers of an earlier context of this device went with it.
+        stage.buf = nullptr;
+        check(cudaHostAlloc(reinterpret_cast<void **>(&stage.buf), 2 * kPinnedSlice, cudaHostAllocDefault),
+              "page-locked staging allocation");
+        stage.context = context;
+    }
+    cudaStream_t stream = nullptr;
+    cudaEvent_t moved[2] = {nullptr, nullptr};
+    struct Release {
+        cudaStream_t &s;
+        cudaEvent_t (&e)[2];
+        ~Release() {
+            if (s) {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+            for (cudaEvent_t ev : e)
+                if (ev) cudaEventDestroy(ev);
+        }
+    } release{stream, moved};
+    check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+    check(cudaEventCreateWithFlags(&moved[0], cudaEventDisableTiming), "event");
+    check(cudaEventCreateWithFlags(&moved[1], cudaEventDisableTiming), "event");
+    std::unique_ptr<Crew> own;
+    if (!crew_in)
+        own = std::make_unique<Crew>(std::min<std::size_t>(15, (total + (std::size_t(4) << 20) - 1) >> 22));
+    Crew &crew = crew_in ? *crew_in : *own;
+    // The crew's share of a slice: its bytes split evenly over the members.
+    auto hostSide = [&](const std::vector<SlicePiece> &slice, char *buf) {
+        std::size_t bytes = 0;
+        for (const SlicePiece &p : slice) bytes += p.bytes;
+        crew.run([&](std::size_t t, std::size_t T) {
+            const std::size_t lo = bytes * t / T, hi = bytes * (t + 1) / T;
+            for (const SlicePiece &p : slice) {
+                const std::size_t a = std::max(lo, p.at), b = std::min(hi, p.at + p.bytes);
+                if (a >= b) continue;
+                if (up) std::memcpy(buf + a, p.host + (a - p.at), b - a);
+                else std::memcpy(p.host + (a - p.at), buf + a, b - a);
+            }
+        });
+    };
+    auto engines = [&](const std::vector<SlicePiece> &slice, char *buf, int k) {
+        for (const SlicePiece &p : slice)
+            check(up ? cudaMemcpyAsync(p.device, buf + p.at, p.bytes, kind, stream)
+                     : cudaMemcpyAsync(buf + p.at, p.device, p.bytes, kind, stream),
+                  "copy");
+        check(cudaEventRecord(moved[k], stream), "event");
+    };
+    char *buf[2] = {stage.buf, stage.buf + kPinnedSlice};
+    const std::size_t S = slices.size();
+    if (up) {
+        for (std::size_t k = 0; k < S; ++k) {
+            const int b = static_cast<int>(k & 1);
+            if (k >= 2) check(cudaEventSynchronize(moved[b]), "copy"); // the engines have read this buffer
+            hostSide(slices[k], buf[b]);
+            engines(slices[k], buf[b], b);
+        }
+    } else {
+        engines(slices[0], buf[0], 0);
+        if (S > 1) engines(slices[1], buf[1], 1);
+        for (std::size_t k = 0; k < S; ++k) {
+            const int b = static_cast<int>(k & 1);
+            check(cudaEventSynchronize(moved[b]), "copy");
+            hostSide(slices[k], buf[b]);
+            if (k + 2 < S) engines(slices[k + 2], buf[b], b);
+        }
+    }
+    check(cudaStreamSynchronize(stream), "copy");
+}
+
+// Copies between pageable host memory and the device. Pinned (above) when a
+// crew is handed in, for every copy from the device, and for a copy to the
+// device that fills at least one slice; otherwise (a small copy to the device,
+// or GBL_HOST_COPY=driver) split into pieces of at most 64 MB copied by
+// several host threads at once (each on its own stream): the driver's staging
+// of pageable memory is host-bound, one thread at a time. Measured: the 4096
+// downloads of a batch's trials 3.0 s pinned, 4.6-4.7 s through the driver;
+// the small host images of 532 served requests admitted in 5.6 s pinned, 3.4 s
+// through the driver. Returns when every piece has arrived.
+void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew = nullptr) {
+    std::size_t total = 0;
+    for (const Segment &g : segments) total += g.bytes;
+    if (crew || (pinnedCopies() && (kind == cudaMemcpyDeviceToHost || total >= kPinnedMinBytes))) {
+        copySegmentsPinned(segments, kind, crew);
+        return;
+    }
     constexpr std::size_t kPiece = std::size_t(64) << 20;
     std::vector<Segment> pieces;
     for (const Segment &g : segments)
@@ -153,14 +373,10 @@ void copyParallel(void *dst, const void *src, std::size_t bytes, cudaMemcpyKind 
     copySegments({{dst, src, bytes}}, kind);
 }
 
-// Whether kernels may read the caller's pageable host memory directly: the
-// device says so (coherent pageable access through the host's page tables,
-// as over a Grace CPU's chip-to-chip link), unless GBL_STAGED_UPLOAD=1 asks
-// for the staged copies every device supports.
-bool pageableAccess() {
+// Whether the device reads pageable host memory coherently through the host's
+// page tables (as over a Grace CPU's chip-to-chip link).
+bool deviceReadsPageable() {
     static const bool yes = [] {
-        const char *env = std::getenv("GBL_STAGED_UPLOAD");
-        if (env && env[0] == '1') return false;
         int dev = 0, access = 0, tables = 0;
         if (cudaGetDevice(&dev) != cudaSuccess) return false;
         if (cudaDeviceGetAttribute(&access, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
@@ -169,6 +385,29 @@ bool pageableAccess() {
         return access == 1 && tables == 1;
     }();
     return yes;
+}
+
+// Whether an upload of `bytes` of caller arrays has its conversion kernels
+// read them in place (where the device reads pageable memory) rather than
+// staged: copied in chunks into device buffers (through the pinned slices, or
+// the driver's staging for small lattices) and converted there. GBL_UPLOAD=
+// in_place or staged fixes the choice; by default a lattice below 1 GiB of
+// arrays is read in place (no host copy, nothing for the host to wait for: a
+// batch's members upload behind one another) and a larger one is staged.
+// Measured on the 9.8 GB impact lattice on a Grace host, per process: in place
+// 0.43-1.35 s on first reads and 0.16-1.17 s again (it varies from process to
+// process: the device's translations of the host's pages), staged through the
+// pinned slices 0.21-0.30 s, staged through the driver's copies 1.36-1.45 s.
+constexpr std::size_t kInPlaceMaxBytes = std::size_t(1) << 30;
+bool uploadInPlace(std::size_t bytes) {
+    if (!deviceReadsPageable()) return false;
+    static const int choice = [] {
+        const char *env = std::getenv("GBL_UPLOAD");
+        if (env && std::strcmp(env, "in_place") == 0) return 1;
+        if (env && std::strcmp(env, "staged") == 0) return 2;
+        return 0;
+    }();
+    return choice == 1 || (choice == 0 && bytes < kInPlaceMaxBytes);
 }
 
 // An allocator that leaves trivial elements uninitialised when a vector is
@@ -293,6 +532,14 @@ template <class R> struct Resident {
     unsigned *flowed_dev_{};         // the in-place conversion's flag, until commitFinish reads it
     cudaEvent_t committed_{};        // commitBegin's work, until commitFinish waits for it
     cudaStream_t commit_stream_{};
+    bool in_place_{};                // this upload's kernels read the caller's arrays in place
+
+    // Bytes of the caller's arrays an upload reads: 14 doubles per node, 41
+    // bytes per neighbour slot, 164 per bond.
+    std::size_t hostBytes() const {
+        return static_cast<std::size_t>(N) * 14 * sizeof(double) + static_cast<std::size_t>(dev.D) * N * 41 +
+               static_cast<std::size_t>(B) * 164;
+    }
 
     // The table size rule of latticeContactBucketMask (LatticePhysics.hpp:239-243),
     // applied to this lattice's own node count.
@@ -722,7 +969,8 @@ template <class R> struct Resident {
         if (B) check(cudaMallocAsync(&staged, hi - lo, stream), "device allocation");
         // Host-side copies on other streams need the allocation made; the
         // in-place path keeps all its work on `stream`.
-        if (image_ || !pageableAccess()) check(cudaStreamSynchronize(stream), "device allocation");
+        in_place_ = !image_ && uploadInPlace(hostBytes());
+        if (!in_place_) check(cudaStreamSynchronize(stream), "device allocation");
         if (image_) {
             const unsigned char *img = image_.get();
             copySegments({{base, img, lo}, {staged, img + lo, B ? hi - lo : 0}, {base + hi, img + hi, filled_ - hi}},
@@ -813,7 +1061,7 @@ template <class R> struct Resident {
     // `staged` in schedule order; then the small arrays.
     void convertOnDevice(char *staged, cudaStream_t stream) {
         const gbl_state_view &st = view_;
-        if (pageableAccess()) {
+        if (in_place_) {
             convertFromHost(staged, stream);
             return;
         }
@@ -824,6 +1072,12 @@ template <class R> struct Resident {
         auto round = [](std::size_t x) { return (x + 255) & ~std::size_t(255); };
         // A multiple of 256 bytes: the second buffer and every part start aligned.
         const std::size_t kStage = round(std::min(std::size_t(256) << 20, whole + 32 * 256));
+        // Pinned copies for a lattice of at least one slice: one crew of host
+        // threads copies every chunk, a thread per 4 MB of the arrays, at
+        // most 16. A smaller lattice's chunks go through the driver's staging.
+        std::unique_ptr<Crew> crew;
+        if (pinnedCopies() && hostBytes() >= kPinnedMinBytes)
+            crew = std::make_unique<Crew>(std::min<std::size_t>(15, hostBytes() >> 22));
         char *stage = nullptr;
         check(cudaMallocAsync(&stage, 2 * kStage + 256, stream), "device allocation");
         unsigned *flowed = reinterpret_cast<unsigned *>(stage + 2 * kStage);
@@ -847,7 +1101,7 @@ template <class R> struct Resident {
                 segments.push_back({buf + off, q.src, q.bytes});
                 off += round(q.bytes);
             }
-            copySegments(segments, cudaMemcpyHostToDevice);
+            copySegments(segments, cudaMemcpyHostToDevice, crew.get());
             convert(at);
             check(cudaGetLastError(), "kernel launch");
             check(cudaEventRecord(used[turn], stream), "event");
@@ -904,7 +1158,7 @@ template <class R> struct Resident {
                        sizeof(std::uint32_t) * (sched.block_count + 1)},
                       {dev.level_begin, level_begin_.data(), sizeof(std::uint32_t) * level_begin_.size()},
                       {dev.sphere, &sphere0, sizeof(sphere0)}},
-                     cudaMemcpyHostToDevice);
+                     cudaMemcpyHostToDevice, crew.get());
         check(cudaMemsetAsync(dev.dirty, 1, N, stream), "memset");
         check(cudaMemsetAsync(dev.dirty + N, 0, 4, stream), "memset");
         check(cudaMemcpyAsync(&flowed_host_, flowed, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "copy");

@@ -76,6 +76,12 @@ struct State {
 
 State buildState(const gbl_matter_view &m, const Schedule &s, const double origin[3]);
 
+// The unique ID of the current CUDA context (cuCtxGetId), or 0 when none is
+// current or the driver cannot say. A context created after a device reset
+// has a new ID, so device pointers and pinned host buffers cached against an
+// ID are known to be stale once it changes.
+unsigned long long currentContextId();
+
 } // namespace gbl
 
 struct gbl_schedule {

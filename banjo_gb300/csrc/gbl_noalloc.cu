@@ -27,6 +27,36 @@
 #include <string>
 
 namespace gbl {
+
+// The current context's unique ID, or 0 when none is current or the driver
+// cannot say. The two driver calls are reached through the runtime's entry
+// point table, so the library does not link the driver library itself.
+unsigned long long currentContextId() {
+    using GetCurrent = int (*)(void **);
+    using GetId = int (*)(void *, unsigned long long *);
+    struct Calls {
+        GetCurrent get_current{};
+        GetId get_id{};
+    };
+    static const Calls calls = [] {
+        Calls c;
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+            c.get_current = reinterpret_cast<GetCurrent>(a);
+            c.get_id = reinterpret_cast<GetId>(b);
+        }
+        return c;
+    }();
+    if (!calls.get_current || !calls.get_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (calls.get_current(&ctx) != 0 || !ctx || calls.get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
 namespace {
 
 constexpr unsigned kNoAllocThreads = 256;
@@ -133,33 +163,6 @@ struct ScratchAddress {
     std::uint32_t *address{};
 };
 ScratchAddress g_scratch[kMaxDevices];
-
-// The current context's unique ID, or 0 when none is current or the driver
-// cannot say. The two driver calls are reached through the runtime's entry
-// point table, so the library does not link the driver library itself.
-unsigned long long currentContextId() {
-    using GetCurrent = int (*)(void **);
-    using GetId = int (*)(void *, unsigned long long *);
-    static GetCurrent get_current = nullptr;
-    static GetId get_id = nullptr;
-    static bool resolved = false;
-    if (!resolved) { // under g_setup_mutex
-        void *a = nullptr, *b = nullptr;
-        cudaDriverEntryPointQueryResult qa{}, qb{};
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
-            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
-            qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
-            get_current = reinterpret_cast<GetCurrent>(a);
-            get_id = reinterpret_cast<GetId>(b);
-        }
-        resolved = true;
-    }
-    if (!get_current || !get_id) return 0;
-    void *ctx = nullptr;
-    unsigned long long id = 0;
-    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
-    return id;
-}
 
 std::uint32_t *scratchForCurrentDevice() {
     int device = 0;

@@ -271,9 +271,7 @@ def run_gb300(args) -> None:
     state = lattice.build_lattice_state(case, sched)
     # The caller's state for the e2e run, built up front as a caller's would
     # be, before the main lattice's memory is freed and reused. The upload
-    # reads it through the host's page tables; its time varies from process
-    # to process on this machine (0.12-1.3 s for the impact lattice, the first
-    # reads of a process's pages costing the most).
+    # copies it through page-locked staging slices on the host's threads.
     e2e_state = lattice.build_lattice_state(case, sched)
     settings = lattice.step_settings(case["settings"])
     sphere = lattice.sphere_state(case["sphere"])
@@ -734,8 +732,8 @@ class ServedRun:
         def submit(i):
             sched, state, _ = self.picks[i]
             # Copied: the request's device image is prepared on the client's
-            # thread, so admission is a copy; borrowed: the device reads the
-            # caller's arrays at admission.
+            # thread, so admission is a copy; borrowed: the caller's arrays
+            # are copied as they are and converted on the device at admission.
             tickets[i] = server.submit(sched, state, sphere, self.horizon, borrow=not self.copy and i not in self.keep)
 
         def produce():

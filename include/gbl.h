@@ -451,9 +451,8 @@ gbl_result gbl_serve_submit(gbl_server *server, const gbl_schedule_view *schedul
 /* As gbl_serve_submit, but the state's arrays are borrowed until the request
  * is admitted (gbl_serve_poll reports RUNNING or DONE, or it is cancelled):
  * the caller keeps them alive and unchanged until then. Only the sweep order
- * is prepared here; at admission the device reads the arrays as they are
- * (in place where it has coherent access to pageable host memory) and
- * converts them, so no host image of the request is written. */
+ * is prepared here; at admission the arrays are copied to the device as
+ * they are and converted there, so no host image of the request is written. */
 gbl_result gbl_serve_submit_borrowed(gbl_server *server, const gbl_schedule_view *schedule,
                                      const gbl_state_view *state, const gbl_sphere *sphere, uint64_t substeps,
                                      uint64_t *ticket);
