@@ -845,8 +845,10 @@ def served_leg(args, lattice, batched: dict | None) -> dict:
                    large_requests=int(sum(w >= len(small) for w in which)))
         points.append(res)
         if keep:
-            out["parity"] = served_parity(lattice, settings, [pool[which[i]] for i in keep], run.results, keep,
-                                          horizon)
+            picks = [pool[which[i]] for i in keep]
+            out["parity"] = served_parity(lattice, settings, picks, run.results, keep, horizon)
+            if args.fp64_steps > 0:
+                out["fp64_error"] = served_fp64(lattice, settings, picks, run.results, keep, horizon)
             parity_done = True
     out["load_sweep"] = points
     if points:
@@ -895,6 +897,46 @@ def served_parity(lattice, settings, picks, results, keep, horizon) -> dict:
             "largest_member_bonds": max(m["bonds"] for m in members.values()),
             "note": "seeded requests of the first load point (one 128^3 among them), bit for bit against the same "
                     "request run alone"}
+
+
+def served_fp64(lattice, settings, picks, results, keep, horizon, members: int = 4) -> dict:
+    """The FP32 served results of the smallest kept requests against the
+    device's FP64 lane (direct arithmetic, which the restatement's FP64 lane
+    holds bit for bit) on the same requests alone: over the whole horizon,
+    and over the substeps before the request's first bond failure (after it
+    the two precisions are different trajectories of a chaotic process)."""
+    s64 = type(settings).from_buffer_copy(settings)
+    s64.direct_arithmetic = 1
+
+    def alone(sched, state, fresh, s, precision, substeps):
+        be = lattice.make_gb300_lattice_backend(sched, precision)
+        be.upload(state, s, lattice.Sphere())
+        st = be.run(lattice.RunControl(max_steps=substeps))
+        out = fresh()
+        sp = be.download(out)
+        del be
+        return lattice.state_outputs(out, sp, np.zeros(0, np.uint32), st)
+
+    order = sorted(range(len(keep)), key=lambda q: picks[q][1].bond_count)[:members]
+    fp = {}
+    for q in order:
+        sched, state, fresh = picks[q]
+        ref = {"ref_pos": np.asarray(state.x0, np.float64)}
+        served = results[keep[q]]
+        row = dict(fp64_error(ref, served, alone(sched, state, fresh, s64, "double", horizon)),
+                   bonds=state.bond_count)
+        first = int(served["status_u64"][1])
+        if 0 < first < horizon:
+            row["before_failure"] = fp64_error(ref, alone(sched, state, fresh, settings, "float", first),
+                                               alone(sched, state, fresh, s64, "double", first))
+        fp[str(keep[q])] = row
+    pre = [v["before_failure"]["max_position_error_over_extent"] for v in fp.values() if "before_failure" in v]
+    return {"members": fp,
+            "max_position_error_over_extent": max((v["max_position_error_over_extent"] for v in fp.values()),
+                                                  default=None),
+            "max_position_error_over_extent_before_failure": max(pre, default=None),
+            "note": f"the {len(fp)} smallest requests of the parity sample, served FP32 against the device's FP64 "
+                    f"lane on the same request alone, over {horizon} substeps and up to the first bond failure"}
 
 
 # ---------------------------------------------------------------------------
