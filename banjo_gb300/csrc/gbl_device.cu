@@ -200,6 +200,7 @@ struct PinnedStage {
     std::mutex m;
     char *buf{};
     unsigned long long context{};
+    bool refused{}; // page-locked memory was refused in this context: copies go through the driver
 };
 PinnedStage &pinnedStage(int device) {
     static PinnedStage *stages = new PinnedStage[kPinnedDevices]; // never destroyed: copies may run at teardown
@@ -219,8 +220,9 @@ struct SlicePiece {
 // slice through the two staging buffers on a stream of its own: to the device,
 // the crew fills one buffer while the copy engines empty the other; from the
 // device, the engines fill one while the crew drains the other (the caller's
-// crew, or one of the copy's own). Returns when every byte has arrived.
-void copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew_in) {
+// crew, or one of the copy's own). Returns true when every byte has arrived,
+// false (having copied nothing) when the slices cannot be allocated.
+bool copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew_in) {
     const bool up = kind == cudaMemcpyHostToDevice;
     std::vector<std::vector<SlicePiece>> slices(1);
     std::size_t used = 0, total = 0;
@@ -239,19 +241,31 @@ void copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kin
             total += n;
         }
     }
-    if (!total) return;
+    if (!total) return true;
     int device = 0;
     check(cudaGetDevice(&device), "device");
     check(cudaSetDevice(device), "device"); // its context current on this thread, so its ID can be read
     PinnedStage &stage = pinnedStage(device);
     std::lock_guard<std::mutex> lock(stage.m);
     const unsigned long long context = currentContextId();
-    if (!stage.buf || (context != 0 && context != stage.context)) {
+    if (context != 0 && context != stage.context) {
         // Buffers of an earlier context of this device went with it.
         stage.buf = nullptr;
-        check(cudaHostAlloc(reinterpret_cast<void **>(&stage.buf), 2 * kPinnedSlice, cudaHostAllocDefault),
-              "page-locked staging allocation");
+        stage.refused = false;
         stage.context = context;
+    }
+    if (stage.refused) return false;
+    if (!stage.buf) {
+        const cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&stage.buf), 2 * kPinnedSlice,
+                                            cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            // Refused (a locked-memory limit, say): the copies are the
+            // driver's. The error is this call's own; it is not left pending.
+            if (cudaPeekAtLastError() == e) cudaGetLastError();
+            stage.buf = nullptr;
+            stage.refused = true;
+            return false;
+        }
     }
     cudaStream_t stream = nullptr;
     cudaEvent_t moved[2] = {nullptr, nullptr};
@@ -315,6 +329,7 @@ void copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kin
         }
     }
     check(cudaStreamSynchronize(stream), "copy");
+    return true;
 }
 
 // Copies between pageable host memory and the device. Pinned (above) when a
@@ -329,10 +344,9 @@ void copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kin
 void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew = nullptr) {
     std::size_t total = 0;
     for (const Segment &g : segments) total += g.bytes;
-    if (crew || (pinnedCopies() && (kind == cudaMemcpyDeviceToHost || total >= kPinnedMinBytes))) {
-        copySegmentsPinned(segments, kind, crew);
+    if ((crew || (pinnedCopies() && (kind == cudaMemcpyDeviceToHost || total >= kPinnedMinBytes))) &&
+        copySegmentsPinned(segments, kind, crew))
         return;
-    }
     constexpr std::size_t kPiece = std::size_t(64) << 20;
     std::vector<Segment> pieces;
     for (const Segment &g : segments)
