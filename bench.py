@@ -32,17 +32,17 @@ Main line (the impact):
             post-upload restart), all host threads.
 
 Legs (each with its own parity, FP64 error and CPU baseline where it applies):
-  cantilever  32x8x8 pinned beam under its load, 240 steps (config 1).
+  cantilever  32x8x8 pinned beam under its load, 240 steps.
   batched   4096 drop trials of uneven size in one batch against the same
             trials one backend at a time ("plain"), device time and through
-            the API (e2e) (config 3).
-  served    requests of config 4's mix (90% config-3 trials, 10% 128^3
-            lattices, 2400 substeps each) arriving as a Poisson process at 50,
+            the API (e2e).
+  served    requests (90% drop trials, 10% 128^3 lattices, 2400 substeps
+            each) arriving as a Poisson process at 50,
             80 and 95% of the batched capacity, with p50/p99 latency, admission
             wait and admission's share of wall time; a 2000/s stress point with
             a short horizon; a sample of requests checked against the same
             request run alone.
-  cascade   the 128x32x32 notched bar under its ramped end load (config 5).
+  cascade   the 128x32x32 notched bar under its ramped end load.
 
 --impl reference times the reference's CPU lane on the same workload, metric
 and window (the substeps of the same K steps after the same W warm-up steps).
@@ -405,7 +405,7 @@ def run_gb300(args) -> None:
 
 
 # ---------------------------------------------------------------------------
-# Config 1: the cantilever
+# The cantilever
 # ---------------------------------------------------------------------------
 def cantilever_leg(args, lattice) -> dict:
     import oracle
@@ -560,7 +560,7 @@ class ScratchDownload:
 
 
 def batched_leg(args, lattice) -> dict:
-    """Config-3 trials in one batch against the same trials run one lattice at
+    """Drop trials in one batch against the same trials run one lattice at
     a time through the single-lattice backend ("plain")."""
     import oracle
     from concurrent.futures import ThreadPoolExecutor
@@ -700,7 +700,7 @@ def batched_leg(args, lattice) -> dict:
 
 
 # ---------------------------------------------------------------------------
-# Config 4: served requests
+# Served requests
 # ---------------------------------------------------------------------------
 class ServedRun:
     """One arrival process against a fresh server: clients submit each
@@ -786,7 +786,7 @@ class ServedRun:
 
 
 def served_leg(args, lattice, batched: dict | None) -> dict:
-    """Config-4 requests: Poisson arrivals of 90% config-3 trials and 10% 128^3
+    """Served requests: Poisson arrivals of 90% drop trials and 10% 128^3
     lattices, 2400 substeps each, admitted against an HBM budget and stepped
     together; a load sweep at fractions of the batched capacity."""
     from concurrent.futures import ThreadPoolExecutor
@@ -868,7 +868,7 @@ def served_leg(args, lattice, batched: dict | None) -> dict:
                    substeps_per_request=args.stress_substeps)
         out["stress"] = res
     out["workload"] = (f"Poisson arrivals of {args.served_completions} requests per point at 50/80/95% of the "
-                       f"batched capacity; 90% drawn from {len(small)} config-3 trials, 10% 128^3 lattices; "
+                       f"batched capacity; 90% drawn from {len(small)} drop trials, 10% 128^3 lattices; "
                        f"{horizon} substeps each; latency = finish observed by the client - scheduled arrival")
     return out
 
@@ -940,7 +940,7 @@ def served_fp64(lattice, settings, picks, results, keep, horizon, members: int =
 
 
 # ---------------------------------------------------------------------------
-# Config 5: the notched bar
+# The notched bar
 # ---------------------------------------------------------------------------
 def cascade_leg(args, lattice) -> dict:
     """The notched bar (energy-scaled law, plastic flow, horizon 2) under its

@@ -263,7 +263,7 @@ Built buildFromCase(const lsio::Case &c) {
     return b;
 }
 
-// Config 5 material: the reference's own compiler, so the oracle thresholds of
+// The notched bar's material: the reference's own compiler, so the oracle thresholds of
 // the notched bar are the reference's numbers (MaterialCompiler.cpp:44-214).
 void compileMaterial(const lsio::Case &c, lsio::Case &out) {
     const auto m = c.get<double>("material"); // density, E, nu, tensile, yield, hardening, Gc, cell, horizon
