@@ -7,9 +7,13 @@ substeps, re-set every step) is run for the whole ramp by the reference's own
 threaded CPU lane (oracle/_ref/ref_harness: makeParallelCpuLatticeBackend,
 compiled from the reference's sources), one substep per run call so that the
 substep at which every bond broke is recorded. A 100,000-substep run takes
-about two hours on six threads of an x86-64 host, so it is recorded once:
+about three and a half hours on six threads of an x86-64 host (the double
+lane, which the FP32 error is measured against, about the same), so each is
+recorded once:
 
-    python tests/golden/make_cascade_long.py [--threads 6] [--precision float]
+    python tests/golden/make_cascade_long.py [--threads 6] [--precision float|double]
+
+writing tests/golden/cascade_long.npz or cascade_long_double.npz.
 
 The fixture keeps what the GPU test compares: the final positions and
 velocities in full (float32 for the float lane: its values are floats widened,
