@@ -155,8 +155,8 @@ def make_case(workload: str) -> tuple[dict, str]:
 def sweep_bytes(n: int, live: float) -> float:
     """Algorithmic bytes of one substep's projection sweeps: per iteration,
     every node's position read and written (16 + 8: the w lane is read only)
-    and every live bond's record, geometry, multiplier and plastic extension
-    (40)."""
+    and every live bond's ends, rest data, rest edge and compliance (32) and
+    its multiplier read and written (8)."""
     return ITERATIONS * (n * 24 + live * 40)
 
 
