@@ -334,19 +334,24 @@ bool copySegmentsPinned(const std::vector<Segment> &segments, cudaMemcpyKind kin
 
 // Copies between pageable host memory and the device. Pinned (above) when a
 // crew is handed in, for every copy from the device, and for a copy to the
-// device that fills at least one slice; otherwise (a small copy to the device,
-// or GBL_HOST_COPY=driver) split into pieces of at most 64 MB copied by
-// several host threads at once (each on its own stream): the driver's staging
-// of pageable memory is host-bound, one thread at a time. Measured: the 4096
-// downloads of a batch's trials 3.0 s pinned, 4.6-4.7 s through the driver;
-// the small host images of 532 served requests admitted in 5.6 s pinned, 3.4 s
-// through the driver. Returns when every piece has arrived.
-void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew = nullptr) {
+// device that fills at least one slice; otherwise (a small copy to the
+// device, a copy the caller sends to the driver, or GBL_HOST_COPY=driver)
+// split into pieces of at most 64 MB copied by several host threads at once
+// (each on its own stream): the driver's staging of pageable memory is
+// host-bound, one thread at a time. Measured: the 4096 downloads of a batch's
+// trials 3.0 s pinned, 4.6-4.7 s through the driver; the host images of 532
+// served requests arriving at 2000/s (a tenth of them 1.2 GB) admitted in
+// 5.6-5.8 s pinned, 3.4 s through the driver, so a served image goes to the
+// driver. Returns when every piece has arrived.
+enum class Staging { kAuto, kDriver };
+void copySegments(const std::vector<Segment> &segments, cudaMemcpyKind kind, Crew *crew = nullptr,
+                  Staging staging = Staging::kAuto) {
     std::size_t total = 0;
     for (const Segment &g : segments) total += g.bytes;
-    if ((crew || (pinnedCopies() && (kind == cudaMemcpyDeviceToHost || total >= kPinnedMinBytes))) &&
-        copySegmentsPinned(segments, kind, crew))
-        return;
+    const bool pinned =
+        crew || (staging == Staging::kAuto && pinnedCopies() &&
+                 (kind == cudaMemcpyDeviceToHost || total >= kPinnedMinBytes));
+    if (pinned && copySegmentsPinned(segments, kind, crew)) return;
     constexpr std::size_t kPiece = std::size_t(64) << 20;
     std::vector<Segment> pieces;
     for (const Segment &g : segments)
@@ -988,7 +993,7 @@ template <class R> struct Resident {
         if (image_) {
             const unsigned char *img = image_.get();
             copySegments({{base, img, lo}, {staged, img + lo, B ? hi - lo : 0}, {base + hi, img + hi, filled_ - hi}},
-                         cudaMemcpyHostToDevice);
+                         cudaMemcpyHostToDevice, nullptr, Staging::kDriver);
         } else {
             convertOnDevice(staged, stream);
         }
