@@ -8,8 +8,12 @@ thrown box with node-to-node contact, a plate strike with plate bending, a
 pinned beam under its load, a small notched bar under its ramp. The checker
 must reproduce the reference harness bit for bit on each, in both lanes:
 every state array, the substep each bond broke, every RunStatus counter. The
-draw is fixed (seed 2026), so a failure names a case that can be rerun.
-They run where the harness is built (the reference tree is present).
+draw is fixed (seed 2026), so a failure names a case that can be rerun; the
+device is held to the checker on the same draw (tests/test_gpu_random.py). A
+second draw (seed 7) layers the optional features on at random -- radial bond
+damping, the energy audit, plastic hardening, a named wrench -- and holds the
+checker alone to the harness. They run where the harness is built (the
+reference tree is present).
 """
 import os
 
@@ -97,3 +101,65 @@ def test_random_scenes_fracture():
         out = oracle.run_port(case, per_substep=False, threads=4)
         broke += int(out["status_u64"][4]) > 0
     assert broke >= len(CASES) // 2
+
+
+# A second draw, for the checker alone: the same kinds with the optional
+# features layered on at random -- radial bond damping, the energy audit,
+# hardening of the plastic flow, and a named wrench (force and torque) on the
+# movable nodes of the top face for part of the run.
+def _with_features(rng, case):
+    from banjo_gb300 import scenes
+
+    case = dict(case)
+    s = np.asarray(case["settings"], np.float64).copy()
+    if s.size < scenes.SETTINGS_WIDTH:
+        s = np.concatenate([s, np.zeros(scenes.SETTINGS_WIDTH - s.size)])
+    notes = []
+    if rng.random() < 0.6:
+        s[scenes.K_DAMP] = float(rng.uniform(0.01, 0.1))
+        notes.append(f"damping {s[scenes.K_DAMP]:.3f}")
+    if rng.random() < 0.6:
+        s[scenes.K_AUDIT] = 1.0
+        notes.append("audit")
+    if s[scenes.K_YIELD] > 0 and rng.random() < 0.7:
+        s[scenes.K_HARDEN] = float(rng.uniform(0.05, 0.3))
+        notes.append(f"hardening {s[scenes.K_HARDEN]:.2f}")
+    case["settings"] = s
+    if rng.random() < 0.7:
+        pos = np.asarray(case["ref_pos"], np.float64).reshape(-1, 3)
+        movable = np.ones(len(pos), dtype=bool)
+        if "pinned" in case:
+            movable &= np.asarray(case["pinned"]) == 0
+        top = np.flatnonzero((pos[:, 1] >= pos[:, 1].max() - 1e-9) & movable)
+        if top.size:
+            mass = 1e-3 * top.size
+            force = rng.uniform(-1.0, 1.0, size=3) * mass * float(rng.uniform(5.0, 50.0))
+            torque = rng.uniform(-1.0, 1.0, size=3) * float(np.abs(force).max()) * 0.01
+            substeps = int(min(int(case["steps"][0]), int(rng.integers(5, 31))))
+            case = scenes.wrenches(case, [("drive", top, pos[top].mean(axis=0), force, torque)], substeps)
+            notes.append(f"wrench {substeps}")
+    return case, notes
+
+
+def _feature_cases():
+    rng = np.random.default_rng(7)
+    out = []
+    for k in range(15):
+        kind = KINDS[k % (len(KINDS) - 1)]  # the notched bar's ramp already re-sets its loads every step
+        label, case = _draw(rng, kind)
+        case, notes = _with_features(rng, case)
+        out.append((label + (" + " + ", ".join(notes) if notes else ""), case))
+    return out
+
+
+FEATURE_CASES = _feature_cases()
+
+
+@pytest.mark.parametrize("precision", ["float", "double"])
+@pytest.mark.parametrize("index", range(len(FEATURE_CASES)), ids=[label for label, _ in FEATURE_CASES])
+def test_checker_matches_reference_on_random_scenes_with_features(index, precision):
+    _, case = FEATURE_CASES[index]
+    ref = oracle.run_reference(case, precision=precision, per_substep=True)
+    port = oracle.run_port(case, precision=precision, per_substep=True, threads=4)
+    assert mismatches(ref, port, STATE_KEYS + ["break_step"]) == []
+    assert status_mismatches(ref, port) == []
